@@ -1,0 +1,1095 @@
+// ss4d_api.cu — the extern "C" ABI of include/ss4d.h: solver handles,
+// workspaces, the SOR loop drivers (host loop and CUDA-graph while loop) and
+// argument checking.  All device work is issued on the handle's stream.
+#include <cuda_runtime.h>
+
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "ss4d_kernels.cuh"
+
+using namespace ss4d;
+
+// ---------------------------------------------------------------------------
+// errors
+
+static thread_local char g_err[512] = "";
+
+static void set_err(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+}
+
+#define CK(call)                                                                                                   \
+    do {                                                                                                           \
+        cudaError_t e_ = (call);                                                                                   \
+        if (e_ != cudaSuccess) {                                                                                   \
+            set_err("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);                   \
+            return e_ == cudaErrorMemoryAllocation ? SS4D_ERR_ALLOC                                                \
+                                                   : (e_ == cudaErrorNoDevice ? SS4D_ERR_NO_DEVICE : SS4D_ERR_CUDA); \
+        }                                                                                                          \
+    } while (0)
+
+#define CKS(expr)                                                                                                  \
+    do {                                                                                                           \
+        ss4d_status s_ = (expr);                                                                                   \
+        if (s_ != SS4D_OK)                                                                                         \
+            return s_;                                                                                             \
+    } while (0)
+
+#define REQ(cond, msg)                                                                                             \
+    do {                                                                                                           \
+        if (!(cond)) {                                                                                             \
+            set_err("invalid argument: %s", msg);                                                                  \
+            return SS4D_ERR_INVALID;                                                                               \
+        }                                                                                                          \
+    } while (0)
+
+static ss4d_status last_launch()
+{
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_err("kernel launch failed: %s", cudaGetErrorString(e));
+        return SS4D_ERR_CUDA;
+    }
+    return SS4D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// the handle
+
+struct ss4d_solver {
+    ss4d_dims dims;
+    Geo geo;
+    Split sp;
+    SweepCfg cfg;
+    ss4d_arith arith;
+    cudaStream_t stream;
+    cudaStream_t cap;
+    int device;
+    int sm_count;
+    int use_graph;
+    long long launches;
+    size_t bytes;
+
+    // reductions / scalars
+    double *d_partial;
+    long long n_partial;
+    double *d_scalar; // 8 doubles
+    double *h_scalar; // pinned mirror
+    // natural-layout scratch
+    double *d_scratch;
+    double *d_coef_nat; // 8 arrays (reference arithmetic)
+    // split form
+    SplitBufs sb;
+    int have_split, have_mixed;
+    LoopState *d_state;
+    LoopState *h_state;
+    DevParams *d_params;
+    DevParams *h_params;
+    // graphs
+    cudaGraph_t graph64, graphmx;
+    cudaGraphExec_t exec64, execmx;
+    unsigned long long cond64, condmx;
+    int graph_failed;
+    int last_graphed; // the last solve ran as a graph
+    // rescale balls
+    int *d_frame_first, *d_frame_count;
+    double *d_bx, *d_by, *d_bz;
+    int balls_cap;
+    cudaEvent_t ev0, ev1;
+    // per-kernel timing (ss4d_solver_set_timing)
+    int timing;
+    double ktime[SS4D_K_COUNT];
+    long long kcount[SS4D_K_COUNT];
+    cudaEvent_t tev0, tev1;
+};
+
+// Launch `fn` and, when timing is on, bracket it with events on the
+// handle's stream and add its device time to kernel kind `kind`.
+template <typename F>
+static void timed(ss4d_solver *s, int kind, bool count, F &&fn)
+{
+    if (!s->timing || !count) {
+        fn();
+        return;
+    }
+    cudaEventRecord(s->tev0, s->stream);
+    fn();
+    cudaEventRecord(s->tev1, s->stream);
+    if (cudaEventSynchronize(s->tev1) == cudaSuccess) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, s->tev0, s->tev1);
+        s->ktime[kind] += ms;
+        s->kcount[kind] += 1;
+    }
+}
+
+static ss4d_status dmalloc(ss4d_solver *s, void **p, size_t bytes)
+{
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_err("cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+        return SS4D_ERR_ALLOC;
+    }
+    if (s)
+        s->bytes += bytes;
+    return SS4D_OK;
+}
+
+extern "C" int ss4d_abi_version(void)
+{
+    return SS4D_ABI_VERSION;
+}
+
+extern "C" const char *ss4d_last_error(void)
+{
+    return g_err;
+}
+
+extern "C" ss4d_status ss4d_device_count(int *count)
+{
+    REQ(count, "count is NULL");
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        *count = 0;
+        set_err("no CUDA device: %s", cudaGetErrorString(e));
+        return SS4D_ERR_NO_DEVICE;
+    }
+    *count = n;
+    return SS4D_OK;
+}
+
+static ss4d_status check_dims(const ss4d_dims *d)
+{
+    REQ(d, "dims is NULL");
+    REQ(d->iMax >= 3 && d->jMax >= 3 && d->kMax >= 3 && d->lMax >= 3, "every padded extent must be >= 3");
+    const long long n = (long long)d->iMax * d->jMax * d->kMax * d->lMax;
+    REQ(n < (1LL << 31), "padded volume must hold fewer than 2^31 voxels (the reference's int indexing)");
+    REQ((long long)(d->kMax - 2) * (d->lMax - 2) <= 65535, "(kMax-2)*(lMax-2) must not exceed 65535");
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_solver_create(const ss4d_dims *dims, ss4d_arith arith, void *stream, ss4d_solver **out)
+{
+    REQ(out, "out is NULL");
+    *out = nullptr;
+    CKS(check_dims(dims));
+    REQ(arith == SS4D_ARITH_REFERENCE || arith == SS4D_ARITH_FP64 || arith == SS4D_ARITH_MIXED, "unknown arithmetic");
+    int ndev = 0;
+    CKS(ss4d_device_count(&ndev));
+    ss4d_solver *s = (ss4d_solver *)calloc(1, sizeof(ss4d_solver));
+    if (!s)
+        return SS4D_ERR_ALLOC;
+    s->dims = *dims;
+    s->geo = make_geo(*dims);
+    s->sp = make_split(s->geo);
+    s->arith = arith;
+    s->stream = (cudaStream_t)stream;
+    s->use_graph = 1;
+    ss4d_status st = SS4D_OK;
+#define FAIL_IF(call)                                                                                              \
+    do {                                                                                                           \
+        cudaError_t e_ = (call);                                                                                   \
+        if (e_ != cudaSuccess) {                                                                                   \
+            set_err("%s failed: %s", #call, cudaGetErrorString(e_));                                               \
+            st = e_ == cudaErrorMemoryAllocation ? SS4D_ERR_ALLOC : SS4D_ERR_CUDA;                                  \
+            goto fail;                                                                                             \
+        }                                                                                                          \
+    } while (0)
+    FAIL_IF(cudaGetDevice(&s->device));
+    FAIL_IF(cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device));
+    s->cfg = make_sweep_cfg(s->geo, s->sp, s->sm_count, 4);
+    FAIL_IF(cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking));
+    FAIL_IF(cudaEventCreate(&s->ev0));
+    FAIL_IF(cudaEventCreate(&s->ev1));
+    FAIL_IF(cudaEventCreate(&s->tev0));
+    FAIL_IF(cudaEventCreate(&s->tev1));
+    {
+        long long nb = interior_blocks(s->geo);
+        long long need = nb * 2;
+        if (need < 8192)
+            need = 8192;
+        if (need < 2LL * s->cfg.grid)
+            need = 2LL * s->cfg.grid;
+        s->n_partial = need;
+    }
+    if ((st = dmalloc(s, (void **)&s->d_partial, sizeof(double) * s->n_partial)) != SS4D_OK)
+        goto fail;
+    if ((st = dmalloc(s, (void **)&s->d_scalar, sizeof(double) * 8)) != SS4D_OK)
+        goto fail;
+    if ((st = dmalloc(s, (void **)&s->d_state, sizeof(LoopState))) != SS4D_OK)
+        goto fail;
+    if ((st = dmalloc(s, (void **)&s->d_params, sizeof(DevParams))) != SS4D_OK)
+        goto fail;
+    FAIL_IF(cudaMallocHost((void **)&s->h_scalar, sizeof(double) * 8));
+    FAIL_IF(cudaMallocHost((void **)&s->h_state, sizeof(LoopState)));
+    FAIL_IF(cudaMallocHost((void **)&s->h_params, sizeof(DevParams)));
+#undef FAIL_IF
+    *out = s;
+    return SS4D_OK;
+fail:
+    ss4d_solver_destroy(s);
+    return st;
+}
+
+static void free_graphs(ss4d_solver *s)
+{
+    if (s->exec64)
+        cudaGraphExecDestroy(s->exec64);
+    if (s->graph64)
+        cudaGraphDestroy(s->graph64);
+    if (s->execmx)
+        cudaGraphExecDestroy(s->execmx);
+    if (s->graphmx)
+        cudaGraphDestroy(s->graphmx);
+    s->exec64 = nullptr;
+    s->graph64 = nullptr;
+    s->execmx = nullptr;
+    s->graphmx = nullptr;
+}
+
+extern "C" ss4d_status ss4d_solver_destroy(ss4d_solver *s)
+{
+    if (!s)
+        return SS4D_OK;
+    if (s->stream || s->cap)
+        cudaStreamSynchronize(s->stream);
+    free_graphs(s);
+    void *dev[] = {s->d_partial, s->d_scalar, s->d_state, s->d_params, s->d_scratch, s->d_coef_nat,
+                   s->sb.R[0], s->sb.Bk, s->sb.P[0], s->sb.coef[0], s->sb.coef32[0], s->sb.dR[0], s->sb.r32[0],
+                   s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz};
+    for (void *p : dev)
+        if (p)
+            cudaFree(p);
+    if (s->h_scalar)
+        cudaFreeHost(s->h_scalar);
+    if (s->h_state)
+        cudaFreeHost(s->h_state);
+    if (s->h_params)
+        cudaFreeHost(s->h_params);
+    if (s->ev0)
+        cudaEventDestroy(s->ev0);
+    if (s->ev1)
+        cudaEventDestroy(s->ev1);
+    if (s->tev0)
+        cudaEventDestroy(s->tev0);
+    if (s->tev1)
+        cudaEventDestroy(s->tev1);
+    if (s->cap)
+        cudaStreamDestroy(s->cap);
+    free(s);
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_solver_set_stream(ss4d_solver *s, void *stream)
+{
+    REQ(s, "solver is NULL");
+    s->stream = (cudaStream_t)stream;
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_solver_set_arith(ss4d_solver *s, ss4d_arith arith)
+{
+    REQ(s, "solver is NULL");
+    REQ(arith == SS4D_ARITH_REFERENCE || arith == SS4D_ARITH_FP64 || arith == SS4D_ARITH_MIXED, "unknown arithmetic");
+    s->arith = arith;
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_solver_set_graph(ss4d_solver *s, int enable)
+{
+    REQ(s, "solver is NULL");
+    s->use_graph = enable ? 1 : 0;
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_solver_workspace_bytes(const ss4d_solver *s, size_t *bytes)
+{
+    REQ(s && bytes, "NULL argument");
+    *bytes = s->bytes;
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_solver_launch_count(const ss4d_solver *s, long long *count)
+{
+    REQ(s && count, "NULL argument");
+    *count = s->launches;
+    return SS4D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// workspaces
+
+static ss4d_status ensure_scratch(ss4d_solver *s)
+{
+    if (!s->d_scratch)
+        CKS(dmalloc(s, (void **)&s->d_scratch, sizeof(double) * s->geo.n));
+    return SS4D_OK;
+}
+
+static ss4d_status ensure_coef_nat(ss4d_solver *s)
+{
+    if (!s->d_coef_nat) {
+        CKS(dmalloc(s, (void **)&s->d_coef_nat, sizeof(double) * 8 * s->geo.n));
+        CK(cudaMemsetAsync(s->d_coef_nat, 0, sizeof(double) * 8 * s->geo.n, s->stream));
+    }
+    return SS4D_OK;
+}
+
+static ss4d_status ensure_split(ss4d_solver *s, int mixed)
+{
+    const long long cs = s->sp.cs;
+    if (!s->have_split) {
+        double *u3 = nullptr, *p2 = nullptr, *cf = nullptr;
+        CKS(dmalloc(s, (void **)&u3, sizeof(double) * 3 * cs));
+        CKS(dmalloc(s, (void **)&p2, sizeof(double) * 2 * cs));
+        CKS(dmalloc(s, (void **)&cf, sizeof(double) * 20 * cs));
+        CK(cudaMemsetAsync(u3, 0, sizeof(double) * 3 * cs, s->stream));
+        CK(cudaMemsetAsync(p2, 0, sizeof(double) * 2 * cs, s->stream));
+        CK(cudaMemsetAsync(cf, 0, sizeof(double) * 20 * cs, s->stream));
+        s->sb.R[0] = u3;
+        s->sb.R[1] = u3 + cs;
+        s->sb.Bk = u3 + 2 * cs;
+        s->sb.P[0] = p2;
+        s->sb.P[1] = p2 + cs;
+        s->sb.coef[0] = cf;
+        s->sb.coef[1] = cf + 10 * cs;
+        s->sb.partial[0] = s->d_partial;
+        s->sb.partial[1] = s->d_partial + s->cfg.grid;
+        s->have_split = 1;
+    }
+    if (mixed && !s->have_mixed) {
+        float *c32 = nullptr, *d3 = nullptr, *r2 = nullptr;
+        CKS(dmalloc(s, (void **)&c32, sizeof(float) * 16 * cs));
+        CKS(dmalloc(s, (void **)&d3, sizeof(float) * 3 * cs));
+        CKS(dmalloc(s, (void **)&r2, sizeof(float) * 2 * cs));
+        CK(cudaMemsetAsync(c32, 0, sizeof(float) * 16 * cs, s->stream));
+        CK(cudaMemsetAsync(d3, 0, sizeof(float) * 3 * cs, s->stream));
+        CK(cudaMemsetAsync(r2, 0, sizeof(float) * 2 * cs, s->stream));
+        s->sb.coef32[0] = c32;
+        s->sb.coef32[1] = c32 + 8 * cs;
+        s->sb.dR[0] = d3;
+        s->sb.dR[1] = d3 + cs;
+        s->sb.dB = d3 + 2 * cs;
+        s->sb.r32[0] = r2;
+        s->sb.r32[1] = r2 + cs;
+        s->have_mixed = 1;
+        free_graphs(s); // kernel arguments changed
+    }
+    return SS4D_OK;
+}
+
+static ss4d_status check_params(const ss4d_params *p)
+{
+    REQ(p, "params is NULL");
+    REQ(p->h > 0 && isfinite(p->h), "h must be positive");
+    REQ(isfinite(p->tau) && isfinite(p->eps2) && isfinite(p->omega_c) && isfinite(p->gsTol), "non-finite parameter");
+    return SS4D_OK;
+}
+
+static ss4d_status upload_params(ss4d_solver *s, const ss4d_params *p)
+{
+    s->h_params->c = p->tau / (p->h * p->h);
+    s->h_params->omega = p->omega_c;
+    s->h_params->h4 = p->h * p->h * p->h * p->h;
+    s->h_params->tol = p->gsTol;
+    s->h_params->maxit = p->maxNoGSIteration;
+    s->h_params->pad_ = 0;
+    // the host mirror is only rewritten after the previous copy completed:
+    // every solve ends with a stream synchronisation
+    CK(cudaMemcpyAsync(s->d_params, s->h_params, sizeof(DevParams), cudaMemcpyHostToDevice, s->stream));
+    return SS4D_OK;
+}
+
+static ss4d_status read_scalar(ss4d_solver *s, int idx, double *out)
+{
+    CK(cudaMemcpyAsync(s->h_scalar, s->d_scalar + idx, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    *out = s->h_scalar[0];
+    return SS4D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// SOR loop drivers
+
+// reference arithmetic: red, black, residual pass, host test (segmentation4D.c:228-309)
+static ss4d_status sor_reference(ss4d_solver *s, const ss4d_params *p, double *u, const double *prev, CPtrs8 a,
+                                 ss4d_step_stats *stats)
+{
+    const Geo &g = s->geo;
+    const double c = p->tau / (p->h * p->h), h4 = p->h * p->h * p->h * p->h;
+    const long long nb = interior_blocks(g);
+    double R = 0.0, R1 = 0.0;
+    int z = 0;
+    do {
+        z = z + 1;
+        launch_sor_half_ref(g, u, prev, a, c, p->omega_c, 0, s->stream);
+        launch_sor_half_ref(g, u, prev, a, c, p->omega_c, 1, s->stream);
+        launch_sor_resid_ref(g, u, prev, a, c, h4, s->d_partial, s->stream);
+        launch_reduce_sum(s->d_partial, nb, s->d_scalar, s->stream);
+        s->launches += 4;
+        CKS(last_launch());
+        CKS(read_scalar(s, 0, &R));
+        if (z == 1)
+            R1 = R;
+    } while (R > p->gsTol && z < p->maxNoGSIteration);
+    if (stats) {
+        stats->iterations = z;
+        stats->residual = R;
+        stats->first_residual = R1;
+        stats->refinements = 0;
+        stats->status = isfinite(R) ? SS4D_OK : SS4D_ERR_NONFINITE;
+    }
+    return isfinite(R) ? SS4D_OK : SS4D_ERR_NONFINITE;
+}
+
+static ss4d_status build_graph(ss4d_solver *s, int mixed)
+{
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphConditionalHandle h;
+    CK(cudaGraphCreate(&graph, 0));
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        set_err("cudaGraphConditionalHandleCreate: %s", cudaGetErrorString(e));
+        return SS4D_ERR_CUDA;
+    }
+    // the C++ view of this union-holding struct has no default constructor:
+    // build it in zeroed storage, as the C API expects unused bytes zero
+    alignas(cudaGraphNodeParams) unsigned char cp_store[sizeof(cudaGraphNodeParams)];
+    memset(cp_store, 0, sizeof cp_store);
+    cudaGraphNodeParams &cp = *reinterpret_cast<cudaGraphNodeParams *>(cp_store);
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        set_err("cudaGraphAddNode(conditional): %s", cudaGetErrorString(e));
+        return SS4D_ERR_CUDA;
+    }
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(s->cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        set_err("cudaStreamBeginCaptureToGraph: %s", cudaGetErrorString(e));
+        return SS4D_ERR_CUDA;
+    }
+    const unsigned long long hv = (unsigned long long)h;
+    if (!mixed) {
+        launch_sweep64(s->geo, s->sp, s->cfg, 1, s->sb, s->d_params, s->d_state, s->cap);
+        launch_sweep64(s->geo, s->sp, s->cfg, 0, s->sb, s->d_params, s->d_state, s->cap);
+        launch_ctrl64(s->sb, s->cfg.grid, s->d_params, s->d_state, hv, 1, s->cap);
+    } else {
+        launch_refine(s->geo, s->sp, s->cfg, 0, s->sb, s->d_params, s->d_state, s->cap);
+        launch_refine(s->geo, s->sp, s->cfg, 1, s->sb, s->d_params, s->d_state, s->cap);
+        launch_zero_delta(s->sp, s->sb, s->d_state, s->cap);
+        launch_sweep32(s->geo, s->sp, s->cfg, 1, s->sb, s->d_params, s->d_state, 0, s->cap);
+        launch_sweep32(s->geo, s->sp, s->cfg, 0, s->sb, s->d_params, s->d_state, 0, s->cap);
+        launch_ctrl_mixed(s->sb, s->cfg.grid, s->d_params, s->d_state, hv, 1, s->cap);
+    }
+    cudaGraph_t captured = nullptr;
+    e = cudaStreamEndCapture(s->cap, &captured);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        cudaGraphDestroy(graph);
+        set_err("cudaStreamEndCapture: %s", cudaGetErrorString(e));
+        return SS4D_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        cudaGraphDestroy(graph);
+        set_err("cudaGraphInstantiate: %s", cudaGetErrorString(e));
+        return SS4D_ERR_CUDA;
+    }
+    if (mixed) {
+        s->graphmx = graph;
+        s->execmx = exec;
+        s->condmx = hv;
+    } else {
+        s->graph64 = graph;
+        s->exec64 = exec;
+        s->cond64 = hv;
+    }
+    return SS4D_OK;
+}
+
+static ss4d_status finish_stats(ss4d_solver *s, ss4d_step_stats *stats, int mixed)
+{
+    CK(cudaMemcpyAsync(s->h_state, s->d_state, sizeof(LoopState), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    const LoopState &L = *s->h_state;
+    if (stats) {
+        stats->iterations = L.z;
+        stats->residual = L.R;
+        stats->first_residual = L.R_first;
+        stats->refinements = mixed ? L.refinements : 0;
+        stats->status = L.status;
+    }
+    if (L.status != SS4D_OK) {
+        set_err("SOR residual became non-finite at iteration %d", L.z);
+        return (ss4d_status)L.status;
+    }
+    return SS4D_OK;
+}
+
+// the loop on the split buffers; u/prev already packed, coefficients assembled
+static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixed)
+{
+    const Geo &g = s->geo;
+    const Split &sp = s->sp;
+    const SweepCfg &cfg = s->cfg;
+    CKS(upload_params(s, p));
+    if (!mixed) {
+        launch_loop_init(s->d_state, 0, s->stream);
+        timed(s, SS4D_K_SWEEP64, true,
+              [&] { launch_sweep64(g, sp, cfg, 0, s->sb, s->d_params, s->d_state, s->stream); });
+        launch_advance(s->d_state, s->stream);
+        s->launches += 3;
+    } else {
+        const size_t fb = sizeof(float) * sp.cs;
+        CK(cudaMemsetAsync(s->sb.dR[0], 0, fb, s->stream));
+        CK(cudaMemsetAsync(s->sb.dR[1], 0, fb, s->stream));
+        CK(cudaMemsetAsync(s->sb.dB, 0, fb, s->stream));
+        launch_loop_init(s->d_state, 0, s->stream);
+        s->launches += 1;
+    }
+    CKS(last_launch());
+    bool graphed = false;
+    if (s->use_graph && !s->graph_failed && !s->timing) {
+        cudaGraphExec_t ex = mixed ? s->execmx : s->exec64;
+        if (!ex) {
+            if (build_graph(s, mixed) != SS4D_OK)
+                s->graph_failed = 1; // fall back to the host loop from now on
+            ex = mixed ? s->execmx : s->exec64;
+        }
+        if (ex) {
+            CK(cudaGraphLaunch(ex, s->stream));
+            graphed = true;
+        }
+    }
+    if (!graphed) {
+        // host-driven form of the same loop: one small readback per iteration
+        int mode = 0; // mixed form: the mode the controller left for this body
+        for (int guard = 0; guard < 4 * (p->maxNoGSIteration + 4) + 16; ++guard) {
+            if (!mixed) {
+                timed(s, SS4D_K_SWEEP64, true,
+                      [&] { launch_sweep64(g, sp, cfg, 1, s->sb, s->d_params, s->d_state, s->stream); });
+                timed(s, SS4D_K_SWEEP64, true,
+                      [&] { launch_sweep64(g, sp, cfg, 0, s->sb, s->d_params, s->d_state, s->stream); });
+                launch_ctrl64(s->sb, cfg.grid, s->d_params, s->d_state, 0, 0, s->stream);
+                s->launches += 3;
+            } else {
+                // kernels whose mode does not match return at once: only the
+                // ones that do the work are timed
+                timed(s, SS4D_K_REFINE, mode == 0,
+                      [&] { launch_refine(g, sp, cfg, 0, s->sb, s->d_params, s->d_state, s->stream); });
+                timed(s, SS4D_K_REFINE, mode == 0,
+                      [&] { launch_refine(g, sp, cfg, 1, s->sb, s->d_params, s->d_state, s->stream); });
+                launch_zero_delta(sp, s->sb, s->d_state, s->stream);
+                timed(s, SS4D_K_SWEEP32, mode == 2,
+                      [&] { launch_sweep32(g, sp, cfg, 1, s->sb, s->d_params, s->d_state, 0, s->stream); });
+                timed(s, SS4D_K_SWEEP32, mode != 0,
+                      [&] { launch_sweep32(g, sp, cfg, 0, s->sb, s->d_params, s->d_state, 0, s->stream); });
+                launch_ctrl_mixed(s->sb, cfg.grid, s->d_params, s->d_state, 0, 0, s->stream);
+                s->launches += 6;
+            }
+            CKS(last_launch());
+            CK(cudaMemcpyAsync(s->h_state, s->d_state, sizeof(LoopState), cudaMemcpyDeviceToHost, s->stream));
+            CK(cudaStreamSynchronize(s->stream));
+            if (s->h_state->stop)
+                break;
+            mode = s->h_state->mode;
+        }
+    }
+    s->last_graphed = graphed ? 1 : 0;
+    return SS4D_OK;
+}
+
+// count the kernels of a graphed loop after the fact: the controller counts
+// the loop bodies it ran
+static void count_graph_launches(ss4d_solver *s, int mixed)
+{
+    if (!s->last_graphed)
+        return;
+    s->launches += (long long)(mixed ? 6 : 3) * s->h_state->bodies;
+}
+
+extern "C" ss4d_status ss4d_solver_set_timing(ss4d_solver *s, int enable)
+{
+    REQ(s, "solver is NULL");
+    s->timing = enable ? 1 : 0;
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_solver_kernel_time(const ss4d_solver *s, int kind, double *total_ms, long long *launches)
+{
+    REQ(s && total_ms && launches, "NULL argument");
+    REQ(kind >= 0 && kind < SS4D_K_COUNT, "unknown kernel kind");
+    *total_ms = s->ktime[kind];
+    *launches = s->kcount[kind];
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_solver_reset_timing(ss4d_solver *s)
+{
+    REQ(s, "solver is NULL");
+    for (int k = 0; k < SS4D_K_COUNT; ++k) {
+        s->ktime[k] = 0.0;
+        s->kcount[k] = 0;
+    }
+    return SS4D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// balls
+
+static ss4d_status upload_balls(ss4d_solver *s, const ss4d_balls *b, double R, int *have)
+{
+    *have = 0;
+    if (!b || b->n == 0)
+        return SS4D_OK;
+    REQ(b->n > 0 && b->l && b->cx && b->cy && b->cz, "balls arrays are NULL");
+    const Geo &g = s->geo;
+    std::vector<int> first(g.lM, 0), count(g.lM, 0);
+    int prev_l = -1;
+    for (int i = 0; i < b->n; ++i) {
+        const int l = b->l[i];
+        REQ(l >= 1 && l <= g.lM - 2, "ball frame index out of range");
+        REQ(l >= prev_l, "balls must be ordered by frame");
+        if (l != prev_l)
+            first[l] = i;
+        count[l] += 1;
+        prev_l = l;
+        const int k0 = (int)(b->cz[i] - R - 0.5), k1 = (int)(b->cz[i] + R + 0.5);
+        const int j0 = (int)(b->cy[i] - R - 0.5), j1 = (int)(b->cy[i] + R + 0.5);
+        const int i0 = (int)(b->cx[i] - R - 0.5), i1 = (int)(b->cx[i] + R + 0.5);
+        REQ(k0 >= 0 && j0 >= 0 && i0 >= 0 && k1 < g.kM && j1 < g.jM && i1 < g.iM,
+            "a ball's box leaves the array (the reference would read out of bounds)");
+    }
+    if (s->balls_cap < b->n) {
+        if (s->d_bx)
+            cudaFree(s->d_bx), cudaFree(s->d_by), cudaFree(s->d_bz);
+        CKS(dmalloc(s, (void **)&s->d_bx, sizeof(double) * b->n));
+        CKS(dmalloc(s, (void **)&s->d_by, sizeof(double) * b->n));
+        CKS(dmalloc(s, (void **)&s->d_bz, sizeof(double) * b->n));
+        s->balls_cap = b->n;
+    }
+    if (!s->d_frame_first) {
+        CKS(dmalloc(s, (void **)&s->d_frame_first, sizeof(int) * g.lM));
+        CKS(dmalloc(s, (void **)&s->d_frame_count, sizeof(int) * g.lM));
+    }
+    // synchronous copies: the host vectors die with this call
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaMemcpy(s->d_frame_first, first.data(), sizeof(int) * g.lM, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->d_frame_count, count.data(), sizeof(int) * g.lM, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->d_bx, b->cx, sizeof(double) * b->n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->d_by, b->cy, sizeof(double) * b->n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->d_bz, b->cz, sizeof(double) * b->n, cudaMemcpyHostToDevice));
+    *have = 1;
+    return SS4D_OK;
+}
+
+static ss4d_status rescale_impl(ss4d_solver *s, const ss4d_params *p, double *d_img, const double *d_Mmask,
+                                const ss4d_balls *balls)
+{
+    int have = 0;
+    CKS(upload_balls(s, balls, p->ballRadius, &have));
+    if (have) {
+        launch_rescale_balls(s->geo, d_img, s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz,
+                             p->ballRadius, s->stream);
+        s->launches += 1;
+    }
+    if (d_Mmask) {
+        launch_mask_zero(s->geo, d_img, d_Mmask, s->stream);
+        s->launches += 1;
+    }
+    return last_launch();
+}
+
+// ---------------------------------------------------------------------------
+// entry points
+
+extern "C" ss4d_status ss4d_reflect(ss4d_solver *s, double *d_img)
+{
+    REQ(s && d_img, "NULL argument");
+    launch_reflect(s->geo, d_img, s->stream);
+    s->launches += 4;
+    return last_launch();
+}
+
+extern "C" ss4d_status ss4d_presmooth_step(ss4d_solver *s, const ss4d_params *p, double *d_img, double *d_scratch,
+                                           ss4d_step_stats *stats)
+{
+    REQ(s && d_img, "NULL argument");
+    CKS(check_params(p));
+    double *prev = d_scratch;
+    if (!prev) {
+        CKS(ensure_scratch(s));
+        prev = s->d_scratch;
+    }
+    const Geo &g = s->geo;
+    CK(cudaEventRecord(s->ev0, s->stream));
+    CK(cudaMemcpyAsync(prev, d_img, sizeof(double) * g.n, cudaMemcpyDeviceToDevice, s->stream));
+    launch_reflect(g, d_img, s->stream);
+    s->launches += 4;
+    const double c = p->sigma / (p->h * p->h), h4 = p->h * p->h * p->h * p->h;
+    const long long nb = interior_blocks(g);
+    double R = 0.0, R1 = 0.0;
+    int z = 0;
+    do {
+        z = z + 1;
+        launch_presmooth_half(g, d_img, prev, c, p->omega_sigma, 0, s->stream);
+        launch_presmooth_half(g, d_img, prev, c, p->omega_sigma, 1, s->stream);
+        launch_presmooth_resid(g, d_img, prev, c, h4, s->d_partial, s->stream);
+        launch_reduce_sum(s->d_partial, nb, s->d_scalar, s->stream);
+        s->launches += 4;
+        CKS(last_launch());
+        CKS(read_scalar(s, 0, &R));
+        if (z == 1)
+            R1 = R;
+    } while (R > p->gsTol && z < p->maxNoGSIteration_sigma);
+    CK(cudaEventRecord(s->ev1, s->stream));
+    CK(cudaEventSynchronize(s->ev1));
+    if (stats) {
+        memset(stats, 0, sizeof *stats);
+        stats->iterations = z;
+        stats->residual = R;
+        stats->first_residual = R1;
+        cudaEventElapsedTime(&stats->ms, s->ev0, s->ev1);
+        stats->status = isfinite(R) ? SS4D_OK : SS4D_ERR_NONFINITE;
+    }
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_edge_detector(ss4d_solver *s, const ss4d_params *p, double *d_i0, double *d_i0_thr,
+                                          double *d_scratch, double *const d_g[8])
+{
+    REQ(s && d_i0 && d_g, "NULL argument");
+    CKS(check_params(p));
+    REQ(d_i0_thr || p->rho_thr == 0.0, "i0_thr may only be NULL when rho_thr == 0");
+    GPtrs8 go;
+    for (int f = 0; f < 8; ++f) {
+        REQ(d_g[f], "a g array is NULL");
+        go.p[f] = d_g[f];
+    }
+    CKS(ss4d_presmooth_step(s, p, d_i0, d_scratch, nullptr));
+    if (d_i0_thr)
+        CKS(ss4d_presmooth_step(s, p, d_i0_thr, d_scratch, nullptr));
+    launch_gfaces(s->geo, d_i0, d_i0_thr, go, p->h, p->K, p->theta_img, p->rho_thr, s->stream);
+    s->launches += 1;
+    return last_launch();
+}
+
+extern "C" ss4d_status ss4d_gs_coefficients(ss4d_solver *s, const ss4d_params *p, const double *d_u,
+                                            const double *const d_g[8], double *const d_coef[8])
+{
+    REQ(s && d_u && d_coef, "NULL argument");
+    CKS(check_params(p));
+    CPtrs8 gi;
+    GPtrs8 co;
+    for (int f = 0; f < 8; ++f) {
+        gi.p[f] = d_g ? d_g[f] : nullptr;
+        REQ(!d_g || d_g[f], "a g array is NULL");
+        REQ(d_coef[f], "a coefficient array is NULL");
+        co.p[f] = d_coef[f];
+    }
+    launch_coef_ref(s->geo, d_u, gi, d_g ? 1 : 0, co, p->h, p->eps2, s->stream);
+    s->launches += 1;
+    return last_launch();
+}
+
+// solve on the split buffers from natural u/prev; coefficients already in place
+static ss4d_status split_solve(ss4d_solver *s, const ss4d_params *p, double *d_u, const double *d_prev,
+                               ss4d_step_stats *stats)
+{
+    const int mixed = s->arith == SS4D_ARITH_MIXED;
+    timed(s, SS4D_K_PACK, true, [&] { launch_pack(s->geo, s->sp, d_u, d_prev, s->sb, s->stream); });
+    s->launches += 1;
+    CKS(last_launch());
+    CKS(run_split_loop(s, p, mixed));
+    timed(s, SS4D_K_PACK, true, [&] { launch_unpack(s->geo, s->sp, s->sb, s->d_state, d_u, s->stream); });
+    s->launches += 1;
+    CKS(last_launch());
+    ss4d_status st = finish_stats(s, stats, mixed);
+    count_graph_launches(s, mixed);
+    return st;
+}
+
+extern "C" ss4d_status ss4d_sor_solve(ss4d_solver *s, const ss4d_params *p, double *d_u, const double *d_prev_u,
+                                      const double *const d_coef[8], ss4d_step_stats *stats)
+{
+    REQ(s && d_u && d_prev_u && d_coef, "NULL argument");
+    CKS(check_params(p));
+    CPtrs8 a;
+    for (int f = 0; f < 8; ++f) {
+        REQ(d_coef[f], "a coefficient array is NULL");
+        a.p[f] = d_coef[f];
+    }
+    if (stats)
+        memset(stats, 0, sizeof *stats);
+    CK(cudaEventRecord(s->ev0, s->stream));
+    ss4d_status st;
+    if (s->arith == SS4D_ARITH_REFERENCE) {
+        st = sor_reference(s, p, d_u, d_prev_u, a, stats);
+    } else {
+        const int mixed = s->arith == SS4D_ARITH_MIXED;
+        CKS(ensure_split(s, mixed));
+        launch_pack_coef(s->geo, s->sp, a, *p, s->sb, mixed, s->stream);
+        s->launches += 1;
+        CKS(last_launch());
+        st = split_solve(s, p, d_u, d_prev_u, stats);
+    }
+    CK(cudaEventRecord(s->ev1, s->stream));
+    CK(cudaEventSynchronize(s->ev1));
+    if (stats)
+        cudaEventElapsedTime(&stats->ms, s->ev0, s->ev1);
+    return st;
+}
+
+extern "C" ss4d_status ss4d_seg_time_step(ss4d_solver *s, const ss4d_params *p, double *d_u, double *d_prev_u,
+                                          const double *const d_g[8], const double *d_Mmask, const ss4d_balls *balls,
+                                          ss4d_step_stats *stats)
+{
+    REQ(s && d_u && d_g, "NULL argument");
+    CKS(check_params(p));
+    CPtrs8 gi;
+    for (int f = 0; f < 8; ++f) {
+        REQ(d_g[f], "a g array is NULL");
+        gi.p[f] = d_g[f];
+    }
+    if (stats)
+        memset(stats, 0, sizeof *stats);
+    const Geo &g = s->geo;
+    CK(cudaEventRecord(s->ev0, s->stream));
+    ss4d_status st;
+    if (s->arith == SS4D_ARITH_REFERENCE) {
+        double *prev = d_prev_u;
+        if (!prev) {
+            CKS(ensure_scratch(s));
+            prev = s->d_scratch;
+        }
+        CKS(ensure_coef_nat(s));
+        CK(cudaMemcpyAsync(prev, d_u, sizeof(double) * g.n, cudaMemcpyDeviceToDevice, s->stream));
+        GPtrs8 co;
+        CPtrs8 ca;
+        for (int f = 0; f < 8; ++f) {
+            co.p[f] = s->d_coef_nat + (size_t)f * g.n;
+            ca.p[f] = co.p[f];
+        }
+        launch_coef_ref(g, d_u, gi, 1, co, p->h, p->eps2, s->stream);
+        s->launches += 1;
+        CKS(last_launch());
+        st = sor_reference(s, p, d_u, prev, ca, stats);
+    } else {
+        const int mixed = s->arith == SS4D_ARITH_MIXED;
+        CKS(ensure_split(s, mixed));
+        if (d_prev_u)
+            CK(cudaMemcpyAsync(d_prev_u, d_u, sizeof(double) * g.n, cudaMemcpyDeviceToDevice, s->stream));
+        timed(s, SS4D_K_ASSEMBLE, true, [&] { launch_assemble(g, s->sp, d_u, gi, 1, *p, s->sb, mixed, s->stream); });
+        s->launches += 1;
+        CKS(last_launch());
+        st = split_solve(s, p, d_u, d_u, stats);
+    }
+    if (st == SS4D_OK)
+        st = rescale_impl(s, p, d_u, d_Mmask, balls);
+    CK(cudaEventRecord(s->ev1, s->stream));
+    CK(cudaEventSynchronize(s->ev1));
+    if (stats)
+        cudaEventElapsedTime(&stats->ms, s->ev0, s->ev1);
+    return st;
+}
+
+extern "C" ss4d_status ss4d_mcf_time_step(ss4d_solver *s, const ss4d_params *p, int numberOfTimeStep, double *d_u,
+                                          double *d_prev_u, ss4d_step_stats *stats)
+{
+    REQ(s && d_u, "NULL argument");
+    CKS(check_params(p));
+    if (stats)
+        memset(stats, 0, sizeof *stats);
+    const Geo &g = s->geo;
+    const double t = p->tau * numberOfTimeStep;
+    double *prev = d_prev_u;
+    if (!prev) {
+        CKS(ensure_scratch(s));
+        prev = s->d_scratch;
+    }
+    CK(cudaEventRecord(s->ev0, s->stream));
+    CK(cudaMemcpyAsync(prev, d_u, sizeof(double) * g.n, cudaMemcpyDeviceToDevice, s->stream));
+    CPtrs8 none;
+    for (int f = 0; f < 8; ++f)
+        none.p[f] = nullptr;
+    ss4d_status st;
+    if (s->arith == SS4D_ARITH_REFERENCE) {
+        CKS(ensure_coef_nat(s));
+        GPtrs8 co;
+        CPtrs8 ca;
+        for (int f = 0; f < 8; ++f) {
+            co.p[f] = s->d_coef_nat + (size_t)f * g.n;
+            ca.p[f] = co.p[f];
+        }
+        launch_coef_ref(g, d_u, none, 0, co, p->h, p->eps2, s->stream);
+        launch_mcf_field(g, d_u, p->h, t, 1, s->stream);
+        s->launches += 2;
+        CKS(last_launch());
+        st = sor_reference(s, p, d_u, prev, ca, stats);
+    } else {
+        const int mixed = s->arith == SS4D_ARITH_MIXED;
+        CKS(ensure_split(s, mixed));
+        timed(s, SS4D_K_ASSEMBLE, true,
+              [&] { launch_assemble(g, s->sp, d_u, none, 0, *p, s->sb, mixed, s->stream); });
+        launch_mcf_field(g, d_u, p->h, t, 1, s->stream);
+        s->launches += 2;
+        CKS(last_launch());
+        st = split_solve(s, p, d_u, prev, stats);
+    }
+    CK(cudaEventRecord(s->ev1, s->stream));
+    CK(cudaEventSynchronize(s->ev1));
+    if (stats)
+        cudaEventElapsedTime(&stats->ms, s->ev0, s->ev1);
+    return st;
+}
+
+extern "C" ss4d_status ss4d_rescale_to_zero_one(ss4d_solver *s, const ss4d_params *p, double *d_img,
+                                                const double *d_Mmask, const ss4d_balls *balls)
+{
+    REQ(s && p && d_img, "NULL argument");
+    return rescale_impl(s, p, d_img, d_Mmask, balls);
+}
+
+extern "C" ss4d_status ss4d_threshold_mask(ss4d_solver *s, const double *d_u, double level, int normalise,
+                                           uint8_t *d_mask)
+{
+    REQ(s && d_u && d_mask, "NULL argument");
+    if (normalise) {
+        launch_minmax(s->geo, d_u, s->d_partial, level, s->d_scalar, s->stream);
+        launch_threshold(s->geo, d_u, s->d_scalar, level, d_mask, s->stream);
+        s->launches += 3;
+    } else {
+        launch_threshold(s->geo, d_u, nullptr, level, d_mask, s->stream);
+        s->launches += 1;
+    }
+    return last_launch();
+}
+
+extern "C" ss4d_status ss4d_l2norm(ss4d_solver *s, double h, const double *d_a, const double *d_b, double *out)
+{
+    REQ(s && d_a && d_b && out, "NULL argument");
+    const int nblk = 1024;
+    launch_l2(s->geo, d_a, d_b, h * h * h * h, s->d_partial, nblk, s->stream);
+    launch_reduce_sum(s->d_partial, nblk, s->d_scalar, s->stream);
+    s->launches += 2;
+    CKS(last_launch());
+    double v = 0;
+    CKS(read_scalar(s, 0, &v));
+    *out = sqrt(v);
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_mass(ss4d_solver *s, double h, const double *d_a, double *out)
+{
+    REQ(s && d_a && out, "NULL argument");
+    const int nblk = 1024;
+    launch_mass(s->geo, d_a, h * h * h * h, s->d_partial, nblk, s->stream);
+    launch_reduce_sum(s->d_partial, nblk, s->d_scalar, s->stream);
+    s->launches += 2;
+    CKS(last_launch());
+    return read_scalar(s, 0, out);
+}
+
+extern "C" ss4d_status ss4d_mcf_set_boundary_exact(ss4d_solver *s, double h, double t, double *d_u)
+{
+    REQ(s && d_u, "NULL argument");
+    launch_mcf_field(s->geo, d_u, h, t, 1, s->stream);
+    s->launches += 1;
+    return last_launch();
+}
+
+extern "C" ss4d_status ss4d_mcf_exact_solution(ss4d_solver *s, double h, double t, double *d_out)
+{
+    REQ(s && d_out, "NULL argument");
+    launch_mcf_field(s->geo, d_out, h, t, 0, s->stream);
+    s->launches += 1;
+    return last_launch();
+}
+
+// ---------------------------------------------------------------------------
+// memory helpers
+
+extern "C" ss4d_status ss4d_dev_alloc(size_t bytes, void **out)
+{
+    REQ(out, "out is NULL");
+    *out = nullptr;
+    return dmalloc(nullptr, out, bytes ? bytes : 1);
+}
+
+extern "C" ss4d_status ss4d_dev_free(void *p)
+{
+    if (p)
+        CK(cudaFree(p));
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_host_alloc(size_t bytes, void **out)
+{
+    REQ(out, "out is NULL");
+    *out = nullptr;
+    cudaError_t e = cudaMallocHost(out, bytes ? bytes : 1);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_err("cudaMallocHost(%zu) failed: %s", bytes, cudaGetErrorString(e));
+        return SS4D_ERR_ALLOC;
+    }
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_host_free(void *p)
+{
+    if (p)
+        CK(cudaFreeHost(p));
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_copy_to_device(ss4d_solver *s, void *d_dst, const void *h_src, size_t bytes)
+{
+    REQ(s && d_dst && h_src, "NULL argument");
+    CK(cudaMemcpyAsync(d_dst, h_src, bytes, cudaMemcpyHostToDevice, s->stream));
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_copy_to_host(ss4d_solver *s, void *h_dst, const void *d_src, size_t bytes)
+{
+    REQ(s && h_dst && d_src, "NULL argument");
+    CK(cudaMemcpyAsync(h_dst, d_src, bytes, cudaMemcpyDeviceToHost, s->stream));
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_copy_device(ss4d_solver *s, void *d_dst, const void *d_src, size_t bytes)
+{
+    REQ(s && d_dst && d_src, "NULL argument");
+    CK(cudaMemcpyAsync(d_dst, d_src, bytes, cudaMemcpyDeviceToDevice, s->stream));
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_synchronize(ss4d_solver *s)
+{
+    REQ(s, "solver is NULL");
+    CK(cudaStreamSynchronize(s->stream));
+    return SS4D_OK;
+}

@@ -1,0 +1,128 @@
+// ss4d_common.cuh — geometry, launch helpers and reductions shared by the
+// solver's kernels.  Device code only uses what is declared here plus the
+// public ss4d.h types.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/ss4d.h"
+
+namespace ss4d {
+
+// ---------------------------------------------------------------------------
+// Natural (reference) layout: ((l*kM + k)*jM + j)*iM + i, one ghost per side.
+struct Geo {
+    int iM, jM, kM, lM;   // padded extents
+    int nx, ny, nz, nt;   // interior extents
+    long long sy, sz, sw; // strides of j, k, l (i stride is 1)
+    long long n;          // padded voxel count
+    long long nint;       // interior voxel count
+};
+
+inline Geo make_geo(const ss4d_dims &d)
+{
+    Geo g;
+    g.iM = d.iMax; g.jM = d.jMax; g.kM = d.kMax; g.lM = d.lMax;
+    g.nx = g.iM - 2; g.ny = g.jM - 2; g.nz = g.kM - 2; g.nt = g.lM - 2;
+    g.sy = g.iM;
+    g.sz = (long long)g.iM * g.jM;
+    g.sw = g.sz * g.kM;
+    g.n = g.sw * g.lM;
+    g.nint = (long long)g.nx * g.ny * g.nz * g.nt;
+    return g;
+}
+
+__host__ __device__ inline long long nat_index(const Geo &g, int i, int j, int k, int l)
+{
+    return (((long long)l * g.kM + k) * g.jM + j) * g.iM + i;
+}
+
+// ---------------------------------------------------------------------------
+// Colour-split layout used by the fast forms.  Voxel (i,j,k,l) of colour
+// c = (i+j+k+l)&1 lives in colour array c at row (l*kM + k)*jM + j and
+// column xs = ((i+1)>>1) + A - 1.  In a row, the interior voxels of either
+// colour occupy columns A .. A + nxh - 1 (so interior data starts on an
+// aligned boundary), the x-ghosts sit at A-1 and A+nxh.  For a target voxel
+// of the row's phase p = (c+j+k+l)&1 at column xs, its x-neighbours (other
+// colour) are at xs-p (i-1) and xs-p+1 (i+1); its j/k/l neighbours are in
+// the neighbouring rows at the same column xs.
+struct Split {
+    int A;          // first interior column
+    int Hs;         // row pitch in elements (multiple of 8)
+    int nxh;        // (nx+1)/2: interior columns per row (upper bound)
+    long long rows; // jM*kM*lM
+    long long cs;   // elements per colour array (rows*Hs)
+};
+
+inline Split make_split(const Geo &g)
+{
+    Split s;
+    s.A = 8;
+    s.nxh = (g.nx + 1) / 2;
+    int need = s.A + s.nxh + 1;
+    s.Hs = (need + 7) & ~7;
+    s.rows = (long long)g.jM * g.kM * g.lM;
+    s.cs = s.rows * s.Hs;
+    return s;
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic block reduction of one double (any blockDim multiple of 32,
+// up to 1024).  Returns the block total in thread 0.
+template <typename T>
+__device__ inline T warp_sum(T v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <typename T>
+__device__ inline T block_sum(T v)
+{
+    __shared__ T red_smem[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0)
+        red_smem[wid] = v;
+    __syncthreads();
+    T t = 0;
+    if (wid == 0) {
+        t = lane < nw ? red_smem[lane] : T(0);
+        t = warp_sum(t);
+    }
+    return t;
+}
+
+__device__ inline double block_min(double v)
+{
+    __shared__ double mn_smem[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v = fmin(v, __shfl_down_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if (lane == 0)
+        mn_smem[wid] = v;
+    __syncthreads();
+    double t = 1e308;
+    if (wid == 0) {
+        t = lane < nw ? mn_smem[lane] : 1e308;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            t = fmin(t, __shfl_down_sync(0xffffffffu, t, o));
+    }
+    return t;
+}
+
+__device__ inline double block_max(double v)
+{
+    return -block_min(-v);
+}
+
+} // namespace ss4d

@@ -1,0 +1,126 @@
+// ss4d_kernels.cuh — kernel-side declarations shared by the kernel
+// translation units and the host orchestration (ss4d_api.cu).
+#pragma once
+
+#include "ss4d_common.cuh"
+
+namespace ss4d {
+
+struct GPtrs8 {
+    double *p[8];
+};
+struct CPtrs8 {
+    const double *p[8];
+};
+
+// ---- natural-layout, reference-order kernels (ss4d_kernels_ref.cu) -------
+long long interior_blocks(const Geo &g);
+void launch_reflect(const Geo &g, double *u, cudaStream_t st);
+void launch_presmooth_half(const Geo &g, double *v, const double *prev, double c, double omega, int colour,
+                           cudaStream_t st);
+void launch_presmooth_resid(const Geo &g, const double *v, const double *prev, double c, double h4, double *partial,
+                            cudaStream_t st);
+void launch_gfaces(const Geo &g, const double *i0, const double *ithr, GPtrs8 gout, double h, double K, double theta,
+                   double rho, cudaStream_t st);
+void launch_coef_ref(const Geo &g, const double *u, CPtrs8 gin, int has_g, GPtrs8 coef, double h, double eps2,
+                     cudaStream_t st);
+void launch_sor_half_ref(const Geo &g, double *u, const double *prev, CPtrs8 a, double c, double omega, int colour,
+                         cudaStream_t st);
+void launch_sor_resid_ref(const Geo &g, const double *u, const double *prev, CPtrs8 a, double c, double h4,
+                          double *partial, cudaStream_t st);
+void launch_reduce_sum(const double *partial, long long n, double *out, cudaStream_t st);
+void launch_l2(const Geo &g, const double *a, const double *b, double h4, double *partial, int nblk, cudaStream_t st);
+void launch_mass(const Geo &g, const double *a, double h4, double *partial, int nblk, cudaStream_t st);
+void launch_mcf_field(const Geo &g, double *u, double h, double t, int ghosts_only, cudaStream_t st);
+void launch_rescale_balls(const Geo &g, double *v, const int *frame_first, const int *frame_count, const double *bx,
+                          const double *by, const double *bz, double R, cudaStream_t st);
+void launch_mask_zero(const Geo &g, double *v, const double *Mmask, cudaStream_t st);
+void launch_minmax(const Geo &g, const double *u, double *partial, double level, double *out3, cudaStream_t st);
+void launch_threshold(const Geo &g, const double *u, const double *level_dev, double level, uint8_t *mask,
+                      cudaStream_t st);
+
+// ---- colour-split fast forms (ss4d_kernels_fast.cu) ------------------------
+
+// Device-resident loop state of one SOR solve.  The controller kernel is its
+// only writer during the loop; sweeps read it to pick their buffers.
+struct LoopState {
+    int z;           // current iteration (fast FP64 form); inner sweeps (mixed)
+    int stop;        // 1 once the loop has ended
+    int status;      // ss4d_status
+    int mode;        // mixed form: 0 refine, 1 start round, 2 inner sweep
+    int refinements; // mixed form: FP64 residual/refinement passes done
+    int round_z;     // mixed form: sweeps in the current round
+    int dsrc;        // mixed form: ping-pong index of the current red correction
+    int final_red;   // red buffer holding the result once the loop stopped
+    int bodies;      // loop bodies the controller has run
+    int pad_;
+    double R;        // last FP64 residual (sum r^2 h^4)
+    double R_first;  // FP64 residual after iteration 1 (fast) / initial (mixed)
+    double Rd;       // mixed form: last FP32 correction residual
+    double target;   // mixed form: round target for Rd
+};
+
+// Scalars the fast kernels read from device memory so that one captured
+// graph serves every call of a solver.
+struct DevParams {
+    double c;        // tau / h^2
+    double omega;    // omega_c
+    double h4;       // h^4
+    double tol;      // gsTol
+    int maxit;       // maxNoGSIteration
+    int pad_;
+};
+
+// Buffers of the colour-split FP64 form.
+struct SplitBufs {
+    double *R[2];       // red u, ping-pong (all cells incl. ghosts)
+    double *Bk;         // black u (all cells incl. ghosts)
+    double *P[2];       // prev (per colour)
+    double *coef[2];    // per colour: 10 arrays of cs: c*a_{e,w,s,n,b,t,bw,fw}, diag, omega/diag
+    float *coef32[2];   // per colour: 8 arrays of cs: c*a_f in FP32 (mixed form)
+    float *dR[2];       // mixed: red correction, ping-pong
+    float *dB;          // mixed: black correction
+    float *r32[2];      // mixed: FP64 residual rounded to FP32, per colour
+    double *partial[2]; // per-block residual partials of the red [0] / black [1] kernels
+};
+
+struct SweepCfg {
+    int threads;   // threads per block (256)
+    int XT;        // threads along x in a tile (power of two)
+    int TJ;        // rows (j) per tile
+    int KB;        // k-block depth of the tile order
+    int nXC;       // x chunks per row
+    int nJG;       // j groups
+    int nKB;       // k blocks
+    long long ntiles;
+    int grid;      // persistent grid (blocks)
+};
+
+SweepCfg make_sweep_cfg(const Geo &g, const Split &s, int sm_count, int kb);
+
+void launch_assemble(const Geo &g, const Split &s, const double *u, CPtrs8 gin, int has_g, const ss4d_params &p,
+                     SplitBufs b, int want32, cudaStream_t st);
+void launch_pack(const Geo &g, const Split &s, const double *u, const double *prev, SplitBufs b, cudaStream_t st);
+void launch_pack_coef(const Geo &g, const Split &s, CPtrs8 a, const ss4d_params &p, SplitBufs b, int want32,
+                      cudaStream_t st);
+void launch_unpack(const Geo &g, const Split &s, SplitBufs b, const LoopState *state, double *u, cudaStream_t st);
+void launch_loop_init(LoopState *state, int mode, cudaStream_t st);
+void launch_sweep64(const Geo &g, const Split &s, const SweepCfg &cfg, int colour, SplitBufs b, const DevParams *dp,
+                    LoopState *state, cudaStream_t st);
+void launch_advance(LoopState *state, cudaStream_t st);
+void launch_ctrl64(SplitBufs b, int nparts, const DevParams *dp, LoopState *state, unsigned long long cond_handle,
+                   int use_cond, cudaStream_t st);
+
+// mixed precision
+void launch_refine(const Geo &g, const Split &s, const SweepCfg &cfg, int colour, SplitBufs b, const DevParams *dp,
+                   LoopState *state, cudaStream_t st);
+void launch_zero_delta(const Split &s, SplitBufs b, LoopState *state, cudaStream_t st);
+void launch_sweep32(const Geo &g, const Split &s, const SweepCfg &cfg, int colour, SplitBufs b, const DevParams *dp,
+                    LoopState *state, int start_mode, cudaStream_t st);
+void launch_ctrl_mixed(SplitBufs b, int nparts, const DevParams *dp, LoopState *state, unsigned long long cond_handle,
+                       int use_cond, cudaStream_t st);
+
+int max_blocks_sweep64();
+int max_blocks_sweep32();
+
+} // namespace ss4d

@@ -1,0 +1,657 @@
+// ss4d_kernels_fast.cu — colour-split red-black SOR forms.
+//
+// Layout: every array is split by colour c = (i+j+k+l)&1 into two arrays of
+// rows (l,k,j) x Hs columns (see Split in ss4d_common.cuh), so a half-sweep
+// streams only the coefficients of its own colour and every warp load is a
+// contiguous run.  The coefficient arrays of a colour hold, per voxel,
+// c*a_f for the 8 faces (+x,-x,+y,-y,+z,-z,+w,-w = e,w,n,s,t,b,fw,bw), the
+// diagonal 1 + c*sum a_f and omega/diagonal (c = tau/h^2), so one update is
+//     r = diag*u - sum (c a_f) u_f - prev,   u <- u - (omega/diag) r
+// which is the reference's u + omega (GS - u) (segmentation4D.c:237-256)
+// rearranged, and r is the reference's residual of that voxel
+// (segmentation4D.c:294-307) before the update.
+//
+// Residual without a third pass: in iteration z the red voxels' residual at
+// the end of z is exactly the pre-update residual the red sweep of z+1
+// computes (same red values, same black neighbours), and a black voxel's
+// residual after its own update is (1-omega) times its pre-update residual
+// (its neighbours are red and do not move during the black sweep).  The red
+// sweep of z+1 writes into the other buffer of a red ping-pong pair, so when
+// the test on the residual of z stops the loop, the red values of z are
+// still there.  The loop controller is a one-block kernel that sums the
+// per-block partials in a fixed order (deterministic) and, inside a CUDA
+// graph, sets the while-node condition.
+#include "ss4d_kernels.cuh"
+
+namespace ss4d {
+
+// ---------------------------------------------------------------------------
+// helpers
+
+__device__ __forceinline__ double ld_stream(const double *p)
+{
+    return __ldcs(p);
+}
+__device__ __forceinline__ float ld_stream(const float *p)
+{
+    return __ldcs(p);
+}
+
+template <typename T>
+__device__ __forceinline__ T ld_ro(const T *p)
+{
+    return __ldg(p);
+}
+
+// Select one of a pair held in a by-value kernel parameter without a runtime
+// array index (which would copy the parameter struct to local memory).
+template <typename T>
+__device__ __forceinline__ T *pick(T *const (&a)[2], int i)
+{
+    return i ? a[1] : a[0];
+}
+
+struct TileCoord {
+    int j, k, l, xi;
+    bool ok;
+};
+
+// Tile order: x chunk fastest, then j group, then k inside a k block, then
+// frame l, then k block.  Consecutive tiles (which a persistent grid works on
+// at the same time) thus cover a few k planes of all frames, so the
+// neighbouring-plane reads of the other colour hit in L2.
+__device__ __forceinline__ TileCoord tile_coord(const Geo &g, const SweepCfg &cfg, long long t, int tx, int ty)
+{
+    TileCoord c;
+    long long r = t;
+    const int xc = (int)(r % cfg.nXC);
+    r /= cfg.nXC;
+    const int jg = (int)(r % cfg.nJG);
+    r /= cfg.nJG;
+    const int kin = (int)(r % cfg.KB);
+    r /= cfg.KB;
+    const int lt = (int)(r % g.nt);
+    const int kb = (int)(r / g.nt);
+    c.k = 1 + kb * cfg.KB + kin;
+    c.l = 1 + lt;
+    c.j = 1 + jg * cfg.TJ + ty;
+    c.xi = xc * cfg.XT + tx;
+    c.ok = c.k <= g.nz && c.j <= g.ny;
+    return c;
+}
+
+// ---------------------------------------------------------------------------
+// assembly: the reference's _gs_coefficients_ per voxel, written to the split
+// coefficient arrays (FP64, and FP32 copies of c*a_f for the mixed form).
+
+__device__ __forceinline__ double face_sq_fast(const double *v, long long c, long long nb, const long long st[4],
+                                               int d, double ih, double iq)
+{
+    double s = 0.0;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        double comp;
+        if (a == d)
+            comp = (v[nb] - v[c]) * ih;
+        else
+            comp = ((v[nb + st[a]] + v[c + st[a]]) - (v[nb - st[a]] + v[c - st[a]])) * iq;
+        s = fma(comp, comp, s);
+    }
+    return s;
+}
+
+__global__ void __launch_bounds__(256) k_assemble(Geo g, Split sp, const double *__restrict__ u, CPtrs8 gin,
+                                                  int has_g, double h, double eps2, double c, double omega, SplitBufs b,
+                                                  int want32)
+{
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = 1 + blockIdx.z % g.nz, l = 1 + blockIdx.z / g.nz;
+    if (i > g.nx || j > g.ny)
+        return;
+    const long long o = nat_index(g, i, j, k, l);
+    const long long st[4] = {1, g.sy, g.sz, g.sw};
+    const double ih = 1.0 / h, iq = 1.0 / (4.0 * h);
+    double nf[8];
+    double sum = 0.0;
+#pragma unroll
+    for (int f = 0; f < 8; ++f) {
+        const int d = f >> 1;
+        const long long nb = (f & 1) ? o - st[d] : o + st[d];
+        nf[f] = sqrt(face_sq_fast(u, o, nb, st, d, ih, iq) + eps2);
+        sum += nf[f];
+    }
+    const double mean = sum * 0.125;
+    const double vc = sqrt(fma(mean, mean, eps2));
+    const int col = (i + j + k + l) & 1;
+    const long long s = (((long long)l * g.kM + k) * g.jM + j) * sp.Hs + ((i + 1) >> 1) + sp.A - 1;
+    double *cf = pick(b.coef, col);
+    float *cf32 = pick(b.coef32, col);
+    double diag = 1.0;
+#pragma unroll
+    for (int f = 0; f < 8; ++f) {
+        const double a = has_g ? vc * __ldg(gin.p[f] + o) / nf[f] : vc / nf[f];
+        const double ac = c * a;
+        diag += ac;
+        __stcs(cf + f * sp.cs + s, ac);
+        if (want32)
+            __stcs(cf32 + f * sp.cs + s, (float)ac);
+    }
+    __stcs(cf + 8 * sp.cs + s, diag);
+    __stcs(cf + 9 * sp.cs + s, omega / diag);
+}
+
+// given natural coefficient arrays e..bw (the reference's layout) -> split
+// FP64 c*a_f, diagonal, omega/diagonal (+ FP32 c*a_f)
+__global__ void __launch_bounds__(256) k_pack_coef(Geo g, Split sp, CPtrs8 a, double c, double omega, SplitBufs b,
+                                                   int want32)
+{
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = 1 + blockIdx.z % g.nz, l = 1 + blockIdx.z / g.nz;
+    if (i > g.nx || j > g.ny)
+        return;
+    const long long o = nat_index(g, i, j, k, l);
+    const int col = (i + j + k + l) & 1;
+    const long long s = (((long long)l * g.kM + k) * g.jM + j) * sp.Hs + ((i + 1) >> 1) + sp.A - 1;
+    double *cf = pick(b.coef, col);
+    float *cf32 = pick(b.coef32, col);
+    double diag = 1.0;
+#pragma unroll
+    for (int f = 0; f < 8; ++f) {
+        const double ac = c * a.p[f][o];
+        diag += ac;
+        cf[f * sp.cs + s] = ac;
+        if (want32)
+            cf32[f * sp.cs + s] = (float)ac;
+    }
+    cf[8 * sp.cs + s] = diag;
+    cf[9 * sp.cs + s] = omega / diag;
+}
+
+// natural -> split copies of u (both red buffers and black, ghosts
+// included) and of prev (interior of both colours)
+__global__ void k_pack(Geo g, Split sp, const double *__restrict__ u, const double *__restrict__ prev, SplitBufs b)
+{
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < g.n; o += (long long)gridDim.x * blockDim.x) {
+        long long r = o;
+        const int i = (int)(r % g.iM);
+        r /= g.iM;
+        const int j = (int)(r % g.jM);
+        r /= g.jM;
+        const int k = (int)(r % g.kM);
+        const int l = (int)(r / g.kM);
+        const int col = (i + j + k + l) & 1;
+        const long long s = (((long long)l * g.kM + k) * g.jM + j) * sp.Hs + ((i + 1) >> 1) + sp.A - 1;
+        const double v = u[o];
+        if (col == 0) {
+            b.R[0][s] = v;
+            b.R[1][s] = v;
+        } else {
+            b.Bk[s] = v;
+        }
+        pick(b.P, col)[s] = prev[o];
+    }
+}
+
+// split -> natural, interior voxels only (the ghosts of u never change)
+__global__ void k_unpack(Geo g, Split sp, SplitBufs b, const LoopState *__restrict__ st, double *u)
+{
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = 1 + blockIdx.z % g.nz, l = 1 + blockIdx.z / g.nz;
+    if (i > g.nx || j > g.ny)
+        return;
+    const int col = (i + j + k + l) & 1;
+    const long long s = (((long long)l * g.kM + k) * g.jM + j) * sp.Hs + ((i + 1) >> 1) + sp.A - 1;
+    const int fr = st->final_red;
+    u[nat_index(g, i, j, k, l)] = col == 0 ? pick(b.R, fr)[s] : b.Bk[s];
+}
+
+__global__ void k_loop_init(LoopState *st, int mode)
+{
+    st->z = 0;
+    st->stop = 0;
+    st->status = 0;
+    st->mode = mode;
+    st->refinements = 0;
+    st->round_z = 0;
+    st->dsrc = 0;
+    st->final_red = 0;
+    st->bodies = 0;
+    st->pad_ = 0;
+    st->R = 0.0;
+    st->R_first = 0.0;
+    st->Rd = 0.0;
+    st->target = 0.0;
+}
+
+__global__ void k_advance(LoopState *st)
+{
+    st->z = 1;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 half-sweep with fused residual
+
+template <int COL>
+__global__ void __launch_bounds__(256) k_sweep64(Geo g, Split sp, SweepCfg cfg, SplitBufs b,
+                                                 const DevParams *__restrict__ dp, const LoopState *__restrict__ st)
+{
+    const int z = st->z;
+    const double *src;
+    double *dst;
+    const double *__restrict__ oth;
+    if (COL == 0) {
+        src = pick(b.R, z & 1);
+        dst = pick(b.R, (z + 1) & 1);
+        oth = b.Bk;
+    } else {
+        src = b.Bk;
+        dst = b.Bk;
+        oth = pick(b.R, z & 1);
+    }
+    const double *__restrict__ cf = b.coef[COL];
+    const double *__restrict__ pv = b.P[COL];
+    const long long cs = sp.cs;
+    const long long Hy = sp.Hs, Hz = Hy * g.jM, Hw = Hz * g.kM;
+    const int tx = threadIdx.x & (cfg.XT - 1), ty = threadIdx.x / cfg.XT;
+    double acc = 0.0;
+    for (long long t = blockIdx.x; t < cfg.ntiles; t += gridDim.x) {
+        const TileCoord tc = tile_coord(g, cfg, t, tx, ty);
+        if (!tc.ok)
+            continue;
+        const int p = (COL + tc.j + tc.k + tc.l) & 1;
+        const int i = 2 * tc.xi + 2 - p;
+        if (i > g.nx)
+            continue;
+        const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * Hy + tc.xi + sp.A;
+        const double u0 = src[s];
+        double S = ld_stream(cf + s) * ld_ro(oth + s - p + 1);
+        S = fma(ld_stream(cf + cs + s), ld_ro(oth + s - p), S);
+        S = fma(ld_stream(cf + 2 * cs + s), ld_ro(oth + s + Hy), S);
+        S = fma(ld_stream(cf + 3 * cs + s), ld_ro(oth + s - Hy), S);
+        S = fma(ld_stream(cf + 4 * cs + s), ld_ro(oth + s + Hz), S);
+        S = fma(ld_stream(cf + 5 * cs + s), ld_ro(oth + s - Hz), S);
+        S = fma(ld_stream(cf + 6 * cs + s), ld_ro(oth + s + Hw), S);
+        S = fma(ld_stream(cf + 7 * cs + s), ld_ro(oth + s - Hw), S);
+        const double diag = ld_stream(cf + 8 * cs + s);
+        const double winv = ld_stream(cf + 9 * cs + s);
+        const double r = fma(diag, u0, -(S + ld_stream(pv + s)));
+        acc = fma(r, r, acc);
+        dst[s] = fma(-winv, r, u0);
+    }
+    acc = block_sum(acc);
+    if (threadIdx.x == 0)
+        b.partial[COL][blockIdx.x] = acc;
+}
+
+// sums the partials of both colours in a fixed order and decides
+__global__ void k_ctrl64(SplitBufs b, int nparts, const DevParams *__restrict__ dp, LoopState *st,
+                         cudaGraphConditionalHandle h, int use_cond)
+{
+    double a = 0.0, c = 0.0;
+    for (int t = threadIdx.x; t < nparts; t += blockDim.x) {
+        a += b.partial[0][t];
+        c += b.partial[1][t];
+    }
+    a = block_sum(a);
+    c = block_sum(c);
+    if (threadIdx.x == 0) {
+        const double om1 = 1.0 - dp->omega;
+        const double R = (a + om1 * om1 * c) * dp->h4;
+        const int z = st->z;
+        st->bodies += 1;
+        if (z == 1)
+            st->R_first = R;
+        st->R = R;
+        const bool fin = isfinite(R);
+        const bool stop = !fin || !(R > dp->tol) || z >= dp->maxit;
+        if (!fin)
+            st->status = SS4D_ERR_NONFINITE;
+        if (stop) {
+            st->stop = 1;
+            st->final_red = z & 1; // red buffer holding the values of iteration z
+        } else {
+            st->z = z + 1;
+        }
+        if (use_cond)
+            cudaGraphSetConditional(h, stop ? 0u : 1u);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// mixed precision: FP64 refinement passes + FP32 sweeps on the correction
+// equation A d = r.  Modes (LoopState::mode): 0 refine, 1 start a round
+// (zero d, first red sweep), 2 inner iteration (black sweep + next red sweep).
+
+// u <- u + d on the target colour, residual of the refined state, r32 = r
+template <int COL>
+__global__ void __launch_bounds__(256) k_refine(Geo g, Split sp, SweepCfg cfg, SplitBufs b,
+                                                const DevParams *__restrict__ dp, const LoopState *__restrict__ st)
+{
+    if (st->mode != 0)
+        return;
+    const int ds = st->dsrc;
+    double *own = COL == 0 ? b.R[0] : b.Bk;
+    const float *__restrict__ down = COL == 0 ? pick(b.dR, ds) : b.dB;
+    const double *__restrict__ oth = COL == 0 ? b.Bk : b.R[0];
+    const float *__restrict__ doth = b.dB; // only used for COL == 0
+    const double *__restrict__ cf = b.coef[COL];
+    const double *__restrict__ pv = b.P[COL];
+    float *__restrict__ rr = b.r32[COL];
+    const long long cs = sp.cs;
+    const long long Hy = sp.Hs, Hz = Hy * g.jM, Hw = Hz * g.kM;
+    const int tx = threadIdx.x & (cfg.XT - 1), ty = threadIdx.x / cfg.XT;
+    double acc = 0.0;
+    for (long long t = blockIdx.x; t < cfg.ntiles; t += gridDim.x) {
+        const TileCoord tc = tile_coord(g, cfg, t, tx, ty);
+        if (!tc.ok)
+            continue;
+        const int p = (COL + tc.j + tc.k + tc.l) & 1;
+        const int i = 2 * tc.xi + 2 - p;
+        if (i > g.nx)
+            continue;
+        const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * Hy + tc.xi + sp.A;
+        const long long nb[8] = {s - p + 1, s - p, s + Hy, s - Hy, s + Hz, s - Hz, s + Hw, s - Hw};
+        const double u0 = own[s] + (double)down[s];
+        double S = 0.0;
+#pragma unroll
+        for (int f = 0; f < 8; ++f) {
+            double v = oth[nb[f]];
+            if (COL == 0)
+                v += (double)doth[nb[f]];
+            S = fma(ld_stream(cf + f * cs + s), v, S);
+        }
+        const double diag = ld_stream(cf + 8 * cs + s);
+        const double r = fma(diag, u0, -(S + ld_stream(pv + s)));
+        acc = fma(r, r, acc);
+        own[s] = u0;
+        rr[s] = (float)r;
+    }
+    acc = block_sum(acc);
+    if (threadIdx.x == 0)
+        b.partial[COL][blockIdx.x] = acc;
+}
+
+// clears the corrections at the start of a round (ghosts stay zero)
+__global__ void k_zero_delta(Split sp, SplitBufs b, const LoopState *__restrict__ st)
+{
+    if (st->mode != 1)
+        return;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < sp.cs; t += (long long)gridDim.x * blockDim.x) {
+        b.dR[0][t] = 0.f;
+        b.dR[1][t] = 0.f;
+        b.dB[t] = 0.f;
+    }
+}
+
+template <int COL>
+__global__ void __launch_bounds__(256) k_sweep32(Geo g, Split sp, SweepCfg cfg, SplitBufs b,
+                                                 const DevParams *__restrict__ dp, const LoopState *__restrict__ st)
+{
+    const int mode = st->mode;
+    if (COL == 0 ? (mode == 0) : (mode != 2))
+        return;
+    const int ds = st->dsrc;
+    const float *src;
+    float *dst;
+    const float *__restrict__ oth;
+    if (COL == 0) {
+        src = pick(b.dR, ds);
+        dst = pick(b.dR, ds ^ 1);
+        oth = b.dB;
+    } else {
+        src = b.dB;
+        dst = b.dB;
+        oth = pick(b.dR, ds);
+    }
+    const float *__restrict__ cf = b.coef32[COL];
+    const float *__restrict__ rhs = b.r32[COL];
+    const float omega = (float)dp->omega;
+    const long long cs = sp.cs;
+    const long long Hy = sp.Hs, Hz = Hy * g.jM, Hw = Hz * g.kM;
+    const int tx = threadIdx.x & (cfg.XT - 1), ty = threadIdx.x / cfg.XT;
+    float acc = 0.f;
+    for (long long t = blockIdx.x; t < cfg.ntiles; t += gridDim.x) {
+        const TileCoord tc = tile_coord(g, cfg, t, tx, ty);
+        if (!tc.ok)
+            continue;
+        const int p = (COL + tc.j + tc.k + tc.l) & 1;
+        const int i = 2 * tc.xi + 2 - p;
+        if (i > g.nx)
+            continue;
+        const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * Hy + tc.xi + sp.A;
+        const float u0 = src[s];
+        const float a0 = ld_stream(cf + s), a1 = ld_stream(cf + cs + s), a2 = ld_stream(cf + 2 * cs + s),
+                    a3 = ld_stream(cf + 3 * cs + s), a4 = ld_stream(cf + 4 * cs + s), a5 = ld_stream(cf + 5 * cs + s),
+                    a6 = ld_stream(cf + 6 * cs + s), a7 = ld_stream(cf + 7 * cs + s);
+        float S = a0 * ld_ro(oth + s - p + 1);
+        S = fmaf(a1, ld_ro(oth + s - p), S);
+        S = fmaf(a2, ld_ro(oth + s + Hy), S);
+        S = fmaf(a3, ld_ro(oth + s - Hy), S);
+        S = fmaf(a4, ld_ro(oth + s + Hz), S);
+        S = fmaf(a5, ld_ro(oth + s - Hz), S);
+        S = fmaf(a6, ld_ro(oth + s + Hw), S);
+        S = fmaf(a7, ld_ro(oth + s - Hw), S);
+        const float diag = 1.f + (((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7)));
+        const float r = fmaf(diag, u0, -(S + ld_stream(rhs + s)));
+        acc = fmaf(r, r, acc);
+        dst[s] = fmaf(-omega / diag, r, u0);
+    }
+    const double tot = block_sum((double)acc);
+    if (threadIdx.x == 0)
+        b.partial[COL][blockIdx.x] = tot;
+}
+
+__global__ void k_ctrl_mixed(SplitBufs b, int nparts, const DevParams *__restrict__ dp, LoopState *st,
+                             cudaGraphConditionalHandle h, int use_cond)
+{
+    const int mode = st->mode;
+    double a = 0.0, c = 0.0;
+    if (mode != 1) {
+        for (int t = threadIdx.x; t < nparts; t += blockDim.x) {
+            a += b.partial[0][t];
+            if (mode == 0 || mode == 2)
+                c += b.partial[1][t];
+        }
+    }
+    a = block_sum(a);
+    c = block_sum(c);
+    if (threadIdx.x != 0)
+        return;
+    st->bodies += 1;
+    bool stop = false;
+    if (mode == 0) {
+        const double R = (a + c) * dp->h4;
+        if (st->refinements == 0)
+            st->R_first = R;
+        st->refinements += 1;
+        st->R = R;
+        const bool fin = isfinite(R);
+        if (!fin)
+            st->status = SS4D_ERR_NONFINITE;
+        if (!fin || !(R > dp->tol) || st->z >= dp->maxit) {
+            stop = true;
+        } else {
+            st->mode = 1;
+            // aim the round at the tolerance, but not below what FP32
+            // corrections can resolve relative to the current residual
+            st->target = fmax(0.5 * dp->tol, 1e-11 * R);
+        }
+    } else if (mode == 1) {
+        st->mode = 2;
+        st->dsrc ^= 1;
+        st->round_z = 0;
+    } else {
+        const double om1 = 1.0 - dp->omega;
+        const double Rd = (a + om1 * om1 * c) * dp->h4;
+        st->Rd = Rd;
+        st->z += 1;
+        st->round_z += 1;
+        if (!isfinite(Rd) || !(Rd > st->target) || st->z >= dp->maxit) {
+            st->mode = 0; // refine with the red correction of this iteration
+        } else {
+            st->dsrc ^= 1;
+        }
+    }
+    if (stop) {
+        st->stop = 1;
+        st->final_red = 0;
+    }
+    if (use_cond)
+        cudaGraphSetConditional(h, stop ? 0u : 1u);
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+
+static int pow2_at_least(int v)
+{
+    int p = 1;
+    while (p < v)
+        p <<= 1;
+    return p;
+}
+
+int max_blocks_sweep64()
+{
+    int a = 0, b = 0, c = 0, d = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_sweep64<0>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_sweep64<1>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_refine<0>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d, k_refine<1>, 256, 0);
+    int m = a < b ? a : b;
+    m = m < c ? m : c;
+    m = m < d ? m : d;
+    return m > 0 ? m : 1;
+}
+
+int max_blocks_sweep32()
+{
+    int a = 0, b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_sweep32<0>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_sweep32<1>, 256, 0);
+    int m = a < b ? a : b;
+    return m > 0 ? m : 1;
+}
+
+SweepCfg make_sweep_cfg(const Geo &g, const Split &s, int sm_count, int kb)
+{
+    SweepCfg c;
+    c.threads = 256;
+    c.XT = pow2_at_least(s.nxh);
+    if (c.XT > 128)
+        c.XT = 128;
+    if (c.XT < 8)
+        c.XT = 8;
+    c.TJ = c.threads / c.XT;
+    c.KB = kb < 1 ? 1 : (kb > g.nz ? g.nz : kb);
+    c.nXC = (s.nxh + c.XT - 1) / c.XT;
+    c.nJG = (g.ny + c.TJ - 1) / c.TJ;
+    c.nKB = (g.nz + c.KB - 1) / c.KB;
+    c.ntiles = (long long)c.nXC * c.nJG * c.KB * g.nt * c.nKB;
+    int per_sm = max_blocks_sweep64();
+    int p32 = max_blocks_sweep32();
+    per_sm = per_sm < p32 ? per_sm : p32;
+    long long grid = (long long)sm_count * per_sm;
+    if (grid > c.ntiles)
+        grid = c.ntiles;
+    c.grid = (int)(grid > 0 ? grid : 1);
+    return c;
+}
+
+static inline void interior_grid(const Geo &g, dim3 &grid, dim3 &block)
+{
+    const int bx = g.nx >= 128 ? 128 : (g.nx >= 64 ? 64 : 32);
+    const int by = 256 / bx;
+    block = dim3(bx, by, 1);
+    grid = dim3((g.nx + bx - 1) / bx, (g.ny + by - 1) / by, g.nz * g.nt);
+}
+
+void launch_assemble(const Geo &g, const Split &s, const double *u, CPtrs8 gin, int has_g, const ss4d_params &p,
+                     SplitBufs b, int want32, cudaStream_t st)
+{
+    dim3 gr, bl;
+    interior_grid(g, gr, bl);
+    const double c = p.tau / (p.h * p.h);
+    k_assemble<<<gr, bl, 0, st>>>(g, s, u, gin, has_g, p.h, p.eps2, c, p.omega_c, b, want32);
+}
+
+void launch_pack(const Geo &g, const Split &s, const double *u, const double *prev, SplitBufs b, cudaStream_t st)
+{
+    k_pack<<<2048, 256, 0, st>>>(g, s, u, prev, b);
+}
+
+void launch_pack_coef(const Geo &g, const Split &s, CPtrs8 a, const ss4d_params &p, SplitBufs b, int want32,
+                      cudaStream_t st)
+{
+    dim3 gr, bl;
+    interior_grid(g, gr, bl);
+    const double c = p.tau / (p.h * p.h);
+    k_pack_coef<<<gr, bl, 0, st>>>(g, s, a, c, p.omega_c, b, want32);
+}
+
+void launch_unpack(const Geo &g, const Split &s, SplitBufs b, const LoopState *state, double *u, cudaStream_t st)
+{
+    dim3 gr, bl;
+    interior_grid(g, gr, bl);
+    k_unpack<<<gr, bl, 0, st>>>(g, s, b, state, u);
+}
+
+void launch_loop_init(LoopState *state, int mode, cudaStream_t st)
+{
+    k_loop_init<<<1, 1, 0, st>>>(state, mode);
+}
+
+void launch_advance(LoopState *state, cudaStream_t st)
+{
+    k_advance<<<1, 1, 0, st>>>(state);
+}
+
+void launch_sweep64(const Geo &g, const Split &s, const SweepCfg &cfg, int colour, SplitBufs b, const DevParams *dp,
+                    LoopState *state, cudaStream_t st)
+{
+    if (colour == 0)
+        k_sweep64<0><<<cfg.grid, cfg.threads, 0, st>>>(g, s, cfg, b, dp, state);
+    else
+        k_sweep64<1><<<cfg.grid, cfg.threads, 0, st>>>(g, s, cfg, b, dp, state);
+}
+
+void launch_ctrl64(SplitBufs b, int nparts, const DevParams *dp, LoopState *state, unsigned long long cond_handle,
+                   int use_cond, cudaStream_t st)
+{
+    k_ctrl64<<<1, 256, 0, st>>>(b, nparts, dp, state, (cudaGraphConditionalHandle)cond_handle, use_cond);
+}
+
+void launch_refine(const Geo &g, const Split &s, const SweepCfg &cfg, int colour, SplitBufs b, const DevParams *dp,
+                   LoopState *state, cudaStream_t st)
+{
+    if (colour == 0)
+        k_refine<0><<<cfg.grid, cfg.threads, 0, st>>>(g, s, cfg, b, dp, state);
+    else
+        k_refine<1><<<cfg.grid, cfg.threads, 0, st>>>(g, s, cfg, b, dp, state);
+}
+
+void launch_zero_delta(const Split &s, SplitBufs b, LoopState *state, cudaStream_t st)
+{
+    k_zero_delta<<<1024, 256, 0, st>>>(s, b, state);
+}
+
+void launch_sweep32(const Geo &g, const Split &s, const SweepCfg &cfg, int colour, SplitBufs b, const DevParams *dp,
+                    LoopState *state, int start_mode, cudaStream_t st)
+{
+    (void)start_mode;
+    if (colour == 0)
+        k_sweep32<0><<<cfg.grid, cfg.threads, 0, st>>>(g, s, cfg, b, dp, state);
+    else
+        k_sweep32<1><<<cfg.grid, cfg.threads, 0, st>>>(g, s, cfg, b, dp, state);
+}
+
+void launch_ctrl_mixed(SplitBufs b, int nparts, const DevParams *dp, LoopState *state, unsigned long long cond_handle,
+                       int use_cond, cudaStream_t st)
+{
+    k_ctrl_mixed<<<1, 256, 0, st>>>(b, nparts, dp, state, (cudaGraphConditionalHandle)cond_handle, use_cond);
+}
+
+} // namespace ss4d

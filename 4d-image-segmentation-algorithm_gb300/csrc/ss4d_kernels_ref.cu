@@ -1,0 +1,554 @@
+// ss4d_kernels_ref.cu — natural-layout FP64 kernels in the reference's
+// expression order.
+//
+// This translation unit is compiled with --fmad=false: every multiply and add
+// is rounded separately, the way the x86-64 reference build rounds them, and
+// division and square root are IEEE round-to-nearest.  The voxel updates here
+// therefore reproduce the reference's arithmetic; only the order of the
+// residual/norm summations differs (a parallel reduction instead of one
+// serial sum).  They serve the SS4D_ARITH_REFERENCE form, the edge detector of
+// every form (run once per segmentation), the MCF boundary and exact
+// solution, the rescale, the mask and the norms.
+#include "ss4d_kernels.cuh"
+
+namespace ss4d {
+
+// ---------------------------------------------------------------------------
+// launch geometry over interior voxels: x along threadIdx.x, y along
+// threadIdx.y, (k, l) along blockIdx.z.
+
+__device__ inline bool interior_ijkl(const Geo &g, int &i, int &j, int &k, int &l)
+{
+    i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int kl = blockIdx.z;
+    k = 1 + kl % g.nz;
+    l = 1 + kl / g.nz;
+    return i <= g.nx && j <= g.ny;
+}
+
+__device__ inline unsigned block_linear()
+{
+    return (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+}
+
+__device__ inline int flat_tid()
+{
+    return threadIdx.y * blockDim.x + threadIdx.x;
+}
+
+// Block reduction over a 2D block (flattened thread order).
+__device__ inline double block_sum2d(double v)
+{
+    __shared__ double s2[32];
+    const int t = flat_tid();
+    const int lane = t & 31, wid = t >> 5;
+    const int nw = (blockDim.x * blockDim.y + 31) >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0)
+        s2[wid] = v;
+    __syncthreads();
+    double r = 0;
+    if (wid == 0) {
+        r = lane < nw ? s2[lane] : 0.0;
+        r = warp_sum(r);
+    }
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// Neumann reflection, one axis per launch (segmentation4D.c:826-864 runs the
+// axes in x, y, z, w order over full padded ranges).
+
+__global__ void k_reflect_axis(Geo g, double *u, int axis)
+{
+    // enumerate the padded cross-section orthogonal to `axis`
+    long long cnt;
+    int e[3];
+    long long st[3], sa;
+    int Ma;
+    if (axis == 0) { e[0] = g.jM; e[1] = g.kM; e[2] = g.lM; st[0] = g.sy; st[1] = g.sz; st[2] = g.sw; sa = 1; Ma = g.iM; }
+    else if (axis == 1) { e[0] = g.iM; e[1] = g.kM; e[2] = g.lM; st[0] = 1; st[1] = g.sz; st[2] = g.sw; sa = g.sy; Ma = g.jM; }
+    else if (axis == 2) { e[0] = g.iM; e[1] = g.jM; e[2] = g.lM; st[0] = 1; st[1] = g.sy; st[2] = g.sw; sa = g.sz; Ma = g.kM; }
+    else { e[0] = g.iM; e[1] = g.jM; e[2] = g.kM; st[0] = 1; st[1] = g.sy; st[2] = g.sz; sa = g.sw; Ma = g.lM; }
+    cnt = (long long)e[0] * e[1] * e[2];
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < cnt; t += (long long)gridDim.x * blockDim.x) {
+        long long r = t;
+        int a0 = (int)(r % e[0]); r /= e[0];
+        int a1 = (int)(r % e[1]);
+        int a2 = (int)(r / e[1]);
+        long long base = a0 * st[0] + a1 * st[1] + a2 * st[2];
+        u[base] = u[base + sa];
+        u[base + (Ma - 1) * sa] = u[base + (Ma - 2) * sa];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// presmoothing (segmentation4D.c:352-404)
+
+__global__ void k_presmooth_half(Geo g, double *v, const double *prev, double c, double omega, int colour)
+{
+    int i, j, k, l;
+    if (!interior_ijkl(g, i, j, k, l) || ((i + j + k + l) & 1) != colour)
+        return;
+    const long long o = nat_index(g, i, j, k, l);
+    double gs = (prev[o] + c * (v[o + 1] + v[o - 1] + v[o - g.sy] + v[o + g.sy] + v[o - g.sz] + v[o + g.sz]
+                                + v[o - g.sw] + v[o + g.sw]))
+                / (1 + c * 8);
+    v[o] = v[o] + omega * (gs - v[o]);
+}
+
+__global__ void k_presmooth_resid(Geo g, const double *v, const double *prev, double c, double h4, double *partial)
+{
+    int i, j, k, l;
+    double acc = 0.0;
+    if (interior_ijkl(g, i, j, k, l)) {
+        const long long o = nat_index(g, i, j, k, l);
+        double r = v[o] * (1 + c * 8)
+                   - c * (v[o + 1] + v[o - 1] + v[o - g.sy] + v[o + g.sy] + v[o - g.sz] + v[o + g.sz] + v[o - g.sw]
+                          + v[o + g.sw])
+                   - prev[o];
+        acc = (r * r) * h4;
+    }
+    acc = block_sum2d(acc);
+    if (flat_tid() == 0)
+        partial[block_linear()] = acc;
+}
+
+// ---------------------------------------------------------------------------
+// face gradients (segmentation4D.c:455-548, :594-821): normal component
+// (v[nb]-v[c])/h, tangential ((v[nb+a]+v[c+a]) - (v[nb-a]+v[c-a]))/(4h),
+// squares summed in x, y, z, w order.
+
+__device__ inline double face_sq(const double *v, long long c, long long nb, const long long st[4], int d,
+                                 double h, double q)
+{
+    double comp[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        if (a == d)
+            comp[a] = (v[nb] - v[c]) / h;
+        else
+            comp[a] = ((v[nb + st[a]] + v[c + st[a]]) - (v[nb - st[a]] + v[c - st[a]])) / q;
+    }
+    return (comp[0] * comp[0]) + (comp[1] * comp[1]) + (comp[2] * comp[2]) + (comp[3] * comp[3]);
+}
+
+__global__ void k_gfaces(Geo g, const double *i0, const double *ithr, GPtrs8 gout, double h, double K, double theta,
+                         double rho)
+{
+    int i, j, k, l;
+    if (!interior_ijkl(g, i, j, k, l))
+        return;
+    const long long o = nat_index(g, i, j, k, l);
+    const long long st[4] = {1, g.sy, g.sz, g.sw};
+    const double q = 4.0 * h;
+#pragma unroll
+    for (int f = 0; f < 8; ++f) {
+        const int d = f >> 1;
+        const long long nb = (f & 1) ? o - st[d] : o + st[d];
+        double s0 = face_sq(i0, o, nb, st, d, h, q);
+        double s1 = ithr ? face_sq(ithr, o, nb, st, d, h, q) : 0.0;
+        gout.p[f][o] = 1.0 / (1 + K * (theta * s0 + rho * s1));
+    }
+}
+
+// _gs_coefficients_ / _gs_coefficients_mcf in reference order
+__global__ void k_coef_ref(Geo g, const double *u, CPtrs8 gin, int has_g, GPtrs8 coef, double h, double eps2)
+{
+    int i, j, k, l;
+    if (!interior_ijkl(g, i, j, k, l))
+        return;
+    const long long o = nat_index(g, i, j, k, l);
+    const long long st[4] = {1, g.sy, g.sz, g.sw};
+    const double q = 4.0 * h;
+    double nf[8];
+#pragma unroll
+    for (int f = 0; f < 8; ++f) {
+        const int d = f >> 1;
+        const long long nb = (f & 1) ? o - st[d] : o + st[d];
+        nf[f] = sqrt(face_sq(u, o, nb, st, d, h, q) + eps2);
+    }
+    double mean = ((nf[0] + nf[1] + nf[2] + nf[3] + nf[4] + nf[5] + nf[6] + nf[7]) / 8.0);
+    double vc = sqrt(mean * mean + eps2);
+#pragma unroll
+    for (int f = 0; f < 8; ++f)
+        coef.p[f][o] = has_g ? vc * gin.p[f][o] * (1.0 / nf[f]) : vc * (1.0 / nf[f]);
+}
+
+// ---------------------------------------------------------------------------
+// red-black SOR in reference order (segmentation4D.c:232-308)
+
+__global__ void k_sor_half_ref(Geo g, double *u, const double *prev, CPtrs8 a, double c, double omega, int colour)
+{
+    int i, j, k, l;
+    if (!interior_ijkl(g, i, j, k, l) || ((i + j + k + l) & 1) != colour)
+        return;
+    const long long o = nat_index(g, i, j, k, l);
+    const double E = a.p[0][o], W = a.p[1][o], N = a.p[2][o], S = a.p[3][o];
+    const double T = a.p[4][o], B = a.p[5][o], FW = a.p[6][o], BW = a.p[7][o];
+    double gs = (prev[o] + c * ((E * u[o + 1]) + (W * u[o - 1]) + (S * u[o - g.sy]) + (N * u[o + g.sy])
+                                + (B * u[o - g.sz]) + (T * u[o + g.sz]) + (BW * u[o - g.sw]) + (FW * u[o + g.sw])))
+                / (1 + c * (E + W + N + S + T + B + FW + BW));
+    u[o] = u[o] + omega * (gs - u[o]);
+}
+
+__global__ void k_sor_resid_ref(Geo g, const double *u, const double *prev, CPtrs8 a, double c, double h4,
+                                double *partial)
+{
+    int i, j, k, l;
+    double acc = 0.0;
+    if (interior_ijkl(g, i, j, k, l)) {
+        const long long o = nat_index(g, i, j, k, l);
+        const double E = a.p[0][o], W = a.p[1][o], N = a.p[2][o], S = a.p[3][o];
+        const double T = a.p[4][o], B = a.p[5][o], FW = a.p[6][o], BW = a.p[7][o];
+        double r = u[o] * (1 + c * (E + W + N + S + T + B + FW + BW))
+                   - c * ((E * u[o + 1]) + (W * u[o - 1]) + (S * u[o - g.sy]) + (N * u[o + g.sy]) + (B * u[o - g.sz])
+                          + (T * u[o + g.sz]) + (BW * u[o - g.sw]) + (FW * u[o + g.sw]))
+                   - prev[o];
+        acc = (r * r) * h4;
+    }
+    acc = block_sum2d(acc);
+    if (flat_tid() == 0)
+        partial[block_linear()] = acc;
+}
+
+// ---------------------------------------------------------------------------
+// deterministic final reductions: one block, fixed order
+
+__global__ void k_reduce_sum(const double *partial, long long n, double *out)
+{
+    double acc = 0.0;
+    for (long long t = threadIdx.x; t < n; t += blockDim.x)
+        acc += partial[t];
+    acc = block_sum(acc);
+    if (threadIdx.x == 0)
+        *out = acc;
+}
+
+// partial holds n (min, max) pairs; out[0] = min, out[1] = max,
+// out[2] = min + level*(max-min)
+__global__ void k_reduce_minmax(const double *partial, long long n, double level, double *out)
+{
+    double mn = 1e308, mx = -1e308;
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+        mn = fmin(mn, partial[2 * t]);
+        mx = fmax(mx, partial[2 * t + 1]);
+    }
+    mn = block_min(mn);
+    mx = block_max(mx);
+    if (threadIdx.x == 0) {
+        out[0] = mn;
+        out[1] = mx;
+        out[2] = mn + level * (mx - mn);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// norms over every padded voxel (segmentation4D.c:194-213, :317-335)
+
+__global__ void k_l2_partial(long long n, const double *a, const double *b, double h4, double *partial)
+{
+    double acc = 0.0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        double d = a[t] - b[t];
+        acc += (d * d) * h4;
+    }
+    acc = block_sum(acc);
+    if (threadIdx.x == 0)
+        partial[blockIdx.x] = acc;
+}
+
+__global__ void k_mass_partial(long long n, const double *a, double h4, double *partial)
+{
+    double acc = 0.0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        acc += (a[t] * h4);
+    acc = block_sum(acc);
+    if (threadIdx.x == 0)
+        partial[blockIdx.x] = acc;
+}
+
+// ---------------------------------------------------------------------------
+// MCF exact solution and Dirichlet ghosts (mcf_4D.c:344-461)
+
+__device__ inline double mcf_coord(int i, double h)
+{
+    return ((i - 1) * h) + (h / 2.) - 1.25;
+}
+
+__device__ inline double mcf_value(double x, double y, double z, double w, double t)
+{
+    return ((x * x + y * y + z * z + w * w - 1.0) / 6.0) + t;
+}
+
+__global__ void k_mcf_field(Geo g, double *u, double h, double t, int ghosts_only)
+{
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < g.n; o += (long long)gridDim.x * blockDim.x) {
+        long long r = o;
+        const int i = (int)(r % g.iM); r /= g.iM;
+        const int j = (int)(r % g.jM); r /= g.jM;
+        const int k = (int)(r % g.kM);
+        const int l = (int)(r / g.kM);
+        const int idx[4] = {i, j, k, l};
+        const int M[4] = {g.iM, g.jM, g.kM, g.lM};
+        double x[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+            x[a] = mcf_coord(idx[a], h);
+        if (ghosts_only) {
+            // the reference's eight passes run x-lo, x-hi, ..., w-hi over full
+            // ranges: the last pass touching a ghost decides its value, and it
+            // uses the special face coordinate on its own axis only.
+            int last = -1;
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+                if (idx[a] == 0 || idx[a] == M[a] - 1)
+                    last = a;
+            if (last < 0)
+                continue;
+            x[last] = idx[last] == M[last] - 1 ? (h / 2.) + 1.25 : -(h / 2.) - 1.25;
+            if (M[last] == 1)
+                x[last] = (h / 2.) + 1.25;
+        }
+        u[o] = mcf_value(x[0], x[1], x[2], x[3], t);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// rescale to [0,1] per ball (segmentation4D.c:1020-1104): one block per
+// frame; the balls of a frame are processed in their order because each
+// ball's min/max sees the values the earlier balls rescaled.
+
+__global__ void k_rescale_balls(Geo g, double *v, const int *frame_first, const int *frame_count, const double *bx,
+                                const double *by, const double *bz, double R)
+{
+    const int l = 1 + blockIdx.x;
+    const int first = frame_first[l], count = frame_count[l];
+    for (int c = 0; c < count; ++c) {
+        const double cx = bx[first + c], cy = by[first + c], cz = bz[first + c];
+        const int k0 = (int)(cz - R - 0.5), k1 = (int)(cz + R + 0.5);
+        const int j0 = (int)(cy - R - 0.5), j1 = (int)(cy + R + 0.5);
+        const int i0 = (int)(cx - R - 0.5), i1 = (int)(cx + R + 0.5);
+        const int ni = i1 - i0 + 1, nj = j1 - j0 + 1, nk = k1 - k0 + 1;
+        const long long cnt = (long long)ni * nj * nk;
+        double mn = 100000, mx = 0;
+        for (long long t = threadIdx.x; t < cnt; t += blockDim.x) {
+            const int i = i0 + (int)(t % ni), j = j0 + (int)((t / ni) % nj), k = k0 + (int)(t / ((long long)ni * nj));
+            const double dx = i - cx, dy = j - cy, dz = k - cz;
+            if (sqrt((dx * dx) + (dy * dy) + (dz * dz)) <= R) {
+                const double val = v[nat_index(g, i, j, k, l)];
+                mn = val < mn ? val : mn;
+                mx = val > mx ? val : mx;
+            }
+        }
+        mn = block_min(mn);
+        mx = block_max(mx);
+        __shared__ double qo[2];
+        if (threadIdx.x == 0) {
+            // ball values never exceed the reference's starting bounds in a
+            // meaningful run; keep its initial values 100000 / 0 exactly
+            const double lo = mn < 100000 ? mn : 100000, hi = mx > 0 ? mx : 0;
+            const double quot = 1. / (hi - lo);
+            qo[0] = quot;
+            qo[1] = lo * quot;
+        }
+        __syncthreads();
+        const double quot = qo[0], off = qo[1];
+        for (long long t = threadIdx.x; t < cnt; t += blockDim.x) {
+            const int i = i0 + (int)(t % ni), j = j0 + (int)((t / ni) % nj), k = k0 + (int)(t / ((long long)ni * nj));
+            const double dx = i - cx, dy = j - cy, dz = k - cz;
+            if (sqrt((dx * dx) + (dy * dy) + (dz * dz)) <= R) {
+                const long long o = nat_index(g, i, j, k, l);
+                const double nv = (quot * v[o]) - off;
+                if (c == 0 || v[o] < nv)
+                    v[o] = nv;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_mask_zero(Geo g, double *v, const double *Mmask)
+{
+    int i, j, k, l;
+    if (!interior_ijkl(g, i, j, k, l))
+        return;
+    const long long o = nat_index(g, i, j, k, l);
+    if (Mmask[o] == 0)
+        v[o] = 0;
+}
+
+// ---------------------------------------------------------------------------
+// threshold to mask (segmentation4D_mpi.c:1470-1478)
+
+__global__ void k_minmax_partial(Geo g, const double *u, double *partial)
+{
+    int i, j, k, l;
+    double mn = 1e308, mx = -1e308;
+    if (interior_ijkl(g, i, j, k, l)) {
+        const double v = u[nat_index(g, i, j, k, l)];
+        mn = v;
+        mx = v;
+    }
+    // flat 2D block: reuse the 1D helpers over the flattened index
+    __shared__ double smn[32], smx[32];
+    const int t = flat_tid(), lane = t & 31, wid = t >> 5, nw = (blockDim.x * blockDim.y + 31) >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fmin(mn, __shfl_down_sync(0xffffffffu, mn, o));
+        mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    }
+    if (lane == 0) {
+        smn[wid] = mn;
+        smx[wid] = mx;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        mn = lane < nw ? smn[lane] : 1e308;
+        mx = lane < nw ? smx[lane] : -1e308;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            mn = fmin(mn, __shfl_down_sync(0xffffffffu, mn, o));
+            mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+        }
+        if (lane == 0) {
+            partial[2 * block_linear()] = mn;
+            partial[2 * block_linear() + 1] = mx;
+        }
+    }
+}
+
+__global__ void k_threshold(Geo g, const double *u, const double *level_dev, double level, uint8_t *mask)
+{
+    int i, j, k, l;
+    if (!interior_ijkl(g, i, j, k, l))
+        return;
+    const double lev = level_dev ? level_dev[2] : level;
+    const long long m = ((((long long)(l - 1) * g.nz + (k - 1)) * g.ny + (j - 1)) * g.nx) + (i - 1);
+    mask[m] = u[nat_index(g, i, j, k, l)] >= lev ? 1 : 0;
+}
+
+// ---------------------------------------------------------------------------
+// host-side launch wrappers
+
+static inline void interior_cfg(const Geo &g, dim3 &grid, dim3 &block)
+{
+    const int bx = g.nx >= 128 ? 128 : (g.nx >= 64 ? 64 : 32);
+    const int by = 256 / bx;
+    block = dim3(bx, by, 1);
+    grid = dim3((g.nx + bx - 1) / bx, (g.ny + by - 1) / by, g.nz * g.nt);
+}
+
+long long interior_blocks(const Geo &g)
+{
+    dim3 gr, bl;
+    interior_cfg(g, gr, bl);
+    return (long long)gr.x * gr.y * gr.z;
+}
+
+void launch_reflect(const Geo &g, double *u, cudaStream_t st)
+{
+    for (int a = 0; a < 4; ++a)
+        k_reflect_axis<<<256, 256, 0, st>>>(g, u, a);
+}
+
+void launch_presmooth_half(const Geo &g, double *v, const double *prev, double c, double omega, int colour,
+                           cudaStream_t st)
+{
+    dim3 gr, bl;
+    interior_cfg(g, gr, bl);
+    k_presmooth_half<<<gr, bl, 0, st>>>(g, v, prev, c, omega, colour);
+}
+
+void launch_presmooth_resid(const Geo &g, const double *v, const double *prev, double c, double h4, double *partial,
+                            cudaStream_t st)
+{
+    dim3 gr, bl;
+    interior_cfg(g, gr, bl);
+    k_presmooth_resid<<<gr, bl, 0, st>>>(g, v, prev, c, h4, partial);
+}
+
+void launch_gfaces(const Geo &g, const double *i0, const double *ithr, GPtrs8 gout, double h, double K, double theta,
+                   double rho, cudaStream_t st)
+{
+    dim3 gr, bl;
+    interior_cfg(g, gr, bl);
+    k_gfaces<<<gr, bl, 0, st>>>(g, i0, ithr, gout, h, K, theta, rho);
+}
+
+void launch_coef_ref(const Geo &g, const double *u, CPtrs8 gin, int has_g, GPtrs8 coef, double h, double eps2,
+                     cudaStream_t st)
+{
+    dim3 gr, bl;
+    interior_cfg(g, gr, bl);
+    k_coef_ref<<<gr, bl, 0, st>>>(g, u, gin, has_g, coef, h, eps2);
+}
+
+void launch_sor_half_ref(const Geo &g, double *u, const double *prev, CPtrs8 a, double c, double omega, int colour,
+                         cudaStream_t st)
+{
+    dim3 gr, bl;
+    interior_cfg(g, gr, bl);
+    k_sor_half_ref<<<gr, bl, 0, st>>>(g, u, prev, a, c, omega, colour);
+}
+
+void launch_sor_resid_ref(const Geo &g, const double *u, const double *prev, CPtrs8 a, double c, double h4,
+                          double *partial, cudaStream_t st)
+{
+    dim3 gr, bl;
+    interior_cfg(g, gr, bl);
+    k_sor_resid_ref<<<gr, bl, 0, st>>>(g, u, prev, a, c, h4, partial);
+}
+
+void launch_reduce_sum(const double *partial, long long n, double *out, cudaStream_t st)
+{
+    k_reduce_sum<<<1, 1024, 0, st>>>(partial, n, out);
+}
+
+void launch_l2(const Geo &g, const double *a, const double *b, double h4, double *partial, int nblk, cudaStream_t st)
+{
+    k_l2_partial<<<nblk, 256, 0, st>>>(g.n, a, b, h4, partial);
+}
+
+void launch_mass(const Geo &g, const double *a, double h4, double *partial, int nblk, cudaStream_t st)
+{
+    k_mass_partial<<<nblk, 256, 0, st>>>(g.n, a, h4, partial);
+}
+
+void launch_mcf_field(const Geo &g, double *u, double h, double t, int ghosts_only, cudaStream_t st)
+{
+    k_mcf_field<<<1024, 256, 0, st>>>(g, u, h, t, ghosts_only);
+}
+
+void launch_rescale_balls(const Geo &g, double *v, const int *frame_first, const int *frame_count, const double *bx,
+                          const double *by, const double *bz, double R, cudaStream_t st)
+{
+    k_rescale_balls<<<g.nt, 256, 0, st>>>(g, v, frame_first, frame_count, bx, by, bz, R);
+}
+
+void launch_mask_zero(const Geo &g, double *v, const double *Mmask, cudaStream_t st)
+{
+    dim3 gr, bl;
+    interior_cfg(g, gr, bl);
+    k_mask_zero<<<gr, bl, 0, st>>>(g, v, Mmask);
+}
+
+void launch_minmax(const Geo &g, const double *u, double *partial, double level, double *out3, cudaStream_t st)
+{
+    dim3 gr, bl;
+    interior_cfg(g, gr, bl);
+    k_minmax_partial<<<gr, bl, 0, st>>>(g, u, partial);
+    k_reduce_minmax<<<1, 1024, 0, st>>>(partial, (long long)gr.x * gr.y * gr.z, level, out3);
+}
+
+void launch_threshold(const Geo &g, const double *u, const double *level_dev, double level, uint8_t *mask,
+                      cudaStream_t st)
+{
+    dim3 gr, bl;
+    interior_cfg(g, gr, bl);
+    k_threshold<<<gr, bl, 0, st>>>(g, u, level_dev, level, mask);
+}
+
+} // namespace ss4d

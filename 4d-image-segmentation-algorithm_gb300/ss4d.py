@@ -1,0 +1,335 @@
+"""Python view of the GB300 solver's C ABI (include/ss4d.h).
+
+The reference is a set of C programs whose "interface" is the functions and
+globals of segmentation4D.c / mcf_4D.c.  This module mirrors that interface
+for Python callers (tests, benchmarks): the same function names in
+`ReferenceLayer`, the same parameter names in `Params`, the same padded
+x-fastest FP64 layout.  Device arrays are passed as integer device pointers
+or as objects with a ``data_ptr()`` method (e.g. torch tensors).
+
+Every call goes to libss4d.so; there is no Python or CPU implementation of
+the solver here.  A missing or unloadable library raises `SS4DError`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libss4d.so")
+SEG_PATH = os.path.join(HERE, "libss4d_seg.so")
+MCF_PATH = os.path.join(HERE, "libss4d_mcf.so")
+
+ARITH = {"reference": 0, "fp64": 1, "mixed": 2}
+STATUS = {0: "OK", 1: "INVALID", 2: "ALLOC", 3: "CUDA", 4: "NONFINITE", 5: "TIMEOUT", 6: "UNSUPPORTED",
+          7: "NO_DEVICE"}
+
+
+class SS4DError(RuntimeError):
+    def __init__(self, status: int, what: str, detail: str = ""):
+        self.status = status
+        super().__init__(f"{what}: {STATUS.get(status, status)} {detail}".strip())
+
+
+class Dims(C.Structure):
+    _fields_ = [("iMax", C.c_int), ("jMax", C.c_int), ("kMax", C.c_int), ("lMax", C.c_int)]
+
+
+class Params(C.Structure):
+    """ss4d_params: the reference's tunables under their own names."""
+    _fields_ = [("K", C.c_double), ("eps2", C.c_double), ("tau", C.c_double), ("h", C.c_double),
+                ("omega_c", C.c_double), ("gsTol", C.c_double), ("maxNoGSIteration", C.c_int),
+                ("maxNoOfTimeSteps", C.c_int), ("segTol", C.c_double), ("sigma", C.c_double),
+                ("omega_sigma", C.c_double), ("maxNoGSIteration_sigma", C.c_double), ("theta_img", C.c_double),
+                ("rho_thr", C.c_double), ("ballRadius", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class StepStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("status", C.c_int), ("residual", C.c_double),
+                ("first_residual", C.c_double), ("refinements", C.c_int), ("warm_started", C.c_int),
+                ("ms", C.c_float)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class Balls(C.Structure):
+    _fields_ = [("n", C.c_int), ("l", C.POINTER(C.c_int)), ("cx", C.POINTER(C.c_double)),
+                ("cy", C.POINTER(C.c_double)), ("cz", C.POINTER(C.c_double))]
+
+
+def scene_params(**over) -> Params:
+    """Parameters of the synthetic-scene workloads: K = 1000, eps2 = 1e-3,
+    h = 1, tau = 0.5, omega_c = 1.8, gsTol = 1e-6, 1000 SOR iterations; the
+    edge detector's presmoothing matches a Gaussian of sigma = 1 voxel in its
+    second moment (sigma = 0.5 h^2), with the reference main's omega_sigma = 1.3
+    and 10 iterations (segmentation4D.c:1353-1363); theta_img = 1, rho_thr = 0."""
+    p = Params(K=1000.0, eps2=1e-3, tau=0.5, h=1.0, omega_c=1.8, gsTol=1e-6, maxNoGSIteration=1000,
+               maxNoOfTimeSteps=20, segTol=0.0, sigma=0.5, omega_sigma=1.3, maxNoGSIteration_sigma=10.0,
+               theta_img=1.0, rho_thr=0.0, ballRadius=8.0)
+    for k, v in over.items():
+        setattr(p, k, v)
+    return p
+
+
+def mcf_params(n: int, steps: int = 4, **over) -> Params:
+    """The MCF known-answer configuration of mcf_4D.c:478-490 for interior n:
+    h = 2.5/n, tau = eps2 = h^2, omega_c = 1.8, gsTol = 1e-12, 1000 iterations."""
+    h = 2.5 / n
+    p = Params(K=0.0, eps2=h * h, tau=h * h, h=h, omega_c=1.8, gsTol=1e-12, maxNoGSIteration=1000,
+               maxNoOfTimeSteps=steps, segTol=0.0, sigma=0.0, omega_sigma=1.0, maxNoGSIteration_sigma=0.0,
+               theta_img=0.0, rho_thr=0.0, ballRadius=0.0)
+    for k, v in over.items():
+        setattr(p, k, v)
+    return p
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libss4d.so (built by build.py) and declare its signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise SS4DError(6, "libss4d.so is not built", f"(expected at {LIB_PATH}; run build.py)")
+    L = C.CDLL(LIB_PATH)
+    vp, dp, st = C.c_void_p, C.POINTER(C.c_double), C.c_int
+    P8 = C.c_void_p * 8
+    sig = {
+        "ss4d_abi_version": ([], C.c_int),
+        "ss4d_last_error": ([], C.c_char_p),
+        "ss4d_device_count": ([C.POINTER(C.c_int)], st),
+        "ss4d_solver_create": ([C.POINTER(Dims), C.c_int, vp, C.POINTER(vp)], st),
+        "ss4d_solver_destroy": ([vp], st),
+        "ss4d_solver_set_stream": ([vp, vp], st),
+        "ss4d_solver_set_arith": ([vp, C.c_int], st),
+        "ss4d_solver_set_graph": ([vp, C.c_int], st),
+        "ss4d_solver_workspace_bytes": ([vp, C.POINTER(C.c_size_t)], st),
+        "ss4d_solver_set_timing": ([vp, C.c_int], st),
+        "ss4d_solver_kernel_time": ([vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong)], st),
+        "ss4d_solver_reset_timing": ([vp], st),
+        "ss4d_solver_launch_count": ([vp, C.POINTER(C.c_longlong)], st),
+        "ss4d_reflect": ([vp, vp], st),
+        "ss4d_presmooth_step": ([vp, C.POINTER(Params), vp, vp, C.POINTER(StepStats)], st),
+        "ss4d_edge_detector": ([vp, C.POINTER(Params), vp, vp, vp, P8], st),
+        "ss4d_gs_coefficients": ([vp, C.POINTER(Params), vp, vp, P8], st),
+        "ss4d_sor_solve": ([vp, C.POINTER(Params), vp, vp, P8, C.POINTER(StepStats)], st),
+        "ss4d_seg_time_step": ([vp, C.POINTER(Params), vp, vp, P8, vp, C.POINTER(Balls), C.POINTER(StepStats)], st),
+        "ss4d_mcf_time_step": ([vp, C.POINTER(Params), C.c_int, vp, vp, C.POINTER(StepStats)], st),
+        "ss4d_rescale_to_zero_one": ([vp, C.POINTER(Params), vp, vp, C.POINTER(Balls)], st),
+        "ss4d_threshold_mask": ([vp, vp, C.c_double, C.c_int, vp], st),
+        "ss4d_l2norm": ([vp, C.c_double, vp, vp, dp], st),
+        "ss4d_mass": ([vp, C.c_double, vp, dp], st),
+        "ss4d_mcf_set_boundary_exact": ([vp, C.c_double, C.c_double, vp], st),
+        "ss4d_mcf_exact_solution": ([vp, C.c_double, C.c_double, vp], st),
+        "ss4d_dev_alloc": ([C.c_size_t, C.POINTER(vp)], st),
+        "ss4d_dev_free": ([vp], st),
+        "ss4d_host_alloc": ([C.c_size_t, C.POINTER(vp)], st),
+        "ss4d_host_free": ([vp], st),
+        "ss4d_copy_to_device": ([vp, vp, vp, C.c_size_t], st),
+        "ss4d_copy_to_host": ([vp, vp, vp, C.c_size_t], st),
+        "ss4d_copy_device": ([vp, vp, vp, C.c_size_t], st),
+        "ss4d_synchronize": ([vp], st),
+        "ss4d_scene_generate": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, vp, vp, C.c_int], st),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def declared_symbols() -> list[str]:
+    """Names of the functions include/ss4d.h declares."""
+    import re
+    hdr = os.path.join(os.path.dirname(HERE), "include", "ss4d.h")
+    text = open(hdr).read()
+    return sorted(set(re.findall(r"\b(ss4d_[a-z0-9_]+)\s*\(", text)))
+
+
+def _ptr(x) -> int | None:
+    if x is None:
+        return None
+    if hasattr(x, "data_ptr"):
+        return int(x.data_ptr())
+    if hasattr(x, "ctypes"):  # numpy array (host memory)
+        return int(x.ctypes.data)
+    return int(x)
+
+
+def _check(status: int, what: str):
+    if status != 0:
+        raise SS4DError(status, what, lib().ss4d_last_error().decode(errors="replace"))
+
+
+def device_count() -> int:
+    n = C.c_int(0)
+    s = lib().ss4d_device_count(C.byref(n))
+    return n.value if s == 0 else 0
+
+
+def scene(kind: int, nx: int, ny: int, nz: int, nt: int, seed: int, threads: int = 0):
+    """Synthetic scene (host numpy arrays i0, u0 in the padded layout)."""
+    import numpy as np
+    shape = (nt + 2, nz + 2, ny + 2, nx + 2)
+    i0 = np.empty(shape, dtype=np.float64)
+    u0 = np.empty(shape, dtype=np.float64)
+    _check(lib().ss4d_scene_generate(kind, nx, ny, nz, nt, seed, i0.ctypes.data, u0.ctypes.data, threads),
+           "scene_generate")
+    return i0, u0
+
+
+def _p8(arrs):
+    if arrs is None:
+        return None
+    P8 = C.c_void_p * 8
+    return P8(*[_ptr(a) for a in arrs])
+
+
+def _balls(balls):
+    """balls: None or a list of (l, cx, cy, cz) in frame order."""
+    if not balls:
+        return None, None
+    n = len(balls)
+    keep = ((C.c_int * n)(*[b[0] for b in balls]), (C.c_double * n)(*[b[1] for b in balls]),
+            (C.c_double * n)(*[b[2] for b in balls]), (C.c_double * n)(*[b[3] for b in balls]))
+    B = Balls(n, C.cast(keep[0], C.POINTER(C.c_int)), C.cast(keep[1], C.POINTER(C.c_double)),
+              C.cast(keep[2], C.POINTER(C.c_double)), C.cast(keep[3], C.POINTER(C.c_double)))
+    return B, keep
+
+
+class Solver:
+    """A solver handle bound to one volume size (padded extents)."""
+
+    def __init__(self, iMax: int, jMax: int, kMax: int, lMax: int, arith: str = "fp64", stream: int | None = None):
+        self.L = lib()
+        self.dims = Dims(iMax, jMax, kMax, lMax)
+        h = C.c_void_p()
+        _check(self.L.ss4d_solver_create(C.byref(self.dims), ARITH[arith], stream, C.byref(h)), "solver_create")
+        self.h = h
+
+    @classmethod
+    def for_interior(cls, nx, ny, nz, nt, **kw):
+        return cls(nx + 2, ny + 2, nz + 2, nt + 2, **kw)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ss4d_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # settings
+    def set_arith(self, arith: str):
+        _check(self.L.ss4d_solver_set_arith(self.h, ARITH[arith]), "set_arith")
+
+    def set_graph(self, on: bool):
+        _check(self.L.ss4d_solver_set_graph(self.h, 1 if on else 0), "set_graph")
+
+    def set_stream(self, stream: int | None):
+        _check(self.L.ss4d_solver_set_stream(self.h, stream), "set_stream")
+
+    KERNELS = ("sweep64", "sweep32", "refine", "assemble", "pack")
+
+    def set_timing(self, on: bool):
+        _check(self.L.ss4d_solver_set_timing(self.h, 1 if on else 0), "set_timing")
+
+    def reset_timing(self):
+        _check(self.L.ss4d_solver_reset_timing(self.h), "reset_timing")
+
+    def kernel_times(self) -> dict:
+        """{kernel: (total ms, launches)} accumulated while timing was on."""
+        out = {}
+        for k, name in enumerate(self.KERNELS):
+            ms, n = C.c_double(0), C.c_longlong(0)
+            _check(self.L.ss4d_solver_kernel_time(self.h, k, C.byref(ms), C.byref(n)), "kernel_time")
+            out[name] = (ms.value, n.value)
+        return out
+
+    def workspace_bytes(self) -> int:
+        v = C.c_size_t(0)
+        _check(self.L.ss4d_solver_workspace_bytes(self.h, C.byref(v)), "workspace_bytes")
+        return v.value
+
+    def launch_count(self) -> int:
+        v = C.c_longlong(0)
+        _check(self.L.ss4d_solver_launch_count(self.h, C.byref(v)), "launch_count")
+        return v.value
+
+    # hot path
+    def reflect(self, img):
+        _check(self.L.ss4d_reflect(self.h, _ptr(img)), "reflect")
+
+    def presmooth_step(self, p: Params, img, scratch=None) -> dict:
+        st = StepStats()
+        _check(self.L.ss4d_presmooth_step(self.h, C.byref(p), _ptr(img), _ptr(scratch), C.byref(st)), "presmooth")
+        return st.as_dict()
+
+    def edge_detector(self, p: Params, i0, i0_thr, g8, scratch=None):
+        _check(self.L.ss4d_edge_detector(self.h, C.byref(p), _ptr(i0), _ptr(i0_thr), _ptr(scratch), _p8(g8)),
+               "edge_detector")
+
+    def gs_coefficients(self, p: Params, u, g8, coef8):
+        _check(self.L.ss4d_gs_coefficients(self.h, C.byref(p), _ptr(u), _p8(g8), _p8(coef8)), "gs_coefficients")
+
+    def sor_solve(self, p: Params, u, prev, coef8) -> dict:
+        st = StepStats()
+        _check(self.L.ss4d_sor_solve(self.h, C.byref(p), _ptr(u), _ptr(prev), _p8(coef8), C.byref(st)), "sor_solve")
+        return st.as_dict()
+
+    def seg_time_step(self, p: Params, u, prev, g8, mmask=None, balls=None) -> dict:
+        st = StepStats()
+        B, keep = _balls(balls)
+        _check(self.L.ss4d_seg_time_step(self.h, C.byref(p), _ptr(u), _ptr(prev), _p8(g8), _ptr(mmask),
+                                         C.byref(B) if B is not None else None, C.byref(st)), "seg_time_step")
+        del keep
+        return st.as_dict()
+
+    def mcf_time_step(self, p: Params, step: int, u, prev=None) -> dict:
+        st = StepStats()
+        _check(self.L.ss4d_mcf_time_step(self.h, C.byref(p), step, _ptr(u), _ptr(prev), C.byref(st)), "mcf_time_step")
+        return st.as_dict()
+
+    def rescale_to_zero_one(self, p: Params, img, mmask=None, balls=None):
+        B, keep = _balls(balls)
+        _check(self.L.ss4d_rescale_to_zero_one(self.h, C.byref(p), _ptr(img), _ptr(mmask),
+                                               C.byref(B) if B is not None else None), "rescale")
+        del keep
+
+    def threshold_mask(self, u, mask, level: float = 0.5, normalise: bool = False):
+        _check(self.L.ss4d_threshold_mask(self.h, _ptr(u), level, 1 if normalise else 0, _ptr(mask)), "threshold_mask")
+
+    def l2norm(self, h: float, a, b) -> float:
+        v = C.c_double(0)
+        _check(self.L.ss4d_l2norm(self.h, h, _ptr(a), _ptr(b), C.byref(v)), "l2norm")
+        return v.value
+
+    def mass(self, h: float, a) -> float:
+        v = C.c_double(0)
+        _check(self.L.ss4d_mass(self.h, h, _ptr(a), C.byref(v)), "mass")
+        return v.value
+
+    def mcf_set_boundary_exact(self, h: float, t: float, u):
+        _check(self.L.ss4d_mcf_set_boundary_exact(self.h, h, t, _ptr(u)), "mcf_set_boundary_exact")
+
+    def mcf_exact_solution(self, h: float, t: float, out):
+        _check(self.L.ss4d_mcf_exact_solution(self.h, h, t, _ptr(out)), "mcf_exact_solution")
+
+    def synchronize(self):
+        _check(self.L.ss4d_synchronize(self.h), "synchronize")

@@ -1,0 +1,420 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 subjective-surfaces segmentation solver.
+
+Metric: time-steps/s of the semi-implicit segmentation at 256x256x128x20
+(the multi-object drifting scene), every step solved by red-black SOR to the
+FP64 residual tolerance sum r^2 h^4 <= 1e-6.  A "step" is one time step:
+coefficient assembly, the SOR solve, the per-step rescale.  Inputs (about
+25 GB of working set) are far larger than the 129 MB L2, so no flush is
+needed between steps.
+
+Prints ONE JSON line on rank 0.  `--impl reference` times the reference's
+CPU algorithm instead (the compiled reference where it runs, else the C
+oracle that restates it), on all host cores.
+
+Multi-GPU: the solver does not shard one volume across GPUs (the reference's
+MPI slab decomposition is not carried over), so N ranks run N independent
+volumes ("replicas", weak scaling); `value` is the steps of all ranks over the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "4d-image-segmentation-algorithm_gb300")
+for _p in (PKG, os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "time-steps/s @256²×128×20 to FP64 res 1e-6: mixed+learned vs plain FP64; HBM %"
+WORKLOAD = ("segmentation time steps, 256x256x128x20 multi-object drifting scene (3 ellipsoids, noise 30, 10% "
+            "boundary erasure), K=1000, eps2=1e-3, tau=0.5, omega=1.8, gsTol=1e-6")
+# algorithmic bytes per interior voxel (each reference array touched once)
+BYTES_FP64_ITER = 88.0  # read u, prev, 8 coefficients; write u
+BYTES_FP32_ITER = 44.0  # the same arrays in FP32
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--size", type=int, nargs=4, default=[256, 256, 128, 20], metavar=("NX", "NY", "NZ", "NT"))
+    ap.add_argument("--forms", default="fp64,mixed")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--seed", type=int, default=1)
+    return ap.parse_args()
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.tmp = None
+
+    def start(self):
+        try:
+            self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.tmp,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.tmp.flush()
+        rows = []
+        with open(self.tmp.name) as fh:
+            for ln in fh:
+                f = [x.strip() for x in ln.split(",")]
+                if len(f) >= 9:
+                    rows.append(f)
+        os.unlink(self.tmp.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1])]
+        mx = [num(r[2]) for r in rows if num(r[2])]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        # samples while the GPU is busy (the upper half of the observed clocks)
+        busy = sorted(sm)[len(sm) // 2:] if sm else []
+        return {"sm_mhz": statistics.median(busy) if busy else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max([num(r[3]) for r in rows if num(r[3])] or [0])}
+
+
+# --------------------------------------------------------------------------
+# our arm
+
+def run_ours(args, rank, world, dist):
+    import numpy as np
+    import torch
+
+    import ss4d
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    nx, ny, nz, nt = args.size
+    p = ss4d.scene_params(maxNoOfTimeSteps=args.steps + args.warmup)
+    i0h, u0h = ss4d.scene(3, nx, ny, nz, nt, seed=args.seed + rank, threads=os.cpu_count() or 1)
+    shape = i0h.shape
+    n_pad = int(np.prod(shape))
+    n_int = nx * ny * nz * nt
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+
+    i0 = torch.from_numpy(i0h).to(dev)
+    g = [torch.empty(shape, dtype=torch.float64, device=dev) for _ in range(8)]
+    S = ss4d.Solver(*shape[::-1], arith="fp64", stream=sh)
+    S.edge_detector(p, i0, None, g)
+    S.synchronize()
+    del i0
+    u0 = torch.from_numpy(u0h).to(dev)
+
+    forms = [f for f in args.forms.split(",") if f]
+    results = {}
+    finals = {}
+    for form in forms:
+        S.set_arith(form)
+        u = u0.clone()
+        its = []
+        for _ in range(args.warmup):
+            st = S.seg_time_step(p, u, None, g)
+            its.append(st["iterations"])
+        launches0 = S.launch_count()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        clk = Clocks(dev.index)
+        clk.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        steps = []
+        for _ in range(args.steps):
+            st = S.seg_time_step(p, u, None, g)
+            steps.append(st)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1)
+        clocks = clk.stop()
+        if dist:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+            dist.barrier()
+        launches = S.launch_count() - launches0
+        ok = all(s["residual"] <= p.gsTol or s["iterations"] >= p.maxNoGSIteration for s in steps)
+        results[form] = {
+            "steps_per_s": args.steps * world / (ms / 1e3),
+            "ms_per_step": ms / args.steps,
+            "iterations_per_step": statistics.mean(s["iterations"] for s in steps),
+            "iterations": [s["iterations"] for s in steps],
+            "refinements_per_step": statistics.mean(s["refinements"] for s in steps),
+            "max_residual": max(s["residual"] for s in steps),
+            "converged": ok,
+            "launches": launches,
+            "clocks": clocks,
+        }
+        finals[form] = u
+
+    # per-kernel device time (CUDA events on the launching stream), one more
+    # step per form with timing on: the roofline of the dominant kernel
+    roof = {}
+    for form in forms:
+        S.set_arith(form)
+        S.set_timing(True)
+        S.reset_timing()
+        u = finals[form].clone()
+        S.seg_time_step(p, u, None, g)
+        kt = S.kernel_times()
+        S.set_timing(False)
+        roof[form] = kt
+    hbm, how = peaks()
+
+    def roofline(form):
+        kt = roof[form]
+        if form == "mixed":
+            ms, n = kt["sweep32"]
+            per_unit = BYTES_FP32_ITER
+        else:
+            ms, n = kt["sweep64"]
+            per_unit = BYTES_FP64_ITER
+        if n == 0:
+            return None
+        per_launch = per_unit * (n_int / 2.0)  # a launch updates one colour: half the voxels
+        avg = ms / n
+        ach = per_launch / (avg / 1e3) / 1e9
+        tot = sum(v[0] for v in kt.values())
+        return {"bound": "hbm", "kernel": "k_sweep32" if form == "mixed" else "k_sweep64", "achieved": ach,
+                "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "peak_source": how, "traffic": None,
+                "avg_launch_ms": avg, "launches": n, "bytes_per_launch": per_launch,
+                "share_of_step_kernel_time": (ms / tot) if tot else None,
+                "kernel_ms": {k: v[0] for k, v in kt.items()}}
+
+    # error of the mixed form against the plain FP64 form after the same steps
+    err = None
+    if "fp64" in finals and "mixed" in finals:
+        a = finals["mixed"][1:-1, 1:-1, 1:-1, 1:-1]
+        b = finals["fp64"][1:-1, 1:-1, 1:-1, 1:-1]
+        d = (a - b)
+        lev = 0.5 * (b.min() + b.max())
+        ma, mb = a >= lev, b >= lev
+        inter = (ma & mb).sum().item()
+        dice = 2.0 * inter / max(1, ma.sum().item() + mb.sum().item())
+        err = {"max_abs": d.abs().max().item(), "max_rel": (d.abs().max() / b.abs().max()).item(),
+               "rel_l2": (d.norm() / b.norm()).item(), "mask_dice": dice, "mask_level": "(min+max)/2 of fp64 u"}
+    S.close()
+    return results, roofline, err, (shape, n_pad, n_int, p, i0h, u0h)
+
+
+def run_e2e(args, form, ctx):
+    """The same steps through the reference-named layer (libss4d_seg.so) with
+    host arrays: every _segTimeStep_() uploads u and Mmask and downloads u and
+    prev_u (page-locked host memory), as a reference driver would call it."""
+    import ctypes as C
+
+    import numpy as np
+
+    import ss4d
+
+    shape, n_pad, n_int, p, i0h, u0h = ctx
+    os.environ["SS4D_ARITH"] = form
+    L = C.CDLL(ss4d.SEG_PATH, mode=os.RTLD_LOCAL)
+    lM, kM, jM, iM = shape
+    for nm, v in (("iMax", iM), ("jMax", jM), ("kMax", kM), ("lMax", lM), ("maxNoGSIteration", p.maxNoGSIteration),
+                  ("maxNoOfTimeSteps", p.maxNoOfTimeSteps)):
+        C.c_int.in_dll(L, nm).value = int(v)
+    for nm in ("K", "eps2", "tau", "h", "omega_c", "gsTol", "segTol", "sigma", "omega_sigma",
+               "maxNoGSIteration_sigma", "theta_img", "rho_thr", "ballRadius"):
+        C.c_double.in_dll(L, nm).value = float(getattr(p, nm))
+    noc = (C.c_int * lM)()
+    C.c_void_p.in_dll(L, "no_of_centers").value = C.addressof(noc)
+    L._allocateMem_.restype = C.c_bool
+    L._segTimeStep_.restype = C.c_bool
+    L._gf_inputImage_plus_thresholdedImage_.restype = C.c_bool
+    assert L._allocateMem_()
+
+    def arr(name):
+        addr = C.c_void_p.in_dll(L, name).value
+        return np.ctypeslib.as_array((C.c_double * n_pad).from_address(addr)).reshape(shape)
+
+    i0, u, mm = arr("i0"), arr("u"), arr("Mmask")
+    i0[...] = i0h
+    mm[...] = 1.0
+    assert L._gf_inputImage_plus_thresholdedImage_(C.c_void_p(i0.ctypes.data), C.c_void_p(u.ctypes.data))
+    u[...] = u0h
+    for _ in range(args.warmup):
+        assert L._segTimeStep_()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        assert L._segTimeStep_()
+    dt = time.perf_counter() - t0
+    L._deallocateMem_()
+    nbytes = 8 * n_pad
+    return {"value": args.steps / dt, "unit": "time-steps/s", "h2d_bytes_per_step": 2 * nbytes,
+            "d2h_bytes_per_step": 2 * nbytes, "path": "libss4d_seg.so _segTimeStep_() on host arrays (u, Mmask up; "
+                                                      "u, prev_u down)", "form": form}
+
+
+# --------------------------------------------------------------------------
+# CPU: the reference's algorithm on the host cores
+
+def cpu_kind():
+    """'reference' when the reference compiled from its own sources loads
+    on this host, else 'port' (the C oracle restating it)."""
+    import ctypes as C
+    ref = os.path.join(ROOT, "oracle", "_ref", "libref_seg.so")
+    if os.path.exists(ref):
+        try:
+            C.CDLL(ref, mode=os.RTLD_LOCAL)
+            return "reference"
+        except OSError:
+            pass
+    return "port"
+
+
+def cpu_steps(size, seed, warmup, steps, threads):
+    """Time `steps` segmentation time steps of the oracle (after `warmup`)
+    on `threads` cores; returns (seconds per step, iterations)."""
+    import numpy as np
+
+    import oracle
+    import ss4d
+
+    nx, ny, nz, nt = size
+    p = ss4d.scene_params()
+    i0, u = ss4d.scene(3, nx, ny, nz, nt, seed=seed, threads=threads)
+    oracle.set_threads(threads)
+    g, _, _ = oracle.edge_detector(p, i0, np.zeros_like(i0))
+    del i0
+    prev = np.zeros_like(u)
+    mm = np.ones_like(u)
+    coef = oracle.new_like(u, 8)
+    for _ in range(warmup):
+        oracle.seg_time_step(p, u, prev, g, coef=coef, mmask=mm)
+    its = []
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        z, _ = oracle.seg_time_step(p, u, prev, g, coef=coef, mmask=mm)
+        its.append(z)
+    return (time.perf_counter() - t0) / max(1, steps), its
+
+
+def cpu_baseline(args):
+    threads = os.cpu_count() or 1
+    sec, its = cpu_steps(args.size, args.seed, 0, 1, threads)
+    return {"value": 1.0 / sec, "unit": "time-steps/s", "cores": threads, "kind": "port",
+            "sample": f"1 time step of the same {args.size[0]}x{args.size[1]}x{args.size[2]}x{args.size[3]} workload "
+                      f"({its[0]} SOR iterations), C oracle restating segmentation4D.c with OpenMP over frames "
+                      f"as mcf_4D_openmp.c does, {threads} threads"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", 0))
+    if rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    sec, its = cpu_steps(args.size, args.seed, args.warmup, args.steps, threads)
+    v = 1.0 / sec
+    kind = "port"  # the compiled reference needs its sources, which only the build host has
+    return {"metric": METRIC, "value": v, "unit": "time-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "nx": args.size[0], "ny": args.size[1], "nz": args.size[2],
+                       "nt": args.size[3], "parallelism": "host cores", "l2": "working set >> L2"},
+            "cpu_baseline": {"value": v, "unit": "time-steps/s", "cores": threads, "kind": kind,
+                             "sample": f"{args.steps} full time steps after {args.warmup} warm-up steps, "
+                                       f"SOR iterations {its}"},
+            "e2e": {"value": v, "unit": "time-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.impl == "reference":
+        line = run_reference(args)
+        if line:
+            print(json.dumps(line))
+        return
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group("nccl")
+    results, roofline, err, ctx = run_ours(args, rank, world, dist)
+    forms = list(results)
+    # headline: the mixed form when it converged every step, else plain FP64
+    head = "mixed" if "mixed" in results and results["mixed"]["converged"] else forms[0]
+    r = results[head]
+    line = {"metric": METRIC, "value": r["steps_per_s"], "unit": "time-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 sweeps + f64 residual/refinement" if head == "mixed" else "f64",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "form": head, "nx": args.size[0], "ny": args.size[1],
+                       "nz": args.size[2], "nt": args.size[3], "parallelism": f"replicas x{world}",
+                       "l2": "inputs >> L2 (about 25 GB working set), no flush"},
+            "roofline": roofline(head), "gpu_launches": r["launches"], "clocks": r["clocks"],
+            "forms": {f: {k: v for k, v in results[f].items() if k != "clocks"} for f in forms}}
+    if "fp64" in results and "mixed" in results:
+        line["mixed_over_fp64"] = results["mixed"]["steps_per_s"] / results["fp64"]["steps_per_s"]
+        line["roofline_fp64"] = roofline("fp64")
+        line["error_mixed_vs_fp64"] = err
+    if rank == 0 and world == 1 and not args.no_e2e:
+        try:
+            line["e2e"] = run_e2e(args, head, ctx)
+        except Exception as ex:  # reported, not hidden
+            line["e2e"] = {"value": None, "unit": "time-steps/s", "error": repr(ex)}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(args)
+    if dist:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,244 @@
+/*
+ * ss4d.h — native C ABI of the GB300 semi-implicit subjective-surfaces /
+ * mean-curvature-flow solver (4D, red-black SOR).
+ *
+ * Every entry point here replaces one function of the reference C programs
+ * segmentation4D.c and mcf_4D.c / mcf_4D_openmp.c (88MARK08/4D-image-
+ * segmentation-algorithm); the citation beside each declaration names it.
+ * The reference works on process-global host arrays; this ABI works on
+ * caller-owned DEVICE arrays with exactly the reference's volume layout:
+ *
+ *     double array of iMax*jMax*kMax*lMax voxels, index
+ *     ((l*kMax + k)*jMax + j)*iMax + i   (x fastest)        segmentation4D.c:61-65
+ *     one ghost voxel per side on every axis: iMax = nx + 2  segmentation4D.c:14
+ *
+ * and the reference's parameter names (struct ss4d_params).  A solver handle
+ * owns the device workspaces the fast forms need (colour-split copies of u,
+ * coefficient arrays, reduction buffers) and the CUDA stream every call is
+ * issued on.  Calls are asynchronous with respect to the host except where a
+ * result is returned by value (norms, stats): those synchronise the stream.
+ *
+ * No CPU fallback exists: without a CUDA device every compute call returns
+ * SS4D_ERR_NO_DEVICE.  Reference-named wrappers over host arrays (a drop-in
+ * for a reference main) live in ss4d_compat.h.
+ */
+#ifndef SS4D_H
+#define SS4D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SS4D_ABI_VERSION 1
+
+typedef enum ss4d_status {
+    SS4D_OK = 0,
+    SS4D_ERR_INVALID = 1,     /* NULL pointer, bad size or parameter; the reference returns false (segmentation4D.c:100-103) */
+    SS4D_ERR_ALLOC = 2,       /* a device/host allocation failed (reference: _allocateMem_ returns false) */
+    SS4D_ERR_CUDA = 3,        /* a CUDA runtime call failed; text via ss4d_last_error() */
+    SS4D_ERR_NONFINITE = 4,   /* the SOR residual became NaN or Inf */
+    SS4D_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+    SS4D_ERR_UNSUPPORTED = 6, /* combination not built (e.g. unknown arithmetic mode) */
+    SS4D_ERR_NO_DEVICE = 7    /* no CUDA device visible */
+} ss4d_status;
+
+/* Arithmetic form of the SOR solve. */
+typedef enum ss4d_arith {
+    /* FP64 in the reference's expression order on the natural layout, three
+     * passes per iteration like segmentation4D.c:228-309.  Slow; it is the
+     * parity anchor (u agrees with the reference to rounding of pow()). */
+    SS4D_ARITH_REFERENCE = 0,
+    /* FP64 on a colour-split layout: fused residual, precomputed diagonal and
+     * relaxation factor, whole sweep loop in one CUDA graph.  The plain form. */
+    SS4D_ARITH_FP64 = 1,
+    /* FP32 red-black sweeps on the correction equation, FP64 residual,
+     * convergence test and refinement of u; same FP64 stopping tolerance. */
+    SS4D_ARITH_MIXED = 2
+} ss4d_arith;
+
+/* Padded extents, as the reference's iMax, jMax, kMax, lMax globals
+ * (segmentation4D.c:14).  Each must be >= 3; the product must stay below 2^31
+ * like the reference's int indexing (segmentation4D.c:61-65). */
+typedef struct ss4d_dims {
+    int iMax, jMax, kMax, lMax;
+} ss4d_dims;
+
+/* The reference's tunables, same names and meaning (segmentation4D.c:45-58,
+ * mcf_4D.c:25-33).  eps2 is used as eps^2 inside sqrt(|grad u|^2 + eps2). */
+typedef struct ss4d_params {
+    double K;                      /* edge-detector constant in g = 1/(1 + K s)           */
+    double eps2;                   /* Evans-Spruck regularisation                          */
+    double tau;                    /* time step                                            */
+    double h;                      /* grid spacing                                         */
+    double omega_c;                /* SOR relaxation of the time step                      */
+    double gsTol;                  /* stop when sum r^2 h^4 <= gsTol                       */
+    int    maxNoGSIteration;       /* SOR iteration cap per time step                      */
+    int    maxNoOfTimeSteps;       /* driver loop cap (used by ss4d_seg_run)               */
+    double segTol;                 /* driver stop on ||u^{n+1}-u^n||_2 (ss4d_seg_run)      */
+    double sigma;                  /* presmoothing (implicit heat) step                    */
+    double omega_sigma;            /* SOR relaxation of the presmoothing                   */
+    double maxNoGSIteration_sigma; /* iteration cap of the presmoothing (a double, as in
+                                      segmentation4D.c:56)                                  */
+    double theta_img;              /* weight of the image gradient in g                    */
+    double rho_thr;                /* weight of the thresholded-image gradient in g        */
+    double ballRadius;             /* radius of the per-centre rescale balls              */
+} ss4d_params;
+
+/* Per-frame rescale centres (segmentation4D.c:38-39, no_of_centers/center_*),
+ * flattened in (frame, centre) order: entries with the same l must be
+ * consecutive and in the reference's centre order.  n == 0 and an all-ones
+ * Mmask make the rescale the identity. */
+typedef struct ss4d_balls {
+    int n;
+    const int *l;          /* frame index of each centre (1..lMax-2), host memory */
+    const double *cx, *cy, *cz;
+} ss4d_balls;
+
+/* What one solve reports instead of the reference's printf
+ * ("Mean square residue is %e and total number of RBSOR is %d"). */
+typedef struct ss4d_step_stats {
+    int    iterations;      /* SOR iterations z at loop exit (mixed: FP32 sweeps)     */
+    int    status;          /* ss4d_status of the step                                */
+    double residual;        /* sum r^2 h^4 at exit, in FP64                           */
+    double first_residual;  /* residual after the first iteration                     */
+    int    refinements;     /* mixed form: FP64 residual/refinement passes            */
+    int    warm_started;    /* 1 when the learned predictor supplied the start        */
+    float  ms;              /* device time of the call (CUDA events on the stream)    */
+} ss4d_step_stats;
+
+typedef struct ss4d_solver ss4d_solver;
+
+/* ---- library / device ------------------------------------------------- */
+int         ss4d_abi_version(void);
+const char *ss4d_last_error(void);            /* thread-local text of the last failure */
+ss4d_status ss4d_device_count(int *count);    /* SS4D_ERR_NO_DEVICE when none visible   */
+
+/* Solver handle.  `stream` is a cudaStream_t (NULL = legacy default stream).
+ * Allocates nothing until a call needs it; all workspaces are sized from dims.
+ * Replaces the allocation role of _allocateMem_ (segmentation4D.c:71-154)
+ * for everything except the caller-visible arrays. */
+ss4d_status ss4d_solver_create(const ss4d_dims *dims, ss4d_arith arith, void *stream,
+                               ss4d_solver **out);
+ss4d_status ss4d_solver_destroy(ss4d_solver *s);
+ss4d_status ss4d_solver_set_stream(ss4d_solver *s, void *stream);
+ss4d_status ss4d_solver_set_arith(ss4d_solver *s, ss4d_arith arith);
+/* Use (1) or bypass (0) the CUDA-graph form of the sweep loop (default 1). */
+ss4d_status ss4d_solver_set_graph(ss4d_solver *s, int enable);
+/* Per-kernel timing.  While enabled, the sweep loop runs host-driven (not
+ * as a graph) and every launch of the kernels below is bracketed by CUDA
+ * events on the handle's stream; totals accumulate until reset. */
+typedef enum ss4d_kernel_kind {
+    SS4D_K_SWEEP64 = 0,   /* FP64 red or black half-sweep with fused residual */
+    SS4D_K_SWEEP32 = 1,   /* FP32 half-sweep of the correction equation       */
+    SS4D_K_REFINE = 2,    /* FP64 refinement + residual pass (one colour)     */
+    SS4D_K_ASSEMBLE = 3,  /* coefficient assembly                             */
+    SS4D_K_PACK = 4,      /* natural <-> colour-split copies                  */
+    SS4D_K_COUNT = 5
+} ss4d_kernel_kind;
+ss4d_status ss4d_solver_set_timing(ss4d_solver *s, int enable);
+ss4d_status ss4d_solver_kernel_time(const ss4d_solver *s, int kind, double *total_ms, long long *launches);
+ss4d_status ss4d_solver_reset_timing(ss4d_solver *s);
+/* Device bytes currently held by the handle. */
+ss4d_status ss4d_solver_workspace_bytes(const ss4d_solver *s, size_t *bytes);
+/* Kernel launches issued by this handle since creation (sweeps, passes,
+ * reductions; a graph launch counts the kernels it contains). */
+ss4d_status ss4d_solver_launch_count(const ss4d_solver *s, long long *count);
+
+/* ---- hot-path entry points (device arrays, reference layout) ---------- */
+
+/* _reflection4Ddata_ (segmentation4D.c:826-864): Neumann ghost layer. */
+ss4d_status ss4d_reflect(ss4d_solver *s, double *d_img);
+
+/* _presmoothStep_ (segmentation4D.c:337-409): one implicit heat step
+ * (I - sigma*Laplace) v = img solved in place by red-black SOR with omega_sigma;
+ * d_scratch receives the copy of the input that the reference keeps in its
+ * global prev_u (may be NULL: the handle then uses its own). */
+ss4d_status ss4d_presmooth_step(ss4d_solver *s, const ss4d_params *p, double *d_img,
+                                double *d_scratch, ss4d_step_stats *stats);
+
+/* _gf_inputImage_plus_thresholdedImage_ (segmentation4D.c:582-823): presmooth
+ * d_i0 and d_i0_thr in place, then the 8 face values of the edge detector
+ * g_f = 1/(1 + K (theta_img |grad I0|_f^2 + rho_thr |grad Ithr|_f^2)) into
+ * d_g[0..7] = g_e, g_w, g_n, g_s, g_t, g_b, g_fw, g_bw.  d_i0_thr may be NULL
+ * when rho_thr == 0 (its presmoothing is then skipped).  d_scratch plays the
+ * reference's prev_u as in ss4d_presmooth_step (may be NULL). */
+ss4d_status ss4d_edge_detector(ss4d_solver *s, const ss4d_params *p, double *d_i0,
+                               double *d_i0_thr, double *d_scratch, double *const d_g[8]);
+
+/* _gs_coefficients_ (segmentation4D.c:446-580) with d_g != NULL, or
+ * _gs_coefficients_mcf (mcf_4D.c:208-342) with d_g == NULL: the 8 co-volume
+ * coefficients e, w, n, s, t, b, fw, bw of every interior voxel. */
+ss4d_status ss4d_gs_coefficients(ss4d_solver *s, const ss4d_params *p, const double *d_u,
+                                 const double *const d_g[8], double *const d_coef[8]);
+
+/* The red-black SOR loop of _segTimeStep_ (segmentation4D.c:228-309) on
+ * given coefficients: solves (1 + c sum a) u - c sum a u_nb = prev, c = tau/h^2,
+ * from the current d_u, until sum r^2 h^4 <= gsTol or maxNoGSIteration. */
+ss4d_status ss4d_sor_solve(ss4d_solver *s, const ss4d_params *p, double *d_u,
+                           const double *d_prev_u, const double *const d_coef[8],
+                           ss4d_step_stats *stats);
+
+/* _segTimeStep_ (segmentation4D.c:215-315): prev_u <- u, coefficients from u
+ * and the face g, SOR solve, then _rescale4DdataToZeroOne_ with d_Mmask/balls.
+ * d_prev_u may be NULL (not returned); d_Mmask may be NULL (all ones). */
+ss4d_status ss4d_seg_time_step(ss4d_solver *s, const ss4d_params *p, double *d_u,
+                               double *d_prev_u, const double *const d_g[8],
+                               const double *d_Mmask, const ss4d_balls *balls,
+                               ss4d_step_stats *stats);
+
+/* _mcfTimeStep (mcf_4D.c:102-205): prev_u <- u, coefficients (g == 1), exact
+ * Dirichlet ghosts at t = tau*numberOfTimeStep, SOR solve. */
+ss4d_status ss4d_mcf_time_step(ss4d_solver *s, const ss4d_params *p, int numberOfTimeStep,
+                               double *d_u, double *d_prev_u, ss4d_step_stats *stats);
+
+/* _rescale4DdataToZeroOne_ (segmentation4D.c:1020-1104). */
+ss4d_status ss4d_rescale_to_zero_one(ss4d_solver *s, const ss4d_params *p, double *d_img,
+                                     const double *d_Mmask, const ss4d_balls *balls);
+
+/* Level-set threshold to a mask, as _writeData_mpi_ (segmentation4D_mpi.c:
+ * 1470-1478): mask = (u >= level) for every interior voxel, written frame by
+ * frame in (l, k, j, i) order, nx*ny*nz*nt bytes of 0/1.  With normalise != 0
+ * the level is taken relative to the interior range: min + level*(max-min). */
+ss4d_status ss4d_threshold_mask(ss4d_solver *s, const double *d_u, double level, int normalise,
+                                uint8_t *d_mask);
+
+/* _l2norm_ (segmentation4D.c:194-213) / _l2norm_mcf (mcf_4D.c:81-100):
+ * sqrt(sum over ALL padded voxels of (a-b)^2 h^4). Synchronises. */
+ss4d_status ss4d_l2norm(ss4d_solver *s, double h, const double *d_a, const double *d_b,
+                        double *out);
+/* _mass4D_ (segmentation4D.c:317-335). Synchronises. */
+ss4d_status ss4d_mass(ss4d_solver *s, double h, const double *d_a, double *out);
+
+/* _set4DBoundaryToExactValues_mcf (mcf_4D.c:344-443) and _exactSolution_mcf
+ * (mcf_4D.c:444-461): u = (x^2+y^2+z^2+w^2-1)/6 + t on [-1.25,1.25]^4. */
+ss4d_status ss4d_mcf_set_boundary_exact(ss4d_solver *s, double h, double t, double *d_u);
+ss4d_status ss4d_mcf_exact_solution(ss4d_solver *s, double h, double t, double *d_out);
+
+/* ---- memory helpers (used by the reference-named layer) --------------- */
+/* Device / pinned-host allocations and copies on the handle's stream.  They
+ * exist so that C callers without the CUDA headers (ss4d_compat.c) can mirror
+ * host arrays; copies between pinned host and device are asynchronous. */
+ss4d_status ss4d_dev_alloc(size_t bytes, void **out);
+ss4d_status ss4d_dev_free(void *p);
+ss4d_status ss4d_host_alloc(size_t bytes, void **out);   /* page-locked */
+ss4d_status ss4d_host_free(void *p);
+ss4d_status ss4d_copy_to_device(ss4d_solver *s, void *d_dst, const void *h_src, size_t bytes);
+ss4d_status ss4d_copy_to_host(ss4d_solver *s, void *h_dst, const void *d_src, size_t bytes);
+ss4d_status ss4d_copy_device(ss4d_solver *s, void *d_dst, const void *d_src, size_t bytes);
+ss4d_status ss4d_synchronize(ss4d_solver *s);
+
+/* ---- synthetic scenes (host; the same generator feeds every test) ----- */
+/* Writes the padded image i0 (intensities/255, as the reference loader,
+ * segmentation4D.c:1320) and the initial u0 of scene `kind`
+ * (1 = single deforming ellipsoid, 2 = large ellipsoid with two erased
+ * sectors, 3 = multi-object drifting scene) for interior nx,ny,nz,nt. */
+ss4d_status ss4d_scene_generate(int kind, int nx, int ny, int nz, int nt, uint64_t seed,
+                                double *h_i0, double *h_u0, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SS4D_H */

@@ -1,0 +1,307 @@
+"""Generate the golden fixtures of tests/golden/ by running the REFERENCE itself.
+
+The reference's segmentation4D.c and mcf_4D.c are compiled from their own,
+unmodified sources into oracle/_ref/ (``make -C oracle ref``; needs the
+reference checkout, so this script runs only where it is present).  This
+script drives them through their global variables and functions exactly as
+their main() does, captures what they print (iteration counts, residuals),
+and stores inputs and outputs as .npz files:
+
+  seg_small.npz   scene kind 1 at 10x8x6x4: edge detector (presmoothing + 8
+                  face g), 5 segmentation time steps (u, prev_u after each,
+                  the coefficients of step 1, iteration counts, residuals,
+                  ||u - prev_u||), masks of the last step
+  seg_balls.npz   the reference main's own parameters (h = tau = 0.01, K = 1,
+                  eps2 = 1, theta = rho = 0.5) with rescale balls: local
+                  thresholding, edge detector with a thresholded image,
+                  initial function in the balls, Mmask, 3 time steps
+  mcf_small.npz   MCF known-answer problem at n = 8 (3 steps) and the
+                  error history at n = 16 (4 steps)
+  seg_config1.npz the 32^3 x 8 scene, 20 steps: per-step iteration counts,
+                  residuals, ||u - prev_u||, u at 4096 fixed probe voxels,
+                  checksums, and the final masks (bit-packed)
+
+Usage:  python tests/golden/make_golden.py   (from the repository root)
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+OUT = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = os.path.join(ROOT, "oracle", "_ref")
+sys.path.insert(0, os.path.join(ROOT, "4d-image-segmentation-algorithm_gb300"))
+import ss4d  # noqa: E402  (scene generator and parameter sets only)
+
+libc = C.CDLL(None)
+
+
+class Captured:
+    """Redirect fd 1 while the reference prints, then return its text."""
+
+    def __enter__(self):
+        libc.fflush(None)
+        self.tmp = tempfile.TemporaryFile(mode="w+b")
+        self.saved = os.dup(1)
+        os.dup2(self.tmp.fileno(), 1)
+        return self
+
+    def __exit__(self, *a):
+        libc.fflush(None)
+        os.dup2(self.saved, 1)
+        os.close(self.saved)
+        self.tmp.seek(0)
+        self.text = self.tmp.read().decode()
+        self.tmp.close()
+
+
+class Ref:
+    """One compiled reference program, driven through its globals."""
+
+    def __init__(self, so: str):
+        self.L = C.CDLL(so, mode=os.RTLD_LOCAL)
+        self.keep = []
+
+    def i(self, name, v=None):
+        x = C.c_int.in_dll(self.L, name)
+        if v is not None:
+            x.value = int(v)
+        return x.value
+
+    def d(self, name, v=None):
+        x = C.c_double.in_dll(self.L, name)
+        if v is not None:
+            x.value = float(v)
+        return x.value
+
+    def arr(self, name, shape):
+        addr = C.c_void_p.in_dll(self.L, name).value
+        n = int(np.prod(shape))
+        return np.ctypeslib.as_array((C.c_double * n).from_address(addr)).reshape(shape)
+
+    def call(self, fn, *args, restype=C.c_bool):
+        f = getattr(self.L, fn)
+        f.restype = restype
+        with Captured() as cap:
+            r = f(*args)
+        return r, cap.text
+
+
+def build_ref():
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+
+
+def parse_steps(text):
+    its = [int(m) for m in re.findall(r"total number of RBSOR is (\d+)", text)]
+    res = [float(m) for m in re.findall(r"Mean square residue is (\S+)", text)]
+    return its, res
+
+
+def seg_setup(R: Ref, shape, p, centers=None):
+    lM, kM, jM, iM = shape
+    R.i("iMax", iM), R.i("jMax", jM), R.i("kMax", kM), R.i("lMax", lM)
+    noc = (C.c_int * lM)(*([0] * lM))
+    if centers:
+        for l, c in centers.items():
+            noc[l] = len(c)
+    R.keep.append(noc)
+    C.c_void_p.in_dll(R.L, "no_of_centers").value = C.addressof(noc)
+    for name in ("K", "eps2", "tau", "h", "omega_c", "gsTol", "segTol", "sigma", "omega_sigma",
+                 "maxNoGSIteration_sigma", "theta_img", "rho_thr", "ballRadius"):
+        R.d(name, getattr(p, name))
+    R.i("maxNoGSIteration", p.maxNoGSIteration)
+    R.i("maxNoOfTimeSteps", p.maxNoOfTimeSteps)
+    ok, _ = R.call("_allocateMem_")
+    assert ok
+    if centers:
+        pp = C.POINTER(C.POINTER(C.c_double))
+        cx, cy, cz = (pp.in_dll(R.L, n) for n in ("center_x", "center_y", "center_z"))
+        for l, cs in centers.items():
+            for c, (x, y, z) in enumerate(cs):
+                cx[l][c], cy[l][c], cz[l][c] = x, y, z
+
+
+def seg_small():
+    R = Ref(os.path.join(REF_DIR, "libref_seg.so"))
+    nx, ny, nz, nt = 10, 8, 6, 4
+    p = ss4d.scene_params(maxNoOfTimeSteps=5)
+    i0_in, u0 = ss4d.scene(1, nx, ny, nz, nt, seed=7)
+    shape = i0_in.shape
+    seg_setup(R, shape, p)
+    i0 = R.arr("i0", shape)
+    u = R.arr("u", shape)
+    prev = R.arr("prev_u", shape)
+    i0[...] = i0_in
+    R.arr("Mmask", shape)[...] = 1.0  # no centres: the per-step rescale is the identity
+    thr_in = u.copy()  # the thresholded-image buffer (u, all zeros here)
+    _, t_gf = R.call("_gf_inputImage_plus_thresholdedImage_", C.c_void_p(i0.ctypes.data),
+                     C.c_void_p(u.ctypes.data))
+    ps = [int(m) for m in re.findall(r"total number of RBSOR is (\d+)", t_gf)]
+    out = {"i0_in": i0_in, "thr_in": thr_in, "u0": u0, "i0_smooth": i0.copy(), "thr_smooth": u.copy(),
+           "presmooth_its": np.array(ps)}
+    for f, nm in enumerate(("g_e", "g_w", "g_n", "g_s", "g_t", "g_b", "g_fw", "g_bw")):
+        out[f"g{f}"] = R.arr(nm, shape).copy()
+    u[...] = u0
+    its, res, l2 = [], [], []
+    us = []
+    for step in range(1, 6):
+        R.i("numberOfTimeStep", step)
+        _, txt = R.call("_segTimeStep_")
+        a, b = parse_steps(txt)
+        its += a
+        res += b
+        d, _ = R.call("_l2norm_", C.c_void_p(prev.ctypes.data), C.c_void_p(u.ctypes.data), restype=C.c_double)
+        l2.append(d)
+        us.append(u.copy())
+        if step == 1:
+            out["prev1"] = prev.copy()
+            for f, nm in enumerate(("e", "w", "n", "s", "t", "b", "fw", "bw")):
+                out[f"coef{f}"] = R.arr(nm, shape).copy()
+    out["u_steps"] = np.stack(us)
+    out["its"] = np.array(its)
+    out["res"] = np.array(res)
+    out["l2"] = np.array(l2)
+    mass, _ = R.call("_mass4D_", C.c_void_p(u.ctypes.data), restype=C.c_double)
+    out["mass"] = np.array(mass)
+    out["params"] = np.array([p.as_dict()[k] for k in sorted(p.as_dict())])
+    out["param_names"] = np.array(sorted(p.as_dict()))
+    np.savez_compressed(os.path.join(OUT, "seg_small.npz"), **out)
+    print("seg_small:", its, ["%.3e" % r for r in res])
+
+
+def seg_balls():
+    """The reference main's parameter set with balls (segmentation4D.c:1338-1371)."""
+    R = Ref(os.path.join(REF_DIR, "libref_seg.so"))
+    nx, ny, nz, nt = 12, 12, 10, 3
+    p = ss4d.Params(K=1.0, eps2=1.0, tau=0.01, h=0.01, omega_c=1.8, gsTol=1e-12, maxNoGSIteration=5,
+                    maxNoOfTimeSteps=3, segTol=1e-12, sigma=0.01 * 0.01 / 8, omega_sigma=1.3,
+                    maxNoGSIteration_sigma=10.0, theta_img=0.5, rho_thr=0.5, ballRadius=3.0)
+    i0_in, _ = ss4d.scene(1, nx, ny, nz, nt, seed=11)
+    shape = i0_in.shape
+    centers = {1: [(6.0, 6.0, 5.0), (8.0, 7.0, 6.0)], 2: [(6.0, 7.0, 5.0)], 3: [(7.0, 6.0, 5.0), (5.0, 5.0, 4.0)]}
+    seg_setup(R, shape, p, centers)
+    R.d("alpha", 0.85), R.d("beta", 0.15)
+    i0 = R.arr("i0", shape)
+    u = R.arr("u", shape)
+    prev = R.arr("prev_u", shape)
+    mm = R.arr("Mmask", shape)
+    i0[...] = i0_in
+    out = {"i0_in": i0_in}
+    R.call("_locallyThreshold4Ddata_", C.c_void_p(i0.ctypes.data), C.c_void_p(u.ctypes.data))
+    out["thr_in"] = u.copy()
+    R.call("_gf_inputImage_plus_thresholdedImage_", C.c_void_p(i0.ctypes.data), C.c_void_p(u.ctypes.data))
+    out["i0_smooth"] = i0.copy()
+    out["thr_smooth"] = u.copy()
+    for f, nm in enumerate(("g_e", "g_w", "g_n", "g_s", "g_t", "g_b", "g_fw", "g_bw")):
+        out[f"g{f}"] = R.arr(nm, shape).copy()
+    R.call("_generate4DsegmFunct_", C.c_void_p(u.ctypes.data))
+    out["u_gen"] = u.copy()
+    out["mmask"] = mm.copy()
+    R.call("_rescale4DdataToZeroOne_", C.c_void_p(u.ctypes.data))
+    out["u0"] = u.copy()
+    its, res, us = [], [], []
+    for step in range(1, 4):
+        R.i("numberOfTimeStep", step)
+        _, txt = R.call("_segTimeStep_")
+        a, b = parse_steps(txt)
+        its += a
+        res += b
+        us.append(u.copy())
+    out["u_steps"] = np.stack(us)
+    out["its"] = np.array(its)
+    out["res"] = np.array(res)
+    balls = [(l, x, y, z) for l in sorted(centers) for (x, y, z) in centers[l]]
+    out["balls"] = np.array(balls, dtype=np.float64)
+    out["params"] = np.array([p.as_dict()[k] for k in sorted(p.as_dict())])
+    out["param_names"] = np.array(sorted(p.as_dict()))
+    np.savez_compressed(os.path.join(OUT, "seg_balls.npz"), **out)
+    print("seg_balls:", its)
+
+
+def mcf_run(n: int, steps: int):
+    R = Ref(os.path.join(REF_DIR, "libref_mcf.so"))
+    M = n + 2
+    for nm in ("iMax", "jMax", "kMax", "lMax"):
+        R.i(nm, M)
+    p = ss4d.mcf_params(n, steps)
+    for nm in ("eps2", "tau", "h", "omega_c", "gsTol"):
+        R.d(nm, getattr(p, nm))
+    R.i("maxNoGSIteration", p.maxNoGSIteration)
+    R.i("maxNoOfTimeSteps", steps)
+    R.d("mcfTol", 1e-12)
+    R.call("_allocateMem_mcf")
+    shape = (M, M, M, M)
+    u = R.arr("u", shape)
+    ex = R.arr("exact_u", shape)
+    R.call("_exactSolution_mcf", C.c_double(0.0), restype=None)
+    u[...] = ex
+    errs, its, us = [], [], []
+    for step in range(1, steps + 1):
+        R.i("numberOfTimeStep", step)
+        _, txt = R.call("_mcfTimeStep")
+        its += [1 for _ in re.findall(r"Residuum is", txt)]
+        R.call("_exactSolution_mcf", C.c_double(step * p.tau), restype=None)
+        e, _ = R.call("_l2norm_mcf", C.c_void_p(ex.ctypes.data), C.c_void_p(u.ctypes.data), restype=C.c_double)
+        errs.append(e)
+        us.append(u.copy())
+    return np.stack(us), np.array(errs)
+
+
+def mcf_small():
+    u8, e8 = mcf_run(8, 3)
+    _, e16 = mcf_run(16, 4)
+    np.savez_compressed(os.path.join(OUT, "mcf_small.npz"), u8=u8, err8=e8, err16=e16)
+    print("mcf: err8", e8, "err16", e16)
+
+
+def seg_config1():
+    R = Ref(os.path.join(REF_DIR, "libref_seg.so"))
+    nx, ny, nz, nt = 32, 32, 32, 8
+    p = ss4d.scene_params(maxNoOfTimeSteps=20)
+    i0_in, u0 = ss4d.scene(1, nx, ny, nz, nt, seed=1)
+    shape = i0_in.shape
+    seg_setup(R, shape, p)
+    i0 = R.arr("i0", shape)
+    u = R.arr("u", shape)
+    prev = R.arr("prev_u", shape)
+    i0[...] = i0_in
+    R.arr("Mmask", shape)[...] = 1.0  # no centres: the per-step rescale is the identity
+    R.call("_gf_inputImage_plus_thresholdedImage_", C.c_void_p(i0.ctypes.data), C.c_void_p(u.ctypes.data))
+    u[...] = u0
+    rng = np.random.default_rng(1234)
+    probes = rng.integers(0, u.size, 4096)
+    its, res, l2, probe_vals, sums = [], [], [], [], []
+    for step in range(1, 21):
+        R.i("numberOfTimeStep", step)
+        _, txt = R.call("_segTimeStep_")
+        a, b = parse_steps(txt)
+        its += a
+        res += b
+        d, _ = R.call("_l2norm_", C.c_void_p(prev.ctypes.data), C.c_void_p(u.ctypes.data), restype=C.c_double)
+        l2.append(d)
+        probe_vals.append(u.reshape(-1)[probes].copy())
+        sums.append((u.sum(), (u * u).sum()))
+    inner = u[1:-1, 1:-1, 1:-1, 1:-1]
+    m05 = (inner >= 0.5).astype(np.uint8).reshape(-1)
+    lo, hi = inner.min(), inner.max()
+    mnorm = (inner >= lo + 0.5 * (hi - lo)).astype(np.uint8).reshape(-1)
+    np.savez_compressed(os.path.join(OUT, "seg_config1.npz"), its=np.array(its), res=np.array(res),
+                        l2=np.array(l2), probes=probes, probe_vals=np.stack(probe_vals), sums=np.array(sums),
+                        mask05=np.packbits(m05), masknorm=np.packbits(mnorm), seed=1,
+                        dims=np.array([nx, ny, nz, nt]))
+    print("config1: its", its)
+
+
+if __name__ == "__main__":
+    build_ref()
+    seg_small()
+    seg_balls()
+    mcf_small()
+    seg_config1()

@@ -1,0 +1,258 @@
+"""CUDA path vs the reference (golden fixtures) and the oracle, through the C ABI.
+
+Bars (the benchmark spec): the plain FP64 forms match the reference's red-black SOR
+to <= 1e-10 relative in u per time step with the same iteration counts, and
+masks are bit-exact.  The reference-order kernels (SS4D_ARITH_REFERENCE) are
+held to 1e-13 (they differ from the reference only where it calls pow()).
+The mixed form must reach the same FP64 residual tolerance every step.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, params_from_golden, rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"reference": 1e-13, "fp64": 1e-10}
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).to("cuda")
+
+
+def host(t):
+    return t.detach().cpu().numpy()
+
+
+def zeros8(torch, shape):
+    return [torch.zeros(shape, dtype=torch.float64, device="cuda") for _ in range(8)]
+
+
+@pytest.mark.parametrize("fixture", ["seg_small.npz", "seg_balls.npz"])
+def test_edge_detector_matches_reference(ss4d, cuda, fixture):
+    torch = cuda
+    d = load_golden(fixture)
+    p = params_from_golden(ss4d, d)
+    shape = d["i0_in"].shape
+    i0 = dev(torch, d["i0_in"])
+    thr = dev(torch, d["thr_in"])
+    g = zeros8(torch, shape)
+    with ss4d.Solver(*shape[::-1], arith="reference") as S:
+        S.edge_detector(p, i0, thr, g)
+        S.synchronize()
+    assert np.array_equal(host(i0), d["i0_smooth"])
+    assert np.array_equal(host(thr), d["thr_smooth"])
+    for f in range(8):
+        assert np.array_equal(host(g[f]), d[f"g{f}"]), f"g face {f}"
+
+
+def test_coefficients_match_reference(ss4d, cuda):
+    torch = cuda
+    d = load_golden("seg_small.npz")
+    p = params_from_golden(ss4d, d)
+    shape = d["u0"].shape
+    u = dev(torch, d["u0"])
+    g = [dev(torch, d[f"g{f}"]) for f in range(8)]
+    coef = zeros8(torch, shape)
+    with ss4d.Solver(*shape[::-1], arith="reference") as S:
+        S.gs_coefficients(p, u, g, coef)
+        S.synchronize()
+    for f in range(8):
+        assert rel_err(host(coef[f]), d[f"coef{f}"]) <= 4e-16, f"coefficient {f}"
+
+
+@pytest.mark.parametrize("arith", ["reference", "fp64"])
+@pytest.mark.parametrize("graph", [True, False])
+def test_seg_time_steps_match_reference(ss4d, cuda, arith, graph):
+    if arith == "reference" and not graph:
+        pytest.skip("the reference form has no graph")
+    torch = cuda
+    d = load_golden("seg_small.npz")
+    p = params_from_golden(ss4d, d)
+    shape = d["u0"].shape
+    u = dev(torch, d["u0"])
+    prev = torch.zeros_like(u)
+    mm = torch.ones_like(u)
+    g = [dev(torch, d[f"g{f}"]) for f in range(8)]
+    with ss4d.Solver(*shape[::-1], arith=arith) as S:
+        S.set_graph(graph)
+        for step in range(5):
+            st = S.seg_time_step(p, u, prev, g, mmask=mm)
+            assert st["iterations"] == d["its"][step], f"step {step + 1}"
+            assert rel_err(st["residual"], d["res"][step]) < 1e-5  # printed with 7 digits
+            assert rel_err(host(u), d["u_steps"][step]) <= TOL[arith], f"u after step {step + 1}"
+            assert abs(S.l2norm(p.h, prev, u) - d["l2"][step]) <= 1e-10 * d["l2"][step]
+
+
+@pytest.mark.parametrize("arith", ["reference", "fp64", "mixed"])
+def test_seg_balls_rescale_path(ss4d, cuda, arith):
+    torch = cuda
+    d = load_golden("seg_balls.npz")
+    p = params_from_golden(ss4d, d)
+    balls = [(int(b[0]), b[1], b[2], b[3]) for b in d["balls"]]
+    shape = d["u0"].shape
+    g = [dev(torch, d[f"g{f}"]) for f in range(8)]
+    mm = dev(torch, d["mmask"])
+    u = dev(torch, d["u_gen"])
+    prev = torch.zeros_like(u)
+    with ss4d.Solver(*shape[::-1], arith=arith) as S:
+        S.rescale_to_zero_one(p, u, mm, balls)
+        S.synchronize()
+        assert rel_err(host(u), d["u0"]) <= 1e-15
+        for step in range(3):
+            st = S.seg_time_step(p, u, prev, g, mmask=mm, balls=balls)
+            if arith == "mixed":
+                # five iterations are the cap here: both stop at the cap
+                assert st["iterations"] <= p.maxNoGSIteration
+                assert rel_err(host(u), d["u_steps"][step]) <= 1e-5
+            else:
+                assert st["iterations"] == d["its"][step]
+                assert rel_err(host(u), d["u_steps"][step]) <= TOL[arith]
+
+
+def test_rescale_rejects_ball_outside_array(ss4d, cuda):
+    torch = cuda
+    p = ss4d.scene_params(ballRadius=3.0)
+    u = torch.zeros((5, 8, 8, 8), dtype=torch.float64, device="cuda")
+    with ss4d.Solver(8, 8, 8, 5) as S:
+        with pytest.raises(ss4d.SS4DError) as ei:
+            S.rescale_to_zero_one(p, u, None, [(1, 1.0, 4.0, 4.0)])
+        assert ei.value.status == 1
+
+
+@pytest.mark.parametrize("arith", ["reference", "fp64"])
+def test_mcf_known_answer(ss4d, cuda, arith):
+    torch = cuda
+    d = load_golden("mcf_small.npz")
+    for n, steps, key in ((8, 3, "err8"), (16, 4, "err16")):
+        p = ss4d.mcf_params(n, steps)
+        shape = (n + 2,) * 4
+        u = torch.zeros(shape, dtype=torch.float64, device="cuda")
+        ex = torch.zeros_like(u)
+        prev = torch.zeros_like(u)
+        with ss4d.Solver(*shape, arith=arith) as S:
+            S.mcf_exact_solution(p.h, 0.0, u)
+            for step in range(1, steps + 1):
+                S.mcf_time_step(p, step, u, prev)
+                S.mcf_exact_solution(p.h, step * p.tau, ex)
+                err = S.l2norm(p.h, ex, u)
+                assert abs(err - d[key][step - 1]) <= 1e-10 * d[key][step - 1]
+                if n == 8:
+                    assert rel_err(host(u), d["u8"][step - 1]) <= TOL[arith]
+
+
+def test_mcf_boundary_matches_oracle(ss4d, oracle, cuda):
+    torch = cuda
+    shape = (6, 5, 7, 8)  # lMax, kMax, jMax, iMax: unequal extents
+    h, t = 0.3125, 0.77
+    u0 = np.random.default_rng(0).standard_normal(shape)
+    want = u0.copy()
+    oracle.mcf_boundary(h, t, want)
+    u = dev(torch, u0)
+    with ss4d.Solver(*shape[::-1]) as S:
+        S.mcf_set_boundary_exact(h, t, u)
+        S.synchronize()
+    assert np.array_equal(host(u), want)
+
+
+@pytest.mark.parametrize("arith", ["reference", "fp64"])
+def test_config1_twenty_steps_match_reference(ss4d, oracle, cuda, arith):
+    """32^3 x 8, 20 steps: iteration counts, step differences, probes and
+    both masks against the reference's run."""
+    torch = cuda
+    d = load_golden("seg_config1.npz")
+    nx, ny, nz, nt = (int(v) for v in d["dims"])
+    p = ss4d.scene_params(maxNoOfTimeSteps=20)
+    i0h, u0h = ss4d.scene(1, nx, ny, nz, nt, seed=int(d["seed"]))
+    shape = i0h.shape
+    i0 = dev(torch, i0h)
+    thr = torch.zeros_like(i0)
+    g = zeros8(torch, shape)
+    u = dev(torch, u0h)
+    prev = torch.zeros_like(u)
+    mm = torch.ones_like(u)
+    nint = nx * ny * nz * nt
+    m05 = torch.zeros(nint, dtype=torch.uint8, device="cuda")
+    mn = torch.zeros_like(m05)
+    with ss4d.Solver(*shape[::-1], arith=arith) as S:
+        S.edge_detector(p, i0, thr, g)
+        for step in range(20):
+            st = S.seg_time_step(p, u, prev, g, mmask=mm)
+            assert st["iterations"] == d["its"][step], f"step {step + 1}"
+            assert abs(S.l2norm(p.h, prev, u) - d["l2"][step]) <= 1e-10 * d["l2"][step]
+            got = host(u).reshape(-1)[d["probes"]]
+            assert rel_err(got, d["probe_vals"][step]) <= TOL[arith]
+        S.threshold_mask(u, m05, 0.5, False)
+        S.threshold_mask(u, mn, 0.5, True)
+        S.synchronize()
+    assert np.array_equal(np.packbits(host(m05)), d["mask05"])
+    assert np.array_equal(np.packbits(host(mn)), d["masknorm"])
+
+
+def test_sor_solve_with_injected_coefficients(ss4d, cuda):
+    """The SOR loop alone on the reference's own step-1 coefficients."""
+    torch = cuda
+    d = load_golden("seg_small.npz")
+    p = params_from_golden(ss4d, d)
+    coef = [dev(torch, d[f"coef{f}"]) for f in range(8)]
+    for arith, tol in (("reference", 1e-13), ("fp64", 1e-10)):
+        u = dev(torch, d["u0"])
+        prev = dev(torch, d["prev1"])
+        with ss4d.Solver(*d["u0"].shape[::-1], arith=arith) as S:
+            st = S.sor_solve(p, u, prev, coef)
+        assert st["iterations"] == d["its"][0]
+        assert rel_err(host(u), d["u_steps"][0]) <= tol
+
+
+@pytest.mark.parametrize("dims", [(9, 7, 5, 3), (1, 1, 1, 1), (33, 6, 4, 2), (2, 3, 2, 5)])
+@pytest.mark.parametrize("arith", ["reference", "fp64", "mixed"])
+def test_ragged_and_minimal_sizes_match_oracle(ss4d, oracle, cuda, dims, arith):
+    torch = cuda
+    nx, ny, nz, nt = dims
+    p = ss4d.scene_params(gsTol=1e-14)
+    i0h, u0h = ss4d.scene(1, nx, ny, nz, nt, seed=9)
+    g = oracle.gfaces(p, i0h, np.zeros_like(i0h))
+    want = u0h.copy()
+    oprev = np.zeros_like(want)
+    zs = []
+    for _ in range(2):
+        z, _ = oracle.seg_time_step(p, want, oprev, g, mmask=np.ones_like(want))
+        zs.append(z)
+    u = dev(torch, u0h)
+    prev = torch.zeros_like(u)
+    gd = [dev(torch, a) for a in g]
+    with ss4d.Solver(*u0h.shape[::-1], arith=arith) as S:
+        for step in range(2):
+            st = S.seg_time_step(p, u, prev, gd)
+            if arith != "mixed":
+                assert st["iterations"] == zs[step]
+            else:
+                assert st["residual"] <= p.gsTol
+    tol = {"reference": 1e-13, "fp64": 1e-10, "mixed": 1e-6}[arith]
+    assert rel_err(host(u), want) <= tol
+
+
+def test_nonfinite_input_is_reported(ss4d, cuda):
+    torch = cuda
+    p = ss4d.scene_params()
+    i0h, u0h = ss4d.scene(1, 8, 8, 8, 3, seed=2)
+    u0h[2, 4, 4, 4] = np.nan
+    u = dev(torch, u0h)
+    g = [torch.ones_like(u) for _ in range(8)]
+    for arith in ("reference", "fp64", "mixed"):
+        with ss4d.Solver(*u0h.shape[::-1], arith=arith) as S:
+            with pytest.raises(ss4d.SS4DError) as ei:
+                S.seg_time_step(p, u.clone(), None, g)
+            assert ei.value.status == 4  # SS4D_ERR_NONFINITE
+
+
+def test_norms_match_oracle(ss4d, oracle, cuda):
+    torch = cuda
+    rng = np.random.default_rng(5)
+    a = rng.standard_normal((5, 6, 7, 9))
+    b = rng.standard_normal((5, 6, 7, 9))
+    with ss4d.Solver(9, 7, 6, 5) as S:
+        l2 = S.l2norm(0.5, dev(torch, a), dev(torch, b))
+        m = S.mass(0.5, dev(torch, a))
+    assert abs(l2 - oracle.l2norm(0.5, a, b)) <= 1e-13 * abs(l2)
+    assert abs(m - oracle.mass(0.5, a)) <= 1e-12 * max(1.0, abs(m))

@@ -221,8 +221,12 @@ extern "C" ss4d_status ss4d_solver_create(const ss4d_dims *dims, ss4d_arith arit
         long long need = nb * 2;
         if (need < 8192)
             need = 8192;
-        if (need < 2LL * s->cfg.grid)
-            need = 2LL * s->cfg.grid;
+        // room for the partials of the largest persistent grid any tiling allows
+        const long long gmax = (long long)s->sm_count * (max_blocks_sweep64() > max_blocks_sweep32()
+                                                             ? max_blocks_sweep64()
+                                                             : max_blocks_sweep32());
+        if (need < 2LL * gmax)
+            need = 2LL * gmax;
         s->n_partial = need;
     }
     if ((st = dmalloc(s, (void **)&s->d_partial, sizeof(double) * s->n_partial)) != SS4D_OK)
@@ -267,8 +271,9 @@ extern "C" ss4d_status ss4d_solver_destroy(ss4d_solver *s)
     if (s->stream || s->cap)
         cudaStreamSynchronize(s->stream);
     free_graphs(s);
+    // allocation bases only: R[1], Bk, P[1], coef[1], ... point inside them
     void *dev[] = {s->d_partial, s->d_scalar, s->d_state, s->d_params, s->d_scratch, s->d_coef_nat,
-                   s->sb.R[0], s->sb.Bk, s->sb.P[0], s->sb.coef[0], s->sb.coef32[0], s->sb.dR[0], s->sb.r32[0],
+                   s->sb.R[0], s->sb.P[0], s->sb.coef[0], s->sb.coef32[0], s->sb.dR[0], s->sb.r32[0],
                    s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz};
     for (void *p : dev)
         if (p)
@@ -305,6 +310,20 @@ extern "C" ss4d_status ss4d_solver_set_arith(ss4d_solver *s, ss4d_arith arith)
     REQ(s, "solver is NULL");
     REQ(arith == SS4D_ARITH_REFERENCE || arith == SS4D_ARITH_FP64 || arith == SS4D_ARITH_MIXED, "unknown arithmetic");
     s->arith = arith;
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_solver_set_tiling(ss4d_solver *s, int k_block, int max_grid)
+{
+    REQ(s, "solver is NULL");
+    REQ(k_block >= 1 && max_grid >= 0, "k_block must be >= 1 and max_grid >= 0");
+    SweepCfg c = make_sweep_cfg(s->geo, s->sp, s->sm_count, k_block);
+    if (max_grid > 0 && c.grid > max_grid)
+        c.grid = max_grid;
+    REQ(2LL * c.grid <= s->n_partial, "grid larger than the partial-sum buffer");
+    s->cfg = c;
+    s->sb.partial[1] = s->d_partial + c.grid;
+    free_graphs(s); // kernel arguments changed
     return SS4D_OK;
 }
 

@@ -367,7 +367,9 @@ __global__ void __launch_bounds__(256) k_refine(Geo g, Split sp, SweepCfg cfg, S
         const double r = fma(diag, u0, -(S + ld_stream(pv + s)));
         acc = fma(r, r, acc);
         own[s] = u0;
-        rr[s] = (float)r;
+        // r = A u - b here; the correction d with A d = b - A u moves u to the
+        // solution, so the FP32 sweeps get the negated residual
+        rr[s] = (float)(-r);
     }
     acc = block_sum(acc);
     if (threadIdx.x == 0)

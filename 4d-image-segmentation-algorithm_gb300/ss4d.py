@@ -111,6 +111,7 @@ def lib() -> C.CDLL:
         "ss4d_solver_set_graph": ([vp, C.c_int], st),
         "ss4d_solver_workspace_bytes": ([vp, C.POINTER(C.c_size_t)], st),
         "ss4d_solver_set_timing": ([vp, C.c_int], st),
+        "ss4d_solver_set_tiling": ([vp, C.c_int, C.c_int], st),
         "ss4d_solver_kernel_time": ([vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong)], st),
         "ss4d_solver_reset_timing": ([vp], st),
         "ss4d_solver_launch_count": ([vp, C.POINTER(C.c_longlong)], st),
@@ -244,6 +245,9 @@ class Solver:
 
     def set_stream(self, stream: int | None):
         _check(self.L.ss4d_solver_set_stream(self.h, stream), "set_stream")
+
+    def set_tiling(self, k_block: int, max_grid: int = 0):
+        _check(self.L.ss4d_solver_set_tiling(self.h, k_block, max_grid), "set_tiling")
 
     KERNELS = ("sweep64", "sweep32", "refine", "assemble", "pack")
 

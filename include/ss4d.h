@@ -125,6 +125,10 @@ ss4d_status ss4d_solver_create(const ss4d_dims *dims, ss4d_arith arith, void *st
 ss4d_status ss4d_solver_destroy(ss4d_solver *s);
 ss4d_status ss4d_solver_set_stream(ss4d_solver *s, void *stream);
 ss4d_status ss4d_solver_set_arith(ss4d_solver *s, ss4d_arith arith);
+/* Tile schedule of the colour-split sweeps: k_block = depth of the k blocks
+ * in the tile order (>= 1), max_grid caps the persistent grid (0 = as many
+ * blocks as fit on the device).  Results do not depend on either. */
+ss4d_status ss4d_solver_set_tiling(ss4d_solver *s, int k_block, int max_grid);
 /* Use (1) or bypass (0) the CUDA-graph form of the sweep loop (default 1). */
 ss4d_status ss4d_solver_set_graph(ss4d_solver *s, int enable);
 /* Per-kernel timing.  While enabled, the sweep loop runs host-driven (not

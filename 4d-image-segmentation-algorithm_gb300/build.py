@@ -32,6 +32,7 @@ CUDA_UNITS = {
     "ss4d_kernels_ref.cu": ["--fmad=false"],
     "ss4d_kernels_fast.cu": [],
     "ss4d_api.cu": [],
+    "ss4d_noalloc.cu": [],
 }
 C_UNITS = {"ss4d_scene.c": ["-fopenmp"]}
 

@@ -53,6 +53,12 @@ static void set_err(const char *fmt, ...)
         }                                                                                                          \
     } while (0)
 
+// error text for entry points defined in other translation units
+void ss4d::set_error_text(const char *msg)
+{
+    snprintf(g_err, sizeof g_err, "%s", msg);
+}
+
 static ss4d_status last_launch()
 {
     cudaError_t e = cudaGetLastError();

@@ -123,4 +123,7 @@ void launch_ctrl_mixed(SplitBufs b, int nparts, const DevParams *dp, LoopState *
 int max_blocks_sweep64();
 int max_blocks_sweep32();
 
+// sets the text ss4d_last_error() returns (ss4d_api.cu)
+void set_error_text(const char *msg);
+
 } // namespace ss4d

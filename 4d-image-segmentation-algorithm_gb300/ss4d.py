@@ -123,6 +123,7 @@ def lib() -> C.CDLL:
         "ss4d_seg_time_step": ([vp, C.POINTER(Params), vp, vp, P8, vp, C.POINTER(Balls), C.POINTER(StepStats)], st),
         "ss4d_mcf_time_step": ([vp, C.POINTER(Params), C.c_int, vp, vp, C.POINTER(StepStats)], st),
         "ss4d_rescale_to_zero_one": ([vp, C.POINTER(Params), vp, vp, C.POINTER(Balls)], st),
+        "ss4d_rescale_to_zero_one_noalloc": ([C.POINTER(Dims), C.POINTER(Params), vp, vp, C.POINTER(Balls), vp], st),
         "ss4d_threshold_mask": ([vp, vp, C.c_double, C.c_int, vp], st),
         "ss4d_l2norm": ([vp, C.c_double, vp, vp, dp], st),
         "ss4d_mass": ([vp, C.c_double, vp, dp], st),
@@ -203,6 +204,18 @@ def _balls(balls):
     B = Balls(n, C.cast(keep[0], C.POINTER(C.c_int)), C.cast(keep[1], C.POINTER(C.c_double)),
               C.cast(keep[2], C.POINTER(C.c_double)), C.cast(keep[3], C.POINTER(C.c_double)))
     return B, keep
+
+
+def rescale_to_zero_one_noalloc(dims: tuple, p: Params, img, mmask=None, balls=None, stream: int | None = None):
+    """ss4d_rescale_to_zero_one_noalloc: the per-step rescale for callers that
+    cannot allocate device memory (no handle; fixed internal table of at most
+    SS4D_NOALLOC_MAX_BALLS centres and frames).  dims = (iMax, jMax, kMax, lMax)."""
+    B, keep = _balls(balls)
+    d = Dims(*dims)
+    _check(lib().ss4d_rescale_to_zero_one_noalloc(C.byref(d), C.byref(p), _ptr(img), _ptr(mmask),
+                                                   C.byref(B) if B is not None else None, stream),
+           "rescale_to_zero_one_noalloc")
+    del keep
 
 
 class Solver:

@@ -202,6 +202,26 @@ ss4d_status ss4d_mcf_time_step(ss4d_solver *s, const ss4d_params *p, int numberO
 ss4d_status ss4d_rescale_to_zero_one(ss4d_solver *s, const ss4d_params *p, double *d_img,
                                      const double *d_Mmask, const ss4d_balls *balls);
 
+/* The same rescale without any device allocation.  This entry point has no
+ * counterpart in the reference.  It is for callers that cannot allocate
+ * device memory: a host application that owns the whole GPU memory budget
+ * through its own pool and forbids further cudaMalloc, or a per-frame loop
+ * that must not pay cudaMalloc's implicit device synchronisation.  It takes
+ * no solver handle (a handle allocates its workspaces); the centre table and
+ * the per-frame index tables are staged in a fixed-size array inside this
+ * library (32 KB per device, kept until the process exits), which limits it
+ * to SS4D_NOALLOC_MAX_BALLS centres and lMax <= SS4D_NOALLOC_MAX_FRAMES;
+ * larger inputs return SS4D_ERR_INVALID.  The first call on a device looks
+ * up that array's device address (cudaGetSymbolAddress); make that first
+ * call before any stream capture.  All calls share the one array, so calls
+ * whose GPU work overlaps (different streams, or different host threads
+ * without ordering) race on it; issue them in one stream.  `stream` is a
+ * cudaStream_t (NULL = legacy default stream); the call is asynchronous. */
+#define SS4D_NOALLOC_MAX_BALLS 1024
+#define SS4D_NOALLOC_MAX_FRAMES 1024
+ss4d_status ss4d_rescale_to_zero_one_noalloc(const ss4d_dims *dims, const ss4d_params *p, double *d_img,
+                                             const double *d_Mmask, const ss4d_balls *balls, void *stream);
+
 /* Level-set threshold to a mask, as _writeData_mpi_ (segmentation4D_mpi.c:
  * 1470-1478): mask = (u >= level) for every interior voxel, written frame by
  * frame in (l, k, j, i) order, nx*ny*nz*nt bytes of 0/1.  With normalise != 0

@@ -183,7 +183,7 @@ static ss4d_status check_dims(const ss4d_dims *d)
     REQ(d->iMax >= 3 && d->jMax >= 3 && d->kMax >= 3 && d->lMax >= 3, "every padded extent must be >= 3");
     const long long n = (long long)d->iMax * d->jMax * d->kMax * d->lMax;
     REQ(n < (1LL << 31), "padded volume must hold fewer than 2^31 voxels (the reference's int indexing)");
-    REQ((long long)(d->kMax - 2) * (d->lMax - 2) <= 65535, "(kMax-2)*(lMax-2) must not exceed 65535");
+    REQ((long long)(d->kMax - 1) * (d->lMax - 1) <= 65535, "(kMax-1)*(lMax-1) must not exceed 65535");
     return SS4D_OK;
 }
 
@@ -279,7 +279,7 @@ extern "C" ss4d_status ss4d_solver_destroy(ss4d_solver *s)
     free_graphs(s);
     // allocation bases only: R[1], Bk, P[1], coef[1], ... point inside them
     void *dev[] = {s->d_partial, s->d_scalar, s->d_state, s->d_params, s->d_scratch, s->d_coef_nat,
-                   s->sb.R[0], s->sb.P[0], s->sb.coef[0], s->sb.coef32[0], s->sb.dR[0], s->sb.r32[0],
+                   s->sb.R[0], s->sb.P[0], s->sb.coef[0], s->sb.coef32[0], s->sb.dR[0], s->sb.r32[0], s->sb.fn[0],
                    s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz};
     for (void *p : dev)
         if (p)
@@ -393,6 +393,12 @@ static ss4d_status ensure_split(ss4d_solver *s, int mixed)
         s->sb.coef[1] = cf + 10 * cs;
         s->sb.partial[0] = s->d_partial;
         s->sb.partial[1] = s->d_partial + s->cfg.grid;
+        double *faces = nullptr; // 4 face norms + 4 face g/norm arrays, natural layout
+        CKS(dmalloc(s, (void **)&faces, sizeof(double) * 8 * (size_t)s->geo.n));
+        for (int d = 0; d < 4; ++d) {
+            s->sb.fn[d] = faces + (size_t)d * s->geo.n;
+            s->sb.fq[d] = faces + (size_t)(4 + d) * s->geo.n;
+        }
         s->have_split = 1;
     }
     if (mixed && !s->have_mixed) {

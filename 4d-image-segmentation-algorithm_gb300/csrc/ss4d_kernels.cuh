@@ -82,6 +82,10 @@ struct SplitBufs {
     float *dB;          // mixed: black correction
     float *r32[2];      // mixed: FP64 residual rounded to FP32, per colour
     double *partial[2]; // per-block residual partials of the red [0] / black [1] kernels
+    // assembly: per voxel v and axis d, the quantities of the face between v
+    // and v + e_d (natural layout): |grad u|_eps and g/|grad u|_eps
+    double *fn[4];
+    double *fq[4];
 };
 
 struct SweepCfg {

@@ -81,28 +81,84 @@ __device__ __forceinline__ TileCoord tile_coord(const Geo &g, const SweepCfg &cf
 }
 
 // ---------------------------------------------------------------------------
-// assembly: the reference's _gs_coefficients_ per voxel, written to the split
-// coefficient arrays (FP64, and FP32 copies of c*a_f for the mixed form).
+// assembly: the reference's _gs_coefficients_ (segmentation4D.c:446-580) in
+// two passes.  The reference evaluates every face twice (the east face of
+// voxel i is the west face of voxel i+1, with identical bits); here k_faces
+// evaluates each face once, for the face between v and v + e_d, and stores
+// its norm |grad u|_eps and g/|grad u|_eps; k_voxel_coef then forms the voxel
+// value vc = sqrt(mean^2 + eps2) and c*a_f = c*vc*g_f/|grad u|_f.
+// 1/sqrt comes from an FP32 seed refined by one FP64 Newton step (relative
+// error ~2e-14), which replaces an FP64 square root and division per face;
+// FP64 runs at 1/68 of the FP32 rate on GB300, so these passes are bounded
+// by the FP64 pipe, not by HBM.
 
-__device__ __forceinline__ double face_sq_fast(const double *v, long long c, long long nb, const long long st[4],
-                                               int d, double ih, double iq)
+// 1/sqrt(x), x > 0: FP32 seed + one Newton step
+__device__ __forceinline__ double rsqrt_nr(double x)
 {
-    double s = 0.0;
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-        double comp;
-        if (a == d)
-            comp = (v[nb] - v[c]) * ih;
-        else
-            comp = ((v[nb + st[a]] + v[c + st[a]]) - (v[nb - st[a]] + v[c - st[a]])) * iq;
-        s = fma(comp, comp, s);
-    }
-    return s;
+    const double y0 = (double)rsqrtf((float)x);
+    const double e = fma(-x * y0, y0, 1.0); // 1 - x y0^2
+    return fma(0.5 * y0, e, y0);
 }
 
-__global__ void __launch_bounds__(256) k_assemble(Geo g, Split sp, const double *__restrict__ u, CPtrs8 gin,
-                                                  int has_g, double h, double eps2, double c, double omega, SplitBufs b,
-                                                  int want32)
+// 1/x, x >= 1: FP32 seed + one Newton step
+__device__ __forceinline__ double rcp_nr(double x)
+{
+    const double y0 = (double)(1.0f / (float)x);
+    const double e = fma(-x, y0, 1.0);
+    return fma(y0, e, y0);
+}
+
+// Threads cover voxels v with every index in [0, n_a]; face d of v (between
+// v and v + e_d) is evaluated when v is interior on the other three axes, so
+// index 0 on axis d yields the face the interior voxel 1 sees backwards.
+__global__ void __launch_bounds__(256) k_faces(Geo g, const double *__restrict__ u, CPtrs8 gin, int has_g, double ih,
+                                               double iq2, double eps2, SplitBufs b)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z % (g.nz + 1), l = blockIdx.z / (g.nz + 1);
+    if (i > g.nx || j > g.ny)
+        return;
+    const int idx[4] = {i, j, k, l};
+    const long long o = nat_index(g, i, j, k, l);
+    const long long st[4] = {1, g.sy, g.sz, g.sw};
+    const double uc = u[o];
+    // central differences at v along each axis where v is interior
+    double D[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+        D[a] = idx[a] >= 1 ? u[o + st[a]] - u[o - st[a]] : 0.0;
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+        bool ok = true;
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+            if (a != d && idx[a] < 1)
+                ok = false;
+        if (!ok)
+            continue;
+        const long long nb = o + st[d];
+        const double cn = (u[nb] - uc) * ih;
+        double tt = 0.0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            if (a == d)
+                continue;
+            const double t = (u[nb + st[a]] - u[nb - st[a]]) + D[a];
+            tt = fma(t, t, tt);
+        }
+        const double s2 = fma(tt, iq2, fma(cn, cn, eps2));
+        const double y = rsqrt_nr(s2);
+        double gv = 1.0;
+        if (has_g)
+            gv = idx[d] >= 1 ? __ldg(gin.p[2 * d] + o) : __ldg(gin.p[2 * d + 1] + nb);
+        __stcs(b.fn[d] + o, s2 * y);
+        __stcs(b.fq[d] + o, gv * y);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_voxel_coef(Geo g, Split sp, double eps2, double c, double omega, SplitBufs b,
+                                                    int want32)
 {
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
@@ -111,18 +167,15 @@ __global__ void __launch_bounds__(256) k_assemble(Geo g, Split sp, const double 
         return;
     const long long o = nat_index(g, i, j, k, l);
     const long long st[4] = {1, g.sy, g.sz, g.sw};
-    const double ih = 1.0 / h, iq = 1.0 / (4.0 * h);
-    double nf[8];
-    double sum = 0.0;
+    double q[8], sum = 0.0;
 #pragma unroll
-    for (int f = 0; f < 8; ++f) {
-        const int d = f >> 1;
-        const long long nb = (f & 1) ? o - st[d] : o + st[d];
-        nf[f] = sqrt(face_sq_fast(u, o, nb, st, d, ih, iq) + eps2);
-        sum += nf[f];
+    for (int d = 0; d < 4; ++d) {
+        sum += __ldg(b.fn[d] + o) + __ldg(b.fn[d] + o - st[d]);
+        q[2 * d] = __ldg(b.fq[d] + o);
+        q[2 * d + 1] = __ldg(b.fq[d] + o - st[d]);
     }
-    const double mean = sum * 0.125;
-    const double vc = sqrt(fma(mean, mean, eps2));
+    const double x = fma(sum * sum, 1.0 / 64.0, eps2); // mean^2 + eps2
+    const double cv = c * (x * rsqrt_nr(x));           // c * vc
     const int col = (i + j + k + l) & 1;
     const long long s = (((long long)l * g.kM + k) * g.jM + j) * sp.Hs + ((i + 1) >> 1) + sp.A - 1;
     double *cf = pick(b.coef, col);
@@ -130,15 +183,14 @@ __global__ void __launch_bounds__(256) k_assemble(Geo g, Split sp, const double 
     double diag = 1.0;
 #pragma unroll
     for (int f = 0; f < 8; ++f) {
-        const double a = has_g ? vc * __ldg(gin.p[f] + o) / nf[f] : vc / nf[f];
-        const double ac = c * a;
+        const double ac = cv * q[f];
         diag += ac;
         __stcs(cf + f * sp.cs + s, ac);
         if (want32)
             __stcs(cf32 + f * sp.cs + s, (float)ac);
     }
     __stcs(cf + 8 * sp.cs + s, diag);
-    __stcs(cf + 9 * sp.cs + s, omega / diag);
+    __stcs(cf + 9 * sp.cs + s, omega * rcp_nr(diag));
 }
 
 // given natural coefficient arrays e..bw (the reference's layout) -> split
@@ -574,10 +626,15 @@ static inline void interior_grid(const Geo &g, dim3 &grid, dim3 &block)
 void launch_assemble(const Geo &g, const Split &s, const double *u, CPtrs8 gin, int has_g, const ss4d_params &p,
                      SplitBufs b, int want32, cudaStream_t st)
 {
+    const int bx = g.nx + 1 >= 128 ? 128 : (g.nx + 1 >= 64 ? 64 : 32);
+    const int by = 256 / bx;
+    dim3 fb(bx, by, 1), fg((g.nx + 1 + bx - 1) / bx, (g.ny + 1 + by - 1) / by, (g.nz + 1) * (g.nt + 1));
+    const double ih = 1.0 / p.h, iq = 1.0 / (4.0 * p.h);
+    k_faces<<<fg, fb, 0, st>>>(g, u, gin, has_g, ih, iq * iq, p.eps2, b);
     dim3 gr, bl;
     interior_grid(g, gr, bl);
     const double c = p.tau / (p.h * p.h);
-    k_assemble<<<gr, bl, 0, st>>>(g, s, u, gin, has_g, p.h, p.eps2, c, p.omega_c, b, want32);
+    k_voxel_coef<<<gr, bl, 0, st>>>(g, s, p.eps2, c, p.omega_c, b, want32);
 }
 
 void launch_pack(const Geo &g, const Split &s, const double *u, const double *prev, SplitBufs b, cudaStream_t st)

@@ -52,6 +52,8 @@ def parse_args():
     ap.add_argument("--forms", default="fp64,mixed")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="run the sweep loop host-driven instead of as one CUDA graph (same kernels)")
     ap.add_argument("--seed", type=int, default=1)
     return ap.parse_args()
 
@@ -146,6 +148,7 @@ def run_ours(args, rank, world, dist):
     i0 = torch.from_numpy(i0h).to(dev)
     g = [torch.empty(shape, dtype=torch.float64, device=dev) for _ in range(8)]
     S = ss4d.Solver(*shape[::-1], arith="fp64", stream=sh)
+    S.set_graph(not args.no_graph)
     S.edge_detector(p, i0, None, g)
     S.synchronize()
     del i0

@@ -380,17 +380,17 @@ static ss4d_status ensure_split(ss4d_solver *s, int mixed)
         double *u3 = nullptr, *p2 = nullptr, *cf = nullptr;
         CKS(dmalloc(s, (void **)&u3, sizeof(double) * 3 * cs));
         CKS(dmalloc(s, (void **)&p2, sizeof(double) * 2 * cs));
-        CKS(dmalloc(s, (void **)&cf, sizeof(double) * 20 * cs));
+        CKS(dmalloc(s, (void **)&cf, sizeof(double) * 20 * s->sp.ct));
         CK(cudaMemsetAsync(u3, 0, sizeof(double) * 3 * cs, s->stream));
         CK(cudaMemsetAsync(p2, 0, sizeof(double) * 2 * cs, s->stream));
-        CK(cudaMemsetAsync(cf, 0, sizeof(double) * 20 * cs, s->stream));
+        CK(cudaMemsetAsync(cf, 0, sizeof(double) * 20 * s->sp.ct, s->stream));
         s->sb.R[0] = u3;
         s->sb.R[1] = u3 + cs;
         s->sb.Bk = u3 + 2 * cs;
         s->sb.P[0] = p2;
         s->sb.P[1] = p2 + cs;
         s->sb.coef[0] = cf;
-        s->sb.coef[1] = cf + 10 * cs;
+        s->sb.coef[1] = cf + 10 * s->sp.ct;
         s->sb.partial[0] = s->d_partial;
         s->sb.partial[1] = s->d_partial + s->cfg.grid;
         double *faces = nullptr; // 4 face norms + 4 face g/norm arrays, natural layout
@@ -403,14 +403,14 @@ static ss4d_status ensure_split(ss4d_solver *s, int mixed)
     }
     if (mixed && !s->have_mixed) {
         float *c32 = nullptr, *d3 = nullptr, *r2 = nullptr;
-        CKS(dmalloc(s, (void **)&c32, sizeof(float) * 16 * cs));
+        CKS(dmalloc(s, (void **)&c32, sizeof(float) * 16 * s->sp.ct));
         CKS(dmalloc(s, (void **)&d3, sizeof(float) * 3 * cs));
         CKS(dmalloc(s, (void **)&r2, sizeof(float) * 2 * cs));
-        CK(cudaMemsetAsync(c32, 0, sizeof(float) * 16 * cs, s->stream));
+        CK(cudaMemsetAsync(c32, 0, sizeof(float) * 16 * s->sp.ct, s->stream));
         CK(cudaMemsetAsync(d3, 0, sizeof(float) * 3 * cs, s->stream));
         CK(cudaMemsetAsync(r2, 0, sizeof(float) * 2 * cs, s->stream));
         s->sb.coef32[0] = c32;
-        s->sb.coef32[1] = c32 + 8 * cs;
+        s->sb.coef32[1] = c32 + 8 * s->sp.ct;
         s->sb.dR[0] = d3;
         s->sb.dR[1] = d3 + cs;
         s->sb.dB = d3 + 2 * cs;

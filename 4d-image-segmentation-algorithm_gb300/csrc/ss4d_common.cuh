@@ -53,7 +53,19 @@ struct Split {
     int nxh;        // (nx+1)/2: interior columns per row (upper bound)
     long long rows; // jM*kM*lM
     long long cs;   // elements per colour array (rows*Hs)
+    long long ct;   // coefficient records per colour: ny*nz*nt*nxh rounded up to 32
 };
+
+// Coefficients are indexed by a compact interior index per colour,
+//   t = (((l-1)*nz + (k-1))*ny + (j-1))*nxh + (i-1)/2,
+// and stored 32 records at a time, component-major ("AoSoA"): component f of
+// record t sits at ((t/32)*nf + f)*32 + t%32.  A warp's 32 consecutive
+// targets then read each component as one contiguous segment, and its whole
+// record set is one contiguous run.
+__host__ __device__ inline long long coef_at(long long t, int f, int nf)
+{
+    return (((t >> 5) * nf + f) << 5) + (t & 31);
+}
 
 inline Split make_split(const Geo &g)
 {
@@ -64,6 +76,7 @@ inline Split make_split(const Geo &g)
     s.Hs = (need + 7) & ~7;
     s.rows = (long long)g.jM * g.kM * g.lM;
     s.cs = s.rows * s.Hs;
+    s.ct = (((long long)g.ny * g.nz * g.nt * s.nxh) + 31) & ~31LL;
     return s;
 }
 

@@ -76,8 +76,9 @@ struct SplitBufs {
     double *R[2];       // red u, ping-pong (all cells incl. ghosts)
     double *Bk;         // black u (all cells incl. ghosts)
     double *P[2];       // prev (per colour)
-    double *coef[2];    // per colour: 10 arrays of cs: c*a_{e,w,s,n,b,t,bw,fw}, diag, omega/diag
-    float *coef32[2];   // per colour: 8 arrays of cs: c*a_f in FP32 (mixed form)
+    double *coef[2];    // per colour, record t (coef_at(t, f, 10)): f < 8: c*a_f (f = e,w,n,s,t,b,fw,bw),
+                        // f = 8: diag, f = 9: omega/diag;  10 * ct doubles
+    float *coef32[2];   // per colour, [8 t + f] = c*a_f in FP32 (mixed form);  8 * ct floats
     float *dR[2];       // mixed: red correction, ping-pong
     float *dB;          // mixed: black correction
     float *r32[2];      // mixed: FP64 residual rounded to FP32, per colour

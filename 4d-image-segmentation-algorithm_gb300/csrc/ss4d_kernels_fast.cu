@@ -3,9 +3,10 @@
 // Layout: every array is split by colour c = (i+j+k+l)&1 into two arrays of
 // rows (l,k,j) x Hs columns (see Split in ss4d_common.cuh), so a half-sweep
 // streams only the coefficients of its own colour and every warp load is a
-// contiguous run.  The coefficient arrays of a colour hold, per voxel,
-// c*a_f for the 8 faces (+x,-x,+y,-y,+z,-z,+w,-w = e,w,n,s,t,b,fw,bw), the
-// diagonal 1 + c*sum a_f and omega/diagonal (c = tau/h^2), so one update is
+// contiguous run.  The coefficients of a voxel (FP64: 32 records per
+// component-major block, see coef_at; FP32: one interleaved 32-byte record)
+// are c*a_f for the 8 faces (+x,-x,+y,-y,+z,-z,+w,-w = e,w,n,s,t,b,fw,bw),
+// the diagonal 1 + c*sum a_f and omega/diagonal (c = tau/h^2), so one update is
 //     r = diag*u - sum (c a_f) u_f - prev,   u <- u - (omega/diag) r
 // which is the reference's u + omega (GS - u) (segmentation4D.c:237-256)
 // rearranged, and r is the reference's residual of that voxel
@@ -41,6 +42,50 @@ template <typename T>
 __device__ __forceinline__ T ld_ro(const T *p)
 {
     return __ldg(p);
+}
+
+__device__ __forceinline__ double2 ld_stream2(const double *p)
+{
+    return __ldcs(reinterpret_cast<const double2 *>(p));
+}
+__device__ __forceinline__ float4 ld_stream4(const float *p)
+{
+    return __ldcs(reinterpret_cast<const float4 *>(p));
+}
+
+// FP32 <-> FP64 conversions by integer bit operations.  On this GPU a
+// conversion instruction to or from FP64 issues at the FP64 rate (1/68 of
+// FP32); these run on the integer pipe instead.
+// Exact float -> double for zero, normal numbers, Inf and NaN (FP32
+// subnormals, below 1.2e-38, become signed zero).
+__device__ __forceinline__ double f2d_bits(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned sign = u & 0x80000000u, e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+    const unsigned de = e == 0xFFu ? 0x7FFu : e + 896u;
+    const unsigned hi = e == 0u ? sign : (sign | (de << 20) | (m >> 3));
+    const unsigned lo = e == 0u ? 0u : (m & 7u) << 29;
+    return __hiloint2double((int)hi, (int)lo);
+}
+// double -> float by truncating the mantissa (error below 2^-23 relative);
+// magnitudes outside the FP32 normal range become zero or Inf, NaN stays NaN.
+__device__ __forceinline__ float d2f_bits(double d)
+{
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const unsigned sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7FFu);
+    const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const int fe = e - 896;
+    unsigned r;
+    if (e == 0x7FF)
+        r = sign | 0x7F800000u | (m ? 0x400000u : 0u);
+    else if (fe <= 0)
+        r = sign;
+    else if (fe >= 255)
+        r = sign | 0x7F800000u;
+    else
+        r = sign | ((unsigned)fe << 23) | m;
+    return __uint_as_float(r);
 }
 
 // Select one of a pair held in a by-value kernel parameter without a runtime
@@ -95,7 +140,7 @@ __device__ __forceinline__ TileCoord tile_coord(const Geo &g, const SweepCfg &cf
 // 1/sqrt(x), x > 0: FP32 seed + one Newton step
 __device__ __forceinline__ double rsqrt_nr(double x)
 {
-    const double y0 = (double)rsqrtf((float)x);
+    const double y0 = f2d_bits(rsqrtf(d2f_bits(x)));
     const double e = fma(-x * y0, y0, 1.0); // 1 - x y0^2
     return fma(0.5 * y0, e, y0);
 }
@@ -103,9 +148,40 @@ __device__ __forceinline__ double rsqrt_nr(double x)
 // 1/x, x >= 1: FP32 seed + one Newton step
 __device__ __forceinline__ double rcp_nr(double x)
 {
-    const double y0 = (double)(1.0f / (float)x);
+    const double y0 = f2d_bits(__fdividef(1.0f, d2f_bits(x)));
     const double e = fma(-x, y0, 1.0);
     return fma(y0, e, y0);
+}
+
+// Coefficient record t of one voxel (layout: coef_at in ss4d_common.cuh):
+// FP64 [c a_0..c a_7, diag, omega/diag] and FP32 [c a_0..c a_7].
+__device__ __forceinline__ void store_coef(double *cf, float *cf32, long long t, const double ac[8], double diag,
+                                           double winv, int want32)
+{
+#pragma unroll
+    for (int f = 0; f < 8; ++f)
+        __stcs(cf + coef_at(t, f, 10), ac[f]);
+    __stcs(cf + coef_at(t, 8, 10), diag);
+    __stcs(cf + coef_at(t, 9, 10), winv);
+    if (want32) {
+        // FP32 records stay interleaved (32 B per target, two 16-byte loads):
+        // the FP32 sweep issues fewer, wider loads that way
+        float4 *f4 = reinterpret_cast<float4 *>(cf32 + 8 * t);
+        __stcs(f4, make_float4(d2f_bits(ac[0]), d2f_bits(ac[1]), d2f_bits(ac[2]), d2f_bits(ac[3])));
+        __stcs(f4 + 1, make_float4(d2f_bits(ac[4]), d2f_bits(ac[5]), d2f_bits(ac[6]), d2f_bits(ac[7])));
+    }
+}
+
+// compact per-colour interior index of a sweep target
+__device__ __forceinline__ long long tile_coef_index(const Geo &g, const Split &sp, const TileCoord &tc)
+{
+    return ((((long long)(tc.l - 1) * g.nz + (tc.k - 1)) * g.ny + (tc.j - 1)) * sp.nxh) + tc.xi;
+}
+
+// compact per-colour interior index of voxel (i, j, k, l)
+__device__ __forceinline__ long long coef_index(const Geo &g, const Split &sp, int i, int j, int k, int l)
+{
+    return ((((long long)(l - 1) * g.nz + (k - 1)) * g.ny + (j - 1)) * sp.nxh) + ((i - 1) >> 1);
 }
 
 // Threads cover voxels v with every index in [0, n_a]; face d of v (between
@@ -177,20 +253,15 @@ __global__ void __launch_bounds__(256) k_voxel_coef(Geo g, Split sp, double eps2
     const double x = fma(sum * sum, 1.0 / 64.0, eps2); // mean^2 + eps2
     const double cv = c * (x * rsqrt_nr(x));           // c * vc
     const int col = (i + j + k + l) & 1;
-    const long long s = (((long long)l * g.kM + k) * g.jM + j) * sp.Hs + ((i + 1) >> 1) + sp.A - 1;
     double *cf = pick(b.coef, col);
     float *cf32 = pick(b.coef32, col);
-    double diag = 1.0;
+    double ac[8], diag = 1.0;
 #pragma unroll
     for (int f = 0; f < 8; ++f) {
-        const double ac = cv * q[f];
-        diag += ac;
-        __stcs(cf + f * sp.cs + s, ac);
-        if (want32)
-            __stcs(cf32 + f * sp.cs + s, (float)ac);
+        ac[f] = cv * q[f];
+        diag += ac[f];
     }
-    __stcs(cf + 8 * sp.cs + s, diag);
-    __stcs(cf + 9 * sp.cs + s, omega * rcp_nr(diag));
+    store_coef(cf, cf32, coef_index(g, sp, i, j, k, l), ac, diag, omega * rcp_nr(diag), want32);
 }
 
 // given natural coefficient arrays e..bw (the reference's layout) -> split
@@ -205,20 +276,15 @@ __global__ void __launch_bounds__(256) k_pack_coef(Geo g, Split sp, CPtrs8 a, do
         return;
     const long long o = nat_index(g, i, j, k, l);
     const int col = (i + j + k + l) & 1;
-    const long long s = (((long long)l * g.kM + k) * g.jM + j) * sp.Hs + ((i + 1) >> 1) + sp.A - 1;
     double *cf = pick(b.coef, col);
     float *cf32 = pick(b.coef32, col);
-    double diag = 1.0;
+    double ac[8], diag = 1.0;
 #pragma unroll
     for (int f = 0; f < 8; ++f) {
-        const double ac = c * a.p[f][o];
-        diag += ac;
-        cf[f * sp.cs + s] = ac;
-        if (want32)
-            cf32[f * sp.cs + s] = (float)ac;
+        ac[f] = c * a.p[f][o];
+        diag += ac[f];
     }
-    cf[8 * sp.cs + s] = diag;
-    cf[9 * sp.cs + s] = omega / diag;
+    store_coef(cf, cf32, coef_index(g, sp, i, j, k, l), ac, diag, omega / diag, want32);
 }
 
 // natural -> split copies of u (both red buffers and black, ghosts
@@ -319,17 +385,18 @@ __global__ void __launch_bounds__(256) k_sweep64(Geo g, Split sp, SweepCfg cfg, 
             continue;
         const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * Hy + tc.xi + sp.A;
         const double u0 = src[s];
-        double S = ld_stream(cf + s) * ld_ro(oth + s - p + 1);
-        S = fma(ld_stream(cf + cs + s), ld_ro(oth + s - p), S);
-        S = fma(ld_stream(cf + 2 * cs + s), ld_ro(oth + s + Hy), S);
-        S = fma(ld_stream(cf + 3 * cs + s), ld_ro(oth + s - Hy), S);
-        S = fma(ld_stream(cf + 4 * cs + s), ld_ro(oth + s + Hz), S);
-        S = fma(ld_stream(cf + 5 * cs + s), ld_ro(oth + s - Hz), S);
-        S = fma(ld_stream(cf + 6 * cs + s), ld_ro(oth + s + Hw), S);
-        S = fma(ld_stream(cf + 7 * cs + s), ld_ro(oth + s - Hw), S);
-        const double diag = ld_stream(cf + 8 * cs + s);
-        const double winv = ld_stream(cf + 9 * cs + s);
-        const double r = fma(diag, u0, -(S + ld_stream(pv + s)));
+        const double *cv = cf + coef_at(tile_coef_index(g, sp, tc), 0, 10); // component f at cv[32 f]
+        double S = fma(ld_stream(cv), ld_ro(oth + s - p + 1), ld_stream(pv + s));
+        S = fma(ld_stream(cv + 32), ld_ro(oth + s - p), S);
+        S = fma(ld_stream(cv + 64), ld_ro(oth + s + Hy), S);
+        S = fma(ld_stream(cv + 96), ld_ro(oth + s - Hy), S);
+        S = fma(ld_stream(cv + 128), ld_ro(oth + s + Hz), S);
+        S = fma(ld_stream(cv + 160), ld_ro(oth + s - Hz), S);
+        S = fma(ld_stream(cv + 192), ld_ro(oth + s + Hw), S);
+        S = fma(ld_stream(cv + 224), ld_ro(oth + s - Hw), S);
+        const double diag = ld_stream(cv + 256);
+        const double winv = ld_stream(cv + 288);
+        const double r = fma(diag, u0, -S); // S includes prev
         acc = fma(r, r, acc);
         dst[s] = fma(-winv, r, u0);
     }
@@ -406,22 +473,23 @@ __global__ void __launch_bounds__(256) k_refine(Geo g, Split sp, SweepCfg cfg, S
             continue;
         const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * Hy + tc.xi + sp.A;
         const long long nb[8] = {s - p + 1, s - p, s + Hy, s - Hy, s + Hz, s - Hz, s + Hw, s - Hw};
-        const double u0 = own[s] + (double)down[s];
+        const double u0 = own[s] + f2d_bits(down[s]);
+        const double *cv = cf + coef_at(tile_coef_index(g, sp, tc), 0, 10);
         double S = 0.0;
 #pragma unroll
         for (int f = 0; f < 8; ++f) {
             double v = oth[nb[f]];
             if (COL == 0)
-                v += (double)doth[nb[f]];
-            S = fma(ld_stream(cf + f * cs + s), v, S);
+                v += f2d_bits(doth[nb[f]]);
+            S = fma(ld_stream(cv + 32 * f), v, S);
         }
-        const double diag = ld_stream(cf + 8 * cs + s);
+        const double diag = ld_stream(cv + 256);
         const double r = fma(diag, u0, -(S + ld_stream(pv + s)));
         acc = fma(r, r, acc);
         own[s] = u0;
         // r = A u - b here; the correction d with A d = b - A u moves u to the
         // solution, so the FP32 sweeps get the negated residual
-        rr[s] = (float)(-r);
+        rr[s] = d2f_bits(-r);
     }
     acc = block_sum(acc);
     if (threadIdx.x == 0)
@@ -477,9 +545,9 @@ __global__ void __launch_bounds__(256) k_sweep32(Geo g, Split sp, SweepCfg cfg, 
             continue;
         const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * Hy + tc.xi + sp.A;
         const float u0 = src[s];
-        const float a0 = ld_stream(cf + s), a1 = ld_stream(cf + cs + s), a2 = ld_stream(cf + 2 * cs + s),
-                    a3 = ld_stream(cf + 3 * cs + s), a4 = ld_stream(cf + 4 * cs + s), a5 = ld_stream(cf + 5 * cs + s),
-                    a6 = ld_stream(cf + 6 * cs + s), a7 = ld_stream(cf + 7 * cs + s);
+        const float *cv = cf + 8 * tile_coef_index(g, sp, tc);
+        const float4 c03 = ld_stream4(cv), c47 = ld_stream4(cv + 4);
+        const float a0 = c03.x, a1 = c03.y, a2 = c03.z, a3 = c03.w, a4 = c47.x, a5 = c47.y, a6 = c47.z, a7 = c47.w;
         float S = a0 * ld_ro(oth + s - p + 1);
         S = fmaf(a1, ld_ro(oth + s - p), S);
         S = fmaf(a2, ld_ro(oth + s + Hy), S);

@@ -33,6 +33,7 @@ CUDA_UNITS = {
     "ss4d_kernels_fast.cu": [],
     "ss4d_api.cu": [],
     "ss4d_noalloc.cu": [],
+    "ss4d_batch.cu": [],
 }
 C_UNITS = {"ss4d_scene.c": ["-fopenmp"]}
 

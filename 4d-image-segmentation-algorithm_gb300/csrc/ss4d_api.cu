@@ -1124,3 +1124,76 @@ extern "C" ss4d_status ss4d_synchronize(ss4d_solver *s)
     CK(cudaStreamSynchronize(s->stream));
     return SS4D_OK;
 }
+
+// ---------------------------------------------------------------------------
+// a handle's colour-split machinery, for the batched solver (ss4d_batch.cu)
+
+int ss4d::solver_sm_count(const ss4d_solver *s)
+{
+    return s->sm_count;
+}
+
+ss4d_status ss4d::solver_view(ss4d_solver *s, SolverView *out)
+{
+    REQ(s && out, "NULL argument");
+    CKS(ensure_split(s, 0));
+    out->g = s->geo;
+    out->sp = s->sp;
+    out->cfg = s->cfg;
+    out->b = s->sb;
+    return SS4D_OK;
+}
+
+ss4d_status ss4d::solver_set_shape(ss4d_solver *s, int xt, int kb)
+{
+    REQ(s && kb >= 1 && xt >= 0 && xt <= 256, "bad tile shape");
+    SweepCfg c = make_sweep_cfg_xt(s->geo, s->sp, s->sm_count, kb, xt);
+    REQ(2LL * c.grid <= s->n_partial, "grid larger than the partial-sum buffer");
+    s->cfg = c;
+    s->sb.partial[1] = s->d_partial + c.grid;
+    free_graphs(s);
+    return SS4D_OK;
+}
+
+ss4d_status ss4d::solver_prepare_step(ss4d_solver *s, const ss4d_params *p, double *d_u, const double *const d_g[8])
+{
+    REQ(s && d_u && d_g, "NULL argument");
+    CKS(check_params(p));
+    CPtrs8 gi;
+    for (int f = 0; f < 8; ++f) {
+        REQ(d_g[f], "a g array is NULL");
+        gi.p[f] = d_g[f];
+    }
+    CKS(ensure_split(s, 0));
+    launch_assemble(s->geo, s->sp, d_u, gi, 1, *p, s->sb, 0, s->stream);
+    launch_pack(s->geo, s->sp, d_u, d_u, s->sb, s->stream);
+    s->launches += 3;
+    return last_launch();
+}
+
+ss4d_status ss4d::solver_finish_step(ss4d_solver *s, const LoopState *d_state, double *d_u)
+{
+    REQ(s && d_state && d_u, "NULL argument");
+    launch_unpack(s->geo, s->sp, s->sb, d_state, d_u, s->stream);
+    s->launches += 1;
+    return last_launch();
+}
+
+ss4d_status ss4d::solver_time_sweeps(ss4d_solver *s, const ss4d_params *p, int iters, float *ms)
+{
+    REQ(s && p && ms && iters > 0, "bad argument");
+    CKS(ensure_split(s, 0));
+    CKS(upload_params(s, p));
+    launch_loop_init(s->d_state, 0, s->stream); // z stays 0: fixed buffers, as in a real loop
+    CK(cudaEventRecord(s->tev0, s->stream));
+    for (int it = 0; it < iters; ++it) {
+        launch_sweep64(s->geo, s->sp, s->cfg, 1, s->sb, s->d_params, s->d_state, s->stream);
+        launch_sweep64(s->geo, s->sp, s->cfg, 0, s->sb, s->d_params, s->d_state, s->stream);
+    }
+    CK(cudaEventRecord(s->tev1, s->stream));
+    CKS(last_launch());
+    CK(cudaEventSynchronize(s->tev1));
+    CK(cudaEventElapsedTime(ms, s->tev0, s->tev1));
+    s->launches += 1 + 2LL * iters;
+    return SS4D_OK;
+}

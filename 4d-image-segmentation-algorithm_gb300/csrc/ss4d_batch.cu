@@ -1,0 +1,516 @@
+// ss4d_batch.cu — batched solves of many independent volumes (uneven sizes,
+// per-volume parameters) in the plain FP64 form.
+//
+// Each volume owns a solver handle for its buffers, its coefficient assembly
+// and its pack/unpack (ss4d_api.cu).  What is batched is the SOR loop: one
+// persistent launch per half-sweep walks the concatenated tile lists of all
+// volumes (volume v owns tiles [tile0_v, tile0_{v+1})), every tile with its
+// volume's own tile shape; a volume whose loop has stopped is skipped
+// tile by tile.  Residual partial sums are kept per (volume, block) in a
+// fixed order, and one controller kernel runs every volume's stopping test
+// and keeps the graph's while loop going while any volume is active.
+#include <cuda_runtime.h>
+
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "ss4d_sweep.cuh"
+
+using namespace ss4d;
+
+#define BMAX SS4D_BATCH_MAX_VOLUMES
+#define BWARPS 8 // 256 threads per block
+
+namespace {
+
+struct BVol {
+    Geo g;
+    Split sp;
+    SweepCfg cfg;
+    SplitBufs b;
+    long long tile0;
+};
+
+struct BParams {
+    double omega, h4, tol;
+    int maxit, pad_;
+};
+
+ss4d_status bfail(ss4d_status st, const char *fmt, ...)
+{
+    char buf[400];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    set_error_text(buf);
+    return st;
+}
+
+#define BCK(call)                                                                                                  \
+    do {                                                                                                           \
+        cudaError_t e_ = (call);                                                                                   \
+        if (e_ != cudaSuccess) {                                                                                   \
+            cudaGetLastError();                                                                                    \
+            return bfail(e_ == cudaErrorMemoryAllocation ? SS4D_ERR_ALLOC : SS4D_ERR_CUDA, "%s failed: %s", #call, \
+                         cudaGetErrorString(e_));                                                                  \
+        }                                                                                                          \
+    } while (0)
+
+#define BCKS(expr)                                                                                                 \
+    do {                                                                                                           \
+        ss4d_status s_ = (expr);                                                                                   \
+        if (s_ != SS4D_OK)                                                                                         \
+            return s_;                                                                                             \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// kernels
+
+template <int COL>
+__global__ void __launch_bounds__(256) k_bsweep64(const BVol *__restrict__ vols, int nv, long long total,
+                                                  const LoopState *__restrict__ st, double *partial)
+{
+    __shared__ double wacc[BWARPS][BMAX];
+    for (int q = threadIdx.x; q < BWARPS * BMAX; q += blockDim.x)
+        (&wacc[0][0])[q] = 0.0;
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int v = 0;
+    for (long long t = blockIdx.x; t < total; t += gridDim.x) {
+        while (v + 1 < nv && t >= vols[v + 1].tile0)
+            ++v; // a block's tiles increase, so its volume index only grows
+        if (st[v].stop)
+            continue; // the whole block skips: v is uniform
+        const BVol &V = vols[v];
+        const Geo g = V.g;
+        const Split sp = V.sp;
+        const SweepCfg cfg = V.cfg;
+        const int z = st[v].z;
+        const double *src;
+        double *dst;
+        const double *oth;
+        if (COL == 0) {
+            src = (z & 1) ? V.b.R[1] : V.b.R[0];
+            dst = (z & 1) ? V.b.R[0] : V.b.R[1];
+            oth = V.b.Bk;
+        } else {
+            src = V.b.Bk;
+            dst = V.b.Bk;
+            oth = (z & 1) ? V.b.R[1] : V.b.R[0];
+        }
+        const double *cf = V.b.coef[COL];
+        const double *pv = V.b.P[COL];
+        const int tx = threadIdx.x & (cfg.XT - 1), ty = threadIdx.x / cfg.XT;
+        const TileCoord tc = tile_coord(g, cfg, t - V.tile0, tx, ty);
+        double r2 = 0.0;
+        if (tc.ok) {
+            const int p = (COL + tc.j + tc.k + tc.l) & 1;
+            const int i = 2 * tc.xi + 2 - p;
+            if (i <= g.nx) {
+                const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * sp.Hs + tc.xi + sp.A;
+                const double r = sweep64_target(g, sp, tc, p, s, src, dst, oth, cf, pv);
+                r2 = r * r;
+            }
+        }
+        r2 = warp_sum(r2);
+        if (lane == 0)
+            wacc[warp][v] += r2;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nv; q += blockDim.x) {
+        double sum = 0.0;
+        for (int w = 0; w < BWARPS; ++w)
+            sum += wacc[w][q];
+        partial[(long long)q * gridDim.x + blockIdx.x] = sum;
+    }
+}
+
+__global__ void k_binit(LoopState *st, int nv, int z)
+{
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv)
+        return;
+    if (z == 0) {
+        memset(&st[v], 0, sizeof(LoopState));
+    } else {
+        st[v].z = z;
+    }
+}
+
+// every volume's stopping test (as k_ctrl64 does for one volume)
+__global__ void k_bctrl(const double *__restrict__ pred, const double *__restrict__ pblack, int grid, int nv,
+                        const BParams *__restrict__ par, LoopState *st, cudaGraphConditionalHandle h, int use_cond)
+{
+    __shared__ int any;
+    if (threadIdx.x == 0)
+        any = 0;
+    __syncthreads();
+    for (int v = 0; v < nv; ++v) {
+        if (st[v].stop)
+            continue;
+        double a = 0.0, c = 0.0;
+        for (int t = threadIdx.x; t < grid; t += blockDim.x) {
+            a += pred[(long long)v * grid + t];
+            c += pblack[(long long)v * grid + t];
+        }
+        a = block_sum(a);
+        c = block_sum(c);
+        if (threadIdx.x == 0) {
+            const double om1 = 1.0 - par[v].omega;
+            const double R = (a + om1 * om1 * c) * par[v].h4;
+            const int z = st[v].z;
+            st[v].bodies += 1;
+            if (z == 1)
+                st[v].R_first = R;
+            st[v].R = R;
+            const bool fin = isfinite(R);
+            const bool stop = !fin || !(R > par[v].tol) || z >= par[v].maxit;
+            if (!fin)
+                st[v].status = SS4D_ERR_NONFINITE;
+            if (stop) {
+                st[v].stop = 1;
+                st[v].final_red = z & 1;
+            } else {
+                st[v].z = z + 1;
+                any = 1;
+            }
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && use_cond)
+        cudaGraphSetConditional(h, any ? 1u : 0u);
+}
+
+int bsweep_blocks_per_sm()
+{
+    int a = 0, b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_bsweep64<0>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bsweep64<1>, 256, 0);
+    const int m = a < b ? a : b;
+    return m > 0 ? m : 1;
+}
+
+} // namespace
+
+// ---------------------------------------------------------------------------
+// the batch handle
+
+struct ss4d_batch {
+    int n;
+    ss4d_solver *vol[BMAX];
+    BVol h_vols[BMAX];
+    BVol *d_vols;
+    LoopState *d_st, *h_st;
+    BParams *d_par, *h_par;
+    double *d_partial;
+    int grid;
+    long long total;
+    int dirty;
+    cudaStream_t stream, cap;
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    int use_graph, graph_failed;
+};
+
+static void bfree_graph(ss4d_batch *b)
+{
+    if (b->exec)
+        cudaGraphExecDestroy(b->exec);
+    if (b->graph)
+        cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+}
+
+extern "C" ss4d_status ss4d_batch_destroy(ss4d_batch *b)
+{
+    if (!b)
+        return SS4D_OK;
+    cudaStreamSynchronize(b->stream);
+    bfree_graph(b);
+    for (int v = 0; v < b->n; ++v)
+        ss4d_solver_destroy(b->vol[v]);
+    if (b->d_vols)
+        cudaFree(b->d_vols);
+    if (b->d_st)
+        cudaFree(b->d_st);
+    if (b->d_par)
+        cudaFree(b->d_par);
+    if (b->d_partial)
+        cudaFree(b->d_partial);
+    if (b->h_st)
+        cudaFreeHost(b->h_st);
+    if (b->h_par)
+        cudaFreeHost(b->h_par);
+    if (b->cap)
+        cudaStreamDestroy(b->cap);
+    free(b);
+    return SS4D_OK;
+}
+
+// refresh the host descriptors (tile ranges follow the volumes' shapes)
+static ss4d_status bdescribe(ss4d_batch *b)
+{
+    long long t0 = 0;
+    for (int v = 0; v < b->n; ++v) {
+        SolverView w;
+        BCKS(solver_view(b->vol[v], &w));
+        b->h_vols[v].g = w.g;
+        b->h_vols[v].sp = w.sp;
+        b->h_vols[v].cfg = w.cfg;
+        b->h_vols[v].b = w.b;
+        b->h_vols[v].tile0 = t0;
+        t0 += w.cfg.ntiles;
+    }
+    if (t0 != b->total)
+        bfree_graph(b); // the tile count is a kernel argument of the graph
+    b->total = t0;
+    BCK(cudaMemcpyAsync(b->d_vols, b->h_vols, sizeof(BVol) * b->n, cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaStreamSynchronize(b->stream)); // h_vols may change before the next call
+    b->dirty = 0;
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_batch_create(int n, const ss4d_dims *dims, void *stream, ss4d_batch **out)
+{
+    if (!out || !dims || n < 1 || n > BMAX)
+        return bfail(SS4D_ERR_INVALID, "invalid argument: need 1..%d volumes, dims and out", BMAX);
+    *out = nullptr;
+    ss4d_batch *b = (ss4d_batch *)calloc(1, sizeof(ss4d_batch));
+    if (!b)
+        return SS4D_ERR_ALLOC;
+    b->n = n;
+    b->stream = (cudaStream_t)stream;
+    b->use_graph = 1;
+    b->dirty = 1;
+    ss4d_status st = SS4D_OK;
+    for (int v = 0; v < n && st == SS4D_OK; ++v) {
+        st = ss4d_solver_create(&dims[v], SS4D_ARITH_FP64, stream, &b->vol[v]);
+        if (st == SS4D_OK) {
+            SolverView w;
+            st = solver_view(b->vol[v], &w); // allocate the split buffers now
+        }
+    }
+    if (st != SS4D_OK) {
+        ss4d_batch_destroy(b);
+        return st;
+    }
+    const int sm = solver_sm_count(b->vol[0]);
+    b->grid = sm * bsweep_blocks_per_sm();
+    cudaError_t e = cudaMalloc((void **)&b->d_vols, sizeof(BVol) * n);
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **)&b->d_st, sizeof(LoopState) * n);
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **)&b->d_par, sizeof(BParams) * n);
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **)&b->d_partial, sizeof(double) * 2 * (size_t)n * b->grid);
+    if (e == cudaSuccess)
+        e = cudaMallocHost((void **)&b->h_st, sizeof(LoopState) * n);
+    if (e == cudaSuccess)
+        e = cudaMallocHost((void **)&b->h_par, sizeof(BParams) * n);
+    if (e == cudaSuccess)
+        e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        ss4d_batch_destroy(b);
+        return bfail(SS4D_ERR_ALLOC, "batch allocation failed: %s", cudaGetErrorString(e));
+    }
+    *out = b;
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_batch_set_graph(ss4d_batch *b, int enable)
+{
+    if (!b)
+        return bfail(SS4D_ERR_INVALID, "invalid argument: batch is NULL");
+    b->use_graph = enable ? 1 : 0;
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_batch_set_shape(ss4d_batch *b, int v, int xt, int k_block)
+{
+    if (!b || v < 0 || v >= b->n)
+        return bfail(SS4D_ERR_INVALID, "invalid argument: no volume %d", v);
+    BCKS(solver_set_shape(b->vol[v], xt, k_block));
+    b->dirty = 1;
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_batch_autotune(ss4d_batch *b, const ss4d_params *p, double *const *d_u,
+                                           const double *const *d_g, int *xt_out, int *kb_out)
+{
+    if (!b || !p || !d_u || !d_g)
+        return bfail(SS4D_ERR_INVALID, "invalid argument: NULL batch, params, u or g");
+    static const int kbs[] = {1, 2, 4, 8};
+    for (int v = 0; v < b->n; ++v) {
+        BCKS(solver_prepare_step(b->vol[v], &p[v], d_u[v], d_g + 8 * v));
+        SolverView w;
+        BCKS(solver_view(b->vol[v], &w));
+        int top = 8;
+        while (top < w.sp.nxh && top < 256)
+            top <<= 1;
+        float best = 1e30f;
+        int bxt = 0, bkb = 4;
+        for (int xt = 8; xt <= top; xt <<= 1) {
+            for (int kb : kbs) {
+                if (kb > w.g.nz)
+                    continue;
+                BCKS(solver_set_shape(b->vol[v], xt, kb));
+                float ms = 0.f;
+                BCKS(solver_time_sweeps(b->vol[v], &p[v], 1, &ms)); // warm-up
+                BCKS(solver_time_sweeps(b->vol[v], &p[v], 3, &ms));
+                if (ms < best) {
+                    best = ms;
+                    bxt = xt;
+                    bkb = kb;
+                }
+            }
+        }
+        BCKS(solver_set_shape(b->vol[v], bxt, bkb));
+        if (xt_out)
+            xt_out[v] = bxt;
+        if (kb_out)
+            kb_out[v] = bkb;
+    }
+    b->dirty = 1;
+    return SS4D_OK;
+}
+
+static void launch_bsweep(ss4d_batch *b, int colour, cudaStream_t st)
+{
+    if (colour == 0)
+        k_bsweep64<0><<<b->grid, 256, 0, st>>>(b->d_vols, b->n, b->total, b->d_st, b->d_partial);
+    else
+        k_bsweep64<1><<<b->grid, 256, 0, st>>>(b->d_vols, b->n, b->total, b->d_st,
+                                               b->d_partial + (size_t)b->n * b->grid);
+}
+
+static void launch_bctrl(ss4d_batch *b, unsigned long long h, int use_cond, cudaStream_t st)
+{
+    k_bctrl<<<1, 256, 0, st>>>(b->d_partial, b->d_partial + (size_t)b->n * b->grid, b->grid, b->n, b->d_par,
+                               b->d_st, (cudaGraphConditionalHandle)h, use_cond);
+}
+
+static ss4d_status bbuild_graph(ss4d_batch *b)
+{
+    cudaGraph_t graph = nullptr;
+    cudaGraphConditionalHandle h;
+    BCK(cudaGraphCreate(&graph, 0));
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+    alignas(cudaGraphNodeParams) unsigned char store[sizeof(cudaGraphNodeParams)];
+    memset(store, 0, sizeof store);
+    cudaGraphNodeParams &cp = *reinterpret_cast<cudaGraphNodeParams *>(store);
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (e == cudaSuccess)
+        e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp);
+    if (e == cudaSuccess)
+        e = cudaStreamBeginCaptureToGraph(b->cap, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        launch_bsweep(b, 1, b->cap);
+        launch_bsweep(b, 0, b->cap);
+        launch_bctrl(b, (unsigned long long)h, 1, b->cap);
+        cudaGraph_t body = nullptr;
+        e = cudaStreamEndCapture(b->cap, &body);
+    }
+    if (e == cudaSuccess)
+        e = cudaGraphInstantiate(&b->exec, graph, 0);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        cudaGraphDestroy(graph);
+        b->exec = nullptr;
+        return bfail(SS4D_ERR_CUDA, "batch graph: %s", cudaGetErrorString(e));
+    }
+    b->graph = graph;
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_batch_seg_time_step(ss4d_batch *b, const ss4d_params *p, double *const *d_u,
+                                                const double *const *d_g, ss4d_step_stats *stats)
+{
+    if (!b || !p || !d_u || !d_g)
+        return bfail(SS4D_ERR_INVALID, "invalid argument: NULL batch, params, u or g");
+    if (stats)
+        memset(stats, 0, sizeof(ss4d_step_stats) * b->n);
+    cudaEvent_t e0, e1;
+    BCK(cudaEventCreate(&e0));
+    BCK(cudaEventCreate(&e1));
+    BCK(cudaEventRecord(e0, b->stream));
+    for (int v = 0; v < b->n; ++v) {
+        BCKS(solver_prepare_step(b->vol[v], &p[v], d_u[v], d_g + 8 * v));
+        b->h_par[v].omega = p[v].omega_c;
+        b->h_par[v].h4 = p[v].h * p[v].h * p[v].h * p[v].h;
+        b->h_par[v].tol = p[v].gsTol;
+        b->h_par[v].maxit = p[v].maxNoGSIteration;
+        b->h_par[v].pad_ = 0;
+    }
+    if (b->dirty)
+        BCKS(bdescribe(b));
+    BCK(cudaMemcpyAsync(b->d_par, b->h_par, sizeof(BParams) * b->n, cudaMemcpyHostToDevice, b->stream));
+    const int ib = (b->n + 63) / 64;
+    k_binit<<<ib, 64, 0, b->stream>>>(b->d_st, b->n, 0);
+    launch_bsweep(b, 0, b->stream);
+    k_binit<<<ib, 64, 0, b->stream>>>(b->d_st, b->n, 1);
+    BCK(cudaGetLastError());
+    bool graphed = false;
+    if (b->use_graph && !b->graph_failed) {
+        if (!b->exec && bbuild_graph(b) != SS4D_OK)
+            b->graph_failed = 1;
+        if (b->exec) {
+            BCK(cudaGraphLaunch(b->exec, b->stream));
+            graphed = true;
+        }
+    }
+    if (!graphed) {
+        int maxit = 0;
+        for (int v = 0; v < b->n; ++v)
+            maxit = p[v].maxNoGSIteration > maxit ? p[v].maxNoGSIteration : maxit;
+        for (int guard = 0; guard < maxit + 8; ++guard) {
+            launch_bsweep(b, 1, b->stream);
+            launch_bsweep(b, 0, b->stream);
+            launch_bctrl(b, 0, 0, b->stream);
+            BCK(cudaGetLastError());
+            BCK(cudaMemcpyAsync(b->h_st, b->d_st, sizeof(LoopState) * b->n, cudaMemcpyDeviceToHost, b->stream));
+            BCK(cudaStreamSynchronize(b->stream));
+            int active = 0;
+            for (int v = 0; v < b->n; ++v)
+                active += !b->h_st[v].stop;
+            if (!active)
+                break;
+        }
+    }
+    for (int v = 0; v < b->n; ++v)
+        BCKS(solver_finish_step(b->vol[v], b->d_st + v, d_u[v]));
+    BCK(cudaEventRecord(e1, b->stream));
+    BCK(cudaMemcpyAsync(b->h_st, b->d_st, sizeof(LoopState) * b->n, cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ss4d_status worst = SS4D_OK;
+    for (int v = 0; v < b->n; ++v) {
+        const LoopState &L = b->h_st[v];
+        if (stats) {
+            stats[v].iterations = L.z;
+            stats[v].residual = L.R;
+            stats[v].first_residual = L.R_first;
+            stats[v].status = L.status;
+            stats[v].ms = ms;
+        }
+        if (L.status != SS4D_OK)
+            worst = (ss4d_status)L.status;
+    }
+    if (worst != SS4D_OK)
+        return bfail(worst, "a volume's SOR residual became non-finite");
+    return SS4D_OK;
+}

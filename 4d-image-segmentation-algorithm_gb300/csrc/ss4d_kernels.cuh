@@ -131,4 +131,23 @@ int max_blocks_sweep32();
 // sets the text ss4d_last_error() returns (ss4d_api.cu)
 void set_error_text(const char *msg);
 
+// ---- a handle's colour-split machinery, for the batched solver ------------
+// (ss4d_api.cu; every call issues work on the handle's stream)
+struct SolverView {
+    Geo g;
+    Split sp;
+    SweepCfg cfg;
+    SplitBufs b;
+};
+SweepCfg make_sweep_cfg_xt(const Geo &g, const Split &s, int sm_count, int kb, int xt);
+ss4d_status solver_view(ss4d_solver *s, SolverView *out);      // allocates the FP64 split buffers
+ss4d_status solver_set_shape(ss4d_solver *s, int xt, int kb);  // tile width (threads along x) and k-block depth
+// assemble the coefficients of u and pack u (= prev) into the split buffers
+ss4d_status solver_prepare_step(ss4d_solver *s, const ss4d_params *p, double *d_u, const double *const d_g[8]);
+// unpack the red buffer state->final_red and black into the interior of u
+ss4d_status solver_finish_step(ss4d_solver *s, const LoopState *d_state, double *d_u);
+// device time of `iters` (black + red) FP64 sweep pairs with the current shape
+ss4d_status solver_time_sweeps(ss4d_solver *s, const ss4d_params *p, int iters, float *ms);
+int solver_sm_count(const ss4d_solver *s);
+
 } // namespace ss4d

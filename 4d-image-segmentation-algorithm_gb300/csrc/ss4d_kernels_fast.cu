@@ -22,36 +22,12 @@
 // still there.  The loop controller is a one-block kernel that sums the
 // per-block partials in a fixed order (deterministic) and, inside a CUDA
 // graph, sets the while-node condition.
-#include "ss4d_kernels.cuh"
+#include "ss4d_sweep.cuh"
 
 namespace ss4d {
 
 // ---------------------------------------------------------------------------
 // helpers
-
-__device__ __forceinline__ double ld_stream(const double *p)
-{
-    return __ldcs(p);
-}
-__device__ __forceinline__ float ld_stream(const float *p)
-{
-    return __ldcs(p);
-}
-
-template <typename T>
-__device__ __forceinline__ T ld_ro(const T *p)
-{
-    return __ldg(p);
-}
-
-__device__ __forceinline__ double2 ld_stream2(const double *p)
-{
-    return __ldcs(reinterpret_cast<const double2 *>(p));
-}
-__device__ __forceinline__ float4 ld_stream4(const float *p)
-{
-    return __ldcs(reinterpret_cast<const float4 *>(p));
-}
 
 // FP32 <-> FP64 conversions by integer bit operations.  On this GPU a
 // conversion instruction to or from FP64 issues at the FP64 rate (1/68 of
@@ -86,43 +62,6 @@ __device__ __forceinline__ float d2f_bits(double d)
     else
         r = sign | ((unsigned)fe << 23) | m;
     return __uint_as_float(r);
-}
-
-// Select one of a pair held in a by-value kernel parameter without a runtime
-// array index (which would copy the parameter struct to local memory).
-template <typename T>
-__device__ __forceinline__ T *pick(T *const (&a)[2], int i)
-{
-    return i ? a[1] : a[0];
-}
-
-struct TileCoord {
-    int j, k, l, xi;
-    bool ok;
-};
-
-// Tile order: x chunk fastest, then j group, then k inside a k block, then
-// frame l, then k block.  Consecutive tiles (which a persistent grid works on
-// at the same time) thus cover a few k planes of all frames, so the
-// neighbouring-plane reads of the other colour hit in L2.
-__device__ __forceinline__ TileCoord tile_coord(const Geo &g, const SweepCfg &cfg, long long t, int tx, int ty)
-{
-    TileCoord c;
-    long long r = t;
-    const int xc = (int)(r % cfg.nXC);
-    r /= cfg.nXC;
-    const int jg = (int)(r % cfg.nJG);
-    r /= cfg.nJG;
-    const int kin = (int)(r % cfg.KB);
-    r /= cfg.KB;
-    const int lt = (int)(r % g.nt);
-    const int kb = (int)(r / g.nt);
-    c.k = 1 + kb * cfg.KB + kin;
-    c.l = 1 + lt;
-    c.j = 1 + jg * cfg.TJ + ty;
-    c.xi = xc * cfg.XT + tx;
-    c.ok = c.k <= g.nz && c.j <= g.ny;
-    return c;
 }
 
 // ---------------------------------------------------------------------------
@@ -170,12 +109,6 @@ __device__ __forceinline__ void store_coef(double *cf, float *cf32, long long t,
         __stcs(f4, make_float4(d2f_bits(ac[0]), d2f_bits(ac[1]), d2f_bits(ac[2]), d2f_bits(ac[3])));
         __stcs(f4 + 1, make_float4(d2f_bits(ac[4]), d2f_bits(ac[5]), d2f_bits(ac[6]), d2f_bits(ac[7])));
     }
-}
-
-// compact per-colour interior index of a sweep target
-__device__ __forceinline__ long long tile_coef_index(const Geo &g, const Split &sp, const TileCoord &tc)
-{
-    return ((((long long)(tc.l - 1) * g.nz + (tc.k - 1)) * g.ny + (tc.j - 1)) * sp.nxh) + tc.xi;
 }
 
 // compact per-colour interior index of voxel (i, j, k, l)
@@ -371,8 +304,6 @@ __global__ void __launch_bounds__(256) k_sweep64(Geo g, Split sp, SweepCfg cfg, 
     }
     const double *__restrict__ cf = b.coef[COL];
     const double *__restrict__ pv = b.P[COL];
-    const long long cs = sp.cs;
-    const long long Hy = sp.Hs, Hz = Hy * g.jM, Hw = Hz * g.kM;
     const int tx = threadIdx.x & (cfg.XT - 1), ty = threadIdx.x / cfg.XT;
     double acc = 0.0;
     for (long long t = blockIdx.x; t < cfg.ntiles; t += gridDim.x) {
@@ -383,22 +314,9 @@ __global__ void __launch_bounds__(256) k_sweep64(Geo g, Split sp, SweepCfg cfg, 
         const int i = 2 * tc.xi + 2 - p;
         if (i > g.nx)
             continue;
-        const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * Hy + tc.xi + sp.A;
-        const double u0 = src[s];
-        const double *cv = cf + coef_at(tile_coef_index(g, sp, tc), 0, 10); // component f at cv[32 f]
-        double S = fma(ld_stream(cv), ld_ro(oth + s - p + 1), ld_stream(pv + s));
-        S = fma(ld_stream(cv + 32), ld_ro(oth + s - p), S);
-        S = fma(ld_stream(cv + 64), ld_ro(oth + s + Hy), S);
-        S = fma(ld_stream(cv + 96), ld_ro(oth + s - Hy), S);
-        S = fma(ld_stream(cv + 128), ld_ro(oth + s + Hz), S);
-        S = fma(ld_stream(cv + 160), ld_ro(oth + s - Hz), S);
-        S = fma(ld_stream(cv + 192), ld_ro(oth + s + Hw), S);
-        S = fma(ld_stream(cv + 224), ld_ro(oth + s - Hw), S);
-        const double diag = ld_stream(cv + 256);
-        const double winv = ld_stream(cv + 288);
-        const double r = fma(diag, u0, -S); // S includes prev
+        const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * sp.Hs + tc.xi + sp.A;
+        const double r = sweep64_target(g, sp, tc, p, s, src, dst, oth, cf, pv);
         acc = fma(r, r, acc);
-        dst[s] = fma(-winv, r, u0);
     }
     acc = block_sum(acc);
     if (threadIdx.x == 0)
@@ -660,11 +578,20 @@ int max_blocks_sweep32()
 
 SweepCfg make_sweep_cfg(const Geo &g, const Split &s, int sm_count, int kb)
 {
+    return make_sweep_cfg_xt(g, s, sm_count, kb, 0);
+}
+
+// xt: threads along x per tile (a power of two in [8, 256]); 0 picks the
+// smallest power of two covering a row's targets, at most 128
+SweepCfg make_sweep_cfg_xt(const Geo &g, const Split &s, int sm_count, int kb, int xt)
+{
     SweepCfg c;
     c.threads = 256;
-    c.XT = pow2_at_least(s.nxh);
-    if (c.XT > 128)
+    c.XT = xt > 0 ? pow2_at_least(xt) : pow2_at_least(s.nxh);
+    if (xt <= 0 && c.XT > 128)
         c.XT = 128;
+    if (c.XT > 256)
+        c.XT = 256;
     if (c.XT < 8)
         c.XT = 8;
     c.TJ = c.threads / c.XT;

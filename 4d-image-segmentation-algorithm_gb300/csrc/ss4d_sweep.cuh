@@ -1,0 +1,104 @@
+// ss4d_sweep.cuh — the tile schedule and the FP64 red-black update shared by
+// the single-volume sweeps (ss4d_kernels_fast.cu) and the batched sweeps
+// (ss4d_batch.cu).  Layouts: ss4d_common.cuh (Split, coef_at).
+#pragma once
+
+#include "ss4d_kernels.cuh"
+
+namespace ss4d {
+
+// streamed once per sweep: evict first
+__device__ __forceinline__ double ld_stream(const double *p)
+{
+    return __ldcs(p);
+}
+__device__ __forceinline__ float ld_stream(const float *p)
+{
+    return __ldcs(p);
+}
+__device__ __forceinline__ double2 ld_stream2(const double *p)
+{
+    return __ldcs(reinterpret_cast<const double2 *>(p));
+}
+__device__ __forceinline__ float4 ld_stream4(const float *p)
+{
+    return __ldcs(reinterpret_cast<const float4 *>(p));
+}
+
+// read-only for the whole kernel (the other colour)
+template <typename T>
+__device__ __forceinline__ T ld_ro(const T *p)
+{
+    return __ldg(p);
+}
+
+// Select one of a pair held in a by-value kernel parameter without a runtime
+// array index (which would copy the parameter struct to local memory).
+template <typename T>
+__device__ __forceinline__ T *pick(T *const (&a)[2], int i)
+{
+    return i ? a[1] : a[0];
+}
+
+struct TileCoord {
+    int j, k, l, xi;
+    bool ok;
+};
+
+// Tile order: x chunk fastest, then j group, then k inside a k block, then
+// frame l, then k block.  Consecutive tiles (which a persistent grid works on
+// at the same time) thus cover a few k planes of all frames, so the
+// neighbouring-plane reads of the other colour hit in L2.
+__device__ __forceinline__ TileCoord tile_coord(const Geo &g, const SweepCfg &cfg, long long t, int tx, int ty)
+{
+    TileCoord c;
+    long long r = t;
+    const int xc = (int)(r % cfg.nXC);
+    r /= cfg.nXC;
+    const int jg = (int)(r % cfg.nJG);
+    r /= cfg.nJG;
+    const int kin = (int)(r % cfg.KB);
+    r /= cfg.KB;
+    const int lt = (int)(r % g.nt);
+    const int kb = (int)(r / g.nt);
+    c.k = 1 + kb * cfg.KB + kin;
+    c.l = 1 + lt;
+    c.j = 1 + jg * cfg.TJ + ty;
+    c.xi = xc * cfg.XT + tx;
+    c.ok = c.k <= g.nz && c.j <= g.ny;
+    return c;
+}
+
+// compact per-colour interior index of a sweep target
+__device__ __forceinline__ long long tile_coef_index(const Geo &g, const Split &sp, const TileCoord &tc)
+{
+    return ((((long long)(tc.l - 1) * g.nz + (tc.k - 1)) * g.ny + (tc.j - 1)) * sp.nxh) + tc.xi;
+}
+
+// One FP64 update of the target at split index s (row phase p):
+//   r = diag*u - (prev + sum_f c a_f u_f),   dst = u - (omega/diag) r.
+// Returns the pre-update residual r.
+__device__ __forceinline__ double sweep64_target(const Geo &g, const Split &sp, const TileCoord &tc, int p,
+                                                 long long s, const double *src, double *dst,
+                                                 const double *__restrict__ oth, const double *__restrict__ cf,
+                                                 const double *__restrict__ pv)
+{
+    const long long Hy = sp.Hs, Hz = Hy * g.jM, Hw = Hz * g.kM;
+    const double u0 = src[s];
+    const double *cv = cf + coef_at(tile_coef_index(g, sp, tc), 0, 10); // component f at cv[32 f]
+    double S = fma(ld_stream(cv), ld_ro(oth + s - p + 1), ld_stream(pv + s));
+    S = fma(ld_stream(cv + 32), ld_ro(oth + s - p), S);
+    S = fma(ld_stream(cv + 64), ld_ro(oth + s + Hy), S);
+    S = fma(ld_stream(cv + 96), ld_ro(oth + s - Hy), S);
+    S = fma(ld_stream(cv + 128), ld_ro(oth + s + Hz), S);
+    S = fma(ld_stream(cv + 160), ld_ro(oth + s - Hz), S);
+    S = fma(ld_stream(cv + 192), ld_ro(oth + s + Hw), S);
+    S = fma(ld_stream(cv + 224), ld_ro(oth + s - Hw), S);
+    const double diag = ld_stream(cv + 256);
+    const double winv = ld_stream(cv + 288);
+    const double r = fma(diag, u0, -S); // S includes prev
+    dst[s] = fma(-winv, r, u0);
+    return r;
+}
+
+} // namespace ss4d

@@ -138,6 +138,13 @@ def lib() -> C.CDLL:
         "ss4d_copy_device": ([vp, vp, vp, C.c_size_t], st),
         "ss4d_synchronize": ([vp], st),
         "ss4d_scene_generate": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, vp, vp, C.c_int], st),
+        "ss4d_batch_create": ([C.c_int, C.POINTER(Dims), vp, C.POINTER(vp)], st),
+        "ss4d_batch_destroy": ([vp], st),
+        "ss4d_batch_set_graph": ([vp, C.c_int], st),
+        "ss4d_batch_set_shape": ([vp, C.c_int, C.c_int, C.c_int], st),
+        "ss4d_batch_autotune": ([vp, C.POINTER(Params), C.POINTER(vp), C.POINTER(vp), C.POINTER(C.c_int),
+                                 C.POINTER(C.c_int)], st),
+        "ss4d_batch_seg_time_step": ([vp, C.POINTER(Params), C.POINTER(vp), C.POINTER(vp), C.POINTER(StepStats)], st),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -350,3 +357,60 @@ class Solver:
 
     def synchronize(self):
         _check(self.L.ss4d_synchronize(self.h), "synchronize")
+
+
+class Batch:
+    """ss4d_batch: many volumes (uneven sizes, own parameters) stepped together
+    in the plain FP64 form, one persistent launch per half-sweep for all."""
+
+    def __init__(self, dims_list, stream: int | None = None):
+        self.L = lib()
+        n = len(dims_list)
+        arr = (Dims * n)(*[Dims(*d) for d in dims_list])
+        h = C.c_void_p()
+        _check(self.L.ss4d_batch_create(n, arr, stream, C.byref(h)), "batch_create")
+        self.h, self.n = h, n
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ss4d_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_graph(self, on: bool):
+        _check(self.L.ss4d_batch_set_graph(self.h, 1 if on else 0), "batch_set_graph")
+
+    def set_shape(self, v: int, xt: int, k_block: int):
+        _check(self.L.ss4d_batch_set_shape(self.h, v, xt, k_block), "batch_set_shape")
+
+    @staticmethod
+    def _args(params, us, gs):
+        n = len(us)
+        P = (Params * n)(*params)
+        U = (C.c_void_p * n)(*[_ptr(u) for u in us])
+        G = (C.c_void_p * (8 * n))(*[_ptr(g) for g8 in gs for g in g8])
+        return P, U, G
+
+    def autotune(self, params, us, gs):
+        P, U, G = self._args(params, us, gs)
+        xt = (C.c_int * self.n)()
+        kb = (C.c_int * self.n)()
+        _check(self.L.ss4d_batch_autotune(self.h, P, U, G, xt, kb), "batch_autotune")
+        return list(zip(list(xt), list(kb)))
+
+    def seg_time_step(self, params, us, gs) -> list:
+        P, U, G = self._args(params, us, gs)
+        S = (StepStats * self.n)()
+        _check(self.L.ss4d_batch_seg_time_step(self.h, P, U, G, S), "batch_seg_time_step")
+        return [s.as_dict() for s in S]

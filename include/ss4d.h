@@ -241,6 +241,35 @@ ss4d_status ss4d_mass(ss4d_solver *s, double h, const double *d_a, double *out);
 ss4d_status ss4d_mcf_set_boundary_exact(ss4d_solver *s, double h, double t, double *d_u);
 ss4d_status ss4d_mcf_exact_solution(ss4d_solver *s, double h, double t, double *d_out);
 
+/* ---- batched volumes --------------------------------------------------- */
+/* Many independent volumes, of different sizes and parameters, advanced
+ * together in the plain FP64 form.  Every half-sweep of all volumes is ONE
+ * persistent launch over the concatenated tiles of the volumes, and the SOR
+ * loop is one CUDA graph; each volume keeps its own stopping test
+ * (sum r^2 h^4 <= its gsTol, or its maxNoGSIteration) and once it has stopped
+ * its tiles return at once.  The reference runs one volume per process, so
+ * these entry points have no counterpart there; per volume the arithmetic is
+ * that of ss4d_seg_time_step in SS4D_ARITH_FP64 without the rescale (no
+ * centres, Mmask == 1).  At most SS4D_BATCH_MAX_VOLUMES volumes. */
+#define SS4D_BATCH_MAX_VOLUMES 64
+typedef struct ss4d_batch ss4d_batch;
+ss4d_status ss4d_batch_create(int n, const ss4d_dims *dims, void *stream, ss4d_batch **out);
+ss4d_status ss4d_batch_destroy(ss4d_batch *b);
+ss4d_status ss4d_batch_set_graph(ss4d_batch *b, int enable);
+/* Tile shape of volume v: xt threads along x (power of two, 8..256; 0 =
+ * automatic) and k-block depth k_block (>= 1).  Results do not depend on it. */
+ss4d_status ss4d_batch_set_shape(ss4d_batch *b, int v, int xt, int k_block);
+/* Autotuner: for every volume, time candidate tile shapes on that volume's
+ * own sweeps (coefficients of d_u[v], d_g[8v..8v+7]; u is not modified) and
+ * keep the fastest.  xt_out/kb_out (n entries each, may be NULL) receive the
+ * chosen shapes. */
+ss4d_status ss4d_batch_autotune(ss4d_batch *b, const ss4d_params *p, double *const *d_u,
+                                const double *const *d_g, int *xt_out, int *kb_out);
+/* One time step of every volume: parameters p[v], u d_u[v] (updated in
+ * place), edge-detector faces d_g[8v + f]; stats[v] (may be NULL). */
+ss4d_status ss4d_batch_seg_time_step(ss4d_batch *b, const ss4d_params *p, double *const *d_u,
+                                     const double *const *d_g, ss4d_step_stats *stats);
+
 /* ---- memory helpers (used by the reference-named layer) --------------- */
 /* Device / pinned-host allocations and copies on the handle's stream.  They
  * exist so that C callers without the CUDA headers (ss4d_compat.c) can mirror

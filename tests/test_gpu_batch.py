@@ -1,0 +1,73 @@
+"""Batched volumes: one persistent launch per half-sweep over volumes of
+different sizes and parameters must give every volume exactly what the
+single-volume FP64 form gives it (same per-voxel arithmetic; only the
+residual summation is organised differently)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).to("cuda")
+
+
+def _volumes(ss4d, oracle, sizes, seed=5):
+    rng = np.random.default_rng(seed)
+    vols = []
+    for n, dims in enumerate(sizes):
+        p = ss4d.scene_params(K=float(rng.uniform(500, 2000)), tau=float(rng.uniform(0.25, 1.0)))
+        i0, u0 = ss4d.scene(1, *dims, seed=seed + n)
+        g = oracle.gfaces(p, i0, np.zeros_like(i0))
+        vols.append((p, u0, g))
+    return vols
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_batch_matches_single_volume_solves(ss4d, oracle, cuda, graph):
+    torch = cuda
+    sizes = [(20, 16, 12, 5), (33, 9, 14, 7), (12, 24, 10, 3)]
+    vols = _volumes(ss4d, oracle, sizes)
+    want, its = [], []
+    for (p, u0, g), dims in zip(vols, sizes):
+        u = _dev(torch, u0)
+        gd = [_dev(torch, a) for a in g]
+        with ss4d.Solver.for_interior(*dims, arith="fp64") as S:
+            z = [S.seg_time_step(p, u, None, gd)["iterations"] for _ in range(2)]
+        want.append(u.cpu().numpy())
+        its.append(z)
+    us = [_dev(torch, u0) for _, u0, _ in vols]
+    gs = [[_dev(torch, a) for a in g] for _, _, g in vols]
+    params = [p for p, _, _ in vols]
+    with ss4d.Batch([(d[0] + 2, d[1] + 2, d[2] + 2, d[3] + 2) for d in sizes]) as B:
+        B.set_graph(graph)
+        got_its = [[s["iterations"] for s in B.seg_time_step(params, us, gs)] for _ in range(2)]
+    for v in range(len(sizes)):
+        assert [got_its[0][v], got_its[1][v]] == its[v], v
+        assert np.array_equal(us[v].cpu().numpy(), want[v]), v
+
+
+def test_batch_autotuned_shapes_do_not_change_results(ss4d, oracle, cuda):
+    torch = cuda
+    sizes = [(40, 20, 12, 4), (17, 30, 9, 6)]
+    vols = _volumes(ss4d, oracle, sizes, seed=9)
+    params = [p for p, _, _ in vols]
+    gs = [[_dev(torch, a) for a in g] for _, _, g in vols]
+    dims = [(d[0] + 2, d[1] + 2, d[2] + 2, d[3] + 2) for d in sizes]
+    out = []
+    for tune in (False, True):
+        us = [_dev(torch, u0) for _, u0, _ in vols]
+        with ss4d.Batch(dims) as B:
+            if tune:
+                shapes = B.autotune(params, us, gs)
+                assert all(xt >= 8 and (xt & (xt - 1)) == 0 and kb >= 1 for xt, kb in shapes)
+                # the autotuner only reads u
+                assert all(np.array_equal(u.cpu().numpy(), v[1]) for u, v in zip(us, vols))
+            else:
+                B.set_shape(0, 8, 1)
+                B.set_shape(1, 64, 8)
+            stats = B.seg_time_step(params, us, gs)
+        out.append(([u.cpu().numpy() for u in us], [s["iterations"] for s in stats]))
+    assert out[0][1] == out[1][1]
+    for a, b in zip(out[0][0], out[1][0]):
+        assert np.array_equal(a, b)

@@ -34,6 +34,8 @@ CUDA_UNITS = {
     "ss4d_api.cu": [],
     "ss4d_noalloc.cu": [],
     "ss4d_batch.cu": [],
+    "ss4d_ws.cu": [],
+    "ss4d_nn.cu": [],
 }
 C_UNITS = {"ss4d_scene.c": ["-fopenmp"]}
 

@@ -112,6 +112,13 @@ struct ss4d_solver {
     double *d_bx, *d_by, *d_bz;
     int balls_cap;
     cudaEvent_t ev0, ev1;
+    // learned warm start (mixed form)
+    ss4d_wsnet *ws_net;
+    const double *ws_i0;
+    void *ws_x0;   // BF16 features [nt][nz][ny][nx][16]
+    float *ws_y;   // prediction [nt][nz][ny][nx]
+    CPtrs8 cur_g;  // g of the segmentation step in progress
+    int have_g;
     // per-kernel timing (ss4d_solver_set_timing)
     int timing;
     double ktime[SS4D_K_COUNT];
@@ -280,7 +287,7 @@ extern "C" ss4d_status ss4d_solver_destroy(ss4d_solver *s)
     // allocation bases only: R[1], Bk, P[1], coef[1], ... point inside them
     void *dev[] = {s->d_partial, s->d_scalar, s->d_state, s->d_params, s->d_scratch, s->d_coef_nat,
                    s->sb.R[0], s->sb.P[0], s->sb.coef[0], s->sb.coef32[0], s->sb.dR[0], s->sb.r32[0], s->sb.fn[0],
-                   s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz};
+                   s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz, s->ws_x0, s->ws_y};
     for (void *p : dev)
         if (p)
             cudaFree(p);
@@ -572,11 +579,95 @@ static ss4d_status finish_stats(ss4d_solver *s, ss4d_step_stats *stats, int mixe
         stats->first_residual = L.R_first;
         stats->refinements = mixed ? L.refinements : 0;
         stats->status = L.status;
+        stats->warm_started = L.warm;
     }
     if (L.status != SS4D_OK) {
         set_err("SOR residual became non-finite at iteration %d", L.z);
         return (ss4d_status)L.status;
     }
+    return SS4D_OK;
+}
+
+static ss4d_status ensure_ws_buffers(ss4d_solver *s)
+{
+    if (!s->ws_x0) {
+        CKS(dmalloc(s, &s->ws_x0, (size_t)s->geo.nint * 32));
+        CKS(dmalloc(s, (void **)&s->ws_y, (size_t)s->geo.nint * 4));
+    }
+    return SS4D_OK;
+}
+
+// mixed form, state in mode 0 with zero corrections: the first FP64
+// refinement pass at u^n (r0 into r32, R_first) and the controller's test;
+// then the network's features, its prediction of the first correction, the
+// check of that prediction and the keep/discard decision (ss4d_ws.cu)
+static ss4d_status ws_first_pass(ss4d_solver *s)
+{
+    const SweepCfg &cfg = s->cfg;
+    launch_refine(s->geo, s->sp, cfg, 0, s->sb, s->d_params, s->d_state, s->stream);
+    launch_refine(s->geo, s->sp, cfg, 1, s->sb, s->d_params, s->d_state, s->stream);
+    launch_ctrl_mixed(s->sb, cfg.grid, s->d_params, s->d_state, 0, 0, s->stream);
+    s->launches += 3;
+    return last_launch();
+}
+
+static ss4d_status warm_start_prologue(ss4d_solver *s)
+{
+    const Geo &g = s->geo;
+    CKS(ensure_ws_buffers(s));
+    CKS(ws_first_pass(s));
+    ss4d_status st = SS4D_OK;
+    timed(s, SS4D_K_WARM, true, [&] {
+        launch_ws_features(g, s->sp, s->sb, s->ws_i0, s->cur_g, s->d_state, s->d_params, s->ws_x0, s->stream);
+        st = ss4d_wsnet_set_stream(s->ws_net, s->stream);
+        if (st == SS4D_OK)
+            st = ss4d_wsnet_forward(s->ws_net, s->ws_x0, g.nx, g.ny, g.nz, g.nt, s->ws_y);
+        launch_ws_apply(g, s->sp, s->sb, s->ws_y, s->d_state, s->d_params, s->stream);
+        launch_ws_check_decide(g, s->sp, s->cfg, s->sb, s->d_state, s->d_params, s->stream);
+    });
+    CKS(st);
+    s->launches += 1 + 4 + 1 + 3;
+    return last_launch();
+}
+
+extern "C" ss4d_status ss4d_solver_set_warm_start(ss4d_solver *s, ss4d_wsnet *n, const double *d_i0)
+{
+    REQ(s, "solver is NULL");
+    REQ(!n || d_i0, "the warm start needs the presmoothed image");
+    s->ws_net = n;
+    s->ws_i0 = n ? d_i0 : nullptr;
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_ws_features(ss4d_solver *s, const ss4d_params *p, double *d_u, const double *const d_g[8],
+                                        const double *d_i0, void *d_x0, double *sigma)
+{
+    REQ(s && d_u && d_g && d_i0 && d_x0 && sigma, "NULL argument");
+    CKS(check_params(p));
+    CPtrs8 gi;
+    for (int f = 0; f < 8; ++f) {
+        REQ(d_g[f], "a g array is NULL");
+        gi.p[f] = d_g[f];
+    }
+    CKS(ensure_split(s, 1));
+    const Split &sp = s->sp;
+    launch_assemble(s->geo, sp, d_u, gi, 1, *p, s->sb, 1, s->stream);
+    launch_pack(s->geo, sp, d_u, d_u, s->sb, s->stream);
+    s->launches += 3;
+    CKS(upload_params(s, p));
+    const size_t fb = sizeof(float) * sp.cs;
+    CK(cudaMemsetAsync(s->sb.dR[0], 0, fb, s->stream));
+    CK(cudaMemsetAsync(s->sb.dR[1], 0, fb, s->stream));
+    CK(cudaMemsetAsync(s->sb.dB, 0, fb, s->stream));
+    launch_loop_init(s->d_state, 0, s->stream);
+    CKS(ws_first_pass(s));
+    launch_ws_features(s->geo, sp, s->sb, d_i0, gi, s->d_state, s->d_params, d_x0, s->stream);
+    s->launches += 2;
+    CKS(last_launch());
+    CK(cudaMemcpyAsync(s->h_state, s->d_state, sizeof(LoopState), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    const double h4 = p->h * p->h * p->h * p->h;
+    *sigma = sqrt(s->h_state->R_first / ((double)s->geo.nint * h4));
     return SS4D_OK;
 }
 
@@ -600,6 +691,8 @@ static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixe
         CK(cudaMemsetAsync(s->sb.dB, 0, fb, s->stream));
         launch_loop_init(s->d_state, 0, s->stream);
         s->launches += 1;
+        if (s->ws_net && s->have_g)
+            CKS(warm_start_prologue(s));
     }
     CKS(last_launch());
     bool graphed = false;
@@ -617,7 +710,7 @@ static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixe
     }
     if (!graphed) {
         // host-driven form of the same loop: one small readback per iteration
-        int mode = 0; // mixed form: the mode the controller left for this body
+        int mode = (mixed && s->ws_net && s->have_g) ? 1 : 0; // the mode the controller left for this body
         for (int guard = 0; guard < 4 * (p->maxNoGSIteration + 4) + 16; ++guard) {
             if (!mixed) {
                 timed(s, SS4D_K_SWEEP64, true,
@@ -934,9 +1027,12 @@ extern "C" ss4d_status ss4d_seg_time_step(ss4d_solver *s, const ss4d_params *p, 
         if (d_prev_u)
             CK(cudaMemcpyAsync(d_prev_u, d_u, sizeof(double) * g.n, cudaMemcpyDeviceToDevice, s->stream));
         timed(s, SS4D_K_ASSEMBLE, true, [&] { launch_assemble(g, s->sp, d_u, gi, 1, *p, s->sb, mixed, s->stream); });
-        s->launches += 1;
+        s->launches += 2; // faces + voxel coefficients
         CKS(last_launch());
+        s->cur_g = gi;
+        s->have_g = 1;
         st = split_solve(s, p, d_u, d_u, stats);
+        s->have_g = 0;
     }
     if (st == SS4D_OK)
         st = rescale_impl(s, p, d_u, d_Mmask, balls);

@@ -53,6 +53,8 @@ struct LoopState {
     int dsrc;        // mixed form: ping-pong index of the current red correction
     int final_red;   // red buffer holding the result once the loop stopped
     int bodies;      // loop bodies the controller has run
+    int keep;        // mixed form: the next round starts from the correction already in place
+    int warm;        // mixed form: this step's first correction came from the learned predictor
     int pad_;
     double R;        // last FP64 residual (sum r^2 h^4)
     double R_first;  // FP64 residual after iteration 1 (fast) / initial (mixed)
@@ -130,6 +132,14 @@ int max_blocks_sweep32();
 
 // sets the text ss4d_last_error() returns (ss4d_api.cu)
 void set_error_text(const char *msg);
+
+// ---- learned warm start, solver side (ss4d_ws.cu) --------------------------
+void launch_ws_features(const Geo &g, const Split &sp, SplitBufs b, const double *i0, CPtrs8 gin,
+                        const LoopState *st, const DevParams *dp, void *x0, cudaStream_t s);
+void launch_ws_apply(const Geo &g, const Split &sp, SplitBufs b, const float *y, const LoopState *st,
+                     const DevParams *dp, cudaStream_t s);
+void launch_ws_check_decide(const Geo &g, const Split &sp, const SweepCfg &cfg, SplitBufs b, LoopState *st,
+                            const DevParams *dp, cudaStream_t s);
 
 // ---- a handle's colour-split machinery, for the batched solver ------------
 // (ss4d_api.cu; every call issues work on the handle's stream)

@@ -29,41 +29,6 @@ namespace ss4d {
 // ---------------------------------------------------------------------------
 // helpers
 
-// FP32 <-> FP64 conversions by integer bit operations.  On this GPU a
-// conversion instruction to or from FP64 issues at the FP64 rate (1/68 of
-// FP32); these run on the integer pipe instead.
-// Exact float -> double for zero, normal numbers, Inf and NaN (FP32
-// subnormals, below 1.2e-38, become signed zero).
-__device__ __forceinline__ double f2d_bits(float f)
-{
-    const unsigned u = __float_as_uint(f);
-    const unsigned sign = u & 0x80000000u, e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
-    const unsigned de = e == 0xFFu ? 0x7FFu : e + 896u;
-    const unsigned hi = e == 0u ? sign : (sign | (de << 20) | (m >> 3));
-    const unsigned lo = e == 0u ? 0u : (m & 7u) << 29;
-    return __hiloint2double((int)hi, (int)lo);
-}
-// double -> float by truncating the mantissa (error below 2^-23 relative);
-// magnitudes outside the FP32 normal range become zero or Inf, NaN stays NaN.
-__device__ __forceinline__ float d2f_bits(double d)
-{
-    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
-    const unsigned sign = hi & 0x80000000u;
-    const int e = (int)((hi >> 20) & 0x7FFu);
-    const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
-    const int fe = e - 896;
-    unsigned r;
-    if (e == 0x7FF)
-        r = sign | 0x7F800000u | (m ? 0x400000u : 0u);
-    else if (fe <= 0)
-        r = sign;
-    else if (fe >= 255)
-        r = sign | 0x7F800000u;
-    else
-        r = sign | ((unsigned)fe << 23) | m;
-    return __uint_as_float(r);
-}
-
 // ---------------------------------------------------------------------------
 // assembly: the reference's _gs_coefficients_ (segmentation4D.c:446-580) in
 // two passes.  The reference evaluates every face twice (the east face of
@@ -109,12 +74,6 @@ __device__ __forceinline__ void store_coef(double *cf, float *cf32, long long t,
         __stcs(f4, make_float4(d2f_bits(ac[0]), d2f_bits(ac[1]), d2f_bits(ac[2]), d2f_bits(ac[3])));
         __stcs(f4 + 1, make_float4(d2f_bits(ac[4]), d2f_bits(ac[5]), d2f_bits(ac[6]), d2f_bits(ac[7])));
     }
-}
-
-// compact per-colour interior index of voxel (i, j, k, l)
-__device__ __forceinline__ long long coef_index(const Geo &g, const Split &sp, int i, int j, int k, int l)
-{
-    return ((((long long)(l - 1) * g.nz + (k - 1)) * g.ny + (j - 1)) * sp.nxh) + ((i - 1) >> 1);
 }
 
 // Threads cover voxels v with every index in [0, n_a]; face d of v (between
@@ -270,6 +229,8 @@ __global__ void k_loop_init(LoopState *st, int mode)
     st->dsrc = 0;
     st->final_red = 0;
     st->bodies = 0;
+    st->keep = 0;
+    st->warm = 0;
     st->pad_ = 0;
     st->R = 0.0;
     st->R_first = 0.0;
@@ -367,7 +328,7 @@ template <int COL>
 __global__ void __launch_bounds__(256) k_refine(Geo g, Split sp, SweepCfg cfg, SplitBufs b,
                                                 const DevParams *__restrict__ dp, const LoopState *__restrict__ st)
 {
-    if (st->mode != 0)
+    if (st->mode != 0 || st->stop)
         return;
     const int ds = st->dsrc;
     double *own = COL == 0 ? b.R[0] : b.Bk;
@@ -414,10 +375,11 @@ __global__ void __launch_bounds__(256) k_refine(Geo g, Split sp, SweepCfg cfg, S
         b.partial[COL][blockIdx.x] = acc;
 }
 
-// clears the corrections at the start of a round (ghosts stay zero)
+// clears the corrections at the start of a round (ghosts stay zero), unless
+// the round is to start from the correction already in place (warm start)
 __global__ void k_zero_delta(Split sp, SplitBufs b, const LoopState *__restrict__ st)
 {
-    if (st->mode != 1)
+    if (st->mode != 1 || st->stop || st->keep)
         return;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < sp.cs; t += (long long)gridDim.x * blockDim.x) {
         b.dR[0][t] = 0.f;
@@ -431,7 +393,7 @@ __global__ void __launch_bounds__(256) k_sweep32(Geo g, Split sp, SweepCfg cfg, 
                                                  const DevParams *__restrict__ dp, const LoopState *__restrict__ st)
 {
     const int mode = st->mode;
-    if (COL == 0 ? (mode == 0) : (mode != 2))
+    if ((COL == 0 ? (mode == 0) : (mode != 2)) || st->stop)
         return;
     const int ds = st->dsrc;
     const float *src;
@@ -487,6 +449,11 @@ __global__ void __launch_bounds__(256) k_sweep32(Geo g, Split sp, SweepCfg cfg, 
 __global__ void k_ctrl_mixed(SplitBufs b, int nparts, const DevParams *__restrict__ dp, LoopState *st,
                              cudaGraphConditionalHandle h, int use_cond)
 {
+    if (st->stop) { // stopped before the loop (the warm-start prologue's test)
+        if (threadIdx.x == 0 && use_cond)
+            cudaGraphSetConditional(h, 0u);
+        return;
+    }
     const int mode = st->mode;
     double a = 0.0, c = 0.0;
     if (mode != 1) {
@@ -523,6 +490,7 @@ __global__ void k_ctrl_mixed(SplitBufs b, int nparts, const DevParams *__restric
         st->mode = 2;
         st->dsrc ^= 1;
         st->round_z = 0;
+        st->keep = 0;
     } else {
         const double om1 = 1.0 - dp->omega;
         const double Rd = (a + om1 * om1 * c) * dp->h4;

@@ -25,6 +25,41 @@ __device__ __forceinline__ float4 ld_stream4(const float *p)
     return __ldcs(reinterpret_cast<const float4 *>(p));
 }
 
+// FP32 <-> FP64 conversions by integer bit operations.  On this GPU a
+// conversion instruction to or from FP64 issues at the FP64 rate (1/68 of
+// FP32); these run on the integer pipe instead.
+// Exact float -> double for zero, normal numbers, Inf and NaN (FP32
+// subnormals, below 1.2e-38, become signed zero).
+__device__ __forceinline__ double f2d_bits(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned sign = u & 0x80000000u, e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+    const unsigned de = e == 0xFFu ? 0x7FFu : e + 896u;
+    const unsigned hi = e == 0u ? sign : (sign | (de << 20) | (m >> 3));
+    const unsigned lo = e == 0u ? 0u : (m & 7u) << 29;
+    return __hiloint2double((int)hi, (int)lo);
+}
+// double -> float by truncating the mantissa (error below 2^-23 relative);
+// magnitudes outside the FP32 normal range become zero or Inf, NaN stays NaN.
+__device__ __forceinline__ float d2f_bits(double d)
+{
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const unsigned sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7FFu);
+    const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const int fe = e - 896;
+    unsigned r;
+    if (e == 0x7FF)
+        r = sign | 0x7F800000u | (m ? 0x400000u : 0u);
+    else if (fe <= 0)
+        r = sign;
+    else if (fe >= 255)
+        r = sign | 0x7F800000u;
+    else
+        r = sign | ((unsigned)fe << 23) | m;
+    return __uint_as_float(r);
+}
+
 // read-only for the whole kernel (the other colour)
 template <typename T>
 __device__ __forceinline__ T ld_ro(const T *p)
@@ -67,6 +102,12 @@ __device__ __forceinline__ TileCoord tile_coord(const Geo &g, const SweepCfg &cf
     c.xi = xc * cfg.XT + tx;
     c.ok = c.k <= g.nz && c.j <= g.ny;
     return c;
+}
+
+// compact per-colour interior index of voxel (i, j, k, l)
+__device__ __forceinline__ long long coef_index(const Geo &g, const Split &sp, int i, int j, int k, int l)
+{
+    return ((((long long)(l - 1) * g.nz + (k - 1)) * g.ny + (j - 1)) * sp.nxh) + ((i - 1) >> 1);
 }
 
 // compact per-colour interior index of a sweep target

@@ -2,9 +2,10 @@
 
 The reference is a set of C programs whose "interface" is the functions and
 globals of segmentation4D.c / mcf_4D.c.  This module mirrors that interface
-for Python callers (tests, benchmarks): the same function names in
-`ReferenceLayer`, the same parameter names in `Params`, the same padded
-x-fastest FP64 layout.  Device arrays are passed as integer device pointers
+for Python callers (tests, benchmarks): the reference's parameter names in
+`Params`, its step functions as `Solver` methods, the same padded x-fastest
+FP64 layout.  The reference-named C layer (libss4d_seg.so / libss4d_mcf.so,
+include/ss4d_compat.h) sits at `SEG_PATH` / `MCF_PATH`.  Device arrays are passed as integer device pointers
 or as objects with a ``data_ptr()`` method (e.g. torch tensors).
 
 Every call goes to libss4d.so; there is no Python or CPU implementation of
@@ -145,6 +146,18 @@ def lib() -> C.CDLL:
         "ss4d_batch_autotune": ([vp, C.POINTER(Params), C.POINTER(vp), C.POINTER(vp), C.POINTER(C.c_int),
                                  C.POINTER(C.c_int)], st),
         "ss4d_batch_seg_time_step": ([vp, C.POINTER(Params), C.POINTER(vp), C.POINTER(vp), C.POINTER(StepStats)], st),
+        "ss4d_wsnet_param_count": ([], C.c_size_t),
+        "ss4d_wsnet_create": ([vp, C.POINTER(vp)], st),
+        "ss4d_wsnet_destroy": ([vp], st),
+        "ss4d_wsnet_set_stream": ([vp, vp], st),
+        "ss4d_wsnet_init": ([vp, C.c_uint64], st),
+        "ss4d_wsnet_set_params": ([vp, vp], st),
+        "ss4d_wsnet_get_params": ([vp, vp], st),
+        "ss4d_wsnet_forward": ([vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp], st),
+        "ss4d_wsnet_train_step": ([vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float,
+                                   C.POINTER(C.c_float), vp], st),
+        "ss4d_ws_features": ([vp, C.POINTER(Params), vp, P8, vp, vp, dp], st),
+        "ss4d_solver_set_warm_start": ([vp, vp, vp], st),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -269,7 +282,7 @@ class Solver:
     def set_tiling(self, k_block: int, max_grid: int = 0):
         _check(self.L.ss4d_solver_set_tiling(self.h, k_block, max_grid), "set_tiling")
 
-    KERNELS = ("sweep64", "sweep32", "refine", "assemble", "pack")
+    KERNELS = ("sweep64", "sweep32", "refine", "assemble", "pack", "warm")
 
     def set_timing(self, on: bool):
         _check(self.L.ss4d_solver_set_timing(self.h, 1 if on else 0), "set_timing")
@@ -324,6 +337,21 @@ class Solver:
                                          C.byref(B) if B is not None else None, C.byref(st)), "seg_time_step")
         del keep
         return st.as_dict()
+
+    def ws_features(self, p: Params, u, g8, i0, x0) -> float:
+        """Warm-start features of the step from u (BF16 [nt][nz][ny][nx][16]
+        into x0); returns the RMS s of the step's initial residual."""
+        sig = C.c_double(0)
+        _check(self.L.ss4d_ws_features(self.h, C.byref(p), _ptr(u), _p8(g8), _ptr(i0), _ptr(x0), C.byref(sig)),
+               "ws_features")
+        return sig.value
+
+    def set_warm_start(self, net, i0):
+        """Attach a `Wsnet` (None detaches); i0 is the presmoothed image.  The
+        mixed-form segmentation steps then start from its prediction."""
+        self._ws_keep = (net, i0)
+        _check(self.L.ss4d_solver_set_warm_start(self.h, net.h if net is not None else None,
+                                                 _ptr(i0) if net is not None else None), "set_warm_start")
 
     def mcf_time_step(self, p: Params, step: int, u, prev=None) -> dict:
         st = StepStats()
@@ -414,3 +442,78 @@ class Batch:
         S = (StepStats * self.n)()
         _check(self.L.ss4d_batch_seg_time_step(self.h, P, U, G, S), "batch_seg_time_step")
         return [s.as_dict() for s in S]
+
+
+class Wsnet:
+    """ss4d_wsnet: the learned warm start's convolutional network (BF16
+    weights/activations, FP32 master parameters and Adam state on the device).
+    Parameter vector layout: per layer L = 0..3, weights [27][cout][cin]
+    (tap = 9 dz + 3 dy + dx, offsets -1..1, x fastest) then bias [cout];
+    channels 16 -> 24 -> 24 -> 24 -> 1."""
+
+    LAYERS = ((16, 24), (24, 24), (24, 24), (24, 1))
+
+    def __init__(self, stream: int | None = None, seed: int | None = 0):
+        self.L = lib()
+        h = C.c_void_p()
+        _check(self.L.ss4d_wsnet_create(stream, C.byref(h)), "wsnet_create")
+        self.h = h
+        self.nparam = int(self.L.ss4d_wsnet_param_count())
+        if seed is not None:
+            self.init(seed)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ss4d_wsnet_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_stream(self, stream: int | None):
+        _check(self.L.ss4d_wsnet_set_stream(self.h, stream), "wsnet_set_stream")
+
+    def init(self, seed: int):
+        _check(self.L.ss4d_wsnet_init(self.h, seed), "wsnet_init")
+
+    def get_params(self):
+        import numpy as np
+        out = np.empty(self.nparam, dtype=np.float32)
+        _check(self.L.ss4d_wsnet_get_params(self.h, out.ctypes.data), "wsnet_get_params")
+        return out
+
+    def set_params(self, params):
+        import numpy as np
+        a = np.ascontiguousarray(params, dtype=np.float32)
+        if a.size != self.nparam:
+            raise SS4DError(1, "wsnet_set_params", f"expected {self.nparam} values, got {a.size}")
+        _check(self.L.ss4d_wsnet_set_params(self.h, a.ctypes.data), "wsnet_set_params")
+
+    def forward(self, x0, nx: int, ny: int, nz: int, nf: int, out):
+        _check(self.L.ss4d_wsnet_forward(self.h, _ptr(x0), nx, ny, nz, nf, _ptr(out)), "wsnet_forward")
+
+    def train_step(self, x0, target, nx: int, ny: int, nz: int, nf: int, margin: int = 0, lr: float = 1e-3,
+                   grad=None) -> float:
+        loss = C.c_float(0)
+        _check(self.L.ss4d_wsnet_train_step(self.h, _ptr(x0), _ptr(target), nx, ny, nz, nf, margin, lr,
+                                            C.byref(loss), _ptr(grad)), "wsnet_train_step")
+        return loss.value
+
+    @classmethod
+    def split(cls, params):
+        """[(W [27][cout][cin], b [cout]) per layer] views of a parameter vector."""
+        out, off = [], 0
+        for cin, cout in cls.LAYERS:
+            nw = 27 * cout * cin
+            out.append((params[off:off + nw].reshape(27, cout, cin), params[off + nw:off + nw + cout]))
+            off += nw + cout
+        return out

@@ -140,7 +140,8 @@ typedef enum ss4d_kernel_kind {
     SS4D_K_REFINE = 2,    /* FP64 refinement + residual pass (one colour)     */
     SS4D_K_ASSEMBLE = 3,  /* coefficient assembly                             */
     SS4D_K_PACK = 4,      /* natural <-> colour-split copies                  */
-    SS4D_K_COUNT = 5
+    SS4D_K_WARM = 5,      /* learned warm start: features, network, checks    */
+    SS4D_K_COUNT = 6
 } ss4d_kernel_kind;
 ss4d_status ss4d_solver_set_timing(ss4d_solver *s, int enable);
 ss4d_status ss4d_solver_kernel_time(const ss4d_solver *s, int kind, double *total_ms, long long *launches);
@@ -269,6 +270,44 @@ ss4d_status ss4d_batch_autotune(ss4d_batch *b, const ss4d_params *p, double *con
  * place), edge-detector faces d_g[8v + f]; stats[v] (may be NULL). */
 ss4d_status ss4d_batch_seg_time_step(ss4d_batch *b, const ss4d_params *p, double *const *d_u,
                                      const double *const *d_g, ss4d_step_stats *stats);
+
+/* ---- learned warm start ------------------------------------------------ */
+/* A 4-layer convolutional network (3x3x3 kernels over each frame, 16 input
+ * features -> 24 -> 24 -> 24 hidden channels with ReLU -> 1, BF16 weights and
+ * activations, FP32 accumulation) that predicts the first correction
+ * d = A^-1 r0 of a mixed-form time step from the residual r0 = b - A u^n
+ * (normalised by its RMS s, at frames l and l+-1), the step's coefficients
+ * (c a_f / diag, 1/diag), the first Jacobi iterate, gbar, u^n and the
+ * presmoothed image; u^n + s * prediction starts the FP32 rounds and SOR
+ * finishes to the unchanged FP64 tolerance.  When the prediction does not
+ * lower the correction equation's residual the step starts from zero instead.
+ * Training and inference are this library's own kernels.  No counterpart in
+ * the reference.  Feature tensors are BF16 [F][nz][ny][nx][16] (interior
+ * voxels, F frames); parameters are FP32, per layer weights [27][cout][cin]
+ * (tap = 9 dz + 3 dy + dx) then biases [cout]. */
+typedef struct ss4d_wsnet ss4d_wsnet;
+size_t ss4d_wsnet_param_count(void);
+ss4d_status ss4d_wsnet_create(void *stream, ss4d_wsnet **out);
+ss4d_status ss4d_wsnet_destroy(ss4d_wsnet *n);
+ss4d_status ss4d_wsnet_set_stream(ss4d_wsnet *n, void *stream);
+ss4d_status ss4d_wsnet_init(ss4d_wsnet *n, uint64_t seed);
+ss4d_status ss4d_wsnet_set_params(ss4d_wsnet *n, const float *h_params);
+ss4d_status ss4d_wsnet_get_params(ss4d_wsnet *n, float *h_params);
+/* prediction [F][nz][ny][nx] FP32 */
+ss4d_status ss4d_wsnet_forward(ss4d_wsnet *n, const void *d_x0, int nx, int ny, int nz, int nf, float *d_out);
+/* one Adam step on a batch of crops (frames F of nx*ny*nz voxels): mean
+ * squared error against d_target over voxels at least `margin` from a crop's
+ * border; lr == 0 only evaluates; d_grad (may be NULL) gets the gradient. */
+ss4d_status ss4d_wsnet_train_step(ss4d_wsnet *n, const void *d_x0, const float *d_target, int nx, int ny,
+                                  int nz, int nf, int margin, float lr, float *loss_out, float *d_grad);
+/* Features of the time step from d_u (training data): assembles the step's
+ * system, computes r0 in FP64 and writes the feature tensor of all nt frames
+ * to d_x0 and s to *sigma.  d_u is not modified. */
+ss4d_status ss4d_ws_features(ss4d_solver *s, const ss4d_params *p, double *d_u, const double *const d_g[8],
+                             const double *d_i0, void *d_x0, double *sigma);
+/* Attach a network (NULL detaches) to a solver; d_i0 is the presmoothed
+ * image.  Used by SS4D_ARITH_MIXED segmentation steps. */
+ss4d_status ss4d_solver_set_warm_start(ss4d_solver *s, ss4d_wsnet *n, const double *d_i0);
 
 /* ---- memory helpers (used by the reference-named layer) --------------- */
 /* Device / pinned-host allocations and copies on the handle's stream.  They

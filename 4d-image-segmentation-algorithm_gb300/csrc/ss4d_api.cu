@@ -119,6 +119,9 @@ struct ss4d_solver {
     float *ws_y;   // prediction [nt][nz][ny][nx]
     CPtrs8 cur_g;  // g of the segmentation step in progress
     int have_g;
+    // mixed form: start from the previous step's change (ss4d_solver_set_extrapolation)
+    int extrap;
+    int have_dprev; // dR[0] / dB hold the last segmentation step's u^{n+1} - u^n
     // per-kernel timing (ss4d_solver_set_timing)
     int timing;
     double ktime[SS4D_K_COUNT];
@@ -323,6 +326,7 @@ extern "C" ss4d_status ss4d_solver_set_arith(ss4d_solver *s, ss4d_arith arith)
     REQ(s, "solver is NULL");
     REQ(arith == SS4D_ARITH_REFERENCE || arith == SS4D_ARITH_FP64 || arith == SS4D_ARITH_MIXED, "unknown arithmetic");
     s->arith = arith;
+    s->have_dprev = 0;
     return SS4D_OK;
 }
 
@@ -650,6 +654,7 @@ extern "C" ss4d_status ss4d_ws_features(ss4d_solver *s, const ss4d_params *p, do
         gi.p[f] = d_g[f];
     }
     CKS(ensure_split(s, 1));
+    s->have_dprev = 0; // the corrections are overwritten below
     const Split &sp = s->sp;
     launch_assemble(s->geo, sp, d_u, gi, 1, *p, s->sb, 1, s->stream);
     launch_pack(s->geo, sp, d_u, d_u, s->sb, s->stream);
@@ -671,6 +676,20 @@ extern "C" ss4d_status ss4d_ws_features(ss4d_solver *s, const ss4d_params *p, do
     return SS4D_OK;
 }
 
+// a segmentation step of the mixed form that starts from u^n + (u^n - u^{n-1})
+static bool extrapolating(const ss4d_solver *s)
+{
+    return s->arith == SS4D_ARITH_MIXED && s->extrap && s->have_dprev && s->have_g && !s->ws_net;
+}
+
+extern "C" ss4d_status ss4d_solver_set_extrapolation(ss4d_solver *s, int enable)
+{
+    REQ(s, "solver is NULL");
+    s->extrap = enable ? 1 : 0;
+    s->have_dprev = 0;
+    return SS4D_OK;
+}
+
 // the loop on the split buffers; u/prev already packed, coefficients assembled
 static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixed)
 {
@@ -685,10 +704,14 @@ static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixe
         launch_advance(s->d_state, s->stream);
         s->launches += 3;
     } else {
+        // the first refinement pass adds the correction in dR[0] / dB to u:
+        // zero, or the previous step's change when extrapolating
         const size_t fb = sizeof(float) * sp.cs;
-        CK(cudaMemsetAsync(s->sb.dR[0], 0, fb, s->stream));
+        if (!extrapolating(s)) {
+            CK(cudaMemsetAsync(s->sb.dR[0], 0, fb, s->stream));
+            CK(cudaMemsetAsync(s->sb.dB, 0, fb, s->stream));
+        }
         CK(cudaMemsetAsync(s->sb.dR[1], 0, fb, s->stream));
-        CK(cudaMemsetAsync(s->sb.dB, 0, fb, s->stream));
         launch_loop_init(s->d_state, 0, s->stream);
         s->launches += 1;
         if (s->ws_net && s->have_g)
@@ -948,7 +971,10 @@ static ss4d_status split_solve(ss4d_solver *s, const ss4d_params *p, double *d_u
     s->launches += 1;
     CKS(last_launch());
     CKS(run_split_loop(s, p, mixed));
-    timed(s, SS4D_K_PACK, true, [&] { launch_unpack(s->geo, s->sp, s->sb, s->d_state, d_u, s->stream); });
+    // keep this step's change for the next one (mixed segmentation steps)
+    const int save = mixed && s->extrap && s->have_g && !s->ws_net;
+    timed(s, SS4D_K_PACK, true, [&] { launch_unpack(s->geo, s->sp, s->sb, s->d_state, d_u, s->stream, save); });
+    s->have_dprev = save;
     s->launches += 1;
     CKS(last_launch());
     ss4d_status st = finish_stats(s, stats, mixed);

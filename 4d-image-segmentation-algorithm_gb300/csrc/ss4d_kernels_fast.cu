@@ -205,7 +205,10 @@ __global__ void k_pack(Geo g, Split sp, const double *__restrict__ u, const doub
 }
 
 // split -> natural, interior voxels only (the ghosts of u never change)
-__global__ void k_unpack(Geo g, Split sp, SplitBufs b, const LoopState *__restrict__ st, double *u)
+// split -> natural interior of u; with save_delta (mixed form) also the
+// step's change u - prev in FP32 into the interior of dR[0] / dB, where the
+// next step's first refinement pass picks it up as its starting correction
+__global__ void k_unpack(Geo g, Split sp, SplitBufs b, const LoopState *__restrict__ st, double *u, int save_delta)
 {
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
@@ -215,7 +218,15 @@ __global__ void k_unpack(Geo g, Split sp, SplitBufs b, const LoopState *__restri
     const int col = (i + j + k + l) & 1;
     const long long s = (((long long)l * g.kM + k) * g.jM + j) * sp.Hs + ((i + 1) >> 1) + sp.A - 1;
     const int fr = st->final_red;
-    u[nat_index(g, i, j, k, l)] = col == 0 ? pick(b.R, fr)[s] : b.Bk[s];
+    const double v = col == 0 ? pick(b.R, fr)[s] : b.Bk[s];
+    u[nat_index(g, i, j, k, l)] = v;
+    if (save_delta) {
+        const float d = d2f_bits(v - pick(b.P, col)[s]);
+        if (col == 0)
+            b.dR[0][s] = d;
+        else
+            b.dB[s] = d;
+    }
 }
 
 __global__ void k_loop_init(LoopState *st, int mode)
@@ -614,11 +625,12 @@ void launch_pack_coef(const Geo &g, const Split &s, CPtrs8 a, const ss4d_params 
     k_pack_coef<<<gr, bl, 0, st>>>(g, s, a, c, p.omega_c, b, want32);
 }
 
-void launch_unpack(const Geo &g, const Split &s, SplitBufs b, const LoopState *state, double *u, cudaStream_t st)
+void launch_unpack(const Geo &g, const Split &s, SplitBufs b, const LoopState *state, double *u, cudaStream_t st,
+                   int save_delta)
 {
     dim3 gr, bl;
     interior_grid(g, gr, bl);
-    k_unpack<<<gr, bl, 0, st>>>(g, s, b, state, u);
+    k_unpack<<<gr, bl, 0, st>>>(g, s, b, state, u, save_delta);
 }
 
 void launch_loop_init(LoopState *state, int mode, cudaStream_t st)

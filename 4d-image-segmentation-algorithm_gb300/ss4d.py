@@ -158,6 +158,7 @@ def lib() -> C.CDLL:
                                    C.POINTER(C.c_float), vp], st),
         "ss4d_ws_features": ([vp, C.POINTER(Params), vp, P8, vp, vp, dp], st),
         "ss4d_solver_set_warm_start": ([vp, vp, vp], st),
+        "ss4d_solver_set_extrapolation": ([vp, C.c_int], st),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -275,6 +276,10 @@ class Solver:
 
     def set_graph(self, on: bool):
         _check(self.L.ss4d_solver_set_graph(self.h, 1 if on else 0), "set_graph")
+
+    def set_extrapolation(self, on: bool):
+        """mixed form: start each segmentation step from u^n + (u^n - u^{n-1})"""
+        _check(self.L.ss4d_solver_set_extrapolation(self.h, 1 if on else 0), "set_extrapolation")
 
     def set_stream(self, stream: int | None):
         _check(self.L.ss4d_solver_set_stream(self.h, stream), "set_stream")

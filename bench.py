@@ -49,9 +49,10 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--size", type=int, nargs=4, default=[256, 256, 128, 20], metavar=("NX", "NY", "NZ", "NT"))
-    ap.add_argument("--forms", default="fp64,mixed,learned",
-                    help="fp64: plain FP64 sweeps; mixed: FP32 sweeps + FP64 refinement; learned: mixed started "
-                         "from the warm-start network (weights/wsnet_seg.npy)")
+    ap.add_argument("--forms", default="fp64,mixed,extrap,learned",
+                    help="fp64: plain FP64 sweeps; mixed: FP32 sweeps + FP64 refinement; extrap: mixed started "
+                         "from u^n + (u^n - u^(n-1)); learned: mixed started from the warm-start network "
+                         "(weights/wsnet_seg.npy)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-graph", action="store_true",
@@ -165,8 +166,9 @@ def run_ours(args, rank, world, dist):
         net.set_params(np.load(os.path.join(PKG, "weights", "wsnet_seg.npy")))
 
     def use_form(form):
-        S.set_arith("mixed" if form == "learned" else form)
+        S.set_arith("mixed" if form in ("learned", "extrap") else form)
         S.set_warm_start(net if form == "learned" else None, i0)
+        S.set_extrapolation(form == "extrap")
 
     results = {}
     finals = {}
@@ -219,9 +221,11 @@ def run_ours(args, rank, world, dist):
     roof = {}
     for form in forms:
         use_form(form)
+        u = finals[form].clone()
+        if form == "extrap":  # one untimed step rebuilds the history
+            S.seg_time_step(p, u, None, g)
         S.set_timing(True)
         S.reset_timing()
-        u = finals[form].clone()
         S.seg_time_step(p, u, None, g)
         kt = S.kernel_times()
         S.set_timing(False)
@@ -233,7 +237,7 @@ def run_ours(args, rank, world, dist):
         if form == "mixed":
             ms, n = kt["sweep32"]
             per_unit = BYTES_FP32_ITER
-        elif form == "learned":
+        elif form in ("learned", "extrap"):
             ms, n = kt["sweep32"]
             per_unit = BYTES_FP32_ITER
         else:
@@ -253,7 +257,7 @@ def run_ours(args, rank, world, dist):
 
     # error of the mixed forms against the plain FP64 form after the same steps
     err = {}
-    for form in ("mixed", "learned"):
+    for form in ("mixed", "extrap", "learned"):
         if "fp64" not in finals or form not in finals:
             continue
         a = finals[form][1:-1, 1:-1, 1:-1, 1:-1]
@@ -283,7 +287,8 @@ def run_e2e(args, form, ctx):
     import ss4d
 
     shape, n_pad, n_int, p, i0h, u0h = ctx
-    os.environ["SS4D_ARITH"] = form
+    os.environ["SS4D_ARITH"] = "mixed" if form == "extrap" else form
+    os.environ["SS4D_EXTRAPOLATE"] = "1" if form == "extrap" else "0"
     L = C.CDLL(ss4d.SEG_PATH, mode=os.RTLD_LOCAL)
     lM, kM, jM, iM = shape
     for nm, v in (("iMax", iM), ("jMax", jM), ("kMax", kM), ("lMax", lM), ("maxNoGSIteration", p.maxNoGSIteration),
@@ -466,13 +471,14 @@ def main():
     forms = list(results)
     # headline: the faster of the mixed forms (with and without the learned
     # warm start) among those that converged every step, else plain FP64
-    fast = [f for f in ("mixed", "learned") if f in results and results[f]["converged"]]
+    fast = [f for f in ("mixed", "extrap", "learned") if f in results and results[f]["converged"]]
     head = max(fast, key=lambda f: results[f]["steps_per_s"]) if fast else forms[0]
     r = results[head]
     line = {"metric": METRIC, "value": r["steps_per_s"], "unit": "time-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": {"fp64": "f64", "mixed": "f32 sweeps + f64 residual/refinement",
+                      "extrap": "f32 sweeps + f64 residual/refinement",
                       "learned": "f32 sweeps + f64 residual/refinement, bf16 warm-start network"}[head],
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "form": head, "nx": args.size[0], "ny": args.size[1],
@@ -481,18 +487,19 @@ def main():
             "roofline": roofline(head), "gpu_launches": r["launches"], "clocks": r["clocks"],
             "forms": {f: {k: v for k, v in results[f].items() if k != "clocks"} for f in forms}}
     if "fp64" in results:
-        for f in ("mixed", "learned"):
+        for f in ("mixed", "extrap", "learned"):
             if f in results:
                 line[f"{f}_over_fp64"] = results[f]["steps_per_s"] / results["fp64"]["steps_per_s"]
         line["roofline_fp64"] = roofline("fp64")
         line["error_vs_fp64"] = err
-    for f in ("mixed", "learned"):
+    for f in ("mixed", "extrap", "learned"):
         if f in results and f != head:
             line[f"roofline_{f}"] = roofline(f)
     if rank == 0 and world == 1 and not args.no_e2e:
         try:
             # the reference-named layer runs the mixed form without the network
             line["e2e"] = run_e2e(args, "mixed" if head == "learned" else head, ctx)
+            line["e2e"]["form"] = "mixed" if head == "learned" else head
         except Exception as ex:  # reported, not hidden
             line["e2e"] = {"value": None, "unit": "time-steps/s", "error": repr(ex)}
     if rank == 0 and world == 1 and not args.no_cpu:

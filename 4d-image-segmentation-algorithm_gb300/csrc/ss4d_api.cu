@@ -119,9 +119,10 @@ struct ss4d_solver {
     float *ws_y;   // prediction [nt][nz][ny][nx]
     CPtrs8 cur_g;  // g of the segmentation step in progress
     int have_g;
-    // mixed form: start from the previous step's change (ss4d_solver_set_extrapolation)
-    int extrap;
-    int have_dprev; // dR[0] / dB hold the last segmentation step's u^{n+1} - u^n
+    // mixed form: start from an extrapolation in time (ss4d_solver_set_extrapolation)
+    int extrap;      // 0 off, 1 linear, 2 quadratic
+    int have_dprev;  // steps in a row whose change was kept: dR[0] / dB hold the next start correction
+    float *hist[2];  // quadratic: the last step's change per colour (split layout)
     // per-kernel timing (ss4d_solver_set_timing)
     int timing;
     double ktime[SS4D_K_COUNT];
@@ -290,7 +291,8 @@ extern "C" ss4d_status ss4d_solver_destroy(ss4d_solver *s)
     // allocation bases only: R[1], Bk, P[1], coef[1], ... point inside them
     void *dev[] = {s->d_partial, s->d_scalar, s->d_state, s->d_params, s->d_scratch, s->d_coef_nat,
                    s->sb.R[0], s->sb.P[0], s->sb.coef[0], s->sb.coef32[0], s->sb.dR[0], s->sb.r32[0], s->sb.fn[0],
-                   s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz, s->ws_x0, s->ws_y};
+                   s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz, s->ws_x0, s->ws_y,
+                   s->hist[0], s->hist[1]};
     for (void *p : dev)
         if (p)
             cudaFree(p);
@@ -682,10 +684,11 @@ static bool extrapolating(const ss4d_solver *s)
     return s->arith == SS4D_ARITH_MIXED && s->extrap && s->have_dprev && s->have_g && !s->ws_net;
 }
 
-extern "C" ss4d_status ss4d_solver_set_extrapolation(ss4d_solver *s, int enable)
+extern "C" ss4d_status ss4d_solver_set_extrapolation(ss4d_solver *s, int order)
 {
     REQ(s, "solver is NULL");
-    s->extrap = enable ? 1 : 0;
+    REQ(order >= 0 && order <= 2, "extrapolation order must be 0, 1 or 2");
+    s->extrap = order;
     s->have_dprev = 0;
     return SS4D_OK;
 }
@@ -971,10 +974,19 @@ static ss4d_status split_solve(ss4d_solver *s, const ss4d_params *p, double *d_u
     s->launches += 1;
     CKS(last_launch());
     CKS(run_split_loop(s, p, mixed));
-    // keep this step's change for the next one (mixed segmentation steps)
-    const int save = mixed && s->extrap && s->have_g && !s->ws_net;
-    timed(s, SS4D_K_PACK, true, [&] { launch_unpack(s->geo, s->sp, s->sb, s->d_state, d_u, s->stream, save); });
-    s->have_dprev = save;
+    // keep the next step's start correction (mixed segmentation steps)
+    int save = mixed && s->extrap && s->have_g && !s->ws_net ? 1 : 0;
+    if (save && s->extrap == 2) {
+        if (!s->hist[0]) {
+            CKS(dmalloc(s, (void **)&s->hist[0], sizeof(float) * s->sp.cs));
+            CKS(dmalloc(s, (void **)&s->hist[1], sizeof(float) * s->sp.cs));
+        }
+        save = s->have_dprev ? 2 : 3;
+    }
+    timed(s, SS4D_K_PACK, true, [&] {
+        launch_unpack(s->geo, s->sp, s->sb, s->d_state, d_u, s->stream, save, s->hist[0], s->hist[1]);
+    });
+    s->have_dprev = save ? (s->have_dprev < 2 ? s->have_dprev + 1 : 2) : 0;
     s->launches += 1;
     CKS(last_launch());
     ss4d_status st = finish_stats(s, stats, mixed);

@@ -111,7 +111,7 @@ void launch_pack(const Geo &g, const Split &s, const double *u, const double *pr
 void launch_pack_coef(const Geo &g, const Split &s, CPtrs8 a, const ss4d_params &p, SplitBufs b, int want32,
                       cudaStream_t st);
 void launch_unpack(const Geo &g, const Split &s, SplitBufs b, const LoopState *state, double *u, cudaStream_t st,
-                   int save_delta = 0);
+                   int save = 0, float *hist_r = nullptr, float *hist_b = nullptr);
 void launch_loop_init(LoopState *state, int mode, cudaStream_t st);
 void launch_sweep64(const Geo &g, const Split &s, const SweepCfg &cfg, int colour, SplitBufs b, const DevParams *dp,
                     LoopState *state, cudaStream_t st);

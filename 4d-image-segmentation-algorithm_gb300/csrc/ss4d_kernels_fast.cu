@@ -205,10 +205,14 @@ __global__ void k_pack(Geo g, Split sp, const double *__restrict__ u, const doub
 }
 
 // split -> natural, interior voxels only (the ghosts of u never change)
-// split -> natural interior of u; with save_delta (mixed form) also the
-// step's change u - prev in FP32 into the interior of dR[0] / dB, where the
-// next step's first refinement pass picks it up as its starting correction
-__global__ void k_unpack(Geo g, Split sp, SplitBufs b, const LoopState *__restrict__ st, double *u, int save_delta)
+// split -> natural interior of u.  With save (mixed form) also the start
+// correction of the next step, d = u - prev of this step in FP32, into the
+// interior of dR[0] / dB, where the next step's first refinement pass adds it
+// to u^{n+1}: save 1 writes d (linear extrapolation in time); save 2 writes
+// 2 d - h with h the previous step's d (quadratic), save 3 writes d and keeps
+// it as h for the next step; with save >= 2, h is replaced by d.
+__global__ void k_unpack(Geo g, Split sp, SplitBufs b, const LoopState *__restrict__ st, double *u, int save,
+                         float *hist_r, float *hist_b)
 {
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
@@ -220,12 +224,18 @@ __global__ void k_unpack(Geo g, Split sp, SplitBufs b, const LoopState *__restri
     const int fr = st->final_red;
     const double v = col == 0 ? pick(b.R, fr)[s] : b.Bk[s];
     u[nat_index(g, i, j, k, l)] = v;
-    if (save_delta) {
+    if (save) {
         const float d = d2f_bits(v - pick(b.P, col)[s]);
+        float *h = col == 0 ? hist_r : hist_b;
+        float guess = d;
+        if (save == 2)
+            guess = fmaf(2.f, d, -h[s]);
+        if (save >= 2)
+            h[s] = d;
         if (col == 0)
-            b.dR[0][s] = d;
+            b.dR[0][s] = guess;
         else
-            b.dB[s] = d;
+            b.dB[s] = guess;
     }
 }
 
@@ -626,11 +636,11 @@ void launch_pack_coef(const Geo &g, const Split &s, CPtrs8 a, const ss4d_params 
 }
 
 void launch_unpack(const Geo &g, const Split &s, SplitBufs b, const LoopState *state, double *u, cudaStream_t st,
-                   int save_delta)
+                   int save, float *hist_r, float *hist_b)
 {
     dim3 gr, bl;
     interior_grid(g, gr, bl);
-    k_unpack<<<gr, bl, 0, st>>>(g, s, b, state, u, save_delta);
+    k_unpack<<<gr, bl, 0, st>>>(g, s, b, state, u, save, hist_r, hist_b);
 }
 
 void launch_loop_init(LoopState *state, int mode, cudaStream_t st)

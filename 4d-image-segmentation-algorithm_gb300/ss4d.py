@@ -277,9 +277,10 @@ class Solver:
     def set_graph(self, on: bool):
         _check(self.L.ss4d_solver_set_graph(self.h, 1 if on else 0), "set_graph")
 
-    def set_extrapolation(self, on: bool):
-        """mixed form: start each segmentation step from u^n + (u^n - u^{n-1})"""
-        _check(self.L.ss4d_solver_set_extrapolation(self.h, 1 if on else 0), "set_extrapolation")
+    def set_extrapolation(self, order: int):
+        """mixed form: start each segmentation step from an extrapolation in
+        time of the earlier steps' changes (0 off, 1 linear, 2 quadratic)"""
+        _check(self.L.ss4d_solver_set_extrapolation(self.h, int(order)), "set_extrapolation")
 
     def set_stream(self, stream: int | None):
         _check(self.L.ss4d_solver_set_stream(self.h, stream), "set_stream")

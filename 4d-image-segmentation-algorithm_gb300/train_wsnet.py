@@ -2,7 +2,8 @@
 """Training and evaluation of the learned warm start (ss4d_wsnet) of the
 mixed-precision segmentation step.
 
-Data: synthetic scenes (ss4d_scene_generate kinds 1-3) stepped by the plain
+Data: synthetic multi-object scenes (ss4d_scene_generate kind 3, the
+256x256x128x20 workload's generator) at 128x128x64x12, stepped by the plain
 FP64 solver to a tight tolerance.  For every time step n the features of
 u^n (ss4d_ws_features: residual, coefficients, g, u, image) and the exact
 first correction (u^{n+1} - u^n) / s, s the RMS of the step's initial
@@ -10,7 +11,7 @@ residual, are cut into crops.  Training: Adam on the mean squared error of
 the crops' inner voxels (a border of 4 voxels, the network's reach, is
 excluded), all on the GPU through the library's own kernels.  Evaluation:
 SOR iterations and time per step of the mixed form with and without the
-network on scenes it has not seen.
+network on scenes it has not seen (other seeds, and the 256x256x128x20 size).
 
     python train_wsnet.py --out weights/wsnet_seg.npy
 """
@@ -136,25 +137,27 @@ def evaluate(torch, net, kind, dims, seed, steps, gs_tol=1e-6):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=os.path.join(HERE, "weights", "wsnet_seg.npy"))
-    ap.add_argument("--dims", type=int, nargs=4, default=[96, 96, 48, 10])
-    ap.add_argument("--scenes", type=int, default=9)
+    ap.add_argument("--dims", type=int, nargs=4, default=[128, 128, 64, 12])
+    ap.add_argument("--kinds", type=int, nargs="+", default=[3], help="scene generator kinds, used in turn")
+    ap.add_argument("--scenes", type=int, default=12)
     ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--crops", type=int, default=32, help="crops per time step")
+    ap.add_argument("--crops", type=int, default=84, help="crops per time step (12 x 20 x 84 = 20160)")
     ap.add_argument("--crop", type=int, nargs=3, default=[40, 40, 20], metavar=("CX", "CY", "CZ"))
-    ap.add_argument("--iters", type=int, default=3000)
+    ap.add_argument("--iters", type=int, default=6000)
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--gs-tol", type=float, default=1e-9)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--eval-dims", type=int, nargs=4, default=[128, 128, 64, 12])
-    ap.add_argument("--eval-steps", type=int, default=10)
+    ap.add_argument("--eval-dims", type=int, nargs=4, default=[256, 256, 128, 20])
+    ap.add_argument("--eval-steps", type=int, default=6)
+    ap.add_argument("--eval-kinds", type=int, nargs="+", default=[3])
     ap.add_argument("--init", default=None, help="start from these parameters (.npy)")
     args = ap.parse_args()
 
     import torch
 
     rng = np.random.default_rng(args.seed)
-    scenes = [(1 + i % 3, 1000 + i) for i in range(args.scenes)]
+    scenes = [(args.kinds[i % len(args.kinds)], 1000 + i) for i in range(args.scenes)]
     t0 = time.time()
     X, T = make_dataset(torch, scenes, args.dims, args.steps, args.crops, args.crop, args.gs_tol, rng)
     print(f"dataset: {X.shape[0]} crops in {time.time() - t0:.0f} s; target rms {T.float().pow(2).mean().sqrt():.4f}")
@@ -168,7 +171,7 @@ def main():
     del X, T
     torch.cuda.empty_cache()
     ev = {}
-    for kind in (1, 2, 3):
+    for kind in args.eval_kinds:
         ev[f"kind{kind}"] = evaluate(torch, net, kind, args.eval_dims, 5000 + kind, args.eval_steps)
         e = ev[f"kind{kind}"]
         print(f"eval kind {kind}: cold its {e['cold']['iterations']} warm its {e['warm']['iterations']} "

@@ -129,14 +129,16 @@ ss4d_status ss4d_solver_set_arith(ss4d_solver *s, ss4d_arith arith);
  * in the tile order (>= 1), max_grid caps the persistent grid (0 = as many
  * blocks as fit on the device).  Results do not depend on either. */
 ss4d_status ss4d_solver_set_tiling(ss4d_solver *s, int k_block, int max_grid);
-/* Mixed form, segmentation steps: start the solve of step n from
- * u^n + (u^n - u^{n-1}), the previous step's change on this handle kept in
- * FP32, instead of from u^n (default 0).  The FP64 stop rule is unchanged, so
- * only the iteration count depends on it.  Not applied while a warm-start
- * network is attached; the history is dropped by this call, by
- * ss4d_solver_set_arith and by any other solve on the handle.  No counterpart
- * in the reference (each of its solves starts from u^n). */
-ss4d_status ss4d_solver_set_extrapolation(ss4d_solver *s, int enable);
+/* Mixed form, segmentation steps: start the solve of step n from an
+ * extrapolation in time instead of from u^n.  order 1: u^n + d_{n-1};
+ * order 2: u^n + 2 d_{n-1} - d_{n-2} (d_{n-1} after one step), with d_m the
+ * change u^{m+1} - u^m of an earlier step on this handle, kept in FP32;
+ * 0 (default): off.  The FP64 stop rule is unchanged, so only the iteration
+ * count depends on it.  Not applied while a warm-start network is attached;
+ * the history is dropped by this call, by ss4d_solver_set_arith and by any
+ * other solve on the handle.  No counterpart in the reference (each of its
+ * solves starts from u^n). */
+ss4d_status ss4d_solver_set_extrapolation(ss4d_solver *s, int order);
 /* Use (1) or bypass (0) the CUDA-graph form of the sweep loop (default 1). */
 ss4d_status ss4d_solver_set_graph(ss4d_solver *s, int enable);
 /* Per-kernel timing.  While enabled, the sweep loop runs host-driven (not

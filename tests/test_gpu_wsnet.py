@@ -211,22 +211,28 @@ def test_bad_prediction_is_discarded(ss4d, oracle, cuda, net, graph):
 
 def test_trained_network_cuts_iterations_on_unseen_scenes(ss4d, oracle, cuda):
     """The committed parameters (weights/wsnet_seg.npy, trained by
-    train_wsnet.py on other seeds and sizes) on scenes they were not trained
-    on: every step keeps the prediction, needs fewer FP32 iterations (6 steps
-    at 96x80x40x8 measured 161 -> 133 and 158 -> 123), meets the same FP64
-    tolerance, and ends where the cold start ends."""
+    train_wsnet.py on 128x128x64x12 multi-object scenes) on scenes of other
+    seeds and sizes: every step keeps the prediction, needs fewer FP32
+    iterations (at 256x256x128x20, 6 steps: 209 -> 152), meets the same FP64
+    tolerance, and ends where the cold start ends (masks differ in at most
+    0.1 % of their voxels)."""
     import os
 
     torch = cuda
     params = np.load(os.path.join(os.path.dirname(ss4d.__file__), "weights", "wsnet_seg.npy"))
     with ss4d.Wsnet(seed=None) as net:
         net.set_params(params)
-        for kind, seed in ((3, 777), (1, 778)):
-            dims = (96, 80, 40, 8)
+        for kind, seed, dims in ((3, 777, (128, 112, 56, 10)), (3, 778, (96, 80, 40, 8))):
             nx, ny, nz, nt = dims
             p = ss4d.scene_params()
             i0h, u0h = ss4d.scene(kind, nx, ny, nz, nt, seed=seed)
-            g = oracle.gfaces(p, i0h, np.zeros_like(i0h))
+            # the edge detector as in training: presmoothed image, its g faces
+            i0d = dev(torch, i0h)
+            gd = [torch.empty_like(i0d) for _ in range(8)]
+            with ss4d.Solver.for_interior(*dims, arith="fp64") as S:
+                S.edge_detector(p, i0d, None, gd)
+                S.synchronize()
+            i0h, g = host(i0d), [host(a) for a in gd]
             cold, cs = _run_steps(ss4d, torch, dims, p, u0h, g, i0h, 6)
             warm, ws = _run_steps(ss4d, torch, dims, p, u0h, g, i0h, 6, net=net)
             assert all(st["warm_started"] == 1 for st in ws)
@@ -236,31 +242,35 @@ def test_trained_network_cuts_iterations_on_unseen_scenes(ss4d, oracle, cuda):
             assert rel_err(warm, cold) <= 1e-3
             lev = 0.5 * (cold.min() + cold.max())
             a, b = warm[1:-1, 1:-1, 1:-1, 1:-1] >= lev, cold[1:-1, 1:-1, 1:-1, 1:-1] >= lev
-            assert 2 * (a & b).sum() / (a.sum() + b.sum()) >= 0.999
+            assert (a ^ b).sum() <= max(2, 1e-3 * (a.sum() + b.sum()))
 
 
 @pytest.mark.parametrize("graph", [True, False])
 def test_extrapolated_start_meets_the_fp64_tolerance(ss4d, oracle, cuda, graph):
-    """Mixed steps started from u^n + (u^n - u^{n-1}): the first step (no
-    history) is bit-identical to a plain mixed step, every step meets the FP64
-    tolerance, and the states agree with the plain mixed steps."""
+    """Mixed steps started from the linear (order 1) or quadratic (order 2)
+    extrapolation of the earlier steps' changes: the first step (no history)
+    is bit-identical to a plain mixed step, every step meets the FP64
+    tolerance, fewer iterations are needed, and the states agree with the
+    plain mixed steps."""
     torch = cuda
     dims = (40, 32, 24, 6)
     p, i0h, u0h, g = _scene(ss4d, oracle, dims, seed=51)
     gd = [dev(torch, a) for a in g]
     runs = {}
-    for extrap in (False, True):
+    for order in (0, 1, 2):
         u = dev(torch, u0h)
         with ss4d.Solver.for_interior(*dims, arith="mixed") as S:
             S.set_graph(graph)
-            S.set_extrapolation(extrap)
+            S.set_extrapolation(order)
             stats, states = [], []
-            for _ in range(5):
+            for _ in range(6):
                 stats.append(S.seg_time_step(p, u, None, gd))
                 states.append(host(u))
-        runs[extrap] = (stats, states)
-    (cs, cu), (xs, xu) = runs[False], runs[True]
-    assert np.array_equal(xu[0], cu[0]) and xs[0]["iterations"] == cs[0]["iterations"]
-    assert all(st["status"] == 0 and st["residual"] <= p.gsTol for st in cs + xs)
-    assert sum(st["iterations"] for st in xs[1:]) < sum(st["iterations"] for st in cs[1:])
-    assert rel_err(xu[-1], cu[-1]) <= 1e-4
+        runs[order] = (stats, states)
+    cs, cu = runs[0]
+    for order in (1, 2):
+        xs, xu = runs[order]
+        assert np.array_equal(xu[0], cu[0]) and xs[0]["iterations"] == cs[0]["iterations"]
+        assert all(st["status"] == 0 and st["residual"] <= p.gsTol for st in cs + xs)
+        assert sum(st["iterations"] for st in xs[1:]) < sum(st["iterations"] for st in cs[1:])
+        assert rel_err(xu[-1], cu[-1]) <= 1e-4

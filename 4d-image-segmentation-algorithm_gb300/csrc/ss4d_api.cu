@@ -292,7 +292,7 @@ extern "C" ss4d_status ss4d_solver_destroy(ss4d_solver *s)
     void *dev[] = {s->d_partial, s->d_scalar, s->d_state, s->d_params, s->d_scratch, s->d_coef_nat,
                    s->sb.R[0], s->sb.P[0], s->sb.coef[0], s->sb.coef32[0], s->sb.dR[0], s->sb.r32[0], s->sb.fn[0],
                    s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz, s->ws_x0, s->ws_y,
-                   s->hist[0], s->hist[1]};
+                   s->hist[0], s->hist[1], s->sb.fd[0]};
     for (void *p : dev)
         if (p)
             cudaFree(p);
@@ -429,6 +429,10 @@ static ss4d_status ensure_split(ss4d_solver *s, int mixed)
         s->sb.dB = d3 + 2 * cs;
         s->sb.r32[0] = r2;
         s->sb.r32[1] = r2 + cs;
+        double *fd = nullptr; // float-float forward differences, 4 axes, natural layout
+        CKS(dmalloc(s, (void **)&fd, sizeof(double) * 4 * (size_t)s->geo.n));
+        for (int d = 0; d < 4; ++d)
+            s->sb.fd[d] = fd + (size_t)d * s->geo.n;
         s->have_mixed = 1;
         free_graphs(s); // kernel arguments changed
     }
@@ -594,6 +598,19 @@ static ss4d_status finish_stats(ss4d_solver *s, ss4d_step_stats *stats, int mixe
     return SS4D_OK;
 }
 
+// coefficient assembly from u into the split records: FP64 (plain form,
+// FP64 throughout) or float-float (mixed form, FP32 records for its sweeps)
+static void assemble(ss4d_solver *s, const ss4d_params *p, const double *d_u, CPtrs8 gi, int has_g, int mixed)
+{
+    if (mixed) {
+        launch_assemble_ff(s->geo, s->sp, d_u, gi, has_g, *p, s->sb, s->sm_count, s->stream);
+        s->launches += 3;
+    } else {
+        launch_assemble(s->geo, s->sp, d_u, gi, has_g, *p, s->sb, 0, s->stream);
+        s->launches += 2;
+    }
+}
+
 static ss4d_status ensure_ws_buffers(ss4d_solver *s)
 {
     if (!s->ws_x0) {
@@ -658,9 +675,9 @@ extern "C" ss4d_status ss4d_ws_features(ss4d_solver *s, const ss4d_params *p, do
     CKS(ensure_split(s, 1));
     s->have_dprev = 0; // the corrections are overwritten below
     const Split &sp = s->sp;
-    launch_assemble(s->geo, sp, d_u, gi, 1, *p, s->sb, 1, s->stream);
+    assemble(s, p, d_u, gi, 1, 1);
     launch_pack(s->geo, sp, d_u, d_u, s->sb, s->stream);
-    s->launches += 3;
+    s->launches += 1;
     CKS(upload_params(s, p));
     const size_t fb = sizeof(float) * sp.cs;
     CK(cudaMemsetAsync(s->sb.dR[0], 0, fb, s->stream));
@@ -1064,8 +1081,7 @@ extern "C" ss4d_status ss4d_seg_time_step(ss4d_solver *s, const ss4d_params *p, 
         CKS(ensure_split(s, mixed));
         if (d_prev_u)
             CK(cudaMemcpyAsync(d_prev_u, d_u, sizeof(double) * g.n, cudaMemcpyDeviceToDevice, s->stream));
-        timed(s, SS4D_K_ASSEMBLE, true, [&] { launch_assemble(g, s->sp, d_u, gi, 1, *p, s->sb, mixed, s->stream); });
-        s->launches += 2; // faces + voxel coefficients
+        timed(s, SS4D_K_ASSEMBLE, true, [&] { assemble(s, p, d_u, gi, 1, mixed); });
         CKS(last_launch());
         s->cur_g = gi;
         s->have_g = 1;
@@ -1117,10 +1133,9 @@ extern "C" ss4d_status ss4d_mcf_time_step(ss4d_solver *s, const ss4d_params *p, 
     } else {
         const int mixed = s->arith == SS4D_ARITH_MIXED;
         CKS(ensure_split(s, mixed));
-        timed(s, SS4D_K_ASSEMBLE, true,
-              [&] { launch_assemble(g, s->sp, d_u, none, 0, *p, s->sb, mixed, s->stream); });
+        timed(s, SS4D_K_ASSEMBLE, true, [&] { assemble(s, p, d_u, none, 0, mixed); });
         launch_mcf_field(g, d_u, p->h, t, 1, s->stream);
-        s->launches += 2;
+        s->launches += 1;
         CKS(last_launch());
         st = split_solve(s, p, d_u, prev, stats);
     }

@@ -1,0 +1,294 @@
+// ss4d_assemble_ff.cu — coefficient assembly of the mixed form in
+// float-float arithmetic.
+//
+// The FP64 assembly (k_faces + k_voxel_coef, ss4d_kernels_fast.cu) executes
+// about 125 FP64 instructions per voxel and is bounded by GB300's FP64 pipe
+// (roughly 1/70 of its FP32 rate).  Here every quantity after the first
+// differences of u is carried as an unevaluated sum of two floats (h + l,
+// 48 significant bits; Dekker's and Knuth's error-free transformations: the
+// rounding error of a float sum is recovered with the two-sum of Knuth, that
+// of a product with one fused multiply-add), so the work runs on the FP32
+// pipe.  FP64 instructions are left only where a double enters or leaves
+// the float-float form: one subtraction per first difference of u and per g
+// value, one addition per coefficient written.
+//
+//   k_fdiff:          F_a(v) = u(v + e_a) - u(v) for the 4 axes (FP64
+//                     difference, split into two floats), natural layout;
+//   k_faces_ff:       per face between v and v + e_d, from F only:
+//                     |grad u|^2 = F_d^2/h^2 + sum_{a != d} (D_a(v+e_d) + D_a(v))^2/(4h)^2
+//                     with D_a(x) = F_a(x) + F_a(x - e_a) the central difference
+//                     (the reference's face formula, segmentation4D.c:446-580),
+//                     s2 = |grad u|^2 + eps2, fn = s2 / sqrt(s2), fq = g / sqrt(s2);
+//   k_voxel_coef_ff:  vc = sqrt(mean(fn)^2 + eps2), c a_f = c vc fq_f,
+//                     diag = 1 + sum c a_f, omega/diag; written as FP64
+//                     records (refinement) and FP32 records (sweeps).
+//
+// Relative error of the coefficients: a few units of 2^-46 (1/sqrt and 1/x by
+// an FP32 seed and two Newton steps in float-float).  The mixed form's
+// refinement passes measure the FP64 residual against these coefficients;
+// their distance to the FP64 assembly's is below 1e-12 relative (tested), so
+// the residual that stops the loop is unchanged far below any tolerance.
+#include "ss4d_sweep.cuh"
+
+namespace ss4d {
+
+namespace {
+
+struct ff {
+    float h, l;
+};
+
+__device__ __forceinline__ ff ff_make(float h, float l)
+{
+    ff r;
+    r.h = h;
+    r.l = l;
+    return r;
+}
+
+// |a| >= |b| (or a == 0): s + e == a + b exactly
+__device__ __forceinline__ ff fast_two_sum(float a, float b)
+{
+    const float s = a + b;
+    return ff_make(s, b - (s - a));
+}
+
+__device__ __forceinline__ ff two_sum(float a, float b)
+{
+    const float s = a + b;
+    const float v = s - a;
+    return ff_make(s, (a - (s - v)) + (b - v));
+}
+
+__device__ __forceinline__ ff ff_add(ff a, ff b)
+{
+    ff s = two_sum(a.h, b.h);
+    const float e = s.l + (a.l + b.l);
+    return fast_two_sum(s.h, e);
+}
+
+__device__ __forceinline__ ff ff_mul(ff a, ff b)
+{
+    const float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, e);
+    e = fmaf(a.l, b.h, e);
+    return fast_two_sum(p, e);
+}
+
+__device__ __forceinline__ ff ff_sqr(ff a)
+{
+    const float p = a.h * a.h;
+    float e = fmaf(a.h, a.h, -p);
+    e = fmaf(2.f * a.h, a.l, e);
+    return fast_two_sum(p, e);
+}
+
+// double -> float-float: the high part truncated, the exact remainder truncated
+__device__ __forceinline__ ff ff_from_d(double d)
+{
+    const float h = d2f_bits(d);
+    return ff_make(h, d2f_bits(d - f2d_bits(h)));
+}
+
+__device__ __forceinline__ double ff_to_d(ff a)
+{
+    return f2d_bits(a.h) + f2d_bits(a.l);
+}
+
+// 1/sqrt(x), x > 0 and normal: FP32 seed, two Newton steps y += y (1 - x y^2) / 2
+__device__ __forceinline__ ff ff_rsqrt(ff x)
+{
+    ff y = ff_make(rsqrtf(x.h), 0.f);
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        const ff xy2 = ff_mul(x, ff_sqr(y));
+        const float r = (1.f - xy2.h) - xy2.l; // small: one float holds it
+        const ff corr = ff_mul(y, ff_make(0.5f * r, 0.f));
+        y = ff_add(y, corr);
+    }
+    return y;
+}
+
+// 1/x, x >= 1: FP32 seed, two Newton steps y += y (1 - x y)
+__device__ __forceinline__ ff ff_rcp(ff x)
+{
+    ff y = ff_make(1.f / x.h, 0.f);
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        const ff xy = ff_mul(x, y);
+        const float r = (1.f - xy.h) - xy.l;
+        y = ff_add(y, ff_mul(y, ff_make(r, 0.f)));
+    }
+    return y;
+}
+
+__device__ __forceinline__ ff ld_ff(const double *p, long long o)
+{
+    const float2 v = __ldg(reinterpret_cast<const float2 *>(p) + o);
+    return ff_make(v.x, v.y);
+}
+
+__device__ __forceinline__ void st_ff(double *p, long long o, ff v)
+{
+    __stcs(reinterpret_cast<float2 *>(p) + o, make_float2(v.h, v.l));
+}
+
+} // namespace
+
+struct FFConst {
+    float ih2h, ih2l;   // 1/h^2
+    float iq2h, iq2l;   // 1/(4h)^2
+    float eps2h, eps2l; // eps2
+    float ch, cl;       // tau/h^2
+    float omh, oml;     // omega
+};
+
+// forward differences of every voxel that has a neighbour along the axis
+__global__ void __launch_bounds__(256) k_fdiff(Geo g, const double *__restrict__ u, SplitBufs b)
+{
+    const long long st[4] = {1, g.sy, g.sz, g.sw};
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < g.n;
+         o += (long long)gridDim.x * blockDim.x) {
+        long long r = o;
+        const int i = (int)(r % g.iM);
+        r /= g.iM;
+        const int j = (int)(r % g.jM);
+        r /= g.jM;
+        const int k = (int)(r % g.kM);
+        const int l = (int)(r / g.kM);
+        const int idx[4] = {i, j, k, l};
+        const int top[4] = {g.iM - 1, g.jM - 1, g.kM - 1, g.lM - 1};
+        const double uc = u[o];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+            st_ff(b.fd[a], o, idx[a] < top[a] ? ff_from_d(u[o + st[a]] - uc) : ff_make(0.f, 0.f));
+    }
+}
+
+// faces of voxels v with every index in [0, n_a], as k_faces
+__global__ void __launch_bounds__(256) k_faces_ff(Geo g, CPtrs8 gin, int has_g, FFConst K, SplitBufs b)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z % (g.nz + 1), l = blockIdx.z / (g.nz + 1);
+    if (i > g.nx || j > g.ny)
+        return;
+    const int idx[4] = {i, j, k, l};
+    const long long o = nat_index(g, i, j, k, l);
+    const long long st[4] = {1, g.sy, g.sz, g.sw};
+    const ff ih2 = ff_make(K.ih2h, K.ih2l), iq2 = ff_make(K.iq2h, K.iq2l), eps2 = ff_make(K.eps2h, K.eps2l);
+    // central differences at v along the axes where v is interior
+    ff D[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+        D[a] = idx[a] >= 1 ? ff_add(ld_ff(b.fd[a], o), ld_ff(b.fd[a], o - st[a])) : ff_make(0.f, 0.f);
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+        bool ok = true;
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+            if (a != d && idx[a] < 1)
+                ok = false;
+        if (!ok)
+            continue;
+        const long long nb = o + st[d];
+        const ff cn = ld_ff(b.fd[d], o);
+        ff tt = ff_make(0.f, 0.f);
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            if (a == d)
+                continue;
+            const ff Dnb = ff_add(ld_ff(b.fd[a], nb), ld_ff(b.fd[a], nb - st[a]));
+            tt = ff_add(tt, ff_sqr(ff_add(Dnb, D[a])));
+        }
+        const ff s2 = ff_add(ff_add(ff_mul(ff_sqr(cn), ih2), ff_mul(tt, iq2)), eps2);
+        const ff y = ff_rsqrt(s2);
+        ff gv = ff_make(1.f, 0.f);
+        if (has_g)
+            gv = ff_from_d(idx[d] >= 1 ? __ldg(gin.p[2 * d] + o) : __ldg(gin.p[2 * d + 1] + nb));
+        st_ff(b.fn[d], o, ff_mul(s2, y));
+        st_ff(b.fq[d], o, ff_mul(gv, y));
+    }
+}
+
+__global__ void __launch_bounds__(256) k_voxel_coef_ff(Geo g, Split sp, FFConst K, SplitBufs b)
+{
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = 1 + blockIdx.z % g.nz, l = 1 + blockIdx.z / g.nz;
+    if (i > g.nx || j > g.ny)
+        return;
+    const long long o = nat_index(g, i, j, k, l);
+    const long long st[4] = {1, g.sy, g.sz, g.sw};
+    ff q[8], sum = ff_make(0.f, 0.f);
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+        sum = ff_add(sum, ff_add(ld_ff(b.fn[d], o), ld_ff(b.fn[d], o - st[d])));
+        q[2 * d] = ld_ff(b.fq[d], o);
+        q[2 * d + 1] = ld_ff(b.fq[d], o - st[d]);
+    }
+    // mean^2 + eps2 with mean = sum / 8 (exact scaling)
+    const ff m = ff_make(sum.h * 0.125f, sum.l * 0.125f);
+    const ff x = ff_add(ff_sqr(m), ff_make(K.eps2h, K.eps2l));
+    const ff cv = ff_mul(ff_make(K.ch, K.cl), ff_mul(x, ff_rsqrt(x))); // c * vc
+    const int col = (i + j + k + l) & 1;
+    double *cf = pick(b.coef, col);
+    float *cf32 = pick(b.coef32, col);
+    const long long t = coef_index(g, sp, i, j, k, l);
+    ff diag = ff_make(1.f, 0.f);
+    float a32[8];
+#pragma unroll
+    for (int f = 0; f < 8; ++f) {
+        const ff a = ff_mul(cv, q[f]);
+        diag = ff_add(diag, a);
+        __stcs(cf + coef_at(t, f, 10), ff_to_d(a));
+        a32[f] = a.h;
+    }
+    __stcs(cf + coef_at(t, 8, 10), ff_to_d(diag));
+    __stcs(cf + coef_at(t, 9, 10), ff_to_d(ff_mul(ff_make(K.omh, K.oml), ff_rcp(diag))));
+    float4 *f4 = reinterpret_cast<float4 *>(cf32 + 8 * t);
+    __stcs(f4, make_float4(a32[0], a32[1], a32[2], a32[3]));
+    __stcs(f4 + 1, make_float4(a32[4], a32[5], a32[6], a32[7]));
+}
+
+static void split_host(double v, float &h, float &l)
+{
+    h = (float)v;
+    l = (float)(v - (double)h);
+}
+
+int max_blocks_fdiff()
+{
+    int a = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_fdiff, 256, 0);
+    return a > 0 ? a : 1;
+}
+
+void launch_assemble_ff(const Geo &g, const Split &s, const double *u, CPtrs8 gin, int has_g, const ss4d_params &p,
+                        SplitBufs b, int sm_count, cudaStream_t st)
+{
+    FFConst K;
+    split_host(1.0 / (p.h * p.h), K.ih2h, K.ih2l);
+    split_host(1.0 / (16.0 * p.h * p.h), K.iq2h, K.iq2l);
+    split_host(p.eps2, K.eps2h, K.eps2l);
+    split_host(p.tau / (p.h * p.h), K.ch, K.cl);
+    split_host(p.omega_c, K.omh, K.oml);
+    k_fdiff<<<sm_count * max_blocks_fdiff(), 256, 0, st>>>(g, u, b);
+    {
+        const int bx = g.nx + 1 >= 128 ? 128 : (g.nx + 1 >= 64 ? 64 : 32);
+        const int by = 256 / bx;
+        dim3 bl(bx, by, 1);
+        dim3 gr((g.nx + 1 + bx - 1) / bx, (g.ny + 1 + by - 1) / by, (g.nz + 1) * (g.nt + 1));
+        k_faces_ff<<<gr, bl, 0, st>>>(g, gin, has_g, K, b);
+    }
+    {
+        const int bx = g.nx >= 128 ? 128 : (g.nx >= 64 ? 64 : 32);
+        const int by = 256 / bx;
+        dim3 bl(bx, by, 1);
+        dim3 gr((g.nx + bx - 1) / bx, (g.ny + by - 1) / by, g.nz * g.nt);
+        k_voxel_coef_ff<<<gr, bl, 0, st>>>(g, s, K, b);
+    }
+}
+
+} // namespace ss4d

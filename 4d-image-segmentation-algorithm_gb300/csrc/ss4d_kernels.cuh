@@ -89,6 +89,9 @@ struct SplitBufs {
     // and v + e_d (natural layout): |grad u|_eps and g/|grad u|_eps
     double *fn[4];
     double *fq[4];
+    // mixed form's float-float assembly (ss4d_assemble_ff.cu): per voxel v and
+    // axis a the forward difference u(v + e_a) - u(v) as two floats
+    double *fd[4];
 };
 
 struct SweepCfg {
@@ -108,6 +111,9 @@ SweepCfg make_sweep_cfg(const Geo &g, const Split &s, int sm_count, int kb);
 void launch_assemble(const Geo &g, const Split &s, const double *u, CPtrs8 gin, int has_g, const ss4d_params &p,
                      SplitBufs b, int want32, cudaStream_t st);
 void launch_pack(const Geo &g, const Split &s, const double *u, const double *prev, SplitBufs b, cudaStream_t st);
+// mixed form: the same coefficient records from float-float arithmetic (3 kernels)
+void launch_assemble_ff(const Geo &g, const Split &s, const double *u, CPtrs8 gin, int has_g, const ss4d_params &p,
+                        SplitBufs b, int sm_count, cudaStream_t st);
 void launch_pack_coef(const Geo &g, const Split &s, CPtrs8 a, const ss4d_params &p, SplitBufs b, int want32,
                       cudaStream_t st);
 void launch_unpack(const Geo &g, const Split &s, SplitBufs b, const LoopState *state, double *u, cudaStream_t st,

@@ -47,3 +47,33 @@ def test_mixed_forms_against_fp64(ss4d, cuda, kind, dims, steps):
         # distance is that of two such iterates (no parity bar), the masks agree
         assert max_rel <= 2e-3 and dice >= 0.999
     assert its["extrap"] < its["mixed"]
+
+
+@pytest.mark.parametrize("arith", ["fp64", "mixed"])
+def test_true_fp64_residual_meets_the_tolerance(ss4d, oracle, cuda, arith):
+    """The mixed form assembles its coefficients in float-float arithmetic
+    (48-bit significands) and measures its FP64 residual against them.  The
+    residual of its result against the oracle's FP64 coefficients (the
+    reference's arithmetic) must meet the same tight tolerance: coefficient
+    errors of FP32 size (1e-7) would leave it near 1e-12 here."""
+    torch = cuda
+    dims = nx, ny, nz, nt = (24, 20, 12, 5)
+    p = ss4d.scene_params(gsTol=1e-14)
+    i0h, u0h = ss4d.scene(3, nx, ny, nz, nt, seed=61)
+    g = oracle.gfaces(p, i0h, np.zeros_like(i0h))
+    u = torch.from_numpy(u0h).cuda()
+    with ss4d.Solver.for_interior(*dims, arith=arith) as S:
+        st = S.seg_time_step(p, u, None, [torch.from_numpy(a).cuda() for a in g])
+    assert st["residual"] <= p.gsTol
+    u1 = u.cpu().numpy()
+    coef = oracle.coefficients(p, u0h, g)
+    c = p.tau / (p.h * p.h)
+    inner = (slice(1, -1),) * 4
+    offs = [(0, 0, 0, 1), (0, 0, 0, -1), (0, 0, 1, 0), (0, 0, -1, 0), (0, 1, 0, 0), (0, -1, 0, 0), (1, 0, 0, 0),
+            (-1, 0, 0, 0)]
+    r = u1[inner] - u0h[inner]
+    for f, o in enumerate(offs):
+        nb = tuple(slice(1 + d, u1.shape[a] - 1 + d) for a, d in enumerate(o))
+        r += c * coef[f][inner] * (u1[inner] - u1[nb])
+    R = float(np.sum(r * r) * p.h ** 4)
+    assert R <= p.gsTol * (1 + 1e-6), R

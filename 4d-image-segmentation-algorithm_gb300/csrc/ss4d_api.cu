@@ -120,9 +120,10 @@ struct ss4d_solver {
     CPtrs8 cur_g;  // g of the segmentation step in progress
     int have_g;
     // mixed form: start from an extrapolation in time (ss4d_solver_set_extrapolation)
-    int extrap;      // 0 off, 1 linear, 2 quadratic
+    int extrap;      // 0 off, else the extrapolation order 1..3
     int have_dprev;  // steps in a row whose change was kept: dR[0] / dB hold the next start correction
-    float *hist[2];  // quadratic: the last step's change per colour (split layout)
+    float *hist[4];  // earlier steps' changes (split layout): h1 red, h1 black, h2 red, h2 black
+    double inner_omega; // mixed form: relaxation factor of the FP32 sweeps (0: omega_c)
     // per-kernel timing (ss4d_solver_set_timing)
     int timing;
     double ktime[SS4D_K_COUNT];
@@ -292,7 +293,7 @@ extern "C" ss4d_status ss4d_solver_destroy(ss4d_solver *s)
     void *dev[] = {s->d_partial, s->d_scalar, s->d_state, s->d_params, s->d_scratch, s->d_coef_nat,
                    s->sb.R[0], s->sb.P[0], s->sb.coef[0], s->sb.coef32[0], s->sb.dR[0], s->sb.r32[0], s->sb.fn[0],
                    s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz, s->ws_x0, s->ws_y,
-                   s->hist[0], s->hist[1], s->sb.fd[0]};
+                   s->hist[0], s->hist[1], s->hist[2], s->hist[3], s->sb.fd[0]};
     for (void *p : dev)
         if (p)
             cudaFree(p);
@@ -450,7 +451,8 @@ static ss4d_status check_params(const ss4d_params *p)
 static ss4d_status upload_params(ss4d_solver *s, const ss4d_params *p)
 {
     s->h_params->c = p->tau / (p->h * p->h);
-    s->h_params->omega = p->omega_c;
+    // the mixed form's FP32 sweeps may relax with their own factor
+    s->h_params->omega = s->arith == SS4D_ARITH_MIXED && s->inner_omega > 0.0 ? s->inner_omega : p->omega_c;
     s->h_params->h4 = p->h * p->h * p->h * p->h;
     s->h_params->tol = p->gsTol;
     s->h_params->maxit = p->maxNoGSIteration;
@@ -630,7 +632,7 @@ static ss4d_status ws_first_pass(ss4d_solver *s)
     launch_refine(s->geo, s->sp, cfg, 0, s->sb, s->d_params, s->d_state, s->stream);
     launch_refine(s->geo, s->sp, cfg, 1, s->sb, s->d_params, s->d_state, s->stream);
     launch_ctrl_mixed(s->sb, cfg.grid, s->d_params, s->d_state, 0, 0, s->stream);
-    s->launches += 3;
+    s->launches += 4; // a refinement pass is 3 launches
     return last_launch();
 }
 
@@ -701,10 +703,18 @@ static bool extrapolating(const ss4d_solver *s)
     return s->arith == SS4D_ARITH_MIXED && s->extrap && s->have_dprev && s->have_g && !s->ws_net;
 }
 
+extern "C" ss4d_status ss4d_solver_set_inner_omega(ss4d_solver *s, double omega)
+{
+    REQ(s, "solver is NULL");
+    REQ(omega == 0.0 || (omega > 0.0 && omega < 2.0), "inner omega must be 0 or in (0, 2)");
+    s->inner_omega = omega;
+    return SS4D_OK;
+}
+
 extern "C" ss4d_status ss4d_solver_set_extrapolation(ss4d_solver *s, int order)
 {
     REQ(s, "solver is NULL");
-    REQ(order >= 0 && order <= 2, "extrapolation order must be 0, 1 or 2");
+    REQ(order >= 0 && order <= 3, "extrapolation order must be 0, 1, 2 or 3");
     s->extrap = order;
     s->have_dprev = 0;
     return SS4D_OK;
@@ -775,7 +785,7 @@ static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixe
                 timed(s, SS4D_K_SWEEP32, mode != 0,
                       [&] { launch_sweep32(g, sp, cfg, 0, s->sb, s->d_params, s->d_state, 0, s->stream); });
                 launch_ctrl_mixed(s->sb, cfg.grid, s->d_params, s->d_state, 0, 0, s->stream);
-                s->launches += 6;
+                s->launches += 7;
             }
             CKS(last_launch());
             CK(cudaMemcpyAsync(s->h_state, s->d_state, sizeof(LoopState), cudaMemcpyDeviceToHost, s->stream));
@@ -795,7 +805,7 @@ static void count_graph_launches(ss4d_solver *s, int mixed)
 {
     if (!s->last_graphed)
         return;
-    s->launches += (long long)(mixed ? 6 : 3) * s->h_state->bodies;
+    s->launches += (long long)(mixed ? 7 : 3) * s->h_state->bodies;
 }
 
 extern "C" ss4d_status ss4d_solver_set_timing(ss4d_solver *s, int enable)
@@ -991,19 +1001,21 @@ static ss4d_status split_solve(ss4d_solver *s, const ss4d_params *p, double *d_u
     s->launches += 1;
     CKS(last_launch());
     CKS(run_split_loop(s, p, mixed));
-    // keep the next step's start correction (mixed segmentation steps)
-    int save = mixed && s->extrap && s->have_g && !s->ws_net ? 1 : 0;
-    if (save && s->extrap == 2) {
-        if (!s->hist[0]) {
-            CKS(dmalloc(s, (void **)&s->hist[0], sizeof(float) * s->sp.cs));
-            CKS(dmalloc(s, (void **)&s->hist[1], sizeof(float) * s->sp.cs));
-        }
-        save = s->have_dprev ? 2 : 3;
+    // keep the next step's start correction (mixed segmentation steps): an
+    // extrapolation from this step's change and up to order-1 earlier ones
+    const int save = mixed && s->extrap && s->have_g && !s->ws_net;
+    int terms = 0, keep = 0;
+    if (save) {
+        keep = s->extrap - 1;
+        for (int q = 0; q < 2 * keep; ++q)
+            if (!s->hist[q])
+                CKS(dmalloc(s, (void **)&s->hist[q], sizeof(float) * s->sp.cs));
+        terms = s->have_dprev + 1 < s->extrap ? s->have_dprev + 1 : s->extrap;
     }
     timed(s, SS4D_K_PACK, true, [&] {
-        launch_unpack(s->geo, s->sp, s->sb, s->d_state, d_u, s->stream, save, s->hist[0], s->hist[1]);
+        launch_unpack(s->geo, s->sp, s->sb, s->d_state, d_u, s->stream, terms, keep, s->hist);
     });
-    s->have_dprev = save ? (s->have_dprev < 2 ? s->have_dprev + 1 : 2) : 0;
+    s->have_dprev = save ? (s->have_dprev < 3 ? s->have_dprev + 1 : 3) : 0;
     s->launches += 1;
     CKS(last_launch());
     ss4d_status st = finish_stats(s, stats, mixed);

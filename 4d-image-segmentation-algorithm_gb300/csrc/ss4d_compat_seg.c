@@ -166,8 +166,8 @@ bool _allocateMem_(void)
         return false;
     const char *sv = getenv("SS4D_COMPAT_STRICT");
     g_strict = sv && sv[0] == '1';
-    const char *xv = getenv("SS4D_EXTRAPOLATE"); /* mixed form: extrapolation order 1 or 2 */
-    if (xv && (xv[0] == '1' || xv[0] == '2'))
+    const char *xv = getenv("SS4D_EXTRAPOLATE"); /* mixed form: extrapolation order 1..3 */
+    if (xv && xv[0] >= '1' && xv[0] <= '3')
         ss4d_solver_set_extrapolation(g_solver, xv[0] - '0');
     g_bytes = sizeof(double) * (size_t)iMax * jMax * kMax * lMax;
     for (int a = 0; a < A_COUNT; ++a) {

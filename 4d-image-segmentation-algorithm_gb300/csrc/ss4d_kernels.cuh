@@ -116,8 +116,9 @@ void launch_assemble_ff(const Geo &g, const Split &s, const double *u, CPtrs8 gi
                         SplitBufs b, int sm_count, cudaStream_t st);
 void launch_pack_coef(const Geo &g, const Split &s, CPtrs8 a, const ss4d_params &p, SplitBufs b, int want32,
                       cudaStream_t st);
+// terms/keep/hist: the mixed form's extrapolated start (k_unpack); hist = {h1 red, h1 black, h2 red, h2 black}
 void launch_unpack(const Geo &g, const Split &s, SplitBufs b, const LoopState *state, double *u, cudaStream_t st,
-                   int save = 0, float *hist_r = nullptr, float *hist_b = nullptr);
+                   int terms = 0, int keep = 0, float *const *hist = nullptr);
 void launch_loop_init(LoopState *state, int mode, cudaStream_t st);
 void launch_sweep64(const Geo &g, const Split &s, const SweepCfg &cfg, int colour, SplitBufs b, const DevParams *dp,
                     LoopState *state, cudaStream_t st);

@@ -205,14 +205,19 @@ __global__ void k_pack(Geo g, Split sp, const double *__restrict__ u, const doub
 }
 
 // split -> natural, interior voxels only (the ghosts of u never change)
-// split -> natural interior of u.  With save (mixed form) also the start
-// correction of the next step, d = u - prev of this step in FP32, into the
-// interior of dR[0] / dB, where the next step's first refinement pass adds it
-// to u^{n+1}: save 1 writes d (linear extrapolation in time); save 2 writes
-// 2 d - h with h the previous step's d (quadratic), save 3 writes d and keeps
-// it as h for the next step; with save >= 2, h is replaced by d.
-__global__ void k_unpack(Geo g, Split sp, SplitBufs b, const LoopState *__restrict__ st, double *u, int save,
-                         float *hist_r, float *hist_b)
+// split -> natural interior of u.  With terms > 0 (mixed form) also the next
+// step's start correction, extrapolated in time from this step's change
+// d = u - prev (FP32) and the changes of earlier steps h1, h2 (per colour):
+// terms 1: d, 2: 2 d - h1, 3: 3 d - 3 h1 + h2, written into the interior of
+// dR[0] / dB, where the next step's first refinement pass adds it to
+// u^{n+1}.  The history then shifts: h2 <- h1 (keep >= 2), h1 <- d (keep >= 1).
+struct History {
+    float *h1[2]; // per colour
+    float *h2[2];
+};
+
+__global__ void k_unpack(Geo g, Split sp, SplitBufs b, const LoopState *__restrict__ st, double *u, int terms,
+                         int keep, History hs)
 {
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
@@ -224,14 +229,20 @@ __global__ void k_unpack(Geo g, Split sp, SplitBufs b, const LoopState *__restri
     const int fr = st->final_red;
     const double v = col == 0 ? pick(b.R, fr)[s] : b.Bk[s];
     u[nat_index(g, i, j, k, l)] = v;
-    if (save) {
+    if (terms > 0) {
         const float d = d2f_bits(v - pick(b.P, col)[s]);
-        float *h = col == 0 ? hist_r : hist_b;
+        float *h1 = pick(hs.h1, col), *h2 = pick(hs.h2, col);
+        const float p1 = terms >= 2 ? h1[s] : 0.f;
+        const float p2 = terms >= 3 ? h2[s] : 0.f;
         float guess = d;
-        if (save == 2)
-            guess = fmaf(2.f, d, -h[s]);
-        if (save >= 2)
-            h[s] = d;
+        if (terms == 2)
+            guess = fmaf(2.f, d, -p1);
+        else if (terms == 3)
+            guess = fmaf(3.f, d - p1, p2);
+        if (keep >= 2 && terms >= 2) // h1 holds an earlier change from the second step on
+            h2[s] = p1;
+        if (keep >= 1)
+            h1[s] = d;
         if (col == 0)
             b.dR[0][s] = guess;
         else
@@ -344,7 +355,29 @@ __global__ void k_ctrl64(SplitBufs b, int nparts, const DevParams *__restrict__ 
 // equation A d = r.  Modes (LoopState::mode): 0 refine, 1 start a round
 // (zero d, first red sweep), 2 inner iteration (black sweep + next red sweep).
 
-// u <- u + d on the target colour, residual of the refined state, r32 = r
+// A refinement pass is three launches: k_apply_black (black u += d_B), then
+// k_refine<0> (red u += d_R and the red residual against the updated black
+// values), then k_refine<1> (the black residual against the updated red
+// values); r32 receives the residual for the next round.  Applying the black
+// correction first spares the red pass adding it to each of 8 neighbours.
+__global__ void __launch_bounds__(256) k_apply_black(Geo g, Split sp, SweepCfg cfg, SplitBufs b,
+                                                     const LoopState *__restrict__ st)
+{
+    if (st->mode != 0 || st->stop)
+        return;
+    const int tx = threadIdx.x & (cfg.XT - 1), ty = threadIdx.x / cfg.XT;
+    for (long long t = blockIdx.x; t < cfg.ntiles; t += gridDim.x) {
+        const TileCoord tc = tile_coord(g, cfg, t, tx, ty);
+        if (!tc.ok)
+            continue;
+        const int p = (1 + tc.j + tc.k + tc.l) & 1;
+        if (2 * tc.xi + 2 - p > g.nx)
+            continue;
+        const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * sp.Hs + tc.xi + sp.A;
+        b.Bk[s] += f2d_bits(b.dB[s]);
+    }
+}
+
 template <int COL>
 __global__ void __launch_bounds__(256) k_refine(Geo g, Split sp, SweepCfg cfg, SplitBufs b,
                                                 const DevParams *__restrict__ dp, const LoopState *__restrict__ st)
@@ -353,13 +386,11 @@ __global__ void __launch_bounds__(256) k_refine(Geo g, Split sp, SweepCfg cfg, S
         return;
     const int ds = st->dsrc;
     double *own = COL == 0 ? b.R[0] : b.Bk;
-    const float *__restrict__ down = COL == 0 ? pick(b.dR, ds) : b.dB;
+    const float *__restrict__ down = pick(b.dR, ds); // only used for COL == 0
     const double *__restrict__ oth = COL == 0 ? b.Bk : b.R[0];
-    const float *__restrict__ doth = b.dB; // only used for COL == 0
     const double *__restrict__ cf = b.coef[COL];
     const double *__restrict__ pv = b.P[COL];
     float *__restrict__ rr = b.r32[COL];
-    const long long cs = sp.cs;
     const long long Hy = sp.Hs, Hz = Hy * g.jM, Hw = Hz * g.kM;
     const int tx = threadIdx.x & (cfg.XT - 1), ty = threadIdx.x / cfg.XT;
     double acc = 0.0;
@@ -373,20 +404,17 @@ __global__ void __launch_bounds__(256) k_refine(Geo g, Split sp, SweepCfg cfg, S
             continue;
         const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * Hy + tc.xi + sp.A;
         const long long nb[8] = {s - p + 1, s - p, s + Hy, s - Hy, s + Hz, s - Hz, s + Hw, s - Hw};
-        const double u0 = own[s] + f2d_bits(down[s]);
+        const double u0 = COL == 0 ? own[s] + f2d_bits(down[s]) : own[s];
         const double *cv = cf + coef_at(tile_coef_index(g, sp, tc), 0, 10);
         double S = 0.0;
 #pragma unroll
-        for (int f = 0; f < 8; ++f) {
-            double v = oth[nb[f]];
-            if (COL == 0)
-                v += f2d_bits(doth[nb[f]]);
-            S = fma(ld_stream(cv + 32 * f), v, S);
-        }
+        for (int f = 0; f < 8; ++f)
+            S = fma(ld_stream(cv + 32 * f), oth[nb[f]], S);
         const double diag = ld_stream(cv + 256);
         const double r = fma(diag, u0, -(S + ld_stream(pv + s)));
         acc = fma(r, r, acc);
-        own[s] = u0;
+        if (COL == 0)
+            own[s] = u0;
         // r = A u - b here; the correction d with A d = b - A u moves u to the
         // solution, so the FP32 sweeps get the negated residual
         rr[s] = d2f_bits(-r);
@@ -636,11 +664,16 @@ void launch_pack_coef(const Geo &g, const Split &s, CPtrs8 a, const ss4d_params 
 }
 
 void launch_unpack(const Geo &g, const Split &s, SplitBufs b, const LoopState *state, double *u, cudaStream_t st,
-                   int save, float *hist_r, float *hist_b)
+                   int terms, int keep, float *const *hist)
 {
     dim3 gr, bl;
     interior_grid(g, gr, bl);
-    k_unpack<<<gr, bl, 0, st>>>(g, s, b, state, u, save, hist_r, hist_b);
+    History hs;
+    for (int c = 0; c < 2; ++c) {
+        hs.h1[c] = hist ? hist[c] : nullptr;
+        hs.h2[c] = hist ? hist[2 + c] : nullptr;
+    }
+    k_unpack<<<gr, bl, 0, st>>>(g, s, b, state, u, terms, keep, hs);
 }
 
 void launch_loop_init(LoopState *state, int mode, cudaStream_t st)
@@ -671,10 +704,12 @@ void launch_ctrl64(SplitBufs b, int nparts, const DevParams *dp, LoopState *stat
 void launch_refine(const Geo &g, const Split &s, const SweepCfg &cfg, int colour, SplitBufs b, const DevParams *dp,
                    LoopState *state, cudaStream_t st)
 {
-    if (colour == 0)
+    if (colour == 0) {
+        k_apply_black<<<cfg.grid, cfg.threads, 0, st>>>(g, s, cfg, b, state);
         k_refine<0><<<cfg.grid, cfg.threads, 0, st>>>(g, s, cfg, b, dp, state);
-    else
+    } else {
         k_refine<1><<<cfg.grid, cfg.threads, 0, st>>>(g, s, cfg, b, dp, state);
+    }
 }
 
 void launch_zero_delta(const Split &s, SplitBufs b, LoopState *state, cudaStream_t st)

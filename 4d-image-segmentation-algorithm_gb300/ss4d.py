@@ -159,6 +159,7 @@ def lib() -> C.CDLL:
         "ss4d_ws_features": ([vp, C.POINTER(Params), vp, P8, vp, vp, dp], st),
         "ss4d_solver_set_warm_start": ([vp, vp, vp], st),
         "ss4d_solver_set_extrapolation": ([vp, C.c_int], st),
+        "ss4d_solver_set_inner_omega": ([vp, C.c_double], st),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -277,9 +278,13 @@ class Solver:
     def set_graph(self, on: bool):
         _check(self.L.ss4d_solver_set_graph(self.h, 1 if on else 0), "set_graph")
 
+    def set_inner_omega(self, omega: float):
+        """mixed form: relaxation factor of the FP32 sweeps (0: the step's omega_c)"""
+        _check(self.L.ss4d_solver_set_inner_omega(self.h, float(omega)), "set_inner_omega")
+
     def set_extrapolation(self, order: int):
         """mixed form: start each segmentation step from an extrapolation in
-        time of the earlier steps' changes (0 off, 1 linear, 2 quadratic)"""
+        time of the earlier steps' changes (0 off, order 1, 2 or 3)"""
         _check(self.L.ss4d_solver_set_extrapolation(self.h, int(order)), "set_extrapolation")
 
     def set_stream(self, stream: int | None):

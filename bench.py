@@ -44,6 +44,7 @@ BYTES_FP32_ITER = 44.0  # the same arrays in FP32
 # dram__bytes_write.sum from ncu on one launch at 128x128x64x8, 4,194,304
 # targets; the summary and command are in profiles/), scaled by the targets
 # of a launch at the benchmarked size
+EXTRAP_ORDER = 3  # the extrap form's order (ss4d_solver_set_extrapolation)
 TRAFFIC_PER_TARGET = {"k_sweep32": 49.7, "k_sweep64": 118.5}
 TRAFFIC_SOURCE = "profiles/sweep_refine_assembly_conv_kernels_128x128x64x8.md"
 
@@ -55,10 +56,14 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--size", type=int, nargs=4, default=[256, 256, 128, 20], metavar=("NX", "NY", "NZ", "NT"))
-    ap.add_argument("--forms", default="fp64,mixed,extrap,learned",
+    ap.add_argument("--forms", default="fp64,mixed,extrap,learned,extrap_w",
                     help="fp64: plain FP64 sweeps; mixed: FP32 sweeps + FP64 refinement; extrap: mixed started "
-                         "from the quadratic extrapolation u^n + 2 d_(n-1) - d_(n-2) of the earlier changes; learned: mixed started from the warm-start network "
-                         "(weights/wsnet_seg.npy)")
+                         "from the cubic extrapolation u^n + 3 d_(n-1) - 3 d_(n-2) + d_(n-3) of the earlier "
+                         "changes; learned: mixed started from the warm-start network (weights/wsnet_seg.npy); "
+                         "extrap_w: extrap with --inner-omega")
+    ap.add_argument("--inner-omega", type=float, default=1.2,
+                    help="relaxation factor of the extra form 'extrap_w' (extrap with its FP32 sweeps relaxed by "
+                         "this instead of the configured omega 1.8; reported, never the headline)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-graph", action="store_true",
@@ -172,9 +177,10 @@ def run_ours(args, rank, world, dist):
         net.set_params(np.load(os.path.join(PKG, "weights", "wsnet_seg.npy")))
 
     def use_form(form):
-        S.set_arith("mixed" if form in ("learned", "extrap") else form)
+        S.set_arith("mixed" if form in ("learned", "extrap", "extrap_w") else form)
         S.set_warm_start(net if form == "learned" else None, i0)
-        S.set_extrapolation(2 if form == "extrap" else 0)
+        S.set_extrapolation(EXTRAP_ORDER if form in ("extrap", "extrap_w") else 0)
+        S.set_inner_omega(args.inner_omega if form == "extrap_w" else 0.0)
 
     results = {}
     finals = {}
@@ -228,9 +234,9 @@ def run_ours(args, rank, world, dist):
     for form in forms:
         use_form(form)
         u = finals[form].clone()
-        if form == "extrap":  # untimed steps rebuild the history
-            S.seg_time_step(p, u, None, g)
-            S.seg_time_step(p, u, None, g)
+        if form in ("extrap", "extrap_w"):  # untimed steps rebuild the history
+            for _ in range(EXTRAP_ORDER):
+                S.seg_time_step(p, u, None, g)
         S.set_timing(True)
         S.reset_timing()
         S.seg_time_step(p, u, None, g)
@@ -244,7 +250,7 @@ def run_ours(args, rank, world, dist):
         if form == "mixed":
             ms, n = kt["sweep32"]
             per_unit = BYTES_FP32_ITER
-        elif form in ("learned", "extrap"):
+        elif form in ("learned", "extrap", "extrap_w"):
             ms, n = kt["sweep32"]
             per_unit = BYTES_FP32_ITER
         else:
@@ -267,7 +273,7 @@ def run_ours(args, rank, world, dist):
 
     # error of the mixed forms against the plain FP64 form after the same steps
     err = {}
-    for form in ("mixed", "extrap", "learned"):
+    for form in ("mixed", "extrap", "extrap_w", "learned"):
         if "fp64" not in finals or form not in finals:
             continue
         a = finals[form][1:-1, 1:-1, 1:-1, 1:-1]
@@ -298,7 +304,7 @@ def run_e2e(args, form, ctx):
 
     shape, n_pad, n_int, p, i0h, u0h = ctx
     os.environ["SS4D_ARITH"] = "mixed" if form == "extrap" else form
-    os.environ["SS4D_EXTRAPOLATE"] = "2" if form == "extrap" else "0"
+    os.environ["SS4D_EXTRAPOLATE"] = str(EXTRAP_ORDER) if form == "extrap" else "0"
     L = C.CDLL(ss4d.SEG_PATH, mode=os.RTLD_LOCAL)
     lM, kM, jM, iM = shape
     for nm, v in (("iMax", iM), ("jMax", jM), ("kMax", kM), ("lMax", lM), ("maxNoGSIteration", p.maxNoGSIteration),
@@ -497,7 +503,7 @@ def main():
             "roofline": roofline(head), "gpu_launches": r["launches"], "clocks": r["clocks"],
             "forms": {f: {k: v for k, v in results[f].items() if k != "clocks"} for f in forms}}
     if "fp64" in results:
-        for f in ("mixed", "extrap", "learned"):
+        for f in ("mixed", "extrap", "extrap_w", "learned"):
             if f in results:
                 line[f"{f}_over_fp64"] = results[f]["steps_per_s"] / results["fp64"]["steps_per_s"]
         line["roofline_fp64"] = roofline("fp64")

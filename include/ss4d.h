@@ -131,7 +131,8 @@ ss4d_status ss4d_solver_set_arith(ss4d_solver *s, ss4d_arith arith);
 ss4d_status ss4d_solver_set_tiling(ss4d_solver *s, int k_block, int max_grid);
 /* Mixed form, segmentation steps: start the solve of step n from an
  * extrapolation in time instead of from u^n.  order 1: u^n + d_{n-1};
- * order 2: u^n + 2 d_{n-1} - d_{n-2} (d_{n-1} after one step), with d_m the
+ * order 2: u^n + 2 d_{n-1} - d_{n-2}; order 3: u^n + 3 d_{n-1} - 3 d_{n-2}
+ * + d_{n-3} (lower orders while fewer earlier steps exist), with d_m the
  * change u^{m+1} - u^m of an earlier step on this handle, kept in FP32;
  * 0 (default): off.  The FP64 stop rule is unchanged, so only the iteration
  * count depends on it.  Not applied while a warm-start network is attached;
@@ -139,6 +140,11 @@ ss4d_status ss4d_solver_set_tiling(ss4d_solver *s, int k_block, int max_grid);
  * other solve on the handle.  No counterpart in the reference (each of its
  * solves starts from u^n). */
 ss4d_status ss4d_solver_set_extrapolation(ss4d_solver *s, int order);
+/* Mixed form: relaxation factor of the FP32 sweeps on the correction
+ * equation (0, the default: the step's omega_c).  Only the iteration count
+ * depends on it: the stop rule is the FP64 residual of u.  No counterpart in
+ * the reference. */
+ss4d_status ss4d_solver_set_inner_omega(ss4d_solver *s, double omega);
 /* Use (1) or bypass (0) the CUDA-graph form of the sweep loop (default 1). */
 ss4d_status ss4d_solver_set_graph(ss4d_solver *s, int enable);
 /* Per-kernel timing.  While enabled, the sweep loop runs host-driven (not

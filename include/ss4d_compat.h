@@ -23,8 +23,8 @@
  * their host copies are refreshed by ss4d_compat_sync_host(), or after every
  * call when the environment variable SS4D_COMPAT_STRICT=1 is set.
  * SS4D_ARITH=reference|fp64|mixed selects the arithmetic form (default fp64);
- * with mixed, SS4D_EXTRAPOLATE=1 or 2 starts each step from the linear or
- * quadratic extrapolation of the earlier steps (ss4d_solver_set_extrapolation).
+ * with mixed, SS4D_EXTRAPOLATE=1, 2 or 3 starts each step from the extrapolation
+ * of that order of the earlier steps (ss4d_solver_set_extrapolation).
  *
  * Behaviour the reference leaves undefined is an error here instead:
  * a rescale ball whose box leaves the array makes _rescale4DdataToZeroOne_

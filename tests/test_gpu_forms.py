@@ -28,7 +28,7 @@ def test_mixed_forms_against_fp64(ss4d, cuda, kind, dims, steps):
         S.edge_detector(p, i0, None, g)
         for form in ("fp64", "mixed", "extrap"):
             S.set_arith("fp64" if form == "fp64" else "mixed")
-            S.set_extrapolation(2 if form == "extrap" else 0)
+            S.set_extrapolation(3 if form == "extrap" else 0)
             u = torch.from_numpy(u0h).cuda()
             st = [S.seg_time_step(p, u, None, g) for _ in range(steps)]
             assert all(s["status"] == 0 and s["residual"] <= p.gsTol for s in st), form
@@ -77,3 +77,28 @@ def test_true_fp64_residual_meets_the_tolerance(ss4d, oracle, cuda, arith):
         r += c * coef[f][inner] * (u1[inner] - u1[nb])
     R = float(np.sum(r * r) * p.h ** 4)
     assert R <= p.gsTol * (1 + 1e-6), R
+
+
+def test_inner_omega_changes_only_the_iteration_count(ss4d, oracle, cuda):
+    """The mixed form's FP32 sweeps relaxed by another factor than omega_c:
+    the same FP64 tolerance every step, the same states to within it; for this
+    operator (c = tau/h^2 = 0.5) 1.2 needs far fewer sweeps than 1.8."""
+    torch = cuda
+    dims = nx, ny, nz, nt = (40, 36, 24, 6)
+    p = ss4d.scene_params(gsTol=1e-10)
+    i0h, u0h = ss4d.scene(3, nx, ny, nz, nt, seed=71)
+    g = [torch.from_numpy(a).cuda() for a in oracle.gfaces(p, i0h, np.zeros_like(i0h))]
+    out = {}
+    for w in (0.0, 1.2):
+        u = torch.from_numpy(u0h).cuda()
+        with ss4d.Solver.for_interior(*dims, arith="mixed") as S:
+            S.set_inner_omega(w)
+            st = [S.seg_time_step(p, u, None, g) for _ in range(4)]
+        assert all(s["status"] == 0 and s["residual"] <= p.gsTol for s in st)
+        out[w] = (u.cpu().numpy(), sum(s["iterations"] for s in st))
+    (a, za), (b, zb) = out[0.0], out[1.2]
+    assert zb < za
+    assert float(np.abs(a - b).max() / np.abs(a).max()) <= 1e-4
+    with pytest.raises(ss4d.SS4DError):
+        with ss4d.Solver.for_interior(*dims, arith="mixed") as S:
+            S.set_inner_omega(2.5)

@@ -247,8 +247,8 @@ def test_trained_network_cuts_iterations_on_unseen_scenes(ss4d, oracle, cuda):
 
 @pytest.mark.parametrize("graph", [True, False])
 def test_extrapolated_start_meets_the_fp64_tolerance(ss4d, oracle, cuda, graph):
-    """Mixed steps started from the linear (order 1) or quadratic (order 2)
-    extrapolation of the earlier steps' changes: the first step (no history)
+    """Mixed steps started from the extrapolation of order 1, 2 or 3 of the
+    earlier steps' changes: the first step (no history)
     is bit-identical to a plain mixed step, every step meets the FP64
     tolerance, fewer iterations are needed, and the states agree with the
     plain mixed steps."""
@@ -257,7 +257,7 @@ def test_extrapolated_start_meets_the_fp64_tolerance(ss4d, oracle, cuda, graph):
     p, i0h, u0h, g = _scene(ss4d, oracle, dims, seed=51)
     gd = [dev(torch, a) for a in g]
     runs = {}
-    for order in (0, 1, 2):
+    for order in (0, 1, 2, 3):
         u = dev(torch, u0h)
         with ss4d.Solver.for_interior(*dims, arith="mixed") as S:
             S.set_graph(graph)
@@ -268,7 +268,7 @@ def test_extrapolated_start_meets_the_fp64_tolerance(ss4d, oracle, cuda, graph):
                 states.append(host(u))
         runs[order] = (stats, states)
     cs, cu = runs[0]
-    for order in (1, 2):
+    for order in (1, 2, 3):
         xs, xu = runs[order]
         assert np.array_equal(xu[0], cu[0]) and xs[0]["iterations"] == cs[0]["iterations"]
         assert all(st["status"] == 0 and st["residual"] <= p.gsTol for st in cs + xs)

@@ -9,8 +9,9 @@
 // rounding error of a float sum is recovered with the two-sum of Knuth, that
 // of a product with one fused multiply-add), so the work runs on the FP32
 // pipe.  FP64 instructions are left only where a double enters or leaves
-// the float-float form: one subtraction per first difference of u and per g
-// value, one addition per coefficient written.
+// the float-float form: one subtraction per first difference of u and one
+// addition per coefficient written (a double is split into two floats by
+// integer operations).
 //
 //   k_fdiff:          F_a(v) = u(v + e_a) - u(v) for the 4 axes (FP64
 //                     difference, split into two floats), natural layout;
@@ -23,11 +24,12 @@
 //                     diag = 1 + sum c a_f, omega/diag; written as FP64
 //                     records (refinement) and FP32 records (sweeps).
 //
-// Relative error of the coefficients: a few units of 2^-46 (1/sqrt and 1/x by
-// an FP32 seed and two Newton steps in float-float).  The mixed form's
-// refinement passes measure the FP64 residual against these coefficients;
-// their distance to the FP64 assembly's is below 1e-12 relative (tested), so
-// the residual that stops the loop is unchanged far below any tolerance.
+// Relative error of the coefficients: about 1e-13 (1/sqrt from an FP32 seed
+// and one Newton step in float-float, 1/x with two; sums and products to
+// 2^-46).  The mixed form's refinement passes measure the FP64 residual
+// against these coefficients; the residual of its result against exact FP64
+// coefficients meets the same tolerance (tested), the coefficient error
+// entering it only squared, far below any tolerance.
 #include "ss4d_sweep.cuh"
 
 namespace ss4d {
@@ -84,11 +86,25 @@ __device__ __forceinline__ ff ff_sqr(ff a)
     return fast_two_sum(p, e);
 }
 
-// double -> float-float: the high part truncated, the exact remainder truncated
+// double -> float-float by integer operations (no FP64 instruction): the high
+// part is d truncated to 24 significant bits; the remainder d - h is the low
+// 29 mantissa bits r times 2^(e - 1075), converted to float by truncation.
+// The low part is dropped (left zero) where that scale is below the FP32
+// normal range, i.e. for |d| < 2^-73.
 __device__ __forceinline__ ff ff_from_d(double d)
 {
     const float h = d2f_bits(d);
-    return ff_make(h, d2f_bits(d - f2d_bits(h)));
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const int e = (int)((hi >> 20) & 0x7FFu);
+    const unsigned r = lo & 0x1FFFFFFFu;
+    const int fe = e - 948; // FP32 biased exponent of 2^(e - 1075)
+    float l = 0.f;
+    if (r != 0u && fe >= 1 && e <= 1150) {
+        l = __uint2float_rz(r) * __uint_as_float((unsigned)fe << 23);
+        if (hi & 0x80000000u)
+            l = -l;
+    }
+    return ff_make(h, l);
 }
 
 __device__ __forceinline__ double ff_to_d(ff a)
@@ -96,12 +112,12 @@ __device__ __forceinline__ double ff_to_d(ff a)
     return f2d_bits(a.h) + f2d_bits(a.l);
 }
 
-// 1/sqrt(x), x > 0 and normal: FP32 seed, two Newton steps y += y (1 - x y^2) / 2
+// 1/sqrt(x), x > 0 and normal: FP32 seed (relative error below 2^-21), one
+// Newton step y += y (1 - x y^2) / 2 in float-float: error about 1.5 e0^2
 __device__ __forceinline__ ff ff_rsqrt(ff x)
 {
     ff y = ff_make(rsqrtf(x.h), 0.f);
-#pragma unroll
-    for (int it = 0; it < 2; ++it) {
+    {
         const ff xy2 = ff_mul(x, ff_sqr(y));
         const float r = (1.f - xy2.h) - xy2.l; // small: one float holds it
         const ff corr = ff_mul(y, ff_make(0.5f * r, 0.f));
@@ -150,13 +166,8 @@ __global__ void __launch_bounds__(256) k_fdiff(Geo g, const double *__restrict__
     const long long st[4] = {1, g.sy, g.sz, g.sw};
     for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < g.n;
          o += (long long)gridDim.x * blockDim.x) {
-        long long r = o;
-        const int i = (int)(r % g.iM);
-        r /= g.iM;
-        const int j = (int)(r % g.jM);
-        r /= g.jM;
-        const int k = (int)(r % g.kM);
-        const int l = (int)(r / g.kM);
+        int i, j, k, l;
+        nat_coords(g, (unsigned)o, i, j, k, l);
         const int idx[4] = {i, j, k, l};
         const int top[4] = {g.iM - 1, g.jM - 1, g.kM - 1, g.lM - 1};
         const double uc = u[o];

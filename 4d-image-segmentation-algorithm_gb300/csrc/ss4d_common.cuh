@@ -11,13 +11,40 @@
 namespace ss4d {
 
 // ---------------------------------------------------------------------------
+// Division by a fixed divisor d of numerators below 2^31:
+// q = (n * m) >> sh with m = ceil(2^sh / d), sh = 31 + ceil(log2 d)
+// (the error term stays below 1/d for every such n).
+struct FastDiv {
+    unsigned d, m;
+    int sh;
+};
+
+inline FastDiv make_fastdiv(unsigned d)
+{
+    FastDiv f;
+    f.d = d;
+    int s = 0;
+    while ((1ull << s) < d)
+        ++s;
+    f.m = (unsigned)(((1ull << (31 + s)) + d - 1) / d);
+    f.sh = 31 + s;
+    return f;
+}
+
+__host__ __device__ __forceinline__ unsigned fdiv(unsigned n, const FastDiv &f)
+{
+    return (unsigned)(((unsigned long long)n * f.m) >> f.sh);
+}
+
+// ---------------------------------------------------------------------------
 // Natural (reference) layout: ((l*kM + k)*jM + j)*iM + i, one ghost per side.
 struct Geo {
     int iM, jM, kM, lM;   // padded extents
     int nx, ny, nz, nt;   // interior extents
     long long sy, sz, sw; // strides of j, k, l (i stride is 1)
-    long long n;          // padded voxel count
+    long long n;          // padded voxel count (below 2^31)
     long long nint;       // interior voxel count
+    FastDiv fiM, fjM, fkM;
 };
 
 inline Geo make_geo(const ss4d_dims &d)
@@ -30,7 +57,24 @@ inline Geo make_geo(const ss4d_dims &d)
     g.sw = g.sz * g.kM;
     g.n = g.sw * g.lM;
     g.nint = (long long)g.nx * g.ny * g.nz * g.nt;
+    g.fiM = make_fastdiv((unsigned)g.iM);
+    g.fjM = make_fastdiv((unsigned)g.jM);
+    g.fkM = make_fastdiv((unsigned)g.kM);
     return g;
+}
+
+// (i, j, k, l) of natural index o < 2^31
+__device__ __forceinline__ void nat_coords(const Geo &g, unsigned o, int &i, int &j, int &k, int &l)
+{
+    unsigned q = fdiv(o, g.fiM);
+    i = (int)(o - q * g.fiM.d);
+    o = q;
+    q = fdiv(o, g.fjM);
+    j = (int)(o - q * g.fjM.d);
+    o = q;
+    q = fdiv(o, g.fkM);
+    k = (int)(o - q * g.fkM.d);
+    l = (int)q;
 }
 
 __host__ __device__ inline long long nat_index(const Geo &g, int i, int j, int k, int l)

@@ -102,8 +102,9 @@ struct SweepCfg {
     int nXC;       // x chunks per row
     int nJG;       // j groups
     int nKB;       // k blocks
-    long long ntiles;
+    long long ntiles;  // below 2^31 (fewer than the voxels)
     int grid;      // persistent grid (blocks)
+    FastDiv dXC, dJG, dKB, dNT; // nXC, nJG, KB, nt for the tile coordinates
 };
 
 SweepCfg make_sweep_cfg(const Geo &g, const Split &s, int sm_count, int kb);

@@ -184,13 +184,8 @@ __global__ void __launch_bounds__(256) k_pack_coef(Geo g, Split sp, CPtrs8 a, do
 __global__ void k_pack(Geo g, Split sp, const double *__restrict__ u, const double *__restrict__ prev, SplitBufs b)
 {
     for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < g.n; o += (long long)gridDim.x * blockDim.x) {
-        long long r = o;
-        const int i = (int)(r % g.iM);
-        r /= g.iM;
-        const int j = (int)(r % g.jM);
-        r /= g.jM;
-        const int k = (int)(r % g.kM);
-        const int l = (int)(r / g.kM);
+        int i, j, k, l;
+        nat_coords(g, (unsigned)o, i, j, k, l);
         const int col = (i + j + k + l) & 1;
         const long long s = (((long long)l * g.kM + k) * g.jM + j) * sp.Hs + ((i + 1) >> 1) + sp.A - 1;
         const double v = u[o];
@@ -617,6 +612,10 @@ SweepCfg make_sweep_cfg_xt(const Geo &g, const Split &s, int sm_count, int kb, i
     c.nJG = (g.ny + c.TJ - 1) / c.TJ;
     c.nKB = (g.nz + c.KB - 1) / c.KB;
     c.ntiles = (long long)c.nXC * c.nJG * c.KB * g.nt * c.nKB;
+    c.dXC = make_fastdiv((unsigned)c.nXC);
+    c.dJG = make_fastdiv((unsigned)c.nJG);
+    c.dKB = make_fastdiv((unsigned)c.KB);
+    c.dNT = make_fastdiv((unsigned)g.nt);
     int per_sm = max_blocks_sweep64();
     int p32 = max_blocks_sweep32();
     per_sm = per_sm < p32 ? per_sm : p32;

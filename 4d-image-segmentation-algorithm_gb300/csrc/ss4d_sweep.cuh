@@ -87,15 +87,19 @@ struct TileCoord {
 __device__ __forceinline__ TileCoord tile_coord(const Geo &g, const SweepCfg &cfg, long long t, int tx, int ty)
 {
     TileCoord c;
-    long long r = t;
-    const int xc = (int)(r % cfg.nXC);
-    r /= cfg.nXC;
-    const int jg = (int)(r % cfg.nJG);
-    r /= cfg.nJG;
-    const int kin = (int)(r % cfg.KB);
-    r /= cfg.KB;
-    const int lt = (int)(r % g.nt);
-    const int kb = (int)(r / g.nt);
+    unsigned r = (unsigned)t; // t < ntiles < 2^31
+    unsigned q = fdiv(r, cfg.dXC);
+    const int xc = (int)(r - q * cfg.dXC.d);
+    r = q;
+    q = fdiv(r, cfg.dJG);
+    const int jg = (int)(r - q * cfg.dJG.d);
+    r = q;
+    q = fdiv(r, cfg.dKB);
+    const int kin = (int)(r - q * cfg.dKB.d);
+    r = q;
+    q = fdiv(r, cfg.dNT);
+    const int lt = (int)(r - q * cfg.dNT.d);
+    const int kb = (int)q;
     c.k = 1 + kb * cfg.KB + kin;
     c.l = 1 + lt;
     c.j = 1 + jg * cfg.TJ + ty;

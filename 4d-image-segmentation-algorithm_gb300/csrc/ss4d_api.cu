@@ -196,6 +196,8 @@ static ss4d_status check_dims(const ss4d_dims *d)
     const long long n = (long long)d->iMax * d->jMax * d->kMax * d->lMax;
     REQ(n < (1LL << 31), "padded volume must hold fewer than 2^31 voxels (the reference's int indexing)");
     REQ((long long)(d->kMax - 1) * (d->lMax - 1) <= 65535, "(kMax-1)*(lMax-1) must not exceed 65535");
+    const Split sp = make_split(make_geo(*d));
+    REQ(sp.cs < (1LL << 31) && sp.ct < (1LL << 31), "a colour-split array must hold fewer than 2^31 elements");
     return SS4D_OK;
 }
 

@@ -145,6 +145,24 @@ class Clocks:
 # --------------------------------------------------------------------------
 # our arm
 
+def slowest_rank_ms(ms: float, dist, device) -> float:
+    """The timed region's duration of the slowest rank (ranks = independent
+    replicas); every rank returns the same value."""
+    if not dist:
+        return ms
+    import torch
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def replica_steps_per_s(steps: int, world: int, ms: float) -> float:
+    """Whole-job throughput: every rank steps its own volume `steps` times."""
+    return steps * world / (ms / 1e3)
+
+
 def run_ours(args, rank, world, dist):
     import numpy as np
     import torch
@@ -207,15 +225,11 @@ def run_ours(args, rank, world, dist):
         torch.cuda.synchronize(dev)
         ms = e0.elapsed_time(e1)
         clocks = clk.stop()
-        if dist:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-            dist.barrier()
+        ms = slowest_rank_ms(ms, dist, dev)
         launches = S.launch_count() - launches0
         ok = all(s["residual"] <= p.gsTol or s["iterations"] >= p.maxNoGSIteration for s in steps)
         results[form] = {
-            "steps_per_s": args.steps * world / (ms / 1e3),
+            "steps_per_s": replica_steps_per_s(args.steps, world, ms),
             "ms_per_step": ms / args.steps,
             "iterations_per_step": statistics.mean(s["iterations"] for s in steps),
             "iterations": [s["iterations"] for s in steps],

@@ -401,12 +401,12 @@ __global__ void __launch_bounds__(256) k_refine(Geo g, Split sp, SweepCfg cfg, S
         const long long nb[8] = {s - p + 1, s - p, s + Hy, s - Hy, s + Hz, s - Hz, s + Hw, s - Hw};
         const double u0 = COL == 0 ? own[s] + f2d_bits(down[s]) : own[s];
         const double *cv = cf + coef_at(tile_coef_index(g, sp, tc), 0, 10);
-        double S = 0.0;
+        double S = ld_stream(pv + s); // prev + sum_f c a_f u_f
 #pragma unroll
         for (int f = 0; f < 8; ++f)
             S = fma(ld_stream(cv + 32 * f), oth[nb[f]], S);
         const double diag = ld_stream(cv + 256);
-        const double r = fma(diag, u0, -(S + ld_stream(pv + s)));
+        const double r = fma(diag, u0, -S);
         acc = fma(r, r, acc);
         if (COL == 0)
             own[s] = u0;

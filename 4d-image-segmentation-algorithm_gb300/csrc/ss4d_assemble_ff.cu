@@ -24,12 +24,14 @@
 //                     diag = 1 + sum c a_f, omega/diag; written as FP64
 //                     records (refinement) and FP32 records (sweeps).
 //
-// Relative error of the coefficients: about 1e-13 (1/sqrt from an FP32 seed
-// and one Newton step in float-float, 1/x with two; sums and products to
-// 2^-46).  The mixed form's refinement passes measure the FP64 residual
+// Relative error of the coefficients: below 1e-12 (1/sqrt from an FP32 seed
+// and one Newton step, about 1.5 (2^-22)^2 each; 1/x with two steps; sums and
+// products to 2^-46).  The mixed form's refinement passes measure the FP64 residual
 // against these coefficients; the residual of its result against exact FP64
 // coefficients meets the same tolerance (tested), the coefficient error
 // entering it only squared, far below any tolerance.
+#include <math.h>
+
 #include "ss4d_sweep.cuh"
 
 namespace ss4d {
@@ -67,6 +69,22 @@ __device__ __forceinline__ ff ff_add(ff a, ff b)
     ff s = two_sum(a.h, b.h);
     const float e = s.l + (a.l + b.l);
     return fast_two_sum(s.h, e);
+}
+
+// a + b keeping the rounding error of the high parts in the low part
+// without renormalising: for operands that do not cancel (sums of positive
+// terms, or a sum whose result is added again) the low part stays within a
+// few units of 2^-24 of the high part
+__device__ __forceinline__ ff ff_add_nr(ff a, ff b)
+{
+    ff s = two_sum(a.h, b.h);
+    s.l += a.l + b.l;
+    return s;
+}
+
+__device__ __forceinline__ ff ff_norm(ff a)
+{
+    return fast_two_sum(a.h, a.l);
 }
 
 __device__ __forceinline__ ff ff_mul(ff a, ff b)
@@ -112,17 +130,22 @@ __device__ __forceinline__ double ff_to_d(ff a)
     return f2d_bits(a.h) + f2d_bits(a.l);
 }
 
-// 1/sqrt(x), x > 0 and normal: FP32 seed (relative error below 2^-21), one
-// Newton step y += y (1 - x y^2) / 2 in float-float: error about 1.5 e0^2
+// 1/sqrt(x), x > 0 and normal: FP32 seed y0 (relative error below 2^-21),
+// one Newton step y = y0 + y0 (1 - x y0^2) / 2 with x y0^2 formed exactly
+// enough (y0^2 as an exact pair, its product with x to float-float): error
+// about 1.5 e0^2
 __device__ __forceinline__ ff ff_rsqrt(ff x)
 {
-    ff y = ff_make(rsqrtf(x.h), 0.f);
-    {
-        const ff xy2 = ff_mul(x, ff_sqr(y));
-        const float r = (1.f - xy2.h) - xy2.l; // small: one float holds it
-        const ff corr = ff_mul(y, ff_make(0.5f * r, 0.f));
-        y = ff_add(y, corr);
-    }
+    const float y0 = rsqrtf(x.h);
+    const float p = y0 * y0, pe = fmaf(y0, y0, -p); // y0^2 = p + pe exactly
+    const float q = x.h * p;
+    float qe = fmaf(x.h, p, -q);
+    qe = fmaf(x.h, pe, qe);
+    qe = fmaf(x.l, p, qe);                          // x y0^2 = q + qe
+    const float hr = 0.5f * ((1.f - q) - qe);       // 1 - q is exact (q near 1)
+    const float c = y0 * hr, ce = fmaf(y0, hr, -c); // y0 hr = c + ce exactly
+    ff y = fast_two_sum(y0, c);
+    y.l += ce;
     return y;
 }
 
@@ -158,6 +181,7 @@ struct FFConst {
     float eps2h, eps2l; // eps2
     float ch, cl;       // tau/h^2
     float omh, oml;     // omega
+    int pow2;           // 1/h^2 and 1/(4h)^2 are powers of two (h is): exact scaling
 };
 
 // forward differences of every voxel that has a neighbour along the axis
@@ -189,11 +213,12 @@ __global__ void __launch_bounds__(256) k_faces_ff(Geo g, CPtrs8 gin, int has_g, 
     const long long o = nat_index(g, i, j, k, l);
     const long long st[4] = {1, g.sy, g.sz, g.sw};
     const ff ih2 = ff_make(K.ih2h, K.ih2l), iq2 = ff_make(K.iq2h, K.iq2l), eps2 = ff_make(K.eps2h, K.eps2l);
-    // central differences at v along the axes where v is interior
+    // central differences at v along the axes where v is interior (each is
+    // added once more below, so left unnormalised)
     ff D[4];
 #pragma unroll
     for (int a = 0; a < 4; ++a)
-        D[a] = idx[a] >= 1 ? ff_add(ld_ff(b.fd[a], o), ld_ff(b.fd[a], o - st[a])) : ff_make(0.f, 0.f);
+        D[a] = idx[a] >= 1 ? ff_add_nr(ld_ff(b.fd[a], o), ld_ff(b.fd[a], o - st[a])) : ff_make(0.f, 0.f);
 #pragma unroll
     for (int d = 0; d < 4; ++d) {
         bool ok = true;
@@ -205,15 +230,21 @@ __global__ void __launch_bounds__(256) k_faces_ff(Geo g, CPtrs8 gin, int has_g, 
             continue;
         const long long nb = o + st[d];
         const ff cn = ld_ff(b.fd[d], o);
-        ff tt = ff_make(0.f, 0.f);
+        ff tt = ff_make(0.f, 0.f); // sum of squares: positive terms, renormalised once
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
             if (a == d)
                 continue;
-            const ff Dnb = ff_add(ld_ff(b.fd[a], nb), ld_ff(b.fd[a], nb - st[a]));
-            tt = ff_add(tt, ff_sqr(ff_add(Dnb, D[a])));
+            const ff Dnb = ff_add_nr(ld_ff(b.fd[a], nb), ld_ff(b.fd[a], nb - st[a]));
+            const ff t = ff_add(Dnb, D[a]); // may cancel: renormalised before squaring
+            const float p = t.h * t.h;
+            tt = ff_add_nr(tt, ff_make(p, fmaf(2.f * t.h, t.l, fmaf(t.h, t.h, -p))));
         }
-        const ff s2 = ff_add(ff_add(ff_mul(ff_sqr(cn), ih2), ff_mul(tt, iq2)), eps2);
+        tt = ff_norm(tt);
+        const ff cn2 = ff_sqr(cn);
+        const ff a1 = K.pow2 ? ff_make(cn2.h * K.ih2h, cn2.l * K.ih2h) : ff_mul(cn2, ih2);
+        const ff a2 = K.pow2 ? ff_make(tt.h * K.iq2h, tt.l * K.iq2h) : ff_mul(tt, iq2);
+        const ff s2 = ff_add(ff_add_nr(a1, a2), eps2);
         const ff y = ff_rsqrt(s2);
         ff gv = ff_make(1.f, 0.f);
         if (has_g)
@@ -234,11 +265,12 @@ __global__ void __launch_bounds__(256) k_voxel_coef_ff(Geo g, Split sp, FFConst 
     const long long st[4] = {1, g.sy, g.sz, g.sw};
     ff q[8], sum = ff_make(0.f, 0.f);
 #pragma unroll
-    for (int d = 0; d < 4; ++d) {
-        sum = ff_add(sum, ff_add(ld_ff(b.fn[d], o), ld_ff(b.fn[d], o - st[d])));
+    for (int d = 0; d < 4; ++d) { // positive terms: renormalised once
+        sum = ff_add_nr(sum, ff_add_nr(ld_ff(b.fn[d], o), ld_ff(b.fn[d], o - st[d])));
         q[2 * d] = ld_ff(b.fq[d], o);
         q[2 * d + 1] = ld_ff(b.fq[d], o - st[d]);
     }
+    sum = ff_norm(sum);
     // mean^2 + eps2 with mean = sum / 8 (exact scaling)
     const ff m = ff_make(sum.h * 0.125f, sum.l * 0.125f);
     const ff x = ff_add(ff_sqr(m), ff_make(K.eps2h, K.eps2l));
@@ -252,10 +284,11 @@ __global__ void __launch_bounds__(256) k_voxel_coef_ff(Geo g, Split sp, FFConst 
 #pragma unroll
     for (int f = 0; f < 8; ++f) {
         const ff a = ff_mul(cv, q[f]);
-        diag = ff_add(diag, a);
+        diag = ff_add_nr(diag, a); // positive terms: renormalised after the loop
         __stcs(cf + coef_at(t, f, 10), ff_to_d(a));
         a32[f] = a.h;
     }
+    diag = ff_norm(diag);
     __stcs(cf + coef_at(t, 8, 10), ff_to_d(diag));
     __stcs(cf + coef_at(t, 9, 10), ff_to_d(ff_mul(ff_make(K.omh, K.oml), ff_rcp(diag))));
     float4 *f4 = reinterpret_cast<float4 *>(cf32 + 8 * t);
@@ -285,6 +318,8 @@ void launch_assemble_ff(const Geo &g, const Split &s, const double *u, CPtrs8 gi
     split_host(p.eps2, K.eps2h, K.eps2l);
     split_host(p.tau / (p.h * p.h), K.ch, K.cl);
     split_host(p.omega_c, K.omh, K.oml);
+    int e1 = 0, e2 = 0;
+    K.pow2 = K.ih2l == 0.f && K.iq2l == 0.f && frexp((double)K.ih2h, &e1) == 0.5 && frexp((double)K.iq2h, &e2) == 0.5;
     k_fdiff<<<sm_count * max_blocks_fdiff(), 256, 0, st>>>(g, u, b);
     {
         const int bx = g.nx + 1 >= 128 ? 128 : (g.nx + 1 >= 64 ? 64 : 32);

@@ -21,12 +21,11 @@
 //                     (the reference's face formula, segmentation4D.c:446-580),
 //                     s2 = |grad u|^2 + eps2, fn = s2 / sqrt(s2), fq = g / sqrt(s2);
 //   k_voxel_coef_ff:  vc = sqrt(mean(fn)^2 + eps2), c a_f = c vc fq_f,
-//                     diag = 1 + sum c a_f, omega/diag; written as FP64
-//                     records (refinement) and FP32 records (sweeps).
+//                     diag = 1 + sum c a_f; written as FP64 records
+//                     (refinement) and FP32 records (sweeps).
 //
 // Relative error of the coefficients: below 1e-12 (1/sqrt from an FP32 seed
-// and one Newton step, about 1.5 (2^-22)^2 each; 1/x with two steps; sums and
-// products to 2^-46).  The mixed form's refinement passes measure the FP64 residual
+// and one Newton step, about 1.5 (2^-22)^2 each; sums and products to 2^-46).  The mixed form's refinement passes measure the FP64 residual
 // against these coefficients; the residual of its result against exact FP64
 // coefficients meets the same tolerance (tested), the coefficient error
 // entering it only squared, far below any tolerance.
@@ -149,19 +148,6 @@ __device__ __forceinline__ ff ff_rsqrt(ff x)
     return y;
 }
 
-// 1/x, x >= 1: FP32 seed, two Newton steps y += y (1 - x y)
-__device__ __forceinline__ ff ff_rcp(ff x)
-{
-    ff y = ff_make(1.f / x.h, 0.f);
-#pragma unroll
-    for (int it = 0; it < 2; ++it) {
-        const ff xy = ff_mul(x, y);
-        const float r = (1.f - xy.h) - xy.l;
-        y = ff_add(y, ff_mul(y, ff_make(r, 0.f)));
-    }
-    return y;
-}
-
 __device__ __forceinline__ ff ld_ff(const double *p, long long o)
 {
     const float2 v = __ldg(reinterpret_cast<const float2 *>(p) + o);
@@ -180,7 +166,6 @@ struct FFConst {
     float iq2h, iq2l;   // 1/(4h)^2
     float eps2h, eps2l; // eps2
     float ch, cl;       // tau/h^2
-    float omh, oml;     // omega
     int pow2;           // 1/h^2 and 1/(4h)^2 are powers of two (h is): exact scaling
 };
 
@@ -290,7 +275,8 @@ __global__ void __launch_bounds__(256) k_voxel_coef_ff(Geo g, Split sp, FFConst 
     }
     diag = ff_norm(diag);
     __stcs(cf + coef_at(t, 8, 10), ff_to_d(diag));
-    __stcs(cf + coef_at(t, 9, 10), ff_to_d(ff_mul(ff_make(K.omh, K.oml), ff_rcp(diag))));
+    // component 9 (omega/diag) serves only the FP64 sweep, whose form always
+    // assembles its own records: not written here
     float4 *f4 = reinterpret_cast<float4 *>(cf32 + 8 * t);
     __stcs(f4, make_float4(a32[0], a32[1], a32[2], a32[3]));
     __stcs(f4 + 1, make_float4(a32[4], a32[5], a32[6], a32[7]));
@@ -317,7 +303,6 @@ void launch_assemble_ff(const Geo &g, const Split &s, const double *u, CPtrs8 gi
     split_host(1.0 / (16.0 * p.h * p.h), K.iq2h, K.iq2l);
     split_host(p.eps2, K.eps2h, K.eps2l);
     split_host(p.tau / (p.h * p.h), K.ch, K.cl);
-    split_host(p.omega_c, K.omh, K.oml);
     int e1 = 0, e2 = 0;
     K.pow2 = K.ih2l == 0.f && K.iq2l == 0.f && frexp((double)K.ih2h, &e1) == 0.5 && frexp((double)K.iq2h, &e2) == 0.5;
     k_fdiff<<<sm_count * max_blocks_fdiff(), 256, 0, st>>>(g, u, b);

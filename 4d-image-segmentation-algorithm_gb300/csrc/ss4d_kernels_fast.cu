@@ -180,26 +180,42 @@ __global__ void __launch_bounds__(256) k_pack_coef(Geo g, Split sp, CPtrs8 a, do
 }
 
 // natural -> split copies of u (both red buffers and black, ghosts
-// included) and of prev (interior of both colours)
-__global__ void k_pack(Geo g, Split sp, const double *__restrict__ u, const double *__restrict__ prev, SplitBufs b)
+// included) and of prev (both colours).  A thread takes two neighbours
+// (i = 2m, 2m + 1) of one row: they have opposite colours and land in
+// columns m + A - 1 and m + A of their colour arrays.
+__global__ void __launch_bounds__(256) k_pack(Geo g, Split sp, const double *__restrict__ u,
+                                              const double *__restrict__ prev, SplitBufs b, FastDiv fpairs)
 {
-    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < g.n; o += (long long)gridDim.x * blockDim.x) {
-        int i, j, k, l;
-        nat_coords(g, (unsigned)o, i, j, k, l);
-        const int col = (i + j + k + l) & 1;
-        const long long s = (((long long)l * g.kM + k) * g.jM + j) * sp.Hs + ((i + 1) >> 1) + sp.A - 1;
-        const double v = u[o];
-        if (col == 0) {
-            b.R[0][s] = v;
-            b.R[1][s] = v;
-        } else {
-            b.Bk[s] = v;
+    const unsigned npairs = fpairs.d;
+    const unsigned total = (unsigned)(g.n / g.iM) * npairs; // rows x pairs, below 2^31
+    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+        const unsigned row = fdiv(q, fpairs);
+        const int m = (int)(q - row * npairs);
+        // row = (l kM + k) jM + j
+        const unsigned rk = fdiv(row, g.fjM);
+        const int j = (int)(row - rk * g.fjM.d);
+        const unsigned l = fdiv(rk, g.fkM);
+        const int k = (int)(rk - l * g.fkM.d);
+        const int c0 = (j + k + (int)l) & 1; // colour of i = 2m
+        const long long o = (long long)row * g.iM + 2 * m;
+        const long long s = (long long)row * sp.Hs + m + sp.A - 1;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (2 * m + h >= g.iM)
+                break;
+            const int col = c0 ^ h;
+            const double v = u[o + h];
+            if (col == 0) {
+                b.R[0][s + h] = v;
+                b.R[1][s + h] = v;
+            } else {
+                b.Bk[s + h] = v;
+            }
+            pick(b.P, col)[s + h] = prev[o + h];
         }
-        pick(b.P, col)[s] = prev[o];
     }
 }
 
-// split -> natural, interior voxels only (the ghosts of u never change)
 // split -> natural interior of u.  With terms > 0 (mixed form) also the next
 // step's start correction, extrapolated in time from this step's change
 // d = u - prev (FP32) and the changes of earlier steps h1, h2 (per colour):
@@ -650,7 +666,7 @@ void launch_assemble(const Geo &g, const Split &s, const double *u, CPtrs8 gin, 
 
 void launch_pack(const Geo &g, const Split &s, const double *u, const double *prev, SplitBufs b, cudaStream_t st)
 {
-    k_pack<<<2048, 256, 0, st>>>(g, s, u, prev, b);
+    k_pack<<<4096, 256, 0, st>>>(g, s, u, prev, b, make_fastdiv((unsigned)((g.iM + 1) / 2)));
 }
 
 void launch_pack_coef(const Geo &g, const Split &s, CPtrs8 a, const ss4d_params &p, SplitBufs b, int want32,

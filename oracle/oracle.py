@@ -51,6 +51,15 @@ def lib() -> C.CDLL:
         _L.or_mcf_set_boundary.argtypes = [vp, C.c_double, C.c_double, vp]
         _L.or_threshold_mask.argtypes = [vp, vp, C.c_double, C.c_int, vp]
         _L.or_rescale.argtypes = [vp, C.c_double, vp, vp, C.c_int, vp, vp, vp, vp]
+        _L.or_max4d.restype = C.c_double
+        _L.or_max4d.argtypes = [vp, vp]
+        _L.or_ball_min_max.restype = C.c_int
+        _L.or_ball_min_max.argtypes = [vp, vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                       C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        _L.or_local_threshold.restype = C.c_int
+        _L.or_local_threshold.argtypes = [vp, C.c_double, C.c_double, C.c_double, vp, vp, C.c_int, vp, vp, vp, vp]
+        _L.or_generate_segm.restype = C.c_int
+        _L.or_generate_segm.argtypes = [vp, C.c_double, vp, vp, C.c_int, vp, vp, vp, vp]
     return _L
 
 
@@ -163,6 +172,36 @@ def rescale(R: float, v, mmask=None, balls=None) -> int:
     return lib().or_rescale(C.byref(d), R, _d(v), _d(mmask) if mmask is not None else None, nb,
                             bl.ctypes.data if nb else None, bx.ctypes.data if nb else None,
                             by.ctypes.data if nb else None, bz.ctypes.data if nb else None)
+
+
+def max4d(v) -> float:
+    """_get4DMax_ (segmentation4D.c:876-895)"""
+    return lib().or_max4d(C.byref(_dims(v.shape)), _d(v))
+
+
+def ball_min_max(v, l: int, cx: float, cy: float, cz: float, R: float):
+    """_get3DMinWithinR_ / _get3DMaxWithinR_ (segmentation4D.c:897-969)"""
+    mn, mx = C.c_double(0), C.c_double(0)
+    rc = lib().or_ball_min_max(C.byref(_dims(v.shape)), _d(v), l, cx, cy, cz, R, C.byref(mn), C.byref(mx))
+    if rc != 0:
+        raise ValueError("ball box leaves the array")
+    return mn.value, mx.value
+
+
+def local_threshold(alpha: float, beta: float, R: float, img, thr, balls) -> int:
+    """_locallyThreshold4Ddata_ (segmentation4D.c:971-1018): thr updated in place"""
+    nb, bl, bx, by, bz = _balls(balls)
+    return lib().or_local_threshold(C.byref(_dims(img.shape)), alpha, beta, R, _d(img), _d(thr), nb,
+                                    bl.ctypes.data if nb else None, bx.ctypes.data if nb else None,
+                                    by.ctypes.data if nb else None, bz.ctypes.data if nb else None)
+
+
+def generate_segm(R: float, u, mmask, balls) -> int:
+    """_generate4DsegmFunct_ (segmentation4D.c:1106-1147): u and mmask updated in place"""
+    nb, bl, bx, by, bz = _balls(balls)
+    return lib().or_generate_segm(C.byref(_dims(u.shape)), R, _d(u), _d(mmask), nb,
+                                  bl.ctypes.data if nb else None, bx.ctypes.data if nb else None,
+                                  by.ctypes.data if nb else None, bz.ctypes.data if nb else None)
 
 
 def threshold_mask(u, level=0.5, normalise=False) -> np.ndarray:

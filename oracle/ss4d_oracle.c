@@ -482,6 +482,124 @@ int or_rescale(const ss4d_dims *d, double R, double *v, const double *Mmask, int
     return 0;
 }
 
+/* ---------------------------------------------------------------------- */
+/* initial segmentation: local thresholding, initial function              */
+
+/* _get4DMax_ (segmentation4D.c:876-895): the largest interior value, the
+ * search starting from 0 (so the result is never negative). */
+double or_max4d(const ss4d_dims *d, const double *v)
+{
+    geo_t g = geo_of(d);
+    double mx = 0;
+    for (int l = 1; l <= g.lM - 2; l++)
+        for (int k = 1; k <= g.kM - 2; k++)
+            for (int j = 1; j <= g.jM - 2; j++)
+                for (int i = 1; i <= g.iM - 2; i++)
+                    if (v[at(&g, i, j, k, l)] > mx)
+                        mx = v[at(&g, i, j, k, l)];
+    return mx;
+}
+
+/* _get3DMinWithinR_ / _get3DMaxWithinR_ (segmentation4D.c:897-969): over the
+ * voxels of frame l whose distance to the centre is at most R, the searches
+ * starting from 100000 and 0.  Returns -1 if the ball's box leaves the array. */
+int or_ball_min_max(const ss4d_dims *d, const double *v, int l, double cx, double cy, double cz, double R,
+                    double *mn_out, double *mx_out)
+{
+    geo_t g = geo_of(d);
+    if (!ball_box_ok(&g, cx, cy, cz, R) || l < 0 || l >= g.lM)
+        return -1;
+    int k0 = (int)(cz - R - 0.5), k1 = (int)(cz + R + 0.5);
+    int j0 = (int)(cy - R - 0.5), j1 = (int)(cy + R + 0.5);
+    int i0 = (int)(cx - R - 0.5), i1 = (int)(cx + R + 0.5);
+    double mn = 100000, mx = 0;
+    for (int k = k0; k <= k1; k++)
+        for (int j = j0; j <= j1; j++)
+            for (int i = i0; i <= i1; i++) {
+                double dx = i - cx, dy = j - cy, dz = k - cz;
+                double r = sqrt((dx * dx) + (dy * dy) + (dz * dz));
+                if (r <= R) {
+                    double val = v[at(&g, i, j, k, l)];
+                    if (val < mn)
+                        mn = val;
+                    if (val > mx)
+                        mx = val;
+                }
+            }
+    *mn_out = mn;
+    *mx_out = mx;
+    return 0;
+}
+
+/* _locallyThreshold4Ddata_ (segmentation4D.c:971-1018): per ball of radius R
+ * the level alpha min + beta max of the input inside it; inside the ball the
+ * thresholded image becomes the global maximum wherever the input exceeds the
+ * level (elsewhere it is left as it is).  Balls flattened in (frame, centre)
+ * order; -1 if a ball box leaves the array. */
+int or_local_threshold(const ss4d_dims *d, double alpha, double beta, double R, const double *in, double *thr, int nb,
+                       const int *bl, const double *bx, const double *by, const double *bz)
+{
+    geo_t g = geo_of(d);
+    for (int b = 0; b < nb; ++b)
+        if (!ball_box_ok(&g, bx[b], by[b], bz[b], R))
+            return -1;
+    const double gmax = or_max4d(d, in);
+    for (int b = 0; b < nb; ++b) {
+        const int l = bl[b];
+        const double cx = bx[b], cy = by[b], cz = bz[b];
+        double mn, mx;
+        or_ball_min_max(d, in, l, cx, cy, cz, R, &mn, &mx);
+        const double level = alpha * mn + beta * mx;
+        int k0 = (int)(cz - R - 0.5), k1 = (int)(cz + R + 0.5);
+        int j0 = (int)(cy - R - 0.5), j1 = (int)(cy + R + 0.5);
+        int i0 = (int)(cx - R - 0.5), i1 = (int)(cx + R + 0.5);
+        for (int k = k0; k <= k1; k++)
+            for (int j = j0; j <= j1; j++)
+                for (int i = i0; i <= i1; i++) {
+                    double dx = i - cx, dy = j - cy, dz = k - cz;
+                    double r = sqrt((dx * dx) + (dy * dy) + (dz * dz));
+                    if (r <= R && in[at(&g, i, j, k, l)] > level)
+                        thr[at(&g, i, j, k, l)] = gmax;
+                }
+    }
+    return 0;
+}
+
+/* _generate4DsegmFunct_ (segmentation4D.c:1106-1147): in the box of each
+ * ball (half-width R + 0.5, R = ballRadius) and within the fixed distance 12
+ * of its centre, u = max(u, |1/(r + 0.5) - 1/12.5|) and Mmask = 1.  -1 if a
+ * ball box leaves the array. */
+int or_generate_segm(const ss4d_dims *d, double R, double *u, double *Mmask, int nb, const int *bl, const double *bx,
+                     const double *by, const double *bz)
+{
+    geo_t g = geo_of(d);
+    const double v = 0.5, Rf = 12.;
+    for (int b = 0; b < nb; ++b)
+        if (!ball_box_ok(&g, bx[b], by[b], bz[b], R))
+            return -1;
+    for (int b = 0; b < nb; ++b) {
+        const int l = bl[b];
+        const double cx = bx[b], cy = by[b], cz = bz[b];
+        int k0 = (int)(cz - R - 0.5), k1 = (int)(cz + R + 0.5);
+        int j0 = (int)(cy - R - 0.5), j1 = (int)(cy + R + 0.5);
+        int i0 = (int)(cx - R - 0.5), i1 = (int)(cx + R + 0.5);
+        for (int k = k0; k <= k1; k++)
+            for (int j = j0; j <= j1; j++)
+                for (int i = i0; i <= i1; i++) {
+                    double dx = i - cx, dy = j - cy, dz = k - cz;
+                    double r = sqrt((dx * dx) + (dy * dy) + (dz * dz));
+                    if (r <= Rf) {
+                        double nv = fabs((1. / (sqrt((dx * dx) + (dy * dy) + (dz * dz)) + v)) - (1. / (Rf + v)));
+                        ptrdiff_t o = at(&g, i, j, k, l);
+                        if (u[o] < nv)
+                            u[o] = nv;
+                        Mmask[o] = 1.;
+                    }
+                }
+    }
+    return 0;
+}
+
 /* Threshold of _writeData_mpi_ (segmentation4D_mpi.c:1470-1478): one byte per
  * interior voxel, 1 where u >= level, frames in (l, k, j, i) order.  With
  * normalise the level is min + level (max - min) over the interior. */

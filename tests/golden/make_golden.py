@@ -20,8 +20,13 @@ and stores inputs and outputs as .npz files:
   seg_config1.npz the 32^3 x 8 scene, 20 steps: per-step iteration counts,
                   residuals, ||u - prev_u||, u at 4096 fixed probe voxels,
                   checksums, and the final masks (bit-packed)
+  seg_init.npz    initial segmentation at 36x34x32x3 with ball radius 13:
+                  global maximum, per-ball minimum/maximum, local
+                  thresholding into a non-zero image, initial function on a
+                  non-zero u with overlapping balls, Mmask
 
-Usage:  python tests/golden/make_golden.py   (from the repository root)
+Usage:  python tests/golden/make_golden.py [fixture ...]   (from the repository root;
+        names are the functions below, all of them by default)
 """
 from __future__ import annotations
 
@@ -299,9 +304,66 @@ def seg_config1():
     print("config1: its", its)
 
 
+def seg_init():
+    """Initial segmentation with a ball radius above the initial function's
+    fixed radius 12 (segmentation4D.c:1110): the reference's _get4DMax_,
+    _get3DMinWithinR_/_get3DMaxWithinR_ per ball, _locallyThreshold4Ddata_
+    into a non-zero thresholded image, _generate4DsegmFunct_ on a non-zero u
+    with overlapping balls."""
+    R = Ref(os.path.join(REF_DIR, "libref_seg.so"))
+    nx, ny, nz, nt = 36, 34, 32, 3
+    p = ss4d.scene_params(ballRadius=13.0)
+    i0_in, u_in = ss4d.scene(1, nx, ny, nz, nt, seed=21)
+    shape = i0_in.shape
+    centers = {1: [(18.0, 17.0, 16.5), (20.5, 18.0, 17.0)], 2: [(17.0, 18.5, 16.0)],
+               3: [(18.5, 17.5, 17.5), (16.0, 16.0, 15.0), (19.0, 19.0, 16.0)]}
+    seg_setup(R, shape, p, centers)
+    R.d("alpha", 0.7), R.d("beta", 0.3)
+    i0 = R.arr("i0", shape)
+    u = R.arr("u", shape)
+    mm = R.arr("Mmask", shape)
+    i0[...] = i0_in
+    out = {"i0_in": i0_in}
+    gmax, _ = R.call("_get4DMax_", C.c_void_p(i0.ctypes.data), restype=C.c_double)
+    out["gmax"] = np.array(gmax)
+    mins, maxs = [], []
+    for l in sorted(centers):
+        for (x, y, z) in centers[l]:
+            args = (C.c_void_p(i0.ctypes.data), C.c_int(l), C.c_double(x), C.c_double(y), C.c_double(z),
+                    C.c_double(p.ballRadius))
+            mn, _ = R.call("_get3DMinWithinR_", *args, restype=C.c_double)
+            mx, _ = R.call("_get3DMaxWithinR_", *args, restype=C.c_double)
+            mins.append(mn)
+            maxs.append(mx)
+    out["ball_min"] = np.array(mins)
+    out["ball_max"] = np.array(maxs)
+    thr0 = 0.25 * u_in  # a non-zero thresholded-image buffer: only some voxels are overwritten
+    u[...] = thr0
+    out["thr_before"] = thr0
+    R.call("_locallyThreshold4Ddata_", C.c_void_p(i0.ctypes.data), C.c_void_p(u.ctypes.data))
+    out["thr_after"] = u.copy()
+    u[...] = u_in
+    mm[...] = 0.0
+    out["u_before"] = u_in
+    R.call("_generate4DsegmFunct_", C.c_void_p(u.ctypes.data))
+    out["u_gen"] = u.copy()
+    out["mmask"] = mm.copy()
+    balls = [(l, x, y, z) for l in sorted(centers) for (x, y, z) in centers[l]]
+    out["balls"] = np.array(balls, dtype=np.float64)
+    out["alpha_beta_R"] = np.array([0.7, 0.3, p.ballRadius])
+    np.savez_compressed(os.path.join(OUT, "seg_init.npz"), **out)
+    print("seg_init: gmax", gmax, "changed thr", int((out["thr_after"] != thr0).sum()),
+          "changed u", int((out["u_gen"] != u_in).sum()))
+
+
 if __name__ == "__main__":
     build_ref()
+    if len(sys.argv) > 1:  # only the named fixtures
+        for name in sys.argv[1:]:
+            globals()[name]()
+        sys.exit(0)
     seg_small()
     seg_balls()
     mcf_small()
     seg_config1()
+    seg_init()

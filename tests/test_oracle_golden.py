@@ -114,3 +114,45 @@ def test_config1_twenty_steps(ss4d, oracle):
     mn = oracle.threshold_mask(u, 0.5, True)
     assert np.array_equal(np.packbits(m05), d["mask05"])
     assert np.array_equal(np.packbits(mn), d["masknorm"])
+
+
+def _balls(d):
+    return [(int(b[0]), float(b[1]), float(b[2]), float(b[3])) for b in d["balls"]]
+
+
+def test_initial_segmentation_small_balls(oracle):
+    """Local thresholding and the initial function of the reference main's
+    pipeline (ball radius 3, alpha 0.85, beta 0.15), bit-exact."""
+    d = load_golden("seg_balls.npz")
+    balls = _balls(d)
+    thr = np.zeros_like(d["i0_in"])
+    assert oracle.local_threshold(0.85, 0.15, 3.0, d["i0_in"].copy(), thr, balls) == 0
+    assert np.array_equal(thr, d["thr_in"])
+    u = d["thr_smooth"].copy()
+    mm = np.zeros_like(u)
+    assert oracle.generate_segm(3.0, u, mm, balls) == 0
+    assert np.array_equal(u, d["u_gen"])
+    assert np.array_equal(mm, d["mmask"])
+
+
+def test_initial_segmentation_large_balls(oracle):
+    """Ball radius 13 (above the initial function's fixed radius 12), a
+    non-zero thresholded image, overlapping balls: global maximum, per-ball
+    minimum/maximum, local thresholding, initial function and Mmask."""
+    d = load_golden("seg_init.npz")
+    alpha, beta, R = (float(v) for v in d["alpha_beta_R"])
+    balls = _balls(d)
+    i0 = d["i0_in"]
+    assert oracle.max4d(i0) == float(d["gmax"])
+    for b, (l, x, y, z) in enumerate(balls):
+        assert oracle.ball_min_max(i0, l, x, y, z, R) == (d["ball_min"][b], d["ball_max"][b])
+    thr = d["thr_before"].copy()
+    assert oracle.local_threshold(alpha, beta, R, i0.copy(), thr, balls) == 0
+    assert np.array_equal(thr, d["thr_after"])
+    u = d["u_before"].copy()
+    mm = np.zeros_like(u)
+    assert oracle.generate_segm(R, u, mm, balls) == 0
+    assert np.array_equal(u, d["u_gen"])
+    assert np.array_equal(mm, d["mmask"])
+    # a ball whose box leaves the array is refused (the reference would read outside it)
+    assert oracle.local_threshold(alpha, beta, R, i0.copy(), thr, [(1, 3.0, 17.0, 16.0)]) == -1

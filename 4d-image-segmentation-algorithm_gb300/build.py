@@ -38,7 +38,7 @@ CUDA_UNITS = {
     "ss4d_nn.cu": [],
     "ss4d_assemble_ff.cu": [],
 }
-C_UNITS = {"ss4d_scene.c": ["-fopenmp"]}
+C_UNITS = {"ss4d_scene.c": ["-fopenmp"], "ss4d_vtk.c": []}
 
 LIB = os.path.join(HERE, "libss4d.so")
 LIB_SEG = os.path.join(HERE, "libss4d_seg.so")

@@ -59,6 +59,12 @@ void ss4d::set_error_text(const char *msg)
     snprintf(g_err, sizeof g_err, "%s", msg);
 }
 
+// the same for this library's C translation units (ss4d_vtk.c)
+extern "C" void ss4d_set_error_text_c(const char *msg)
+{
+    snprintf(g_err, sizeof g_err, "%s", msg);
+}
+
 static ss4d_status last_launch()
 {
     cudaError_t e = cudaGetLastError();
@@ -1165,6 +1171,87 @@ extern "C" ss4d_status ss4d_rescale_to_zero_one(ss4d_solver *s, const ss4d_param
 {
     REQ(s && p && d_img, "NULL argument");
     return rescale_impl(s, p, d_img, d_Mmask, balls);
+}
+
+extern "C" ss4d_status ss4d_frame_from_bytes(ss4d_solver *s, double *d_img, int l, const uint8_t *d_bytes)
+{
+    REQ(s && d_img && d_bytes, "NULL argument");
+    REQ(l >= 1 && l <= s->geo.nt, "frame index out of range (interior frames are 1..lMax-2)");
+    launch_frame_bytes(s->geo, d_img, nullptr, l, 0, d_bytes, nullptr, s->stream);
+    s->launches += 1;
+    return last_launch();
+}
+
+extern "C" ss4d_status ss4d_frame_to_bytes(ss4d_solver *s, const double *d_img, int l, int mode, uint8_t *d_bytes)
+{
+    REQ(s && d_img && d_bytes, "NULL argument");
+    REQ(l >= 1 && l <= s->geo.nt, "frame index out of range (interior frames are 1..lMax-2)");
+    REQ(mode == 0 || mode == 1, "mode must be 0 (scaled bytes) or 1 (mask)");
+    launch_frame_bytes(s->geo, nullptr, d_img, l, mode, nullptr, d_bytes, s->stream);
+    s->launches += 1;
+    return last_launch();
+}
+
+extern "C" ss4d_status ss4d_max4d(ss4d_solver *s, const double *d_img, double *out)
+{
+    REQ(s && d_img && out, "NULL argument");
+    launch_minmax(s->geo, d_img, s->d_partial, 0.0, s->d_scalar, s->stream);
+    s->launches += 2;
+    CKS(last_launch());
+    CK(cudaMemcpyAsync(s->h_scalar, s->d_scalar, sizeof(double) * 2, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    *out = s->h_scalar[1] > 0 ? s->h_scalar[1] : 0.0; // the reference's search starts from 0
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_ball_min_max(ss4d_solver *s, const double *d_img, int l, double cx, double cy, double cz,
+                                         double R, double *mn, double *mx)
+{
+    REQ(s && d_img && mn && mx, "NULL argument");
+    const Geo &g = s->geo;
+    REQ(l >= 0 && l < g.lM, "frame index out of range");
+    const int k0 = (int)(cz - R - 0.5), k1 = (int)(cz + R + 0.5);
+    const int j0 = (int)(cy - R - 0.5), j1 = (int)(cy + R + 0.5);
+    const int i0 = (int)(cx - R - 0.5), i1 = (int)(cx + R + 0.5);
+    REQ(k0 >= 0 && j0 >= 0 && i0 >= 0 && k1 < g.kM && j1 < g.jM && i1 < g.iM,
+        "the ball's box leaves the array (the reference would read out of bounds)");
+    launch_ball_min_max(g, d_img, l, cx, cy, cz, R, s->d_scalar, s->stream);
+    s->launches += 1;
+    CKS(last_launch());
+    CK(cudaMemcpyAsync(s->h_scalar, s->d_scalar, sizeof(double) * 2, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    *mn = s->h_scalar[0];
+    *mx = s->h_scalar[1];
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_local_threshold(ss4d_solver *s, double alpha, double beta, double ballRadius,
+                                            const double *d_in, double *d_thr, const ss4d_balls *balls)
+{
+    REQ(s && d_in && d_thr, "NULL argument");
+    int have = 0;
+    CKS(upload_balls(s, balls, ballRadius, &have));
+    if (!have)
+        return SS4D_OK;
+    launch_minmax(s->geo, d_in, s->d_partial, 0.0, s->d_scalar, s->stream);
+    launch_local_threshold(s->geo, d_in, d_thr, s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz,
+                           ballRadius, alpha, beta, s->d_scalar, s->stream);
+    s->launches += 3;
+    return last_launch();
+}
+
+extern "C" ss4d_status ss4d_generate_segm_function(ss4d_solver *s, double ballRadius, double *d_u, double *d_Mmask,
+                                                   const ss4d_balls *balls)
+{
+    REQ(s && d_u && d_Mmask, "NULL argument");
+    int have = 0;
+    CKS(upload_balls(s, balls, ballRadius, &have));
+    if (!have)
+        return SS4D_OK;
+    launch_generate_segm(s->geo, d_u, d_Mmask, s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz,
+                         ballRadius, s->stream);
+    s->launches += 1;
+    return last_launch();
 }
 
 extern "C" ss4d_status ss4d_threshold_mask(ss4d_solver *s, const double *d_u, double level, int normalise,

@@ -7,6 +7,7 @@
  * a device mirror; the functions move the caller-visible arrays across and
  * run the device path of include/ss4d.h.
  */
+#include <ctype.h>
 #include <stdbool.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -50,6 +51,7 @@ static double *g_tmp2;
 static size_t g_bytes;        /* bytes of one padded array */
 static int g_strict;
 static ss4d_step_stats g_last;
+static uint8_t *g_frame_dev, *g_frame_host; /* one frame's file bytes (device, page-locked host) */
 
 static double **host_slot(int a)
 {
@@ -215,6 +217,10 @@ bool _deallocateMem_(void)
     ss4d_dev_free(g_tmp);
     ss4d_dev_free(g_tmp2);
     g_tmp = g_tmp2 = NULL;
+    ss4d_dev_free(g_frame_dev);
+    ss4d_host_free(g_frame_host);
+    g_frame_dev = NULL;
+    g_frame_host = NULL;
     if (center_x) {
         for (int l = 0; l < lMax; ++l) {
             free(center_x[l]);
@@ -316,6 +322,196 @@ bool _rescale4DdataToZeroOne_(double *imagePtr)
     if (!rescale_dev(d))
         return false;
     return down(imagePtr, d) && finish();
+}
+
+/* ---- initial segmentation (segmentation4D.c:876-1018, 1106-1147) ------- */
+
+double _get4DMax_(double *imagePtr)
+{
+    if (!imagePtr)
+        exit(1); /* as the reference (segmentation4D.c:880) */
+    if (!g_solver)
+        return 0;
+    double *d = mirror_of(imagePtr, g_tmp);
+    double mx = 0;
+    if (!up(imagePtr, d))
+        return 0;
+    ss4d_status st = ss4d_max4d(g_solver, d, &mx);
+    report("max4d", st);
+    return mx;
+}
+
+static double ball_extreme(double *imagePtr, int l, double cx, double cy, double cz, double R, int want_max)
+{
+    if (!imagePtr)
+        exit(1); /* as the reference (segmentation4D.c:901, 938) */
+    if (!g_solver)
+        return 0;
+    double *d = mirror_of(imagePtr, g_tmp);
+    double mn = 0, mx = 0;
+    if (!up(imagePtr, d))
+        return 0;
+    ss4d_status st = ss4d_ball_min_max(g_solver, d, l, cx, cy, cz, R, &mn, &mx);
+    report("ball min/max", st);
+    return want_max ? mx : mn;
+}
+
+double _get3DMinWithinR_(double *imagePtr, int l, double center_x, double center_y, double center_z, double R)
+{
+    return ball_extreme(imagePtr, l, center_x, center_y, center_z, R, 0);
+}
+
+double _get3DMaxWithinR_(double *imagePtr, int l, double center_x, double center_y, double center_z, double R)
+{
+    return ball_extreme(imagePtr, l, center_x, center_y, center_z, R, 1);
+}
+
+bool _locallyThreshold4Ddata_(double *inputImagePtr, double *thresholdedImagePtr)
+{
+    if (!g_solver || !inputImagePtr || !thresholdedImagePtr)
+        return false;
+    double *di = mirror_of(inputImagePtr, g_tmp);
+    double *dt = mirror_of(thresholdedImagePtr, g_tmp2);
+    if (!up(inputImagePtr, di) || !up(thresholdedImagePtr, dt))
+        return false;
+    balls_t bb;
+    if (!balls_make(&bb))
+        return false;
+    ss4d_balls B = {bb.nb, bb.l, bb.x, bb.y, bb.z};
+    ss4d_status st = ss4d_local_threshold(g_solver, alpha, beta, ballRadius, di, dt, &B);
+    balls_free(&bb);
+    report("local threshold", st);
+    return st == SS4D_OK && down(thresholdedImagePtr, dt) && finish();
+}
+
+bool _generate4DsegmFunct_(double *segmFuntionPtr)
+{
+    if (!g_solver || !segmFuntionPtr)
+        return false;
+    double *d = mirror_of(segmFuntionPtr, g_tmp);
+    if (!up(segmFuntionPtr, d) || !up(Mmask, g_dev[A_MASK]))
+        return false;
+    balls_t bb;
+    if (!balls_make(&bb))
+        return false;
+    ss4d_balls B = {bb.nb, bb.l, bb.x, bb.y, bb.z};
+    ss4d_status st = ss4d_generate_segm_function(g_solver, ballRadius, d, g_dev[A_MASK], &B);
+    balls_free(&bb);
+    report("initial function", st);
+    return st == SS4D_OK && down(segmFuntionPtr, d) && down(Mmask, g_dev[A_MASK]) && finish();
+}
+
+/* ---- file formats (segmentation4D.c:1149-1324) --------------------------- */
+
+static size_t frame_voxels(void)
+{
+    return (size_t)(iMax - 2) * (jMax - 2) * (kMax - 2);
+}
+
+static bool frame_buffers(void)
+{
+    if (g_frame_dev)
+        return true;
+    ss4d_status st = ss4d_dev_alloc(frame_voxels(), (void **)&g_frame_dev);
+    if (st == SS4D_OK)
+        st = ss4d_host_alloc(frame_voxels(), (void **)&g_frame_host);
+    report("frame buffers", st);
+    return st == SS4D_OK;
+}
+
+/* file bytes of frame l into the device image d (host -> device: one byte per voxel) */
+static bool frame_in(double *d, int l, const char *path)
+{
+    ss4d_status st = ss4d_vtk_read_frame(path, iMax - 2, jMax - 2, kMax - 2, g_frame_host);
+    if (st == SS4D_OK)
+        st = ss4d_copy_to_device(g_solver, g_frame_dev, g_frame_host, frame_voxels());
+    if (st == SS4D_OK)
+        st = ss4d_frame_from_bytes(g_solver, d, l, g_frame_dev);
+    report("frame read", st);
+    return st == SS4D_OK;
+}
+
+void _readNumberFromFile_(char *dim, FILE *input_file)
+{
+    int count = 0, var;
+    do {
+        var = fgetc(input_file);
+        dim[count++] = (char)var;
+    } while (var != EOF && !isspace(var));
+}
+
+void _readMetaData_(FILE *input_file)
+{
+    int c;
+    while ((c = getc(input_file)) == '#')
+        while ((c = getc(input_file)) != '\n' && c != EOF)
+            ;
+    for (int h = 0; h < 3 && c != EOF; ++h)
+        while ((c = getc(input_file)) != '\n' && c != EOF)
+            ;
+}
+
+bool _load3dDataArrayVTK_(double *imageDataPtr, int l, unsigned char *pathPtr)
+{
+    if (!imageDataPtr || !pathPtr || !g_solver || l < 1 || l > lMax - 2 || !frame_buffers())
+        return false;
+    double *d = mirror_of(imageDataPtr, g_tmp);
+    /* the other frames and the ghosts of the host array stay as they are */
+    if (!up(imageDataPtr, d) || !frame_in(d, l, (const char *)pathPtr))
+        return false;
+    return down(imageDataPtr, d) && finish();
+}
+
+void _readData_(double *inputImage, unsigned char *fileDirectory)
+{
+    if (!inputImage || !fileDirectory || !g_solver || !frame_buffers())
+        exit(1);
+    double *d = mirror_of(inputImage, g_tmp);
+    if (!up(inputImage, d))
+        exit(1);
+    const double sp[3] = {spacing_x, spacing_y, spacing_z};
+    char path[1024];
+    for (int l = 1; l <= lMax - 2; ++l) {
+        snprintf(path, sizeof path, "%s/movingBalls_457_at_time_%03d.vtk", (const char *)fileDirectory, l);
+        if (!frame_in(d, l, path))
+            exit(1); /* as the reference, for a missing frame file */
+        snprintf(path, sizeof path, "%s/movingBalls_457_centers_at_timestep_%03d.vtk", (const char *)fileDirectory,
+                 l);
+        int np = 0;
+        const int cap = no_of_centers ? no_of_centers[l] : 0;
+        ss4d_status st = ss4d_vtk_read_centers(path, sp, cap, center_x[l], center_y[l], center_z[l], &np);
+        report("centre file", st);
+        if (st != SS4D_OK)
+            exit(1); /* missing file, or more centres than no_of_centers[l] allocated */
+    }
+    if (!down(inputImage, d) || !finish())
+        exit(1);
+}
+
+bool _writeData_(double *array4DPtr, unsigned char *pathPtr)
+{
+    if (!array4DPtr || !pathPtr || !g_solver || !frame_buffers())
+        return false;
+    double *d = mirror_of(array4DPtr, g_tmp);
+    if (!up(array4DPtr, d))
+        return false;
+    const double origin[3] = {origin_x, origin_y, origin_z};
+    const double sp[3] = {spacing_x, spacing_y, spacing_z};
+    char path[1024];
+    for (int l = 1; l <= lMax - 2; ++l) {
+        ss4d_status st = ss4d_frame_to_bytes(g_solver, d, l, 0, g_frame_dev);
+        if (st == SS4D_OK)
+            st = ss4d_copy_to_host(g_solver, g_frame_host, g_frame_dev, frame_voxels());
+        if (st == SS4D_OK)
+            st = ss4d_synchronize(g_solver);
+        snprintf(path, sizeof path, "%s_at_time_%03d.vtk", (const char *)pathPtr, l);
+        if (st == SS4D_OK)
+            st = ss4d_vtk_write_frame(path, iMax - 2, jMax - 2, kMax - 2, origin, sp, g_frame_host);
+        report("frame write", st);
+        if (st != SS4D_OK)
+            puts("File could not be opened."); /* as the reference; it goes on with the next frame */
+    }
+    return true;
 }
 
 bool _reflection4Ddata_(double *v)

@@ -35,6 +35,18 @@ void launch_mcf_field(const Geo &g, double *u, double h, double t, int ghosts_on
 void launch_rescale_balls(const Geo &g, double *v, const int *frame_first, const int *frame_count, const double *bx,
                           const double *by, const double *bz, double R, cudaStream_t st);
 void launch_mask_zero(const Geo &g, double *v, const double *Mmask, cudaStream_t st);
+// one frame <-> file bytes: img_out != null: bytes_in -> frame l of img_out;
+// else frame l of img_in -> bytes_out (mode 0 scaled, 1 mask)
+void launch_frame_bytes(const Geo &g, double *img_out, const double *img_in, int l, int mode, const uint8_t *bytes_in,
+                        uint8_t *bytes_out, cudaStream_t st);
+// initial segmentation (segmentation4D.c:876-1018, 1106-1147)
+void launch_ball_min_max(const Geo &g, const double *v, int l, double cx, double cy, double cz, double R, double *out2,
+                         cudaStream_t st);
+void launch_local_threshold(const Geo &g, const double *in, double *thr, const int *frame_first, const int *frame_count,
+                            const double *bx, const double *by, const double *bz, double R, double alpha, double beta,
+                            const double *minmax, cudaStream_t st);
+void launch_generate_segm(const Geo &g, double *u, double *Mmask, const int *frame_first, const int *frame_count,
+                          const double *bx, const double *by, const double *bz, double R, cudaStream_t st);
 void launch_minmax(const Geo &g, const double *u, double *partial, double level, double *out3, cudaStream_t st);
 void launch_threshold(const Geo &g, const double *u, const double *level_dev, double level, uint8_t *mask,
                       cudaStream_t st);

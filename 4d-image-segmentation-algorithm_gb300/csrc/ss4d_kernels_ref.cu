@@ -370,6 +370,150 @@ __global__ void k_rescale_balls(Geo g, double *v, const int *frame_first, const 
     }
 }
 
+// ---------------------------------------------------------------------------
+// initial segmentation (segmentation4D.c:876-1018, 1106-1147).  One block per
+// frame walks that frame's balls in order, as k_rescale_balls does.
+
+// minimum (from 100000) and maximum (from 0) of frame l inside the ball of
+// radius R: _get3DMinWithinR_ / _get3DMaxWithinR_ (segmentation4D.c:897-969);
+// the results in every thread
+__device__ void ball_min_max(const Geo &g, const double *v, int l, double cx, double cy, double cz, double R,
+                             double &mn_out, double &mx_out)
+{
+    const int k0 = (int)(cz - R - 0.5), k1 = (int)(cz + R + 0.5);
+    const int j0 = (int)(cy - R - 0.5), j1 = (int)(cy + R + 0.5);
+    const int i0 = (int)(cx - R - 0.5), i1 = (int)(cx + R + 0.5);
+    const int ni = i1 - i0 + 1, nj = j1 - j0 + 1, nk = k1 - k0 + 1;
+    const long long cnt = (long long)ni * nj * nk;
+    double mn = 100000, mx = 0;
+    for (long long t = threadIdx.x; t < cnt; t += blockDim.x) {
+        const int i = i0 + (int)(t % ni), j = j0 + (int)((t / ni) % nj), k = k0 + (int)(t / ((long long)ni * nj));
+        const double dx = i - cx, dy = j - cy, dz = k - cz;
+        if (sqrt((dx * dx) + (dy * dy) + (dz * dz)) <= R) {
+            const double val = v[nat_index(g, i, j, k, l)];
+            mn = val < mn ? val : mn;
+            mx = val > mx ? val : mx;
+        }
+    }
+    mn = block_min(mn);
+    mx = block_max(mx);
+    __shared__ double r2[2];
+    if (threadIdx.x == 0) {
+        r2[0] = mn;
+        r2[1] = mx;
+    }
+    __syncthreads();
+    mn_out = r2[0];
+    mx_out = r2[1];
+    __syncthreads();
+}
+
+__global__ void k_ball_min_max(Geo g, const double *v, int l, double cx, double cy, double cz, double R, double *out)
+{
+    double mn, mx;
+    ball_min_max(g, v, l, cx, cy, cz, R, mn, mx);
+    if (threadIdx.x == 0) {
+        out[0] = mn;
+        out[1] = mx;
+    }
+}
+
+// _locallyThreshold4Ddata_ (segmentation4D.c:971-1018): per ball the level
+// alpha min + beta max of the input inside it; thr = the global maximum
+// (from 0, _get4DMax_) wherever the input inside the ball exceeds it
+__global__ void k_local_threshold(Geo g, const double *in, double *thr, const int *frame_first, const int *frame_count,
+                                  const double *bx, const double *by, const double *bz, double R, double alpha,
+                                  double beta, const double *minmax)
+{
+    const int l = 1 + blockIdx.x;
+    const double gmax = minmax[1] > 0 ? minmax[1] : 0;
+    const int first = frame_first[l], count = frame_count[l];
+    for (int c = 0; c < count; ++c) {
+        const double cx = bx[first + c], cy = by[first + c], cz = bz[first + c];
+        double mn, mx;
+        ball_min_max(g, in, l, cx, cy, cz, R, mn, mx);
+        const double level = alpha * mn + beta * mx;
+        const int k0 = (int)(cz - R - 0.5), k1 = (int)(cz + R + 0.5);
+        const int j0 = (int)(cy - R - 0.5), j1 = (int)(cy + R + 0.5);
+        const int i0 = (int)(cx - R - 0.5), i1 = (int)(cx + R + 0.5);
+        const int ni = i1 - i0 + 1, nj = j1 - j0 + 1, nk = k1 - k0 + 1;
+        const long long cnt = (long long)ni * nj * nk;
+        for (long long t = threadIdx.x; t < cnt; t += blockDim.x) {
+            const int i = i0 + (int)(t % ni), j = j0 + (int)((t / ni) % nj), k = k0 + (int)(t / ((long long)ni * nj));
+            const double dx = i - cx, dy = j - cy, dz = k - cz;
+            if (sqrt((dx * dx) + (dy * dy) + (dz * dz)) <= R) {
+                const long long o = nat_index(g, i, j, k, l);
+                if (in[o] > level)
+                    thr[o] = gmax;
+            }
+        }
+    }
+}
+
+// _generate4DsegmFunct_ (segmentation4D.c:1106-1147): in each ball's box
+// (half-width R + 0.5) and within the fixed distance 12 of its centre,
+// u = max(u, |1/(r + 0.5) - 1/12.5|) and Mmask = 1; balls in order
+__global__ void k_generate_segm(Geo g, double *u, double *Mmask, const int *frame_first, const int *frame_count,
+                                const double *bx, const double *by, const double *bz, double R)
+{
+    const int l = 1 + blockIdx.x;
+    const double v = 0.5, Rf = 12.;
+    const int first = frame_first[l], count = frame_count[l];
+    for (int c = 0; c < count; ++c) {
+        const double cx = bx[first + c], cy = by[first + c], cz = bz[first + c];
+        const int k0 = (int)(cz - R - 0.5), k1 = (int)(cz + R + 0.5);
+        const int j0 = (int)(cy - R - 0.5), j1 = (int)(cy + R + 0.5);
+        const int i0 = (int)(cx - R - 0.5), i1 = (int)(cx + R + 0.5);
+        const int ni = i1 - i0 + 1, nj = j1 - j0 + 1, nk = k1 - k0 + 1;
+        const long long cnt = (long long)ni * nj * nk;
+        for (long long t = threadIdx.x; t < cnt; t += blockDim.x) {
+            const int i = i0 + (int)(t % ni), j = j0 + (int)((t / ni) % nj), k = k0 + (int)(t / ((long long)ni * nj));
+            const double dx = i - cx, dy = j - cy, dz = k - cz;
+            if (sqrt((dx * dx) + (dy * dy) + (dz * dz)) <= Rf) {
+                const double nv = fabs((1. / (sqrt((dx * dx) + (dy * dy) + (dz * dz)) + v)) - (1. / (Rf + v)));
+                const long long o = nat_index(g, i, j, k, l);
+                if (u[o] < nv)
+                    u[o] = nv;
+                Mmask[o] = 1.;
+            }
+        }
+        __syncthreads(); // the next ball may cover the same voxels
+    }
+}
+
+// ---------------------------------------------------------------------------
+// one frame's interior <-> the bytes of its file (x fastest, then y, z):
+// _load3dDataArrayVTK_ (segmentation4D.c:1317-1320), _writeData_ (:1250-1254),
+// _writeData_mpi_ (segmentation4D_mpi.c:1466-1473)
+
+__global__ void k_frame_from_bytes(Geo g, double *img, int l, const uint8_t *__restrict__ bytes)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y, z = blockIdx.z;
+    if (x >= g.nx || y >= g.ny)
+        return;
+    const long long q = ((long long)z * g.ny + y) * g.nx + x;
+    img[nat_index(g, x + 1, y + 1, z + 1, l)] = bytes[q] / 255.;
+}
+
+// mode 0: (unsigned char)(255 v + 0.5), clamped to [0, 255] (the reference's
+// conversion is undefined outside); mode 1: 1 where v >= 0.5, else 0
+__global__ void k_frame_to_bytes(Geo g, const double *img, int l, int mode, uint8_t *__restrict__ bytes)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y, z = blockIdx.z;
+    if (x >= g.nx || y >= g.ny)
+        return;
+    const long long q = ((long long)z * g.ny + y) * g.nx + x;
+    const double v = img[nat_index(g, x + 1, y + 1, z + 1, l)];
+    uint8_t out;
+    if (mode == 1) {
+        out = v >= 0.5 ? 1 : 0;
+    } else {
+        const double w = 255 * v + 0.5;
+        out = w >= 255. ? 255 : (w > 0. ? (uint8_t)(int)w : 0);
+    }
+    bytes[q] = out;
+}
+
 __global__ void k_mask_zero(Geo g, double *v, const double *Mmask)
 {
     int i, j, k, l;
@@ -533,6 +677,36 @@ void launch_mask_zero(const Geo &g, double *v, const double *Mmask, cudaStream_t
     dim3 gr, bl;
     interior_cfg(g, gr, bl);
     k_mask_zero<<<gr, bl, 0, st>>>(g, v, Mmask);
+}
+
+void launch_ball_min_max(const Geo &g, const double *v, int l, double cx, double cy, double cz, double R, double *out2,
+                         cudaStream_t st)
+{
+    k_ball_min_max<<<1, 256, 0, st>>>(g, v, l, cx, cy, cz, R, out2);
+}
+
+void launch_local_threshold(const Geo &g, const double *in, double *thr, const int *frame_first, const int *frame_count,
+                            const double *bx, const double *by, const double *bz, double R, double alpha, double beta,
+                            const double *minmax, cudaStream_t st)
+{
+    k_local_threshold<<<g.nt, 256, 0, st>>>(g, in, thr, frame_first, frame_count, bx, by, bz, R, alpha, beta, minmax);
+}
+
+void launch_generate_segm(const Geo &g, double *u, double *Mmask, const int *frame_first, const int *frame_count,
+                          const double *bx, const double *by, const double *bz, double R, cudaStream_t st)
+{
+    k_generate_segm<<<g.nt, 256, 0, st>>>(g, u, Mmask, frame_first, frame_count, bx, by, bz, R);
+}
+
+void launch_frame_bytes(const Geo &g, double *img_out, const double *img_in, int l, int mode, const uint8_t *bytes_in,
+                        uint8_t *bytes_out, cudaStream_t st)
+{
+    const int bx = g.nx >= 128 ? 128 : (g.nx >= 64 ? 64 : 32);
+    dim3 bl(bx, 256 / bx, 1), gr((g.nx + bx - 1) / bx, (g.ny + 256 / bx - 1) / (256 / bx), g.nz);
+    if (img_out)
+        k_frame_from_bytes<<<gr, bl, 0, st>>>(g, img_out, l, bytes_in);
+    else
+        k_frame_to_bytes<<<gr, bl, 0, st>>>(g, img_in, l, mode, bytes_out);
 }
 
 void launch_minmax(const Geo &g, const double *u, double *partial, double level, double *out3, cudaStream_t st)

@@ -126,6 +126,10 @@ def lib() -> C.CDLL:
         "ss4d_rescale_to_zero_one": ([vp, C.POINTER(Params), vp, vp, C.POINTER(Balls)], st),
         "ss4d_rescale_to_zero_one_noalloc": ([C.POINTER(Dims), C.POINTER(Params), vp, vp, C.POINTER(Balls), vp], st),
         "ss4d_threshold_mask": ([vp, vp, C.c_double, C.c_int, vp], st),
+        "ss4d_max4d": ([vp, vp, dp], st),
+        "ss4d_ball_min_max": ([vp, vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, dp, dp], st),
+        "ss4d_local_threshold": ([vp, C.c_double, C.c_double, C.c_double, vp, vp, C.POINTER(Balls)], st),
+        "ss4d_generate_segm_function": ([vp, C.c_double, vp, vp, C.POINTER(Balls)], st),
         "ss4d_l2norm": ([vp, C.c_double, vp, vp, dp], st),
         "ss4d_mass": ([vp, C.c_double, vp, dp], st),
         "ss4d_mcf_set_boundary_exact": ([vp, C.c_double, C.c_double, vp], st),
@@ -373,6 +377,30 @@ class Solver:
         B, keep = _balls(balls)
         _check(self.L.ss4d_rescale_to_zero_one(self.h, C.byref(p), _ptr(img), _ptr(mmask),
                                                C.byref(B) if B is not None else None), "rescale")
+        del keep
+
+    # initial segmentation (segmentation4D.c:876-1018, 1106-1147)
+    def max4d(self, img) -> float:
+        v = C.c_double(0)
+        _check(self.L.ss4d_max4d(self.h, _ptr(img), C.byref(v)), "max4d")
+        return v.value
+
+    def ball_min_max(self, img, l: int, cx: float, cy: float, cz: float, R: float):
+        mn, mx = C.c_double(0), C.c_double(0)
+        _check(self.L.ss4d_ball_min_max(self.h, _ptr(img), l, cx, cy, cz, R, C.byref(mn), C.byref(mx)),
+               "ball_min_max")
+        return mn.value, mx.value
+
+    def local_threshold(self, alpha: float, beta: float, ball_radius: float, img, thr, balls):
+        B, keep = _balls(balls)
+        _check(self.L.ss4d_local_threshold(self.h, alpha, beta, ball_radius, _ptr(img), _ptr(thr),
+                                           C.byref(B) if B is not None else None), "local_threshold")
+        del keep
+
+    def generate_segm_function(self, ball_radius: float, u, mmask, balls):
+        B, keep = _balls(balls)
+        _check(self.L.ss4d_generate_segm_function(self.h, ball_radius, _ptr(u), _ptr(mmask),
+                                                  C.byref(B) if B is not None else None), "generate_segm_function")
         del keep
 
     def threshold_mask(self, u, mask, level: float = 0.5, normalise: bool = False):

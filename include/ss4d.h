@@ -239,6 +239,56 @@ ss4d_status ss4d_rescale_to_zero_one(ss4d_solver *s, const ss4d_params *p, doubl
 ss4d_status ss4d_rescale_to_zero_one_noalloc(const ss4d_dims *dims, const ss4d_params *p, double *d_img,
                                              const double *d_Mmask, const ss4d_balls *balls, void *stream);
 
+/* ---- file formats (segmentation4D.c:1149-1324, segmentation4D_mpi.c:
+ * 1424-1482): a frame file is a VTK STRUCTURED_POINTS header of ten lines
+ * followed by nx*ny*nz unsigned bytes, x fastest; a centre file lists the
+ * balls of one frame.  The files are read and written on the host; the
+ * byte <-> double conversion of a frame runs on the GPU, so a frame crosses
+ * the bus as one byte per voxel. ----------------------------------------- */
+/* Write the reference's header (DIMENSIONS, ORIGIN, SPACING as it prints
+ * them) and the bytes. */
+ss4d_status ss4d_vtk_write_frame(const char *path, int nx, int ny, int nz, const double origin[3],
+                                 const double spacing[3], const uint8_t *h_bytes);
+/* Skip ten header lines as _load3dDataArrayVTK_ does and read nx*ny*nz
+ * bytes; SS4D_ERR_INVALID if the file holds fewer. */
+ss4d_status ss4d_vtk_read_frame(const char *path, int nx, int ny, int nz, uint8_t *h_bytes);
+/* The centre-file parse of _readData_ (with _readMetaData_ and
+ * _readNumberFromFile_): *n points, each centre (double)(int)(x / spacing +
+ * 0.5) per axis; SS4D_ERR_INVALID if there are more than max_points. */
+ss4d_status ss4d_vtk_read_centers(const char *path, const double spacing[3], int max_points, double *cx,
+                                  double *cy, double *cz, int *n);
+/* Interior of frame l (1..lMax-2) of d_img = byte / 255. */
+ss4d_status ss4d_frame_from_bytes(ss4d_solver *s, double *d_img, int l, const uint8_t *d_bytes);
+/* Interior of frame l to bytes: mode 0 (unsigned char)(255 v + 0.5) as
+ * _writeData_ writes (clamped to 0..255; the reference's conversion is
+ * undefined outside), mode 1 the mask v >= 0.5 of _writeData_mpi_. */
+ss4d_status ss4d_frame_to_bytes(ss4d_solver *s, const double *d_img, int l, int mode, uint8_t *d_bytes);
+
+/* ---- initial segmentation (the reference main's pipeline before the time
+ * steps, segmentation4D.c:1383-1393) ------------------------------------ */
+/* _get4DMax_ (segmentation4D.c:876-895): largest interior value, the search
+ * starting from 0. Synchronises. */
+ss4d_status ss4d_max4d(ss4d_solver *s, const double *d_img, double *out);
+/* _get3DMinWithinR_ / _get3DMaxWithinR_ (segmentation4D.c:897-969): minimum
+ * (from 100000) and maximum (from 0) of frame l over the voxels within
+ * distance R of (cx, cy, cz).  SS4D_ERR_INVALID if the ball's box leaves the
+ * array.  Synchronises. */
+ss4d_status ss4d_ball_min_max(ss4d_solver *s, const double *d_img, int l, double cx, double cy, double cz,
+                              double R, double *min, double *max);
+/* _locallyThreshold4Ddata_ (segmentation4D.c:971-1018): for each ball
+ * (radius ballRadius) the level alpha*min + beta*max of d_in inside it;
+ * d_thr becomes the global maximum of d_in where d_in exceeds the level
+ * inside the ball and is left unchanged elsewhere.  alpha and beta are the
+ * reference's globals of the same names. */
+ss4d_status ss4d_local_threshold(ss4d_solver *s, double alpha, double beta, double ballRadius,
+                                 const double *d_in, double *d_thr, const ss4d_balls *balls);
+/* _generate4DsegmFunct_ (segmentation4D.c:1106-1147): inside each ball's box
+ * (half-width ballRadius + 0.5) and within distance 12 of the centre (the
+ * reference's fixed radius), u = max(u, |1/(r + 0.5) - 1/12.5|) and
+ * Mmask = 1. */
+ss4d_status ss4d_generate_segm_function(ss4d_solver *s, double ballRadius, double *d_u, double *d_Mmask,
+                                        const ss4d_balls *balls);
+
 /* Level-set threshold to a mask, as _writeData_mpi_ (segmentation4D_mpi.c:
  * 1470-1478): mask = (u >= level) for every interior voxel, written frame by
  * frame in (l, k, j, i) order, nx*ny*nz*nt bytes of 0/1.  With normalise != 0

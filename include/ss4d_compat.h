@@ -34,6 +34,7 @@
 #define SS4D_COMPAT_H
 
 #include <stdbool.h>
+#include <stdio.h>
 #include <stddef.h>
 
 #ifdef __cplusplus
@@ -54,6 +55,18 @@ int ijkl(int i, int j, int k, int l);                                   /* segme
 double _gFunction_(double value, double coef);                          /* segmentation4D.c:67   */
 bool _reflection4Ddata_(double *u);                                     /* segmentation4D.c:826  */
 double _mass4D_(double *a);                                             /* segmentation4D.c:317  */
+double _get4DMax_(double *imagePtr);                                    /* segmentation4D.c:876  */
+double _get3DMinWithinR_(double *imagePtr, int l, double center_x, double center_y,
+                         double center_z, double R);                    /* segmentation4D.c:897  */
+double _get3DMaxWithinR_(double *imagePtr, int l, double center_x, double center_y,
+                         double center_z, double R);                    /* segmentation4D.c:934  */
+bool _locallyThreshold4Ddata_(double *inputImagePtr, double *thresholdedImagePtr); /* segmentation4D.c:971 */
+bool _generate4DsegmFunct_(double *segmFuntionPtr);                     /* segmentation4D.c:1106 */
+void _readData_(double *inputImage, unsigned char *fileDirectory);      /* segmentation4D.c:1149 */
+bool _writeData_(double *array4DPtr, unsigned char *pathPtr);           /* segmentation4D.c:1217 */
+void _readNumberFromFile_(char *dim, FILE *input_file);                 /* segmentation4D.c:1262 */
+void _readMetaData_(FILE *input_file);                                  /* segmentation4D.c:1275 */
+bool _load3dDataArrayVTK_(double *imageDataPtr, int l, unsigned char *pathPtr); /* segmentation4D.c:1289 */
 
 /* ---- libss4d_mcf.so: mcf_4D.h ------------------------------------------- */
 bool _allocateMem_mcf(void);                                            /* mcf_4D.c:42   */

@@ -127,6 +127,11 @@ def lib() -> C.CDLL:
         "ss4d_rescale_to_zero_one_noalloc": ([C.POINTER(Dims), C.POINTER(Params), vp, vp, C.POINTER(Balls), vp], st),
         "ss4d_threshold_mask": ([vp, vp, C.c_double, C.c_int, vp], st),
         "ss4d_max4d": ([vp, vp, dp], st),
+        "ss4d_vtk_write_frame": ([C.c_char_p, C.c_int, C.c_int, C.c_int, dp, dp, vp], st),
+        "ss4d_vtk_read_frame": ([C.c_char_p, C.c_int, C.c_int, C.c_int, vp], st),
+        "ss4d_vtk_read_centers": ([C.c_char_p, dp, C.c_int, dp, dp, dp, C.POINTER(C.c_int)], st),
+        "ss4d_frame_from_bytes": ([vp, vp, C.c_int, vp], st),
+        "ss4d_frame_to_bytes": ([vp, vp, C.c_int, C.c_int, vp], st),
         "ss4d_ball_min_max": ([vp, vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, dp, dp], st),
         "ss4d_local_threshold": ([vp, C.c_double, C.c_double, C.c_double, vp, vp, C.POINTER(Balls)], st),
         "ss4d_generate_segm_function": ([vp, C.c_double, vp, vp, C.POINTER(Balls)], st),
@@ -211,6 +216,32 @@ def scene(kind: int, nx: int, ny: int, nz: int, nt: int, seed: int, threads: int
     _check(lib().ss4d_scene_generate(kind, nx, ny, nz, nt, seed, i0.ctypes.data, u0.ctypes.data, threads),
            "scene_generate")
     return i0, u0
+
+
+def vtk_write_frame(path: str, bytes_xyz, origin=(0.0, 0.0, 0.0), spacing=(1.0, 1.0, 1.0)):
+    """One frame file (the reference's header, then the bytes); bytes_xyz is a
+    uint8 array [nz][ny][nx]."""
+    import numpy as np
+    b = np.ascontiguousarray(bytes_xyz, dtype=np.uint8)
+    nz, ny, nx = b.shape
+    o, sp = (C.c_double * 3)(*origin), (C.c_double * 3)(*spacing)
+    _check(lib().ss4d_vtk_write_frame(path.encode(), nx, ny, nz, o, sp, b.ctypes.data), "vtk_write_frame")
+
+
+def vtk_read_frame(path: str, nx: int, ny: int, nz: int):
+    import numpy as np
+    out = np.empty((nz, ny, nx), dtype=np.uint8)
+    _check(lib().ss4d_vtk_read_frame(path.encode(), nx, ny, nz, out.ctypes.data), "vtk_read_frame")
+    return out
+
+
+def vtk_read_centers(path: str, spacing=(1.0, 1.0, 1.0), max_points: int = 4096):
+    """[(x, y, z)] in voxel units, as the reference's _readData_ converts them"""
+    cx, cy, cz = ((C.c_double * max_points)() for _ in range(3))
+    n = C.c_int(0)
+    sp = (C.c_double * 3)(*spacing)
+    _check(lib().ss4d_vtk_read_centers(path.encode(), sp, max_points, cx, cy, cz, C.byref(n)), "vtk_read_centers")
+    return [(cx[i], cy[i], cz[i]) for i in range(n.value)]
 
 
 def _p8(arrs):
@@ -378,6 +409,13 @@ class Solver:
         _check(self.L.ss4d_rescale_to_zero_one(self.h, C.byref(p), _ptr(img), _ptr(mmask),
                                                C.byref(B) if B is not None else None), "rescale")
         del keep
+
+    # frame files (segmentation4D.c:1149-1324)
+    def frame_from_bytes(self, img, l: int, dbytes):
+        _check(self.L.ss4d_frame_from_bytes(self.h, _ptr(img), l, _ptr(dbytes)), "frame_from_bytes")
+
+    def frame_to_bytes(self, img, l: int, dbytes, mode: int = 0):
+        _check(self.L.ss4d_frame_to_bytes(self.h, _ptr(img), l, mode, _ptr(dbytes)), "frame_to_bytes")
 
     # initial segmentation (segmentation4D.c:876-1018, 1106-1147)
     def max4d(self, img) -> float:

@@ -20,6 +20,8 @@ and stores inputs and outputs as .npz files:
   seg_config1.npz the 32^3 x 8 scene, 20 steps: per-step iteration counts,
                   residuals, ||u - prev_u||, u at 4096 fixed probe voxels,
                   checksums, and the final masks (bit-packed)
+  vtk_io.npz      the reference's frame and centre files: _readData_ on a
+                  directory of frame/centre files, _writeData_ of a volume
   seg_init.npz    initial segmentation at 36x34x32x3 with ball radius 13:
                   global maximum, per-ball minimum/maximum, local
                   thresholding into a non-zero image, initial function on a
@@ -356,6 +358,70 @@ def seg_init():
           "changed u", int((out["u_gen"] != u_in).sum()))
 
 
+VTK_HEADER = ("# vtk DataFile Version 3.0\nmovingBalls test frame\nBINARY\nDATASET STRUCTURED_POINTS\n"
+              "DIMENSIONS {nx} {ny} {nz}\nORIGIN 0 0 0\nSPACING 0.5 0.25 1\nPOINT_DATA {n}\n"
+              "SCALARS scalars unsigned_char\nLOOKUP_TABLE default\n")
+
+
+def vtk_io():
+    """The reference's file formats: _readData_ on a directory of frame files
+    (random bytes, including newline bytes in the payload) and centre files
+    (two comment lines, a POINTS line with a type word, non-integral
+    coordinates at spacing 0.5 / 0.25 / 1), and _writeData_ of a volume in
+    [0, 1] with values on the rounding boundaries."""
+    R = Ref(os.path.join(REF_DIR, "libref_seg.so"))
+    nx, ny, nz, nt = 9, 7, 5, 3
+    shape = (nt + 2, nz + 2, ny + 2, nx + 2)
+    p = ss4d.scene_params(ballRadius=1.0)
+    rng = np.random.default_rng(31)
+    pts = {1: [(2.1, 1.3, 2.9), (3.3, 0.8, 1.1)], 2: [(1.74, 1.12, 2.5)],
+           3: [(2.6, 1.0, 3.0), (1.2, 0.9, 2.0), (3.9, 1.62, 1.7)]}
+    seg_setup(R, shape, p, {l: [(0.0, 0.0, 0.0)] * len(c) for l, c in pts.items()})
+    for nm, v in (("spacing_x", 0.5), ("spacing_y", 0.25), ("spacing_z", 1.0), ("origin_x", 0.5),
+                  ("origin_y", -1.25), ("origin_z", 2.0)):
+        R.d(nm, v)
+    out = {"dims": np.array([nx, ny, nz, nt])}
+    with tempfile.TemporaryDirectory() as td:
+        payloads, ctexts = [], []
+        for l in range(1, nt + 1):
+            pay = rng.integers(0, 256, nx * ny * nz, dtype=np.uint8)
+            pay[::37] = 10  # newline bytes inside the payload
+            payloads.append(pay)
+            with open(os.path.join(td, "movingBalls_457_at_time_%03d.vtk" % l), "wb") as fh:
+                fh.write(VTK_HEADER.format(nx=nx, ny=ny, nz=nz, n=nx * ny * nz).encode() + pay.tobytes())
+            txt = ("# vtk DataFile Version 3.0\n# centres of frame %d\ncentres\nASCII\nDATASET POLYDATA\n"
+                   "POINTS %d float\n" % (l, len(pts[l])) + "".join("%g %g %g\n" % q for q in pts[l]))
+            ctexts.append(txt)
+            with open(os.path.join(td, "movingBalls_457_centers_at_timestep_%03d.vtk" % l), "w") as fh:
+                fh.write(txt)
+        i0 = R.arr("i0", shape)
+        i0[...] = -1.0  # ghosts and untouched voxels keep this value
+        R.call("_readData_", C.c_void_p(i0.ctypes.data), C.c_char_p(td.encode()), restype=None)
+        out["payloads"] = np.stack(payloads)
+        out["centre_texts"] = np.array(ctexts)
+        out["i0_read"] = i0.copy()
+        pp = C.POINTER(C.POINTER(C.c_double))
+        cx, cy, cz = (pp.in_dll(R.L, n) for n in ("center_x", "center_y", "center_z"))
+        out["centres"] = np.array([(l, cx[l][c], cy[l][c], cz[l][c]) for l in sorted(pts)
+                                   for c in range(len(pts[l]))])
+        u = R.arr("u", shape)
+        v = rng.random(shape)
+        v.reshape(-1)[::11] = (np.arange(v.size)[::11] % 255 + 0.5) / 255.0  # rounding boundaries
+        v.reshape(-1)[::13] = 0.0
+        v.reshape(-1)[::17] = 1.0
+        u[...] = v
+        out["u_written"] = v
+        R.call("_writeData_", C.c_void_p(u.ctypes.data), C.c_char_p(os.path.join(td, "out").encode()))
+        files = []
+        for l in range(1, nt + 1):
+            with open(os.path.join(td, "out_at_time_%03d.vtk" % l), "rb") as fh:
+                files.append(np.frombuffer(fh.read(), dtype=np.uint8))
+        out["written"] = np.stack(files).astype(np.uint8)  # equal lengths: same header and size per frame
+    out["origin_spacing"] = np.array([0.5, -1.25, 2.0, 0.5, 0.25, 1.0])
+    np.savez_compressed(os.path.join(OUT, "vtk_io.npz"), **out)
+    print("vtk_io: centres", out["centres"].tolist())
+
+
 if __name__ == "__main__":
     build_ref()
     if len(sys.argv) > 1:  # only the named fixtures
@@ -367,3 +433,4 @@ if __name__ == "__main__":
     mcf_small()
     seg_config1()
     seg_init()
+    vtk_io()

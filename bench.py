@@ -45,7 +45,7 @@ BYTES_FP32_ITER = 44.0  # the same arrays in FP32
 # targets; the summary and command are in profiles/), scaled by the targets
 # of a launch at the benchmarked size
 EXTRAP_ORDER = 3  # the extrap form's order (ss4d_solver_set_extrapolation)
-TRAFFIC_PER_TARGET = {"k_sweep32": 49.7, "k_sweep64": 118.9}
+TRAFFIC_PER_TARGET = {"k_sweep32": 49.7, "k_sweep64": 118.6}
 TRAFFIC_SOURCE = "profiles/sweep_refine_assembly_conv_kernels_128x128x64x8.md"
 
 

@@ -20,6 +20,8 @@ and stores inputs and outputs as .npz files:
   seg_config1.npz the 32^3 x 8 scene, 20 steps: per-step iteration counts,
                   residuals, ||u - prev_u||, u at 4096 fixed probe voxels,
                   checksums, and the final masks (bit-packed)
+  pipeline.npz    the reference main's whole sequence on frame and centre
+                  files at 24x22x20x4, ending in _writeData_
   vtk_io.npz      the reference's frame and centre files: _readData_ on a
                   directory of frame/centre files, _writeData_ of a volume
   seg_init.npz    initial segmentation at 36x34x32x3 with ball radius 13:
@@ -422,6 +424,77 @@ def vtk_io():
     print("vtk_io: centres", out["centres"].tolist())
 
 
+def pipeline():
+    """The reference main's whole sequence (segmentation4D.c:1325-1420) on
+    files: _readData_ of frame and centre files, _locallyThreshold4Ddata_,
+    _gf_inputImage_plus_thresholdedImage_, _generate4DsegmFunct_,
+    _rescale4DdataToZeroOne_, time steps with _l2norm_ until segTol or
+    maxNoOfTimeSteps, _writeData_.  Its parameters (h = tau = 0.01, K = 1,
+    eps2 = 1, theta = rho = 0.5, alpha 0.85, beta 0.15, 5 SOR iterations);
+    ball radius 6 at 24x22x20x4."""
+    R = Ref(os.path.join(REF_DIR, "libref_seg.so"))
+    nx, ny, nz, nt = 24, 22, 20, 4
+    shape = (nt + 2, nz + 2, ny + 2, nx + 2)
+    p = ss4d.Params(K=1.0, eps2=1.0, tau=0.01, h=0.01, omega_c=1.8, gsTol=1e-12, maxNoGSIteration=5,
+                    maxNoOfTimeSteps=4, segTol=1e-12, sigma=0.01 * 0.01 / 8, omega_sigma=1.3,
+                    maxNoGSIteration_sigma=10.0, theta_img=0.5, rho_thr=0.5, ballRadius=6.0)
+    img, _ = ss4d.scene(1, nx, ny, nz, nt, seed=41)
+    pay = [np.clip(np.rint(img[l, 1:-1, 1:-1, 1:-1] * 255.0), 0, 255).astype(np.uint8).reshape(-1)
+           for l in range(1, nt + 1)]
+    sp = (0.5, 0.5, 0.5)
+    pts = {1: [(6.1, 5.4, 5.0), (7.2, 6.1, 4.7)], 2: [(6.4, 5.6, 5.2)], 3: [(5.8, 5.3, 4.9), (6.9, 6.4, 5.6)],
+           4: [(6.2, 5.9, 5.1)]}
+    seg_setup(R, shape, p, {l: [(0.0, 0.0, 0.0)] * len(c) for l, c in pts.items()})
+    for nm, v in (("spacing_x", sp[0]), ("spacing_y", sp[1]), ("spacing_z", sp[2]), ("origin_x", 0.0),
+                  ("origin_y", 0.0), ("origin_z", 0.0), ("alpha", 0.85), ("beta", 0.15)):
+        R.d(nm, v)
+    i0, u, prev = R.arr("i0", shape), R.arr("u", shape), R.arr("prev_u", shape)
+    out = {"dims": np.array([nx, ny, nz, nt]), "payloads": np.stack(pay)}
+    with tempfile.TemporaryDirectory() as td:
+        texts = []
+        for l in range(1, nt + 1):
+            with open(os.path.join(td, "movingBalls_457_at_time_%03d.vtk" % l), "wb") as fh:
+                fh.write(VTK_HEADER.format(nx=nx, ny=ny, nz=nz, n=nx * ny * nz).encode() + pay[l - 1].tobytes())
+            txt = ("# vtk DataFile Version 3.0\ncentres\nASCII\nDATASET POLYDATA\nPOINTS %d float\n" % len(pts[l])
+                   + "".join("%g %g %g\n" % q for q in pts[l]))
+            texts.append(txt)
+            with open(os.path.join(td, "movingBalls_457_centers_at_timestep_%03d.vtk" % l), "w") as fh:
+                fh.write(txt)
+        out["centre_texts"] = np.array(texts)
+        with Captured() as cap:
+            R.L._readData_.restype = None
+            R.L._readData_(C.c_void_p(i0.ctypes.data), C.c_char_p(td.encode()))
+            R.L._locallyThreshold4Ddata_(C.c_void_p(i0.ctypes.data), C.c_void_p(u.ctypes.data))
+            R.L._gf_inputImage_plus_thresholdedImage_(C.c_void_p(i0.ctypes.data), C.c_void_p(u.ctypes.data))
+            R.L._generate4DsegmFunct_(C.c_void_p(u.ctypes.data))
+            R.L._rescale4DdataToZeroOne_(C.c_void_p(u.ctypes.data))
+            R.L._l2norm_.restype = C.c_double
+            l2s = []
+            t = 1
+            while True:
+                R.i("numberOfTimeStep", t)
+                R.L._segTimeStep_()
+                l2s.append(R.L._l2norm_(C.c_void_p(prev.ctypes.data), C.c_void_p(u.ctypes.data)))
+                t += 1
+                if not (t <= p.maxNoOfTimeSteps and l2s[-1] > p.segTol):
+                    break
+            R.L._writeData_(C.c_void_p(u.ctypes.data), C.c_char_p(os.path.join(td, "result").encode()))
+        its, res = parse_steps(cap.text)
+        files = []
+        for l in range(1, nt + 1):
+            with open(os.path.join(td, "result_at_time_%03d.vtk" % l), "rb") as fh:
+                files.append(np.frombuffer(fh.read(), dtype=np.uint8))
+    out["written"] = np.stack(files).astype(np.uint8)
+    out["u_final"] = u.copy()
+    out["its"] = np.array(its)
+    out["l2"] = np.array(l2s)
+    out["params"] = np.array([p.as_dict()[k] for k in sorted(p.as_dict())])
+    out["param_names"] = np.array(sorted(p.as_dict()))
+    out["spacing"] = np.array(sp)
+    np.savez_compressed(os.path.join(OUT, "pipeline.npz"), **out)
+    print("pipeline: its", its, "l2", ["%.3e" % v for v in l2s])
+
+
 if __name__ == "__main__":
     build_ref()
     if len(sys.argv) > 1:  # only the named fixtures
@@ -434,3 +507,4 @@ if __name__ == "__main__":
     seg_config1()
     seg_init()
     vtk_io()
+    pipeline()

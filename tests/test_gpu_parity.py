@@ -256,3 +256,26 @@ def test_norms_match_oracle(ss4d, oracle, cuda):
         m = S.mass(0.5, dev(torch, a))
     assert abs(l2 - oracle.l2norm(0.5, a, b)) <= 1e-13 * abs(l2)
     assert abs(m - oracle.mass(0.5, a)) <= 1e-12 * max(1.0, abs(m))
+
+
+@pytest.mark.parametrize("arith", ["fp64", "mixed"])
+def test_sweeps_do_not_depend_on_block_order(ss4d, oracle, cuda, arith):
+    """Red-black colour independence: each half-sweep reads only the other
+    colour, so the tile order and grid size (k-block depth, persistent grid)
+    must not change u.  The residual's per-block partial sums are grouped
+    differently, so the iteration counts are compared, and u bit for bit."""
+    torch = cuda
+    dims = nx, ny, nz, nt = (37, 21, 13, 5)
+    p = ss4d.scene_params(gsTol=1e-10)
+    i0h, u0h = ss4d.scene(3, nx, ny, nz, nt, seed=81)
+    g = [dev(torch, a) for a in oracle.gfaces(p, i0h, np.zeros_like(i0h))]
+    runs = []
+    for k_block, max_grid in ((4, 0), (1, 7), (8, 300), (2, 1)):
+        u = dev(torch, u0h)
+        with ss4d.Solver.for_interior(*dims, arith=arith) as S:
+            S.set_tiling(k_block, max_grid)
+            its = [S.seg_time_step(p, u, None, g)["iterations"] for _ in range(2)]
+        runs.append((its, host(u)))
+    for its, u in runs[1:]:
+        assert its == runs[0][0]
+        assert np.array_equal(u, runs[0][1])

@@ -17,7 +17,7 @@ and stores inputs and outputs as .npz files:
                   initial function in the balls, Mmask, 3 time steps
   mcf_small.npz   MCF known-answer problem at n = 8 (3 steps) and the
                   error history at n = 16 (4 steps)
-  seg_config1.npz the 32^3 x 8 scene, 20 steps: per-step iteration counts,
+  seg_32x32x32x8.npz the 32^3 x 8 scene, 20 steps: per-step iteration counts,
                   residuals, ||u - prev_u||, u at 4096 fixed probe voxels,
                   checksums, and the final masks (bit-packed)
   pipeline.npz    the reference main's whole sequence on frame and centre
@@ -270,7 +270,7 @@ def mcf_small():
     print("mcf: err8", e8, "err16", e16)
 
 
-def seg_config1():
+def seg_32x32x32x8():
     R = Ref(os.path.join(REF_DIR, "libref_seg.so"))
     nx, ny, nz, nt = 32, 32, 32, 8
     p = ss4d.scene_params(maxNoOfTimeSteps=20)
@@ -301,11 +301,11 @@ def seg_config1():
     m05 = (inner >= 0.5).astype(np.uint8).reshape(-1)
     lo, hi = inner.min(), inner.max()
     mnorm = (inner >= lo + 0.5 * (hi - lo)).astype(np.uint8).reshape(-1)
-    np.savez_compressed(os.path.join(OUT, "seg_config1.npz"), its=np.array(its), res=np.array(res),
+    np.savez_compressed(os.path.join(OUT, "seg_32x32x32x8.npz"), its=np.array(its), res=np.array(res),
                         l2=np.array(l2), probes=probes, probe_vals=np.stack(probe_vals), sums=np.array(sums),
                         mask05=np.packbits(m05), masknorm=np.packbits(mnorm), seed=1,
                         dims=np.array([nx, ny, nz, nt]))
-    print("config1: its", its)
+    print("seg_32x32x32x8: its", its)
 
 
 def seg_init():
@@ -504,7 +504,7 @@ if __name__ == "__main__":
     seg_small()
     seg_balls()
     mcf_small()
-    seg_config1()
+    seg_32x32x32x8()
     seg_init()
     vtk_io()
     pipeline()

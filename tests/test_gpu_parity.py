@@ -1,6 +1,6 @@
 """CUDA path vs the reference (golden fixtures) and the oracle, through the C ABI.
 
-Bars (the benchmark spec): the plain FP64 forms match the reference's red-black SOR
+Bars: the plain FP64 forms match the reference's red-black SOR
 to <= 1e-10 relative in u per time step with the same iteration counts, and
 masks are bit-exact.  The reference-order kernels (SS4D_ARITH_REFERENCE) are
 held to 1e-13 (they differ from the reference only where it calls pow()).
@@ -156,11 +156,11 @@ def test_mcf_boundary_matches_oracle(ss4d, oracle, cuda):
 
 
 @pytest.mark.parametrize("arith", ["reference", "fp64"])
-def test_config1_twenty_steps_match_reference(ss4d, oracle, cuda, arith):
+def test_32x32x32x8_twenty_steps_match_reference(ss4d, oracle, cuda, arith):
     """32^3 x 8, 20 steps: iteration counts, step differences, probes and
     both masks against the reference's run."""
     torch = cuda
-    d = load_golden("seg_config1.npz")
+    d = load_golden("seg_32x32x32x8.npz")
     nx, ny, nz, nt = (int(v) for v in d["dims"])
     p = ss4d.scene_params(maxNoOfTimeSteps=20)
     i0h, u0h = ss4d.scene(1, nx, ny, nz, nt, seed=int(d["seed"]))

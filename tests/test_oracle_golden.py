@@ -87,11 +87,11 @@ def test_mcf_known_answer_bit_exact(ss4d, oracle):
     assert d["err16"][0] < d["err8"][0] / 4
 
 
-def test_config1_twenty_steps(ss4d, oracle):
+def test_32x32x32x8_twenty_steps(ss4d, oracle):
     """The 32^3 x 8 workload: the oracle reproduces the reference's
     iteration counts, residual print-outs, step differences, probes and
     masks over 20 steps."""
-    d = load_golden("seg_config1.npz")
+    d = load_golden("seg_32x32x32x8.npz")
     nx, ny, nz, nt = (int(v) for v in d["dims"])
     p = ss4d.scene_params(maxNoOfTimeSteps=20)
     i0, u = ss4d.scene(1, nx, ny, nz, nt, seed=int(d["seed"]))

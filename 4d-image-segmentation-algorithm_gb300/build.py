@@ -113,7 +113,7 @@ def build(verbose: bool = False, force: bool = False) -> dict:
         srcp = os.path.join(CSRC, src)
         if force or _stale(lib, [srcp, LIB] + hdrs):
             _run(["gcc", "-O2", "-fPIC", "-shared", "-std=gnu11", "-o", lib, srcp, f"-L{HERE}", "-lss4d",
-                  "-Wl,-Bsymbolic", "-Wl,-rpath,$ORIGIN"], os.path.join(BUILD, src + ".log"))
+                  "-lpthread", "-Wl,-Bsymbolic", "-Wl,-rpath,$ORIGIN"], os.path.join(BUILD, src + ".log"))
     if verbose:
         print(f"built {LIB}, {LIB_SEG}, {LIB_MCF}")
     return {"lib": LIB, "seg": LIB_SEG, "mcf": LIB_MCF}

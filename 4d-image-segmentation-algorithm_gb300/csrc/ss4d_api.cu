@@ -86,6 +86,8 @@ struct ss4d_solver {
     ss4d_arith arith;
     cudaStream_t stream;
     cudaStream_t cap;
+    cudaStream_t side;   // ss4d_copy_to_device_side
+    cudaEvent_t side_ev; // the last side copy
     int device;
     int sm_count;
     int use_graph;
@@ -238,6 +240,8 @@ extern "C" ss4d_status ss4d_solver_create(const ss4d_dims *dims, ss4d_arith arit
     FAIL_IF(cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device));
     s->cfg = make_sweep_cfg(s->geo, s->sp, s->sm_count, 4);
     FAIL_IF(cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking));
+    FAIL_IF(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+    FAIL_IF(cudaEventCreateWithFlags(&s->side_ev, cudaEventDisableTiming));
     FAIL_IF(cudaEventCreate(&s->ev0));
     FAIL_IF(cudaEventCreate(&s->ev1));
     FAIL_IF(cudaEventCreate(&s->tev0));
@@ -321,6 +325,12 @@ extern "C" ss4d_status ss4d_solver_destroy(ss4d_solver *s)
         cudaEventDestroy(s->tev1);
     if (s->cap)
         cudaStreamDestroy(s->cap);
+    if (s->side) {
+        cudaStreamSynchronize(s->side);
+        cudaStreamDestroy(s->side);
+    }
+    if (s->side_ev)
+        cudaEventDestroy(s->side_ev);
     free(s);
     return SS4D_OK;
 }
@@ -1351,6 +1361,24 @@ extern "C" ss4d_status ss4d_copy_to_device(ss4d_solver *s, void *d_dst, const vo
 {
     REQ(s && d_dst && h_src, "NULL argument");
     CK(cudaMemcpyAsync(d_dst, h_src, bytes, cudaMemcpyHostToDevice, s->stream));
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_copy_to_device_side(ss4d_solver *s, void *d_dst, const void *h_src, size_t bytes)
+{
+    REQ(s && d_dst && h_src, "NULL argument");
+    // after what the handle's stream has queued (d_dst may be in use there)
+    CK(cudaEventRecord(s->side_ev, s->stream));
+    CK(cudaStreamWaitEvent(s->side, s->side_ev, 0));
+    CK(cudaMemcpyAsync(d_dst, h_src, bytes, cudaMemcpyHostToDevice, s->side));
+    CK(cudaEventRecord(s->side_ev, s->side));
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_join_side(ss4d_solver *s)
+{
+    REQ(s, "solver is NULL");
+    CK(cudaStreamWaitEvent(s->stream, s->side_ev, 0));
     return SS4D_OK;
 }
 

@@ -145,6 +145,8 @@ def lib() -> C.CDLL:
         "ss4d_host_free": ([vp], st),
         "ss4d_copy_to_device": ([vp, vp, vp, C.c_size_t], st),
         "ss4d_copy_to_host": ([vp, vp, vp, C.c_size_t], st),
+        "ss4d_copy_to_device_side": ([vp, vp, vp, C.c_size_t], st),
+        "ss4d_join_side": ([vp], st),
         "ss4d_copy_device": ([vp, vp, vp, C.c_size_t], st),
         "ss4d_synchronize": ([vp], st),
         "ss4d_scene_generate": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, vp, vp, C.c_int], st),
@@ -462,6 +464,17 @@ class Solver:
 
     def synchronize(self):
         _check(self.L.ss4d_synchronize(self.h), "synchronize")
+
+    def copy_to_device_side(self, dst, src: np.ndarray):
+        """Host -> device copy on the handle's side stream (after the work queued
+        so far); ``join_side`` orders it before the calls that follow.  ``src``
+        must stay alive until then."""
+        src = np.ascontiguousarray(src)
+        _check(self.L.ss4d_copy_to_device_side(self.h, _ptr(dst), src.ctypes.data, src.nbytes), "copy_to_device_side")
+        return src
+
+    def join_side(self):
+        _check(self.L.ss4d_join_side(self.h), "join_side")
 
 
 class Batch:

@@ -352,8 +352,9 @@ def run_e2e(args, form, ctx):
     L._deallocateMem_()
     nbytes = 8 * n_pad
     return {"value": args.steps / dt, "unit": "time-steps/s", "h2d_bytes_per_step": 2 * nbytes,
-            "d2h_bytes_per_step": 2 * nbytes, "path": "libss4d_seg.so _segTimeStep_() on host arrays (u, Mmask up; "
-                                                      "u, prev_u down)", "form": form}
+            "d2h_bytes_per_step": nbytes, "path": "libss4d_seg.so _segTimeStep_() on host arrays (u, Mmask up, "
+                                                  "Mmask beside the solve; u down; prev_u <- u on the host)",
+            "form": form}
 
 
 # --------------------------------------------------------------------------

@@ -385,6 +385,12 @@ ss4d_status ss4d_host_alloc(size_t bytes, void **out);   /* page-locked */
 ss4d_status ss4d_host_free(void *p);
 ss4d_status ss4d_copy_to_device(ss4d_solver *s, void *d_dst, const void *h_src, size_t bytes);
 ss4d_status ss4d_copy_to_host(ss4d_solver *s, void *h_dst, const void *d_src, size_t bytes);
+/* Host -> device copy on the handle's side stream, after the work already
+ * queued on the handle's stream, so that it overlaps the calls that follow;
+ * ss4d_join_side makes the handle's stream wait for the side copies issued
+ * so far.  h_src must be page-locked for the copy to run asynchronously. */
+ss4d_status ss4d_copy_to_device_side(ss4d_solver *s, void *d_dst, const void *h_src, size_t bytes);
+ss4d_status ss4d_join_side(ss4d_solver *s);
 ss4d_status ss4d_copy_device(ss4d_solver *s, void *d_dst, const void *d_src, size_t bytes);
 ss4d_status ss4d_synchronize(ss4d_solver *s);
 

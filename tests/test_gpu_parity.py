@@ -246,6 +246,30 @@ def test_nonfinite_input_is_reported(ss4d, cuda):
             assert ei.value.status == 4  # SS4D_ERR_NONFINITE
 
 
+def test_side_copy_lands_before_the_calls_after_the_join(ss4d, cuda):
+    """A mask uploaded on the side stream, joined before the rescale, gives the
+    rescale of a mask uploaded in order (the overlap the reference-named time
+    step uses)."""
+    torch = cuda
+    rng = np.random.default_rng(9)
+    shape = (3, 10, 9, 12)
+    img = rng.random(shape)
+    mask = (rng.random(shape) > 0.3).astype(np.float64)
+    p = ss4d.scene_params()
+    with ss4d.Solver(*shape[::-1]) as S:
+        want = dev(torch, img)
+        S.rescale_to_zero_one(p, want, dev(torch, mask), None)
+        got = dev(torch, img)
+        d_mask = torch.zeros(shape, dtype=torch.float64, device="cuda")
+        keep = S.copy_to_device_side(d_mask, mask)
+        S.join_side()
+        S.rescale_to_zero_one(p, got, d_mask, None)
+        S.synchronize()
+        del keep
+    assert np.array_equal(host(got), host(want))
+    assert np.array_equal(host(d_mask), mask)
+
+
 def test_norms_match_oracle(ss4d, oracle, cuda):
     torch = cuda
     rng = np.random.default_rng(5)

@@ -248,7 +248,7 @@ extern "C" ss4d_status ss4d_solver_create(const ss4d_dims *dims, ss4d_arith arit
     FAIL_IF(cudaEventCreate(&s->tev1));
     {
         long long nb = interior_blocks(s->geo);
-        long long need = nb * 2;
+        long long need = nb * 2 + 4096; // per-block partials (min/max pairs) and a second reduction stage
         if (need < 8192)
             need = 8192;
         // room for the partials of the largest persistent grid any tiling allows
@@ -498,7 +498,7 @@ static ss4d_status sor_reference(ss4d_solver *s, const ss4d_params *p, double *u
 {
     const Geo &g = s->geo;
     const double c = p->tau / (p->h * p->h), h4 = p->h * p->h * p->h * p->h;
-    const long long nb = interior_blocks(g);
+    const long long nb = resid_blocks(g);
     double R = 0.0, R1 = 0.0;
     int z = 0;
     do {
@@ -506,8 +506,7 @@ static ss4d_status sor_reference(ss4d_solver *s, const ss4d_params *p, double *u
         launch_sor_half_ref(g, u, prev, a, c, p->omega_c, 0, s->stream);
         launch_sor_half_ref(g, u, prev, a, c, p->omega_c, 1, s->stream);
         launch_sor_resid_ref(g, u, prev, a, c, h4, s->d_partial, s->stream);
-        launch_reduce_sum(s->d_partial, nb, s->d_scalar, s->stream);
-        s->launches += 4;
+        s->launches += 3 + launch_reduce_sum(s->d_partial, nb, s->d_scalar, s->stream);
         CKS(last_launch());
         CKS(read_scalar(s, 0, &R));
         if (z == 1)
@@ -945,7 +944,7 @@ extern "C" ss4d_status ss4d_presmooth_step(ss4d_solver *s, const ss4d_params *p,
     launch_reflect(g, d_img, s->stream);
     s->launches += 4;
     const double c = p->sigma / (p->h * p->h), h4 = p->h * p->h * p->h * p->h;
-    const long long nb = interior_blocks(g);
+    const long long nb = resid_blocks(g);
     double R = 0.0, R1 = 0.0;
     int z = 0;
     do {
@@ -953,8 +952,7 @@ extern "C" ss4d_status ss4d_presmooth_step(ss4d_solver *s, const ss4d_params *p,
         launch_presmooth_half(g, d_img, prev, c, p->omega_sigma, 0, s->stream);
         launch_presmooth_half(g, d_img, prev, c, p->omega_sigma, 1, s->stream);
         launch_presmooth_resid(g, d_img, prev, c, h4, s->d_partial, s->stream);
-        launch_reduce_sum(s->d_partial, nb, s->d_scalar, s->stream);
-        s->launches += 4;
+        s->launches += 3 + launch_reduce_sum(s->d_partial, nb, s->d_scalar, s->stream);
         CKS(last_launch());
         CKS(read_scalar(s, 0, &R));
         if (z == 1)
@@ -971,6 +969,32 @@ extern "C" ss4d_status ss4d_presmooth_step(ss4d_solver *s, const ss4d_params *p,
         stats->status = isfinite(R) ? SS4D_OK : SS4D_ERR_NONFINITE;
     }
     return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_presmooth_explicit(ss4d_solver *s, const ss4d_params *p, int timeStepsNum, double *d_img,
+                                               double *d_scratch)
+{
+    REQ(s && d_img, "NULL argument");
+    CKS(check_params(p));
+    REQ(timeStepsNum >= 0, "timeStepsNum must not be negative");
+    double *prev = d_scratch;
+    if (!prev) {
+        CKS(ensure_scratch(s));
+        prev = s->d_scratch;
+    }
+    const Geo &g = s->geo;
+    CK(cudaMemcpyAsync(prev, d_img, sizeof(double) * g.n, cudaMemcpyDeviceToDevice, s->stream));
+    launch_reflect(g, d_img, s->stream);
+    s->launches += 4;
+    // prev is not refreshed between the reference's steps, so every step after
+    // the first recomputes the same values: one step is the result of any
+    // number >= 1 (bit for bit)
+    if (timeStepsNum > 0) {
+        launch_presmooth_explicit(g, d_img, prev, p->sigma / (p->h * p->h), s->stream);
+        launch_reflect(g, d_img, s->stream);
+        s->launches += 5;
+    }
+    return last_launch();
 }
 
 extern "C" ss4d_status ss4d_edge_detector(ss4d_solver *s, const ss4d_params *p, double *d_i0, double *d_i0_thr,
@@ -1205,8 +1229,7 @@ extern "C" ss4d_status ss4d_frame_to_bytes(ss4d_solver *s, const double *d_img, 
 extern "C" ss4d_status ss4d_max4d(ss4d_solver *s, const double *d_img, double *out)
 {
     REQ(s && d_img && out, "NULL argument");
-    launch_minmax(s->geo, d_img, s->d_partial, 0.0, s->d_scalar, s->stream);
-    s->launches += 2;
+    s->launches += launch_minmax(s->geo, d_img, s->d_partial, 0.0, s->d_scalar, s->stream);
     CKS(last_launch());
     CK(cudaMemcpyAsync(s->h_scalar, s->d_scalar, sizeof(double) * 2, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
@@ -1243,10 +1266,10 @@ extern "C" ss4d_status ss4d_local_threshold(ss4d_solver *s, double alpha, double
     CKS(upload_balls(s, balls, ballRadius, &have));
     if (!have)
         return SS4D_OK;
-    launch_minmax(s->geo, d_in, s->d_partial, 0.0, s->d_scalar, s->stream);
+    s->launches += launch_minmax(s->geo, d_in, s->d_partial, 0.0, s->d_scalar, s->stream);
     launch_local_threshold(s->geo, d_in, d_thr, s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz,
                            ballRadius, alpha, beta, s->d_scalar, s->stream);
-    s->launches += 3;
+    s->launches += 1;
     return last_launch();
 }
 
@@ -1269,9 +1292,9 @@ extern "C" ss4d_status ss4d_threshold_mask(ss4d_solver *s, const double *d_u, do
 {
     REQ(s && d_u && d_mask, "NULL argument");
     if (normalise) {
-        launch_minmax(s->geo, d_u, s->d_partial, level, s->d_scalar, s->stream);
+        s->launches += launch_minmax(s->geo, d_u, s->d_partial, level, s->d_scalar, s->stream);
         launch_threshold(s->geo, d_u, s->d_scalar, level, d_mask, s->stream);
-        s->launches += 3;
+        s->launches += 1;
     } else {
         launch_threshold(s->geo, d_u, nullptr, level, d_mask, s->stream);
         s->launches += 1;
@@ -1284,8 +1307,7 @@ extern "C" ss4d_status ss4d_l2norm(ss4d_solver *s, double h, const double *d_a, 
     REQ(s && d_a && d_b && out, "NULL argument");
     const int nblk = 1024;
     launch_l2(s->geo, d_a, d_b, h * h * h * h, s->d_partial, nblk, s->stream);
-    launch_reduce_sum(s->d_partial, nblk, s->d_scalar, s->stream);
-    s->launches += 2;
+    s->launches += 1 + launch_reduce_sum(s->d_partial, nblk, s->d_scalar, s->stream);
     CKS(last_launch());
     double v = 0;
     CKS(read_scalar(s, 0, &v));
@@ -1298,8 +1320,7 @@ extern "C" ss4d_status ss4d_mass(ss4d_solver *s, double h, const double *d_a, do
     REQ(s && d_a && out, "NULL argument");
     const int nblk = 1024;
     launch_mass(s->geo, d_a, h * h * h * h, s->d_partial, nblk, s->stream);
-    launch_reduce_sum(s->d_partial, nblk, s->d_scalar, s->stream);
-    s->launches += 2;
+    s->launches += 1 + launch_reduce_sum(s->d_partial, nblk, s->d_scalar, s->stream);
     CKS(last_launch());
     return read_scalar(s, 0, out);
 }

@@ -541,6 +541,20 @@ bool _presmoothStep_(double *v)
     return st == SS4D_OK && down(v, d) && down(prev_u, g_dev[A_PREV]) && finish();
 }
 
+void _presmoothStepEXP_(double *v)
+{
+    if (!g_solver || !v)
+        return;
+    double *d = mirror_of(v, g_tmp);
+    if (!up(v, d))
+        return;
+    ss4d_params p = params_from_globals();
+    ss4d_status st = ss4d_presmooth_explicit(g_solver, &p, timeStepsNum, d, g_dev[A_PREV]);
+    report("explicit presmoothing", st);
+    if (st == SS4D_OK && down(v, d) && down(prev_u, g_dev[A_PREV]))
+        finish();
+}
+
 bool _gf_inputImage_plus_thresholdedImage_(double *img, double *thr)
 {
     if (!g_solver || !img || !thr)

@@ -15,9 +15,11 @@ struct CPtrs8 {
 
 // ---- natural-layout, reference-order kernels (ss4d_kernels_ref.cu) -------
 long long interior_blocks(const Geo &g);
+long long resid_blocks(const Geo &g); // partials of the residual passes
 void launch_reflect(const Geo &g, double *u, cudaStream_t st);
 void launch_presmooth_half(const Geo &g, double *v, const double *prev, double c, double omega, int colour,
                            cudaStream_t st);
+void launch_presmooth_explicit(const Geo &g, double *v, const double *prev, double coeff, cudaStream_t st);
 void launch_presmooth_resid(const Geo &g, const double *v, const double *prev, double c, double h4, double *partial,
                             cudaStream_t st);
 void launch_gfaces(const Geo &g, const double *i0, const double *ithr, GPtrs8 gout, double h, double K, double theta,
@@ -28,7 +30,8 @@ void launch_sor_half_ref(const Geo &g, double *u, const double *prev, CPtrs8 a, 
                          cudaStream_t st);
 void launch_sor_resid_ref(const Geo &g, const double *u, const double *prev, CPtrs8 a, double c, double h4,
                           double *partial, cudaStream_t st);
-void launch_reduce_sum(const double *partial, long long n, double *out, cudaStream_t st);
+// sums n partials into *out; may use partial[n .. n + 1024) (returns the launches)
+int launch_reduce_sum(double *partial, long long n, double *out, cudaStream_t st);
 void launch_l2(const Geo &g, const double *a, const double *b, double h4, double *partial, int nblk, cudaStream_t st);
 void launch_mass(const Geo &g, const double *a, double h4, double *partial, int nblk, cudaStream_t st);
 void launch_mcf_field(const Geo &g, double *u, double h, double t, int ghosts_only, cudaStream_t st);
@@ -47,7 +50,9 @@ void launch_local_threshold(const Geo &g, const double *in, double *thr, const i
                             const double *minmax, cudaStream_t st);
 void launch_generate_segm(const Geo &g, double *u, double *Mmask, const int *frame_first, const int *frame_count,
                           const double *bx, const double *by, const double *bz, double R, cudaStream_t st);
-void launch_minmax(const Geo &g, const double *u, double *partial, double level, double *out3, cudaStream_t st);
+// interior min, max and min + level (max - min) of u into out3; partial needs
+// 4096 doubles (returns the launches)
+int launch_minmax(const Geo &g, const double *u, double *partial, double level, double *out3, cudaStream_t st);
 void launch_threshold(const Geo &g, const double *u, const double *level_dev, double level, uint8_t *mask,
                       cudaStream_t st);
 

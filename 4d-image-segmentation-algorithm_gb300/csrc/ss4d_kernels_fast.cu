@@ -471,7 +471,6 @@ __global__ void __launch_bounds__(256) k_sweep32(Geo g, Split sp, SweepCfg cfg, 
     const float *__restrict__ cf = b.coef32[COL];
     const float *__restrict__ rhs = b.r32[COL];
     const float omega = (float)dp->omega;
-    const long long cs = sp.cs;
     const long long Hy = sp.Hs, Hz = Hy * g.jM, Hw = Hz * g.kM;
     const int tx = threadIdx.x & (cfg.XT - 1), ty = threadIdx.x / cfg.XT;
     float acc = 0.f;

@@ -27,6 +27,21 @@ __device__ inline bool interior_ijkl(const Geo &g, int &i, int &j, int &k, int &
     return i <= g.nx && j <= g.ny;
 }
 
+// the voxels of one colour ((i + j + k + l) & 1 == colour), one per thread:
+// thread x indexes the pairs (i, i+1) of a row, so every lane of a warp
+// updates a voxel (a lane masked off by a colour test costs the FP64 pipe as
+// much as an active one)
+__device__ inline bool colour_ijkl(const Geo &g, int colour, int &i, int &j, int &k, int &l)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int kl = blockIdx.z;
+    k = 1 + kl % g.nz;
+    l = 1 + kl / g.nz;
+    i = 1 + 2 * t + ((colour + j + k + l + 1) & 1);
+    return i <= g.nx && j <= g.ny;
+}
+
 __device__ inline unsigned block_linear()
 {
     return (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
@@ -85,35 +100,104 @@ __global__ void k_reflect_axis(Geo g, double *u, int axis)
 }
 
 // ---------------------------------------------------------------------------
-// presmoothing (segmentation4D.c:352-404)
+// x / d, rounded to nearest, for a divisor d > 0 known in advance with
+// y = 1/d rounded to nearest (y == 0: no fast path).  A quotient from the
+// reciprocal and one remainder correction (Markstein's iteration), then an
+// exact acceptance test: the remainder x - q d (one FMA, correctly rounded) must
+// be below d times half the spacing from q to its nearer neighbour; since
+// that bound is a power-of-two multiple of d, hence exact, and rounding is
+// monotonic, passing it proves q is the double nearest to x / d.  Otherwise
+// (near a tie, zero, q outside [2^-400, 2^601)) the IEEE division decides.
+__device__ inline double div_by_const(double x, double d, double y)
+{
+    if (y != 0.0) {
+        const double q0 = x * y;
+        const double q = fma(fma(-q0, d, x), y, q0);
+        const long long b = __double_as_longlong(q);
+        const int E = (int)((b >> 52) & 0x7ff) - 1023;
+        if (E >= -400 && E <= 600) {
+            const int e = E - 53 - ((b & 0xfffffffffffffLL) == 0 ? 1 : 0); // half spacing 2^e
+            // d 2^e (a normal number: d in [2^-300, 2^300]) by adding e to d's
+            // exponent, and |r| < d 2^e compared as the bit patterns of two
+            // non-negative doubles: integer work only
+            const long long lim = __double_as_longlong(d) + ((long long)e << 52);
+            if ((__double_as_longlong(fma(-q, d, x)) & 0x7fffffffffffffffLL) < lim)
+                return q;
+        }
+    }
+    return x / d;
+}
 
-__global__ void k_presmooth_half(Geo g, double *v, const double *prev, double c, double omega, int colour)
+// reciprocal for div_by_const, or 0 where the divisor is outside the range
+// its test needs (d in [2^-300, 2^300])
+static inline double div_const_recip(double d)
+{
+    return (d >= 0x1p-300 && d <= 0x1p300) ? 1.0 / d : 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// presmoothing (segmentation4D.c:352-404); d = 1 + 8c (the same rounding on
+// the host), y its reciprocal for div_by_const
+
+__global__ void k_presmooth_half(Geo g, double *v, const double *prev, double c, double d, double y, double omega,
+                                 int colour)
 {
     int i, j, k, l;
-    if (!interior_ijkl(g, i, j, k, l) || ((i + j + k + l) & 1) != colour)
+    if (!colour_ijkl(g, colour, i, j, k, l))
         return;
     const long long o = nat_index(g, i, j, k, l);
-    double gs = (prev[o] + c * (v[o + 1] + v[o - 1] + v[o - g.sy] + v[o + g.sy] + v[o - g.sz] + v[o + g.sz]
-                                + v[o - g.sw] + v[o + g.sw]))
-                / (1 + c * 8);
+    double gs = div_by_const(prev[o] + c * (v[o + 1] + v[o - 1] + v[o - g.sy] + v[o + g.sy] + v[o - g.sz]
+                                            + v[o + g.sz] + v[o - g.sw] + v[o + g.sw]),
+                             d, y);
     v[o] = v[o] + omega * (gs - v[o]);
 }
 
-__global__ void k_presmooth_resid(Geo g, const double *v, const double *prev, double c, double h4, double *partial)
+// residual passes: a thread sums RESID_K k-planes before the block reduction
+#define RESID_K 4
+
+__device__ inline bool resid_ijl(const Geo &g, int &i, int &j, int &k0, int &l)
 {
-    int i, j, k, l;
+    i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int nkb = (g.nz + RESID_K - 1) / RESID_K;
+    k0 = 1 + (blockIdx.z % nkb) * RESID_K;
+    l = 1 + blockIdx.z / nkb;
+    return i <= g.nx && j <= g.ny;
+}
+
+__global__ void k_presmooth_resid(Geo g, const double *v, const double *prev, double c, double d, double h4,
+                                  double *partial)
+{
+    int i, j, k0, l;
     double acc = 0.0;
-    if (interior_ijkl(g, i, j, k, l)) {
-        const long long o = nat_index(g, i, j, k, l);
-        double r = v[o] * (1 + c * 8)
-                   - c * (v[o + 1] + v[o - 1] + v[o - g.sy] + v[o + g.sy] + v[o - g.sz] + v[o + g.sz] + v[o - g.sw]
-                          + v[o + g.sw])
-                   - prev[o];
-        acc = (r * r) * h4;
+    if (resid_ijl(g, i, j, k0, l)) {
+        for (int k = k0; k < k0 + RESID_K && k <= g.nz; ++k) {
+            const long long o = nat_index(g, i, j, k, l);
+            double r = v[o] * d
+                       - c * (v[o + 1] + v[o - 1] + v[o - g.sy] + v[o + g.sy] + v[o - g.sz] + v[o + g.sz]
+                              + v[o - g.sw] + v[o + g.sw])
+                       - prev[o];
+            acc += (r * r) * h4;
+        }
     }
     acc = block_sum2d(acc);
     if (flat_tid() == 0)
         partial[block_linear()] = acc;
+}
+
+// explicit smoother (segmentation4D.c:422-441): one Jacobi-style step from
+// prev over i = 1 .. iMax-3 (the reference's x loop stops one column short)
+// and the interior j, k, l; the neighbours are summed in the reference's order
+
+__global__ void k_presmooth_explicit(Geo g, double *v, const double *prev, double coeff)
+{
+    int i, j, k, l;
+    if (!interior_ijkl(g, i, j, k, l) || i > g.nx - 1)
+        return;
+    const long long o = nat_index(g, i, j, k, l);
+    v[o] = (1.0 - 8.0 * coeff) * prev[o]
+           + coeff * (prev[o + 1] + prev[o - 1] + prev[o + g.sy] + prev[o - g.sy] + prev[o + g.sz] + prev[o - g.sz]
+                      + prev[o + g.sw] + prev[o - g.sw]);
 }
 
 // ---------------------------------------------------------------------------
@@ -135,23 +219,74 @@ __device__ inline double face_sq(const double *v, long long c, long long nb, con
     return (comp[0] * comp[0]) + (comp[1] * comp[1]) + (comp[2] * comp[2]) + (comp[3] * comp[3]);
 }
 
-__global__ void k_gfaces(Geo g, const double *i0, const double *ithr, GPtrs8 gout, double h, double K, double theta,
-                         double rho)
+// face_sq of the face between o and o + st[d], in the reference's expression
+// order.  POW2: h is a power of two, so x / h == x * (1/h) and x / (4h) ==
+// x * (1/(4h)) exactly (one rounding of the same real number); otherwise the
+// divisions by h and 4h go through div_by_const (ih, iq: its reciprocals).
+template <bool POW2, int D>
+__device__ inline double face_sq_plus(const double *v, long long o, const long long st[4], double h, double q,
+                                      double ih, double iq)
 {
-    int i, j, k, l;
-    if (!interior_ijkl(g, i, j, k, l))
+    const long long nb = o + st[D];
+    double comp[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        if (a == D) {
+            const double t = v[nb] - v[o];
+            comp[a] = POW2 ? t * ih : div_by_const(t, h, ih);
+        } else {
+            const double t = (v[nb + st[a]] + v[o + st[a]]) - (v[nb - st[a]] + v[o - st[a]]);
+            comp[a] = POW2 ? t * iq : div_by_const(t, q, iq);
+        }
+    }
+    return (comp[0] * comp[0]) + (comp[1] * comp[1]) + (comp[2] * comp[2]) + (comp[3] * comp[3]);
+}
+
+// The 8 g faces of every interior voxel, each shared face computed once.  The
+// reference's value for the + face of voxel o along axis d and for the - face
+// of voxel o + st[d] is the same number: the normal difference only changes
+// sign (exactly) before it is squared, and the tangential sums add the same
+// pairs (IEEE addition is commutative).  The thread at o computes the + face
+// along d when o's other coordinates are interior, and stores it as g[2d][o]
+// (o interior along d) and g[2d+1][o + st[d]] (o + st[d] interior along d).
+// Threads cover coordinates 0..n along every axis.
+template <bool POW2, int D>
+__device__ inline void gface_plus(const Geo &g, const int c[4], const int n[4], long long o, const long long st[4],
+                                  const double *i0, const double *ithr, GPtrs8 &gout, double h, double q, double ih,
+                                  double iq, double K, double theta, double rho)
+{
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+        if (a != D && c[a] < 1)
+            return;
+    const double s0 = face_sq_plus<POW2, D>(i0, o, st, h, q, ih, iq);
+    const double s1 = ithr ? face_sq_plus<POW2, D>(ithr, o, st, h, q, ih, iq) : 0.0;
+    const double gv = 1.0 / (1 + K * (theta * s0 + rho * s1));
+    if (c[D] >= 1)
+        gout.p[2 * D][o] = gv;
+    if (c[D] < n[D])
+        gout.p[2 * D + 1][o + st[D]] = gv;
+}
+
+template <bool POW2>
+__global__ void k_gfaces(Geo g, const double *i0, const double *ithr, GPtrs8 gout, double h, double K, double theta,
+                         double rho, double ih, double iq)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int kl = blockIdx.z;
+    const int k = kl % (g.nz + 1), l = kl / (g.nz + 1);
+    if (i > g.nx || j > g.ny)
         return;
+    const int c[4] = {i, j, k, l};
+    const int n[4] = {g.nx, g.ny, g.nz, g.nt};
     const long long o = nat_index(g, i, j, k, l);
     const long long st[4] = {1, g.sy, g.sz, g.sw};
     const double q = 4.0 * h;
-#pragma unroll
-    for (int f = 0; f < 8; ++f) {
-        const int d = f >> 1;
-        const long long nb = (f & 1) ? o - st[d] : o + st[d];
-        double s0 = face_sq(i0, o, nb, st, d, h, q);
-        double s1 = ithr ? face_sq(ithr, o, nb, st, d, h, q) : 0.0;
-        gout.p[f][o] = 1.0 / (1 + K * (theta * s0 + rho * s1));
-    }
+    gface_plus<POW2, 0>(g, c, n, o, st, i0, ithr, gout, h, q, ih, iq, K, theta, rho);
+    gface_plus<POW2, 1>(g, c, n, o, st, i0, ithr, gout, h, q, ih, iq, K, theta, rho);
+    gface_plus<POW2, 2>(g, c, n, o, st, i0, ithr, gout, h, q, ih, iq, K, theta, rho);
+    gface_plus<POW2, 3>(g, c, n, o, st, i0, ithr, gout, h, q, ih, iq, K, theta, rho);
 }
 
 // _gs_coefficients_ / _gs_coefficients_mcf in reference order
@@ -183,7 +318,7 @@ __global__ void k_coef_ref(Geo g, const double *u, CPtrs8 gin, int has_g, GPtrs8
 __global__ void k_sor_half_ref(Geo g, double *u, const double *prev, CPtrs8 a, double c, double omega, int colour)
 {
     int i, j, k, l;
-    if (!interior_ijkl(g, i, j, k, l) || ((i + j + k + l) & 1) != colour)
+    if (!colour_ijkl(g, colour, i, j, k, l))
         return;
     const long long o = nat_index(g, i, j, k, l);
     const double E = a.p[0][o], W = a.p[1][o], N = a.p[2][o], S = a.p[3][o];
@@ -197,17 +332,19 @@ __global__ void k_sor_half_ref(Geo g, double *u, const double *prev, CPtrs8 a, d
 __global__ void k_sor_resid_ref(Geo g, const double *u, const double *prev, CPtrs8 a, double c, double h4,
                                 double *partial)
 {
-    int i, j, k, l;
+    int i, j, k0, l;
     double acc = 0.0;
-    if (interior_ijkl(g, i, j, k, l)) {
-        const long long o = nat_index(g, i, j, k, l);
-        const double E = a.p[0][o], W = a.p[1][o], N = a.p[2][o], S = a.p[3][o];
-        const double T = a.p[4][o], B = a.p[5][o], FW = a.p[6][o], BW = a.p[7][o];
-        double r = u[o] * (1 + c * (E + W + N + S + T + B + FW + BW))
-                   - c * ((E * u[o + 1]) + (W * u[o - 1]) + (S * u[o - g.sy]) + (N * u[o + g.sy]) + (B * u[o - g.sz])
-                          + (T * u[o + g.sz]) + (BW * u[o - g.sw]) + (FW * u[o + g.sw]))
-                   - prev[o];
-        acc = (r * r) * h4;
+    if (resid_ijl(g, i, j, k0, l)) {
+        for (int k = k0; k < k0 + RESID_K && k <= g.nz; ++k) {
+            const long long o = nat_index(g, i, j, k, l);
+            const double E = a.p[0][o], W = a.p[1][o], N = a.p[2][o], S = a.p[3][o];
+            const double T = a.p[4][o], B = a.p[5][o], FW = a.p[6][o], BW = a.p[7][o];
+            double r = u[o] * (1 + c * (E + W + N + S + T + B + FW + BW))
+                       - c * ((E * u[o + 1]) + (W * u[o - 1]) + (S * u[o - g.sy]) + (N * u[o + g.sy])
+                              + (B * u[o - g.sz]) + (T * u[o + g.sz]) + (BW * u[o - g.sw]) + (FW * u[o + g.sw]))
+                       - prev[o];
+            acc += (r * r) * h4;
+        }
     }
     acc = block_sum2d(acc);
     if (flat_tid() == 0)
@@ -216,6 +353,18 @@ __global__ void k_sor_resid_ref(Geo g, const double *u, const double *prev, CPtr
 
 // ---------------------------------------------------------------------------
 // deterministic final reductions: one block, fixed order
+
+// first stage of a long reduction: block b combines in[b*per, (b+1)*per)
+__global__ void k_reduce_sum_part(const double *in, long long n, long long per, double *out)
+{
+    const long long beg = blockIdx.x * per, end = beg + per < n ? beg + per : n;
+    double acc = 0.0;
+    for (long long t = beg + threadIdx.x; t < end; t += blockDim.x)
+        acc += in[t];
+    acc = block_sum(acc);
+    if (threadIdx.x == 0)
+        out[blockIdx.x] = acc;
+}
 
 __global__ void k_reduce_sum(const double *partial, long long n, double *out)
 {
@@ -486,13 +635,23 @@ __global__ void k_generate_segm(Geo g, double *u, double *Mmask, const int *fram
 // _load3dDataArrayVTK_ (segmentation4D.c:1317-1320), _writeData_ (:1250-1254),
 // _writeData_mpi_ (segmentation4D_mpi.c:1466-1473)
 
+// byte / 255. from a table of the 256 quotients (the same IEEE divisions),
+// built once per block; a block walks FRAME_Z_PER_BLOCK planes
+#define FRAME_Z_PER_BLOCK 32
 __global__ void k_frame_from_bytes(Geo g, double *img, int l, const uint8_t *__restrict__ bytes)
 {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y, z = blockIdx.z;
+    __shared__ double lut[256];
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    if (t < 256)
+        lut[t] = t / 255.;
+    __syncthreads();
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= g.nx || y >= g.ny)
         return;
-    const long long q = ((long long)z * g.ny + y) * g.nx + x;
-    img[nat_index(g, x + 1, y + 1, z + 1, l)] = bytes[q] / 255.;
+    for (int z = blockIdx.z; z < g.nz; z += gridDim.z) {
+        const long long q = ((long long)z * g.ny + y) * g.nx + x;
+        img[nat_index(g, x + 1, y + 1, z + 1, l)] = lut[bytes[q]];
+    }
 }
 
 // mode 0: (unsigned char)(255 v + 0.5), clamped to [0, 255] (the reference's
@@ -527,22 +686,40 @@ __global__ void k_mask_zero(Geo g, double *v, const double *Mmask)
 // ---------------------------------------------------------------------------
 // threshold to mask (segmentation4D_mpi.c:1470-1478)
 
+// ordered 64-bit keys of doubles: a signed comparison of two keys compares the
+// numbers (-0 below +0); the map is its own inverse.  NaN is skipped.
+__device__ inline long long dkey(long long b)
+{
+    return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+
+#define MINMAX_BLOCKS 2048
+// interior min and max of u per block, as (min, max) pairs in partial; a
+// block walks whole rows (threads along x), comparing integer keys so the
+// FP64 pipe is not used; a block without a number reports (1e308, -1e308)
 __global__ void k_minmax_partial(Geo g, const double *u, double *partial)
 {
-    int i, j, k, l;
-    double mn = 1e308, mx = -1e308;
-    if (interior_ijkl(g, i, j, k, l)) {
-        const double v = u[nat_index(g, i, j, k, l)];
-        mn = v;
-        mx = v;
+    long long mn = 0x7fffffffffffffffLL, mx = -0x7fffffffffffffffLL - 1;
+    const int rows = g.ny * g.nz * g.nt;
+    for (int r = blockIdx.x * blockDim.y + threadIdx.y; r < rows; r += gridDim.x * blockDim.y) {
+        const int j = r % g.ny, kl = r / g.ny;
+        const long long base = nat_index(g, 0, j + 1, 1 + kl % g.nz, 1 + kl / g.nz);
+        for (int i = 1 + threadIdx.x; i <= g.nx; i += blockDim.x) {
+            const long long b = __double_as_longlong(u[base + i]);
+            if ((b & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL) {
+                const long long key = dkey(b);
+                mn = key < mn ? key : mn;
+                mx = key > mx ? key : mx;
+            }
+        }
     }
-    // flat 2D block: reuse the 1D helpers over the flattened index
-    __shared__ double smn[32], smx[32];
+    __shared__ long long smn[32], smx[32];
     const int t = flat_tid(), lane = t & 31, wid = t >> 5, nw = (blockDim.x * blockDim.y + 31) >> 5;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        mn = fmin(mn, __shfl_down_sync(0xffffffffu, mn, o));
-        mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+        const long long a = __shfl_down_sync(0xffffffffu, mn, o), b = __shfl_down_sync(0xffffffffu, mx, o);
+        mn = a < mn ? a : mn;
+        mx = b > mx ? b : mx;
     }
     if (lane == 0) {
         smn[wid] = mn;
@@ -550,16 +727,18 @@ __global__ void k_minmax_partial(Geo g, const double *u, double *partial)
     }
     __syncthreads();
     if (wid == 0) {
-        mn = lane < nw ? smn[lane] : 1e308;
-        mx = lane < nw ? smx[lane] : -1e308;
+        mn = lane < nw ? smn[lane] : 0x7fffffffffffffffLL;
+        mx = lane < nw ? smx[lane] : -0x7fffffffffffffffLL - 1;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            mn = fmin(mn, __shfl_down_sync(0xffffffffu, mn, o));
-            mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+            const long long a = __shfl_down_sync(0xffffffffu, mn, o), b = __shfl_down_sync(0xffffffffu, mx, o);
+            mn = a < mn ? a : mn;
+            mx = b > mx ? b : mx;
         }
         if (lane == 0) {
-            partial[2 * block_linear()] = mn;
-            partial[2 * block_linear() + 1] = mx;
+            const bool none = mn == 0x7fffffffffffffffLL;
+            partial[2 * blockIdx.x] = none ? 1e308 : __longlong_as_double(dkey(mn));
+            partial[2 * blockIdx.x + 1] = none ? -1e308 : __longlong_as_double(dkey(mx));
         }
     }
 }
@@ -598,28 +777,68 @@ void launch_reflect(const Geo &g, double *u, cudaStream_t st)
         k_reflect_axis<<<256, 256, 0, st>>>(g, u, a);
 }
 
+// one colour: ceil(nx/2) threads along a row
+static inline void colour_cfg(const Geo &g, dim3 &grid, dim3 &block)
+{
+    const int nxh = (g.nx + 1) / 2;
+    const int bx = nxh >= 128 ? 128 : (nxh >= 64 ? 64 : 32);
+    const int by = 256 / bx;
+    block = dim3(bx, by, 1);
+    grid = dim3((nxh + bx - 1) / bx, (g.ny + by - 1) / by, g.nz * g.nt);
+}
+
 void launch_presmooth_half(const Geo &g, double *v, const double *prev, double c, double omega, int colour,
                            cudaStream_t st)
 {
     dim3 gr, bl;
-    interior_cfg(g, gr, bl);
-    k_presmooth_half<<<gr, bl, 0, st>>>(g, v, prev, c, omega, colour);
+    colour_cfg(g, gr, bl);
+    const double d = 1 + c * 8;
+    k_presmooth_half<<<gr, bl, 0, st>>>(g, v, prev, c, d, div_const_recip(d), omega, colour);
+}
+
+static inline void resid_cfg(const Geo &g, dim3 &grid, dim3 &block)
+{
+    interior_cfg(g, grid, block);
+    grid.z = ((g.nz + RESID_K - 1) / RESID_K) * g.nt;
+}
+
+long long resid_blocks(const Geo &g)
+{
+    dim3 gr, bl;
+    resid_cfg(g, gr, bl);
+    return (long long)gr.x * gr.y * gr.z;
 }
 
 void launch_presmooth_resid(const Geo &g, const double *v, const double *prev, double c, double h4, double *partial,
                             cudaStream_t st)
 {
     dim3 gr, bl;
+    resid_cfg(g, gr, bl);
+    k_presmooth_resid<<<gr, bl, 0, st>>>(g, v, prev, c, 1 + c * 8, h4, partial);
+}
+
+void launch_presmooth_explicit(const Geo &g, double *v, const double *prev, double coeff, cudaStream_t st)
+{
+    dim3 gr, bl;
     interior_cfg(g, gr, bl);
-    k_presmooth_resid<<<gr, bl, 0, st>>>(g, v, prev, c, h4, partial);
+    k_presmooth_explicit<<<gr, bl, 0, st>>>(g, v, prev, coeff);
 }
 
 void launch_gfaces(const Geo &g, const double *i0, const double *ithr, GPtrs8 gout, double h, double K, double theta,
                    double rho, cudaStream_t st)
 {
-    dim3 gr, bl;
-    interior_cfg(g, gr, bl);
-    k_gfaces<<<gr, bl, 0, st>>>(g, i0, ithr, gout, h, K, theta, rho);
+    const int bx = g.nx + 1 >= 128 ? 128 : (g.nx + 1 >= 64 ? 64 : 32);
+    const int by = 256 / bx;
+    dim3 bl(bx, by, 1), gr((g.nx + 1 + bx - 1) / bx, (g.ny + 1 + by - 1) / by, (g.nz + 1) * (g.nt + 1));
+    int e = 0;
+    const double m = frexp(h, &e);
+    const double ih = 1.0 / h, iq = 1.0 / (4.0 * h);
+    // a power of two whose reciprocals are normal numbers
+    if (m == 0.5 && ih * h == 1.0 && iq * (4.0 * h) == 1.0 && isnormal(ih) && isnormal(iq) && isnormal(4.0 * h))
+        k_gfaces<true><<<gr, bl, 0, st>>>(g, i0, ithr, gout, h, K, theta, rho, ih, iq);
+    else
+        k_gfaces<false><<<gr, bl, 0, st>>>(g, i0, ithr, gout, h, K, theta, rho, div_const_recip(h),
+                                           div_const_recip(4.0 * h));
 }
 
 void launch_coef_ref(const Geo &g, const double *u, CPtrs8 gin, int has_g, GPtrs8 coef, double h, double eps2,
@@ -634,7 +853,7 @@ void launch_sor_half_ref(const Geo &g, double *u, const double *prev, CPtrs8 a, 
                          cudaStream_t st)
 {
     dim3 gr, bl;
-    interior_cfg(g, gr, bl);
+    colour_cfg(g, gr, bl);
     k_sor_half_ref<<<gr, bl, 0, st>>>(g, u, prev, a, c, omega, colour);
 }
 
@@ -642,13 +861,35 @@ void launch_sor_resid_ref(const Geo &g, const double *u, const double *prev, CPt
                           double *partial, cudaStream_t st)
 {
     dim3 gr, bl;
-    interior_cfg(g, gr, bl);
+    resid_cfg(g, gr, bl);
     k_sor_resid_ref<<<gr, bl, 0, st>>>(g, u, prev, a, c, h4, partial);
 }
 
-void launch_reduce_sum(const double *partial, long long n, double *out, cudaStream_t st)
+// n partials: one block when n is small; else up to 1024 blocks first, their
+// results written behind the partials (partial[n ..]), then one block.
+// Returns the number of launches.
+static long long reduce_split(long long n, long long &per)
 {
-    k_reduce_sum<<<1, 1024, 0, st>>>(partial, n, out);
+    per = 4096;
+    long long nb = (n + per - 1) / per;
+    if (nb > 1024) {
+        per = (n + 1023) / 1024;
+        nb = (n + per - 1) / per;
+    }
+    return nb;
+}
+
+int launch_reduce_sum(double *partial, long long n, double *out, cudaStream_t st)
+{
+    if (n <= 16384) {
+        k_reduce_sum<<<1, 1024, 0, st>>>(partial, n, out);
+        return 1;
+    }
+    long long per;
+    const long long nb = reduce_split(n, per);
+    k_reduce_sum_part<<<(unsigned)nb, 256, 0, st>>>(partial, n, per, partial + n);
+    k_reduce_sum<<<1, 1024, 0, st>>>(partial + n, nb, out);
+    return 2;
 }
 
 void launch_l2(const Geo &g, const double *a, const double *b, double h4, double *partial, int nblk, cudaStream_t st)
@@ -703,18 +944,21 @@ void launch_frame_bytes(const Geo &g, double *img_out, const double *img_in, int
 {
     const int bx = g.nx >= 128 ? 128 : (g.nx >= 64 ? 64 : 32);
     dim3 bl(bx, 256 / bx, 1), gr((g.nx + bx - 1) / bx, (g.ny + 256 / bx - 1) / (256 / bx), g.nz);
-    if (img_out)
+    if (img_out) {
+        gr.z = (g.nz + FRAME_Z_PER_BLOCK - 1) / FRAME_Z_PER_BLOCK;
         k_frame_from_bytes<<<gr, bl, 0, st>>>(g, img_out, l, bytes_in);
-    else
+    } else {
         k_frame_to_bytes<<<gr, bl, 0, st>>>(g, img_in, l, mode, bytes_out);
+    }
 }
 
-void launch_minmax(const Geo &g, const double *u, double *partial, double level, double *out3, cudaStream_t st)
+int launch_minmax(const Geo &g, const double *u, double *partial, double level, double *out3, cudaStream_t st)
 {
-    dim3 gr, bl;
-    interior_cfg(g, gr, bl);
-    k_minmax_partial<<<gr, bl, 0, st>>>(g, u, partial);
-    k_reduce_minmax<<<1, 1024, 0, st>>>(partial, (long long)gr.x * gr.y * gr.z, level, out3);
+    const long long rows = (long long)g.ny * g.nz * g.nt;
+    const int nb = (int)(rows / 2 < MINMAX_BLOCKS ? (rows + 1) / 2 : MINMAX_BLOCKS);
+    k_minmax_partial<<<nb, dim3(128, 2, 1), 0, st>>>(g, u, partial);
+    k_reduce_minmax<<<1, 1024, 0, st>>>(partial, nb, level, out3);
+    return 2;
 }
 
 void launch_threshold(const Geo &g, const double *u, const double *level_dev, double level, uint8_t *mask,

@@ -412,11 +412,6 @@ const Layer kLayers[4] = {
     {24, 1, 32, 8, 16, 0, 0},
 };
 
-size_t layer_params(int L)
-{
-    return (size_t)27 * kLayers[L].cout * kLayers[L].cin + kLayers[L].cout;
-}
-
 ss4d_status nfail(ss4d_status st, const char *fmt, ...)
 {
     char buf[400];

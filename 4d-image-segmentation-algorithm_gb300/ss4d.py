@@ -146,6 +146,7 @@ def lib() -> C.CDLL:
         "ss4d_copy_to_device": ([vp, vp, vp, C.c_size_t], st),
         "ss4d_copy_to_host": ([vp, vp, vp, C.c_size_t], st),
         "ss4d_copy_to_device_side": ([vp, vp, vp, C.c_size_t], st),
+        "ss4d_presmooth_explicit": ([vp, C.POINTER(Params), C.c_int, vp, vp], st),
         "ss4d_join_side": ([vp], st),
         "ss4d_copy_device": ([vp, vp, vp, C.c_size_t], st),
         "ss4d_synchronize": ([vp], st),
@@ -366,6 +367,11 @@ class Solver:
         _check(self.L.ss4d_presmooth_step(self.h, C.byref(p), _ptr(img), _ptr(scratch), C.byref(st)), "presmooth")
         return st.as_dict()
 
+    def presmooth_explicit(self, p: Params, steps: int, img, scratch=None):
+        """_presmoothStepEXP_ on img; scratch (optional) receives the reference's prev_u"""
+        _check(self.L.ss4d_presmooth_explicit(self.h, C.byref(p), int(steps), _ptr(img), _ptr(scratch)),
+               "presmooth_explicit")
+
     def edge_detector(self, p: Params, i0, i0_thr, g8, scratch=None):
         _check(self.L.ss4d_edge_detector(self.h, C.byref(p), _ptr(i0), _ptr(i0_thr), _ptr(scratch), _p8(g8)),
                "edge_detector")
@@ -465,10 +471,11 @@ class Solver:
     def synchronize(self):
         _check(self.L.ss4d_synchronize(self.h), "synchronize")
 
-    def copy_to_device_side(self, dst, src: np.ndarray):
+    def copy_to_device_side(self, dst, src):
         """Host -> device copy on the handle's side stream (after the work queued
         so far); ``join_side`` orders it before the calls that follow.  ``src``
         must stay alive until then."""
+        import numpy as np
         src = np.ascontiguousarray(src)
         _check(self.L.ss4d_copy_to_device_side(self.h, _ptr(dst), src.ctypes.data, src.nbytes), "copy_to_device_side")
         return src

@@ -66,6 +66,8 @@ def parse_args():
                          "this instead of the configured omega 1.8; reported, never the headline)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-frontend", action="store_true",
+                    help="skip the timing of the work around the time loop (thresholding, edge detector, ...)")
     ap.add_argument("--no-graph", action="store_true",
                     help="run the sweep loop host-driven instead of as one CUDA graph (same kernels)")
     ap.add_argument("--workload", choices=["single", "batch"], default="single",
@@ -306,6 +308,131 @@ def run_ours(args, rank, world, dist):
     return results, roofline, err, (shape, n_pad, n_int, p, i0h, u0h)
 
 
+def frontend_balls(nx, ny, nz, nt, seed, per_frame=5, radius=8.0):
+    """Seeded ball centres for the front-end measurement: `per_frame` per
+    frame, integral coordinates, every ball box inside the array (the reference
+    main's radius 8 and 4 to 7 centres per frame, segmentation4D.c:1337-1348)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    lo = int(radius) + 2
+    return [(l, float(rng.integers(lo, nx - lo + 1)), float(rng.integers(lo, ny - lo + 1)),
+             float(rng.integers(lo, nz - lo + 1))) for l in range(1, nt + 1) for _ in range(per_frame)]
+
+
+def run_frontend(args, ctx):
+    """The reference main's work around the time loop (segmentation4D.c:
+    1380-1393: local thresholding, edge detector on both images, initial
+    function, rescale; frame conversion for reading and writing; the explicit
+    smoother) on the benchmarked volume with the reference main's front-end
+    parameters (radius-8 balls, alpha 0.85, beta 0.15, theta_img = rho_thr =
+    0.5).  Each component: one untimed call, then the median of 3 calls timed
+    with CUDA events on the launching stream (inputs restored between calls,
+    outside the timed region); algorithmic bytes per call and the fraction of
+    the measured copy bandwidth.  The C oracle times the same sequence on a
+    two-frame sample of the volume on all host cores."""
+    import numpy as np
+    import torch
+
+    import oracle
+    import ss4d
+
+    shape, n_pad, n_int, p0, i0h, u0h = ctx
+    nx, ny, nz, nt = args.size
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    stream = torch.cuda.current_stream(dev)
+    hbm, how = peaks()
+    R = 8.0
+    p = ss4d.scene_params(ballRadius=R, theta_img=0.5, rho_thr=0.5)
+    balls = frontend_balls(nx, ny, nz, nt, args.seed)
+    box = (2 * int(R) + 2) ** 3  # voxels of one ball's box (R = 8: 18^3)
+    fb = torch.from_numpy(np.rint(i0h[1:-1, 1:-1, 1:-1, 1:-1] * 255.0).astype(np.uint8)).to(dev)
+    i0 = torch.from_numpy(i0h).to(dev)
+    u0 = torch.from_numpy(u0h).to(dev)
+    img, thr, u, mm = (torch.empty_like(i0) for _ in range(4))
+    g = [torch.empty_like(i0) for _ in range(8)]
+    scratch = torch.empty_like(i0)
+    out = {}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ss4d.Solver(*shape[::-1], arith="fp64", stream=stream.cuda_stream) as S:
+
+        def measure(name, setup, fn, bytes_per_call, note):
+            """bytes_per_call: a number, or a function of fn's last result"""
+            setup()
+            fn()
+            ts = []
+            for _ in range(3):
+                setup()
+                torch.cuda.synchronize(dev)
+                e0.record(stream)
+                r = fn()
+                e1.record(stream)
+                torch.cuda.synchronize(dev)
+                ts.append(e0.elapsed_time(e1))
+            ms = statistics.median(ts)
+            nb = bytes_per_call(r) if callable(bytes_per_call) else bytes_per_call
+            gbs = nb / (ms / 1e3) / 1e9
+            out[name] = {"ms": ms, "bytes": nb, "GB/s": gbs, "frac": gbs / hbm, "bytes_counted": note}
+            return r
+
+        def restore(*pairs):
+            def f():
+                for dst, src in pairs:
+                    dst.copy_(src)
+            return f
+
+        measure("frames_from_bytes", lambda: None,
+                lambda: [S.frame_from_bytes(img, l, fb[l - 1]) for l in range(1, nt + 1)],
+                9.0 * n_int, "1 B read + 8 B written per interior voxel")
+        z = measure("presmooth_implicit", restore((img, i0)),
+                    lambda: S.presmooth_step(p, img, scratch)["iterations"], lambda z: (16.0 + 40.0 * z) * n_int,
+                    "copy 16 B + per iteration 24 B (two half-sweeps: read u, prev, write u) + 16 B (residual: "
+                    "read u, prev) per voxel")
+        out["presmooth_implicit"]["iterations"] = z
+        measure("presmooth_explicit", restore((img, i0)), lambda: S.presmooth_explicit(p, 1, img, scratch),
+                32.0 * n_int, "copy 16 B + read prev 8 B + write u 8 B per voxel")
+        measure("max4d", lambda: None, lambda: S.max4d(i0), 8.0 * n_pad, "8 B read per voxel")
+        measure("local_threshold", restore((thr, u0)), lambda: S.local_threshold(0.85, 0.15, R, i0, thr, balls),
+                8.0 * n_pad + 24.0 * box * len(balls), "max4d pass + per ball box: min/max read, threshold read "
+                                                      "and write")
+        measure("edge_detector", restore((img, i0), (thr, u0)), lambda: S.edge_detector(p, img, thr, g, scratch),
+                (2 * (16.0 + 40.0 * z) + 80.0) * n_int, "two presmoothings as above + g faces: read 2 images, "
+                                                      "write 8 faces")
+        measure("initial_function", restore((u, u0), (mm, torch.zeros_like(u0))),
+                lambda: S.generate_segm_function(R, u, mm, balls), 24.0 * box * len(balls),
+                "per ball box: read u, write u and Mmask")
+        measure("rescale", restore((u, u0)), lambda: S.rescale_to_zero_one(p, u, mm, balls),
+                24.0 * box * len(balls) + 24.0 * n_int, "per ball box: min/max read, rescale read and write; "
+                                                       "Mmask pass: read u, Mmask, write u")
+        measure("frames_to_bytes", lambda: None,
+                lambda: [S.frame_to_bytes(u, l, fb[l - 1], 1) for l in range(1, nt + 1)],
+                9.0 * n_int, "8 B read + 1 B written per interior voxel")
+    del img, thr, u, mm, g, scratch, i0, u0, fb
+    torch.cuda.empty_cache()
+    total = sum(v["ms"] for k, v in out.items() if k in ("local_threshold", "edge_detector", "initial_function",
+                                                          "rescale"))
+
+    # the oracle on a two-frame sample: the same front-end sequence
+    ntc = 2
+    ci0, cu0 = ss4d.scene(3, nx, ny, nz, ntc, seed=args.seed, threads=os.cpu_count() or 1)
+    cb = frontend_balls(nx, ny, nz, ntc, args.seed)
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    t0 = time.perf_counter()
+    cthr = cu0.copy()
+    oracle.local_threshold(0.85, 0.15, R, ci0, cthr, cb)
+    oracle.edge_detector(p, ci0, cthr)
+    cmm = np.zeros_like(cu0)
+    oracle.generate_segm(R, cu0, cmm, cb)
+    oracle.rescale(R, cu0, cmm, cb)
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    return {"workload": f"{nx}x{ny}x{nz}x{nt}, {len(balls)} balls of radius {R:g} (5 per frame)",
+            "peak": hbm, "peak_source": how, "components": out,
+            "main_front_end_ms": total,
+            "cpu": {"ms": cpu_ms, "frames": ntc, "ms_per_frame": cpu_ms / ntc, "cores": threads, "kind": "port",
+                    "sequence": "local threshold, edge detector, initial function, rescale"},
+            "gpu_ms_per_frame": total / nt}
+
+
 def run_e2e(args, form, ctx):
     """The same steps through the reference-named layer (libss4d_seg.so) with
     host arrays: every _segTimeStep_() uploads u and Mmask and downloads u and
@@ -533,6 +660,8 @@ def main():
             line["e2e"]["form"] = "mixed" if head == "learned" else head
         except Exception as ex:  # reported, not hidden
             line["e2e"] = {"value": None, "unit": "time-steps/s", "error": repr(ex)}
+    if rank == 0 and world == 1 and not args.no_frontend:
+        line["frontend"] = run_frontend(args, ctx)
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args)
     if dist:

@@ -180,6 +180,17 @@ ss4d_status ss4d_reflect(ss4d_solver *s, double *d_img);
 ss4d_status ss4d_presmooth_step(ss4d_solver *s, const ss4d_params *p, double *d_img,
                                 double *d_scratch, ss4d_step_stats *stats);
 
+/* _presmoothStepEXP_ (segmentation4D.c:410-444), the explicit smoother the
+ * reference declares next to _presmoothStep_: d_scratch (the reference's
+ * prev_u; NULL = internal) <- d_img, reflect d_img, then timeStepsNum times
+ * d_img <- (1 - 8c) prev + c * (sum of prev's 8 neighbours), c = sigma/h^2,
+ * over i = 1 .. iMax-3 (as the reference's loop) and the interior j, k, l,
+ * and reflect d_img.  As in the reference, prev is not refreshed between the
+ * steps, so any timeStepsNum >= 1 gives the result of one step.
+ * Asynchronous on the handle's stream. */
+ss4d_status ss4d_presmooth_explicit(ss4d_solver *s, const ss4d_params *p, int timeStepsNum,
+                                    double *d_img, double *d_scratch);
+
 /* _gf_inputImage_plus_thresholdedImage_ (segmentation4D.c:582-823): presmooth
  * d_i0 and d_i0_thr in place, then the 8 face values of the edge detector
  * g_f = 1/(1 + K (theta_img |grad I0|_f^2 + rho_thr |grad Ithr|_f^2)) into

@@ -48,6 +48,7 @@ double _l2norm_(double *a, double *b);                                  /* segme
 bool _gs_coefficients_(void);                                           /* segmentation4D.c:446  */
 bool _segTimeStep_(void);                                               /* segmentation4D.c:215  */
 bool _presmoothStep_(double *u);                                        /* segmentation4D.c:337  */
+void _presmoothStepEXP_(double *u);                                     /* segmentation4D.c:410  */
 bool _rescale4DdataToZeroOne_(double *imagePtr);                        /* segmentation4D.c:1020 */
 bool _gf_inputImage_plus_thresholdedImage_(double *i0, double *i0_thr); /* segmentation4D.c:582  */
 void _copy4DdataFromSrcToDest_(double *srcDataPtr, double *destDataPtr);/* segmentation4D.c:866  */

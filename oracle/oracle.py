@@ -43,8 +43,6 @@ def lib() -> C.CDLL:
         _L.or_l2norm.restype = C.c_double
         _L.or_mass.restype = C.c_double
         _L.or_max_threads.restype = C.c_int
-        for f in ("or_l2norm", "or_mass", "or_mcf_exact_solution", "or_mcf_set_boundary"):
-            pass
         _L.or_l2norm.argtypes = [vp, C.c_double, vp, vp]
         _L.or_mass.argtypes = [vp, C.c_double, vp]
         _L.or_mcf_exact_solution.argtypes = [vp, C.c_double, C.c_double, vp]
@@ -100,6 +98,14 @@ def presmooth(p, v: np.ndarray, scratch: np.ndarray | None = None):
     R = C.c_double(0)
     z = lib().or_presmooth(C.byref(d), C.byref(p), C.c_void_p(_d(v)), C.c_void_p(_d(scratch)), C.byref(R))
     return z, R.value
+
+
+def presmooth_explicit(p, steps: int, v: np.ndarray, scratch: np.ndarray | None = None):
+    """_presmoothStepEXP_ in place on v; scratch receives the reference's prev_u"""
+    d = _dims(v.shape)
+    scratch = np.zeros_like(v) if scratch is None else scratch
+    lib().or_presmooth_explicit(C.byref(d), C.byref(p), C.c_int(steps), C.c_void_p(_d(v)), C.c_void_p(_d(scratch)))
+    return scratch
 
 
 def gfaces(p, i0: np.ndarray, ithr: np.ndarray):

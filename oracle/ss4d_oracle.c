@@ -272,6 +272,36 @@ int or_presmooth(const ss4d_dims *d, const ss4d_params *p, double *v, double *sc
     return z;
 }
 
+/* _presmoothStepEXP_ (segmentation4D.c:410-444), the explicit smoother the
+ * reference declares but its main never calls: scratch (the reference's
+ * prev_u) <- v, reflect v, then `steps` times: v <- (1 - 8c) prev + c * (sum
+ * of the 8 neighbours of prev, in the order i+1, i-1, j+1, j-1, k+1, k-1,
+ * l+1, l-1) over i = 1 .. iMax-3 (the reference's loop stops one short of the
+ * last interior column) and the interior j, k, l, and reflect v.  prev is
+ * not refreshed between the steps, as in the reference. */
+void or_presmooth_explicit(const ss4d_dims *d, const ss4d_params *p, int steps, double *v, double *scratch)
+{
+    geo_t g = geo_of(d);
+    const double coeff = p->sigma / (p->h * p->h);
+    const ptrdiff_t sx = g.sx, sy = g.sy, sz = g.sz, sw = g.sw;
+    int l;
+    or_copy(d, v, scratch);
+    or_reflect(d, v);
+    for (int t = 0; t < steps; t++) {
+#pragma omp parallel for schedule(static)
+        for (l = 1; l <= g.lM - 2; l++)
+            for (int k = 1; k <= g.kM - 2; k++)
+                for (int j = 1; j <= g.jM - 2; j++)
+                    for (int i = 1; i < g.iM - 2; i++) {
+                        ptrdiff_t o = at(&g, i, j, k, l);
+                        v[o] = (1.0 - 8.0 * coeff) * scratch[o]
+                               + coeff * (scratch[o + sx] + scratch[o - sx] + scratch[o + sy] + scratch[o - sy]
+                                          + scratch[o + sz] + scratch[o - sz] + scratch[o + sw] + scratch[o - sw]);
+                    }
+        or_reflect(d, v);
+    }
+}
+
 /* ---------------------------------------------------------------------- */
 /* edge detector                                                            */
 

@@ -360,6 +360,31 @@ def seg_init():
           "changed u", int((out["u_gen"] != u_in).sum()))
 
 
+def presmooth_exp():
+    """The reference's explicit smoother _presmoothStepEXP_ (declared, never
+    called by its main) on a ragged volume with random ghosts, h != 1, for
+    timeStepsNum 0, 1 and 3: u and prev_u after the call."""
+    R = Ref(os.path.join(REF_DIR, "libref_seg.so"))
+    nx, ny, nz, nt = 13, 10, 9, 4
+    p = ss4d.scene_params(sigma=0.07, h=0.9)
+    shape = (nt + 2, nz + 2, ny + 2, nx + 2)
+    seg_setup(R, shape, p)
+    rng = np.random.default_rng(33)
+    v0 = rng.random(shape)
+    u, prev = R.arr("u", shape), R.arr("prev_u", shape)
+    out = {"v_in": v0, "sigma_h": np.array([p.sigma, p.h])}
+    for steps in (0, 1, 3):
+        R.i("timeStepsNum", steps)
+        u[...] = v0
+        prev[...] = 0.0
+        R.call("_presmoothStepEXP_", C.c_void_p(u.ctypes.data), restype=None)
+        out["u_%d" % steps] = u.copy()
+        out["prev_%d" % steps] = prev.copy()
+    np.savez_compressed(os.path.join(OUT, "presmooth_exp.npz"), **out)
+    print("presmooth_exp: changed", int((out["u_1"] != v0).sum()), "of", v0.size,
+          "3 == 1:", bool(np.array_equal(out["u_3"], out["u_1"])))
+
+
 VTK_HEADER = ("# vtk DataFile Version 3.0\nmovingBalls test frame\nBINARY\nDATASET STRUCTURED_POINTS\n"
               "DIMENSIONS {nx} {ny} {nz}\nORIGIN 0 0 0\nSPACING 0.5 0.25 1\nPOINT_DATA {n}\n"
               "SCALARS scalars unsigned_char\nLOOKUP_TABLE default\n")
@@ -506,5 +531,6 @@ if __name__ == "__main__":
     mcf_small()
     seg_32x32x32x8()
     seg_init()
+    presmooth_exp()
     vtk_io()
     pipeline()

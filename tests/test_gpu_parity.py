@@ -6,6 +6,9 @@ masks are bit-exact.  The reference-order kernels (SS4D_ARITH_REFERENCE) are
 held to 1e-13 (they differ from the reference only where it calls pow()).
 The mixed form must reach the same FP64 residual tolerance every step.
 """
+import ctypes as C
+import os
+
 import numpy as np
 import pytest
 
@@ -303,3 +306,54 @@ def test_sweeps_do_not_depend_on_block_order(ss4d, oracle, cuda, arith):
     for its, u in runs[1:]:
         assert its == runs[0][0]
         assert np.array_equal(u, runs[0][1])
+
+
+@pytest.mark.parametrize("steps", [0, 1, 3])
+def test_explicit_presmoothing_matches_reference(ss4d, cuda, steps):
+    """_presmoothStepEXP_ on a ragged volume with random ghosts: u and prev_u
+    bit-exact with the reference, through the native ABI."""
+    torch = cuda
+    d = load_golden("presmooth_exp.npz")
+    sigma, h = (float(v) for v in d["sigma_h"])
+    p = ss4d.scene_params(sigma=sigma, h=h)
+    shape = d["v_in"].shape
+    with ss4d.Solver(*shape[::-1]) as S:
+        v = dev(torch, d["v_in"])
+        prev = torch.zeros_like(v)
+        S.presmooth_explicit(p, steps, v, prev)
+        S.synchronize()
+    assert np.array_equal(host(v), d[f"u_{steps}"])
+    assert np.array_equal(host(prev), d[f"prev_{steps}"])
+
+
+def test_explicit_presmoothing_through_reference_named_layer(ss4d, cuda):
+    """_presmoothStepEXP_(u) of libss4d_seg.so on its host arrays, driven
+    through the reference's globals (timeStepsNum, sigma, h)."""
+    d = load_golden("presmooth_exp.npz")
+    sigma, h = (float(v) for v in d["sigma_h"])
+    shape = d["v_in"].shape
+    lM, kM, jM, iM = shape
+    L = C.CDLL(ss4d.SEG_PATH, mode=os.RTLD_LOCAL)
+    for nm, v in (("iMax", iM), ("jMax", jM), ("kMax", kM), ("lMax", lM), ("timeStepsNum", 3)):
+        C.c_int.in_dll(L, nm).value = v
+    for nm, v in (("sigma", sigma), ("h", h)):
+        C.c_double.in_dll(L, nm).value = v
+    noc = (C.c_int * lM)()
+    C.c_void_p.in_dll(L, "no_of_centers").value = C.addressof(noc)
+    L._allocateMem_.restype = C.c_bool
+    L._presmoothStepEXP_.restype = None
+    assert L._allocateMem_()
+    try:
+        n = int(np.prod(shape))
+
+        def arr(name):
+            addr = C.c_void_p.in_dll(L, name).value
+            return np.ctypeslib.as_array((C.c_double * n).from_address(addr)).reshape(shape)
+
+        u, prev = arr("u"), arr("prev_u")
+        u[...] = d["v_in"]
+        L._presmoothStepEXP_(C.c_void_p(u.ctypes.data))
+        assert np.array_equal(u, d["u_3"])
+        assert np.array_equal(prev, d["prev_3"])
+    finally:
+        L._deallocateMem_()

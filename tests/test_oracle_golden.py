@@ -156,3 +156,14 @@ def test_initial_segmentation_large_balls(oracle):
     assert np.array_equal(mm, d["mmask"])
     # a ball whose box leaves the array is refused (the reference would read outside it)
     assert oracle.local_threshold(alpha, beta, R, i0.copy(), thr, [(1, 3.0, 17.0, 16.0)]) == -1
+
+
+@pytest.mark.parametrize("steps", [0, 1, 3])
+def test_explicit_presmoothing_bit_exact(ss4d, oracle, steps):
+    d = load_golden("presmooth_exp.npz")
+    sigma, h = (float(v) for v in d["sigma_h"])
+    p = ss4d.scene_params(sigma=sigma, h=h)
+    v = d["v_in"].copy()
+    prev = oracle.presmooth_explicit(p, steps, v)
+    assert np.array_equal(v, d[f"u_{steps}"])
+    assert np.array_equal(prev, d[f"prev_{steps}"])

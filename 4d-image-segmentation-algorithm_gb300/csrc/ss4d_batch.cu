@@ -79,10 +79,23 @@ __global__ void __launch_bounds__(256) k_bsweep64(const BVol *__restrict__ vols,
         (&wacc[0][0])[q] = 0.0;
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // a thread sums its residuals while the block stays in one volume and
+    // hands the sum to that volume's slot when the volume changes (a block's
+    // tiles increase, so its volume index only grows; v is uniform over the
+    // block).  The volume's description is read per tile (it stays in L1):
+    // keeping it in registers doubled the registers and halved occupancy.
     int v = 0;
+    double acc = 0.0;
     for (long long t = blockIdx.x; t < total; t += gridDim.x) {
-        while (v + 1 < nv && t >= vols[v + 1].tile0)
-            ++v; // a block's tiles increase, so its volume index only grows
+        if (v + 1 < nv && t >= vols[v + 1].tile0) {
+            acc = warp_sum(acc);
+            if (lane == 0)
+                wacc[warp][v] += acc;
+            acc = 0.0;
+            do
+                ++v;
+            while (v + 1 < nv && t >= vols[v + 1].tile0);
+        }
         if (st[v].stop)
             continue; // the whole block skips: v is uniform
         const BVol &V = vols[v];
@@ -106,20 +119,19 @@ __global__ void __launch_bounds__(256) k_bsweep64(const BVol *__restrict__ vols,
         const double *pv = V.b.P[COL];
         const int tx = threadIdx.x & (cfg.XT - 1), ty = threadIdx.x / cfg.XT;
         const TileCoord tc = tile_coord(g, cfg, t - V.tile0, tx, ty);
-        double r2 = 0.0;
-        if (tc.ok) {
-            const int p = (COL + tc.j + tc.k + tc.l) & 1;
-            const int i = 2 * tc.xi + 2 - p;
-            if (i <= g.nx) {
-                const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * sp.Hs + tc.xi + sp.A;
-                const double r = sweep64_target(g, sp, tc, p, s, src, dst, oth, cf, pv);
-                r2 = r * r;
-            }
-        }
-        r2 = warp_sum(r2);
-        if (lane == 0)
-            wacc[warp][v] += r2;
+        if (!tc.ok)
+            continue;
+        const int p = (COL + tc.j + tc.k + tc.l) & 1;
+        const int i = 2 * tc.xi + 2 - p;
+        if (i > g.nx)
+            continue;
+        const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * sp.Hs + tc.xi + sp.A;
+        const double r = sweep64_target(g, sp, tc, p, s, src, dst, oth, cf, pv);
+        acc = fma(r, r, acc);
     }
+    acc = warp_sum(acc);
+    if (lane == 0)
+        wacc[warp][v] += acc;
     __syncthreads();
     for (int q = threadIdx.x; q < nv; q += blockDim.x) {
         double sum = 0.0;

@@ -466,6 +466,16 @@ static ss4d_status check_params(const ss4d_params *p)
     return SS4D_OK;
 }
 
+// The residual is a sum of nint non-negative terms; a serial left-to-right
+// sum of them (the reference's) differs from any other order by at most
+// about nint * 2^-53 relative.  A stop test with R that close to the
+// tolerance is reported (ss4d_step_stats.near_tolerance): there the
+// reference could have stopped one iteration earlier or later.
+static double near_band(double tol, long long nint)
+{
+    return fabs(tol) * (double)nint * 0x1p-53;
+}
+
 static ss4d_status upload_params(ss4d_solver *s, const ss4d_params *p)
 {
     s->h_params->c = p->tau / (p->h * p->h);
@@ -475,6 +485,7 @@ static ss4d_status upload_params(ss4d_solver *s, const ss4d_params *p)
     s->h_params->tol = p->gsTol;
     s->h_params->maxit = p->maxNoGSIteration;
     s->h_params->pad_ = 0;
+    s->h_params->near_band = near_band(p->gsTol, s->geo.nint);
     // the host mirror is only rewritten after the previous copy completed:
     // every solve ends with a stream synchronisation
     CK(cudaMemcpyAsync(s->d_params, s->h_params, sizeof(DevParams), cudaMemcpyHostToDevice, s->stream));
@@ -499,8 +510,9 @@ static ss4d_status sor_reference(ss4d_solver *s, const ss4d_params *p, double *u
     const Geo &g = s->geo;
     const double c = p->tau / (p->h * p->h), h4 = p->h * p->h * p->h * p->h;
     const long long nb = resid_blocks(g);
+    const double band = near_band(p->gsTol, g.nint);
     double R = 0.0, R1 = 0.0;
-    int z = 0;
+    int z = 0, near = 0;
     do {
         z = z + 1;
         launch_sor_half_ref(g, u, prev, a, c, p->omega_c, 0, s->stream);
@@ -511,12 +523,14 @@ static ss4d_status sor_reference(ss4d_solver *s, const ss4d_params *p, double *u
         CKS(read_scalar(s, 0, &R));
         if (z == 1)
             R1 = R;
+        near |= fabs(R - p->gsTol) <= band;
     } while (R > p->gsTol && z < p->maxNoGSIteration);
     if (stats) {
         stats->iterations = z;
         stats->residual = R;
         stats->first_residual = R1;
         stats->refinements = 0;
+        stats->near_tolerance = near;
         stats->status = isfinite(R) ? SS4D_OK : SS4D_ERR_NONFINITE;
     }
     return isfinite(R) ? SS4D_OK : SS4D_ERR_NONFINITE;
@@ -609,6 +623,7 @@ static ss4d_status finish_stats(ss4d_solver *s, ss4d_step_stats *stats, int mixe
         stats->refinements = mixed ? L.refinements : 0;
         stats->status = L.status;
         stats->warm_started = L.warm;
+        stats->near_tolerance = L.near;
     }
     if (L.status != SS4D_OK) {
         set_err("SOR residual became non-finite at iteration %d", L.z);
@@ -945,8 +960,9 @@ extern "C" ss4d_status ss4d_presmooth_step(ss4d_solver *s, const ss4d_params *p,
     s->launches += 4;
     const double c = p->sigma / (p->h * p->h), h4 = p->h * p->h * p->h * p->h;
     const long long nb = resid_blocks(g);
+    const double band = near_band(p->gsTol, g.nint);
     double R = 0.0, R1 = 0.0;
-    int z = 0;
+    int z = 0, near = 0;
     do {
         z = z + 1;
         launch_presmooth_half(g, d_img, prev, c, p->omega_sigma, 0, s->stream);
@@ -957,6 +973,7 @@ extern "C" ss4d_status ss4d_presmooth_step(ss4d_solver *s, const ss4d_params *p,
         CKS(read_scalar(s, 0, &R));
         if (z == 1)
             R1 = R;
+        near |= fabs(R - p->gsTol) <= band;
     } while (R > p->gsTol && z < p->maxNoGSIteration_sigma);
     CK(cudaEventRecord(s->ev1, s->stream));
     CK(cudaEventSynchronize(s->ev1));
@@ -965,6 +982,7 @@ extern "C" ss4d_status ss4d_presmooth_step(ss4d_solver *s, const ss4d_params *p,
         stats->iterations = z;
         stats->residual = R;
         stats->first_residual = R1;
+        stats->near_tolerance = near;
         cudaEventElapsedTime(&stats->ms, s->ev0, s->ev1);
         stats->status = isfinite(R) ? SS4D_OK : SS4D_ERR_NONFINITE;
     }

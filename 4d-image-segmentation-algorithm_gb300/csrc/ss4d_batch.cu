@@ -37,6 +37,7 @@ struct BVol {
 struct BParams {
     double omega, h4, tol;
     int maxit, pad_;
+    double near_band; // as DevParams::near_band
 };
 
 ss4d_status bfail(ss4d_status st, const char *fmt, ...)
@@ -179,6 +180,8 @@ __global__ void k_bctrl(const double *__restrict__ pred, const double *__restric
             if (z == 1)
                 st[v].R_first = R;
             st[v].R = R;
+            if (fabs(R - par[v].tol) <= par[v].near_band)
+                st[v].near = 1;
             const bool fin = isfinite(R);
             const bool stop = !fin || !(R > par[v].tol) || z >= par[v].maxit;
             if (!fin)
@@ -467,6 +470,8 @@ extern "C" ss4d_status ss4d_batch_seg_time_step(ss4d_batch *b, const ss4d_params
     }
     if (b->dirty)
         BCKS(bdescribe(b));
+    for (int v = 0; v < b->n; ++v) // after the volumes are described
+        b->h_par[v].near_band = fabs(p[v].gsTol) * (double)b->h_vols[v].g.nint * 0x1p-53;
     BCK(cudaMemcpyAsync(b->d_par, b->h_par, sizeof(BParams) * b->n, cudaMemcpyHostToDevice, b->stream));
     const int ib = (b->n + 63) / 64;
     k_binit<<<ib, 64, 0, b->stream>>>(b->d_st, b->n, 0);
@@ -517,6 +522,7 @@ extern "C" ss4d_status ss4d_batch_seg_time_step(ss4d_batch *b, const ss4d_params
             stats[v].residual = L.R;
             stats[v].first_residual = L.R_first;
             stats[v].status = L.status;
+            stats[v].near_tolerance = L.near;
             stats[v].ms = ms;
         }
         if (L.status != SS4D_OK)

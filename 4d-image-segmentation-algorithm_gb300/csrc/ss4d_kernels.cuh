@@ -72,7 +72,7 @@ struct LoopState {
     int bodies;      // loop bodies the controller has run
     int keep;        // mixed form: the next round starts from the correction already in place
     int warm;        // mixed form: this step's first correction came from the learned predictor
-    int pad_;
+    int near;        // 1 once a stop test saw |R - tol| <= near_band
     double R;        // last FP64 residual (sum r^2 h^4)
     double R_first;  // FP64 residual after iteration 1 (fast) / initial (mixed)
     double Rd;       // mixed form: last FP32 correction residual
@@ -88,6 +88,9 @@ struct DevParams {
     double tol;      // gsTol
     int maxit;       // maxNoGSIteration
     int pad_;
+    // |R - tol| below this band: a serial sum of the same terms (the
+    // reference's order) could have decided the stop test the other way
+    double near_band;
 };
 
 // Buffers of the colour-split FP64 form.

@@ -274,7 +274,7 @@ __global__ void k_loop_init(LoopState *st, int mode)
     st->bodies = 0;
     st->keep = 0;
     st->warm = 0;
-    st->pad_ = 0;
+    st->near = 0;
     st->R = 0.0;
     st->R_first = 0.0;
     st->Rd = 0.0;
@@ -346,6 +346,8 @@ __global__ void k_ctrl64(SplitBufs b, int nparts, const DevParams *__restrict__ 
         if (z == 1)
             st->R_first = R;
         st->R = R;
+        if (fabs(R - dp->tol) <= dp->near_band)
+            st->near = 1;
         const bool fin = isfinite(R);
         const bool stop = !fin || !(R > dp->tol) || z >= dp->maxit;
         if (!fin)
@@ -534,6 +536,8 @@ __global__ void k_ctrl_mixed(SplitBufs b, int nparts, const DevParams *__restric
             st->R_first = R;
         st->refinements += 1;
         st->R = R;
+        if (fabs(R - dp->tol) <= dp->near_band)
+            st->near = 1;
         const bool fin = isfinite(R);
         if (!fin)
             st->status = SS4D_ERR_NONFINITE;

@@ -51,7 +51,7 @@ class Params(C.Structure):
 class StepStats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("status", C.c_int), ("residual", C.c_double),
                 ("first_residual", C.c_double), ("refinements", C.c_int), ("warm_started", C.c_int),
-                ("ms", C.c_float)]
+                ("ms", C.c_float), ("near_tolerance", C.c_int)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -89,6 +89,7 @@ def mcf_params(n: int, steps: int = 4, **over) -> Params:
 
 
 _lib = None
+ABI_VERSION = 2  # include/ss4d.h SS4D_ABI_VERSION: the structures above mirror it
 
 
 def lib() -> C.CDLL:
@@ -177,6 +178,9 @@ def lib() -> C.CDLL:
         fn = getattr(L, name)
         fn.argtypes = args
         fn.restype = res
+    if L.ss4d_abi_version() != ABI_VERSION:
+        raise SS4DError(6, "libss4d.so has another ABI version",
+                        f"({L.ss4d_abi_version()}, this binding expects {ABI_VERSION}; rebuild)")
     _lib = L
     return L
 

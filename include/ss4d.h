@@ -32,7 +32,8 @@
 extern "C" {
 #endif
 
-#define SS4D_ABI_VERSION 1
+/* 2: ss4d_step_stats.near_tolerance */
+#define SS4D_ABI_VERSION 2
 
 typedef enum ss4d_status {
     SS4D_OK = 0,
@@ -107,6 +108,10 @@ typedef struct ss4d_step_stats {
     int    refinements;     /* mixed form: FP64 residual/refinement passes            */
     int    warm_started;    /* 1 when the learned predictor supplied the start        */
     float  ms;              /* device time of the call (CUDA events on the stream)    */
+    int    near_tolerance;  /* 1 when a stop test saw |sum - gsTol| within nint * 2^-53
+                               * gsTol: the reference's serial sum of the same terms
+                               * could have decided that test the other way (one
+                               * iteration more or fewer); reported, not corrected   */
 } ss4d_step_stats;
 
 typedef struct ss4d_solver ss4d_solver;

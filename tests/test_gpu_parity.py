@@ -357,3 +357,51 @@ def test_explicit_presmoothing_through_reference_named_layer(ss4d, cuda):
         assert np.array_equal(prev, d["prev_3"])
     finally:
         L._deallocateMem_()
+
+
+@pytest.mark.parametrize("arith", ["reference", "fp64"])
+def test_stop_test_at_the_tolerance_is_reported(ss4d, cuda, arith):
+    """A stop test whose residual lies within the summation-order band of
+    gsTol sets near_tolerance (the reference's serial sum could have decided
+    it the other way); one 0.1 % away does not.  The solve is repeated with
+    gsTol set to the residual it ended on, which the same device reproduces
+    exactly."""
+    torch = cuda
+    d = load_golden("seg_small.npz")
+    p = params_from_golden(ss4d, d)
+    g = [dev(torch, d[f"g{f}"]) for f in range(8)]
+    shape = d["u0"].shape
+    with ss4d.Solver(*shape[::-1], arith=arith) as S:
+        u = dev(torch, d["u0"])
+        st = S.seg_time_step(p, u, None, g)
+        assert st["near_tolerance"] == 0
+        z, R = st["iterations"], st["residual"]
+        for tol, near in ((R, 1), (R * 1.001, 0)):
+            q = params_from_golden(ss4d, d)
+            q.gsTol = tol
+            u = dev(torch, d["u0"])
+            st = S.seg_time_step(q, u, None, g)
+            assert st["iterations"] == z
+            assert st["residual"] == R
+            assert st["near_tolerance"] == near
+
+
+def test_allocation_failure_is_reported_and_the_context_survives(ss4d, cuda):
+    """An allocation the device or host cannot serve returns SS4D_ERR_ALLOC
+    (the reference's _allocateMem_ returns false) and leaves the context
+    usable for the next solve."""
+    import ctypes as C
+
+    torch = cuda
+    L = ss4d.lib()
+    ptr = C.c_void_p()
+    assert L.ss4d_dev_alloc(1 << 60, C.byref(ptr)) == 2  # SS4D_ERR_ALLOC
+    assert L.ss4d_host_alloc(1 << 60, C.byref(ptr)) == 2
+    assert b"failed" in L.ss4d_last_error()
+    d = load_golden("seg_small.npz")
+    p = params_from_golden(ss4d, d)
+    g = [dev(torch, d[f"g{f}"]) for f in range(8)]
+    with ss4d.Solver(*d["u0"].shape[::-1], arith="fp64") as S:
+        u = dev(torch, d["u0"])
+        st = S.seg_time_step(p, u, None, g)
+    assert st["iterations"] == d["its"][0]

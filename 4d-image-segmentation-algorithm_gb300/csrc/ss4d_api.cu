@@ -735,6 +735,19 @@ static bool extrapolating(const ss4d_solver *s)
     return s->arith == SS4D_ARITH_MIXED && s->extrap && s->have_dprev && s->have_g && !s->ws_net;
 }
 
+// the mixed loop's start correction: zero, or the extrapolation the previous
+// step's unpack left in dR[0] / dB (applied by the first refinement pass)
+static ss4d_status clear_corrections(ss4d_solver *s)
+{
+    const size_t fb = sizeof(float) * s->sp.cs;
+    if (!extrapolating(s)) {
+        CK(cudaMemsetAsync(s->sb.dR[0], 0, fb, s->stream));
+        CK(cudaMemsetAsync(s->sb.dB, 0, fb, s->stream));
+    }
+    CK(cudaMemsetAsync(s->sb.dR[1], 0, fb, s->stream));
+    return SS4D_OK;
+}
+
 extern "C" ss4d_status ss4d_solver_set_inner_omega(ss4d_solver *s, double omega)
 {
     REQ(s, "solver is NULL");
@@ -766,14 +779,8 @@ static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixe
         launch_advance(s->d_state, s->stream);
         s->launches += 3;
     } else {
-        // the first refinement pass adds the correction in dR[0] / dB to u:
-        // zero, or the previous step's change when extrapolating
-        const size_t fb = sizeof(float) * sp.cs;
-        if (!extrapolating(s)) {
-            CK(cudaMemsetAsync(s->sb.dR[0], 0, fb, s->stream));
-            CK(cudaMemsetAsync(s->sb.dB, 0, fb, s->stream));
-        }
-        CK(cudaMemsetAsync(s->sb.dR[1], 0, fb, s->stream));
+        // the first refinement pass adds the correction in dR[0] / dB to u
+        CKS(clear_corrections(s));
         launch_loop_init(s->d_state, 0, s->stream);
         s->launches += 1;
         if (s->ws_net && s->have_g)
@@ -1053,16 +1060,12 @@ extern "C" ss4d_status ss4d_gs_coefficients(ss4d_solver *s, const ss4d_params *p
 }
 
 // solve on the split buffers from natural u/prev; coefficients already in place
-static ss4d_status split_solve(ss4d_solver *s, const ss4d_params *p, double *d_u, const double *d_prev,
-                               ss4d_step_stats *stats)
+// split -> natural u after a loop whose state is d_state; in mixed
+// segmentation steps with extrapolation it also keeps the next step's start
+// correction: an extrapolation from this step's change and up to order-1
+// earlier ones
+static ss4d_status unpack_step(ss4d_solver *s, const LoopState *d_state, double *d_u, int mixed)
 {
-    const int mixed = s->arith == SS4D_ARITH_MIXED;
-    timed(s, SS4D_K_PACK, true, [&] { launch_pack(s->geo, s->sp, d_u, d_prev, s->sb, s->stream); });
-    s->launches += 1;
-    CKS(last_launch());
-    CKS(run_split_loop(s, p, mixed));
-    // keep the next step's start correction (mixed segmentation steps): an
-    // extrapolation from this step's change and up to order-1 earlier ones
     const int save = mixed && s->extrap && s->have_g && !s->ws_net;
     int terms = 0, keep = 0;
     if (save) {
@@ -1072,12 +1075,22 @@ static ss4d_status split_solve(ss4d_solver *s, const ss4d_params *p, double *d_u
                 CKS(dmalloc(s, (void **)&s->hist[q], sizeof(float) * s->sp.cs));
         terms = s->have_dprev + 1 < s->extrap ? s->have_dprev + 1 : s->extrap;
     }
-    timed(s, SS4D_K_PACK, true, [&] {
-        launch_unpack(s->geo, s->sp, s->sb, s->d_state, d_u, s->stream, terms, keep, s->hist);
-    });
+    timed(s, SS4D_K_PACK, true,
+          [&] { launch_unpack(s->geo, s->sp, s->sb, d_state, d_u, s->stream, terms, keep, s->hist); });
     s->have_dprev = save ? (s->have_dprev < 3 ? s->have_dprev + 1 : 3) : 0;
     s->launches += 1;
+    return last_launch();
+}
+
+static ss4d_status split_solve(ss4d_solver *s, const ss4d_params *p, double *d_u, const double *d_prev,
+                               ss4d_step_stats *stats)
+{
+    const int mixed = s->arith == SS4D_ARITH_MIXED;
+    timed(s, SS4D_K_PACK, true, [&] { launch_pack(s->geo, s->sp, d_u, d_prev, s->sb, s->stream); });
+    s->launches += 1;
     CKS(last_launch());
+    CKS(run_split_loop(s, p, mixed));
+    CKS(unpack_step(s, s->d_state, d_u, mixed));
     ss4d_status st = finish_stats(s, stats, mixed);
     count_graph_launches(s, mixed);
     return st;
@@ -1453,7 +1466,7 @@ int ss4d::solver_sm_count(const ss4d_solver *s)
 ss4d_status ss4d::solver_view(ss4d_solver *s, SolverView *out)
 {
     REQ(s && out, "NULL argument");
-    CKS(ensure_split(s, 0));
+    CKS(ensure_split(s, s->arith == SS4D_ARITH_MIXED));
     out->g = s->geo;
     out->sp = s->sp;
     out->cfg = s->cfg;
@@ -1481,19 +1494,26 @@ ss4d_status ss4d::solver_prepare_step(ss4d_solver *s, const ss4d_params *p, doub
         REQ(d_g[f], "a g array is NULL");
         gi.p[f] = d_g[f];
     }
-    CKS(ensure_split(s, 0));
-    launch_assemble(s->geo, s->sp, d_u, gi, 1, *p, s->sb, 0, s->stream);
-    launch_pack(s->geo, s->sp, d_u, d_u, s->sb, s->stream);
-    s->launches += 3;
+    const int mixed = s->arith == SS4D_ARITH_MIXED;
+    CKS(ensure_split(s, mixed));
+    timed(s, SS4D_K_ASSEMBLE, true, [&] { assemble(s, p, d_u, gi, 1, mixed); });
+    CKS(last_launch());
+    timed(s, SS4D_K_PACK, true, [&] { launch_pack(s->geo, s->sp, d_u, d_u, s->sb, s->stream); });
+    s->launches += 1;
+    if (mixed) {
+        s->have_g = 1; // a segmentation step: its change feeds the extrapolation
+        CKS(clear_corrections(s));
+    }
     return last_launch();
 }
 
 ss4d_status ss4d::solver_finish_step(ss4d_solver *s, const LoopState *d_state, double *d_u)
 {
     REQ(s && d_state && d_u, "NULL argument");
-    launch_unpack(s->geo, s->sp, s->sb, d_state, d_u, s->stream);
-    s->launches += 1;
-    return last_launch();
+    const int mixed = s->arith == SS4D_ARITH_MIXED;
+    ss4d_status st = unpack_step(s, d_state, d_u, mixed);
+    s->have_g = 0;
+    return st;
 }
 
 ss4d_status ss4d::solver_time_sweeps(ss4d_solver *s, const ss4d_params *p, int iters, float *ms)

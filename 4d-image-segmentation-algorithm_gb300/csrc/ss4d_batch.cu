@@ -1,14 +1,16 @@
 // ss4d_batch.cu — batched solves of many independent volumes (uneven sizes,
-// per-volume parameters) in the plain FP64 form.
+// per-volume parameters) in the plain FP64 form or the mixed form.
 //
 // Each volume owns a solver handle for its buffers, its coefficient assembly
-// and its pack/unpack (ss4d_api.cu).  What is batched is the SOR loop: one
-// persistent launch per half-sweep walks the concatenated tile lists of all
-// volumes (volume v owns tiles [tile0_v, tile0_{v+1})), every tile with its
-// volume's own tile shape; a volume whose loop has stopped is skipped
-// tile by tile.  Residual partial sums are kept per (volume, block) in a
-// fixed order, and one controller kernel runs every volume's stopping test
-// and keeps the graph's while loop going while any volume is active.
+// and its pack/unpack (ss4d_api.cu), extrapolated start included.  What is
+// batched is the SOR loop: one persistent launch per loop kernel walks the
+// concatenated tile lists of all volumes (volume v owns tiles [tile0_v,
+// tile0_{v+1})), every tile with its volume's own tile shape; a tile whose
+// volume has stopped, or (mixed form) is in another phase of its loop, is
+// skipped.  Residual partial sums are kept per (volume, block) in a fixed
+// order, and one controller kernel runs every volume's stopping test (the
+// single-volume state machines of ss4d_sweep.cuh) and keeps the graph's
+// while loop going while any volume is active.
 #include <cuda_runtime.h>
 
 #include <math.h>
@@ -34,11 +36,6 @@ struct BVol {
     long long tile0;
 };
 
-struct BParams {
-    double omega, h4, tol;
-    int maxit, pad_;
-    double near_band; // as DevParams::near_band
-};
 
 ss4d_status bfail(ss4d_status st, const char *fmt, ...)
 {
@@ -71,27 +68,91 @@ ss4d_status bfail(ss4d_status st, const char *fmt, ...)
 // ---------------------------------------------------------------------------
 // kernels
 
+// Walks the block's tiles of all volumes (grid-stride over the concatenated
+// tile lists).  For every target of a volume that want(v) admits it calls
+// body(v, V, g, sp, tc, p, s); when the block moves on from volume v it calls
+// flush(v) (uniform over the block: t is).  The volume's description is read
+// per tile (it stays in L1): holding it in registers doubled them.
+template <int COL, class Want, class Body, class Flush>
+__device__ __forceinline__ void walk_targets(const BVol *__restrict__ vols, int nv, long long total, Want want,
+                                             Body body, Flush flush)
+{
+    int v = 0;
+    for (long long t = blockIdx.x; t < total; t += gridDim.x) {
+        if (v + 1 < nv && t >= vols[v + 1].tile0) {
+            flush(v);
+            do
+                ++v;
+            while (v + 1 < nv && t >= vols[v + 1].tile0);
+        }
+        if (!want(v))
+            continue; // the whole block skips: v is uniform
+        const BVol &V = vols[v];
+        const Geo g = V.g;
+        const Split sp = V.sp;
+        const SweepCfg cfg = V.cfg;
+        const int tx = threadIdx.x & (cfg.XT - 1), ty = threadIdx.x / cfg.XT;
+        const TileCoord tc = tile_coord(g, cfg, t - V.tile0, tx, ty);
+        if (!tc.ok)
+            continue;
+        const int p = (COL + tc.j + tc.k + tc.l) & 1;
+        if (2 * tc.xi + 2 - p > g.nx)
+            continue;
+        const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * sp.Hs + tc.xi + sp.A;
+        body(v, V, g, sp, tc, p, s);
+    }
+    flush(v);
+}
+
+// per-(volume, block) residual sums: a thread's sum goes to its warp's slot
+// of the volume at each volume change, the block's to partial[v * grid + b]
+// for the volumes the kernel worked on (the partials of the others belong to
+// the kernel of their phase in the same loop body)
+struct VolumeSums {
+    double (*wacc)[BMAX];
+    __device__ void clear()
+    {
+        for (int q = threadIdx.x; q < BWARPS * BMAX; q += blockDim.x)
+            (&wacc[0][0])[q] = 0.0;
+        __syncthreads();
+    }
+    __device__ void add(int v, double acc)
+    {
+        acc = warp_sum(acc);
+        if ((threadIdx.x & 31) == 0)
+            wacc[threadIdx.x >> 5][v] += acc;
+    }
+    template <class Want>
+    __device__ void write(int nv, double *partial, Want want)
+    {
+        __syncthreads();
+        for (int q = threadIdx.x; q < nv; q += blockDim.x) {
+            if (!want(q))
+                continue;
+            double sum = 0.0;
+            for (int w = 0; w < BWARPS; ++w)
+                sum += wacc[w][q];
+            partial[(long long)q * gridDim.x + blockIdx.x] = sum;
+        }
+    }
+};
+
+// ---- plain FP64 form
+
+// Its own loop rather than walk_targets: the walker form of this kernel
+// measured 8 % slower on the 16-volume workload (A/B on one box).
 template <int COL>
 __global__ void __launch_bounds__(256) k_bsweep64(const BVol *__restrict__ vols, int nv, long long total,
                                                   const LoopState *__restrict__ st, double *partial)
 {
     __shared__ double wacc[BWARPS][BMAX];
-    for (int q = threadIdx.x; q < BWARPS * BMAX; q += blockDim.x)
-        (&wacc[0][0])[q] = 0.0;
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // a thread sums its residuals while the block stays in one volume and
-    // hands the sum to that volume's slot when the volume changes (a block's
-    // tiles increase, so its volume index only grows; v is uniform over the
-    // block).  The volume's description is read per tile (it stays in L1):
-    // keeping it in registers doubled the registers and halved occupancy.
+    VolumeSums sums{wacc};
+    sums.clear();
     int v = 0;
     double acc = 0.0;
     for (long long t = blockIdx.x; t < total; t += gridDim.x) {
         if (v + 1 < nv && t >= vols[v + 1].tile0) {
-            acc = warp_sum(acc);
-            if (lane == 0)
-                wacc[warp][v] += acc;
+            sums.add(v, acc);
             acc = 0.0;
             do
                 ++v;
@@ -130,16 +191,108 @@ __global__ void __launch_bounds__(256) k_bsweep64(const BVol *__restrict__ vols,
         const double r = sweep64_target(g, sp, tc, p, s, src, dst, oth, cf, pv);
         acc = fma(r, r, acc);
     }
-    acc = warp_sum(acc);
-    if (lane == 0)
-        wacc[warp][v] += acc;
-    __syncthreads();
-    for (int q = threadIdx.x; q < nv; q += blockDim.x) {
-        double sum = 0.0;
-        for (int w = 0; w < BWARPS; ++w)
-            sum += wacc[w][q];
-        partial[(long long)q * gridDim.x + blockIdx.x] = sum;
+    sums.add(v, acc);
+    sums.write(nv, partial, [&](int q) { return !st[q].stop; });
+}
+
+// ---- mixed form (the single-volume kernels k_apply_black, k_refine,
+// k_zero_delta, k_sweep32 of ss4d_kernels_fast.cu, per volume in its mode)
+
+__global__ void __launch_bounds__(256) k_bapply_black(const BVol *__restrict__ vols, int nv, long long total,
+                                                      const LoopState *__restrict__ st)
+{
+    walk_targets<1>(
+        vols, nv, total, [&](int v) { return st[v].mode == 0 && !st[v].stop; },
+        [&](int, const BVol &V, const Geo &, const Split &, const TileCoord &, int, long long s) {
+            V.b.Bk[s] += f2d_bits(V.b.dB[s]);
+        },
+        [](int) {});
+}
+
+template <int COL>
+__global__ void __launch_bounds__(256) k_brefine(const BVol *__restrict__ vols, int nv, long long total,
+                                                 const LoopState *__restrict__ st, double *partial)
+{
+    __shared__ double wacc[BWARPS][BMAX];
+    VolumeSums sums{wacc};
+    sums.clear();
+    double acc = 0.0;
+    auto want = [&](int v) { return st[v].mode == 0 && !st[v].stop; };
+    walk_targets<COL>(
+        vols, nv, total, want,
+        [&](int v, const BVol &V, const Geo &g, const Split &sp, const TileCoord &tc, int p, long long s) {
+            double *own = COL == 0 ? V.b.R[0] : V.b.Bk;
+            const float *down = st[v].dsrc ? V.b.dR[1] : V.b.dR[0];
+            const double *oth = COL == 0 ? V.b.Bk : V.b.R[0];
+            const long long Hy = sp.Hs, Hz = Hy * g.jM, Hw = Hz * g.kM;
+            const RefineOut o =
+                refine_target<COL>(g, sp, tc, p, s, Hy, Hz, Hw, own, down, oth, V.b.coef[COL], V.b.P[COL]);
+            acc = fma(o.r, o.r, acc);
+            if (COL == 0)
+                own[s] = o.u;
+            V.b.r32[COL][s] = d2f_bits(-o.r);
+        },
+        [&](int v) {
+            sums.add(v, acc);
+            acc = 0.0;
+        });
+    sums.write(nv, partial, want);
+}
+
+// zero the corrections of the volumes that start a round (unless the round
+// keeps the correction in place)
+__global__ void k_bzero_delta(const BVol *__restrict__ vols, int nv, const LoopState *__restrict__ st)
+{
+    for (int v = 0; v < nv; ++v) {
+        if (st[v].mode != 1 || st[v].stop || st[v].keep)
+            continue;
+        const BVol &V = vols[v];
+        for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < V.sp.cs;
+             t += (long long)gridDim.x * blockDim.x) {
+            V.b.dR[0][t] = 0.f;
+            V.b.dR[1][t] = 0.f;
+            V.b.dB[t] = 0.f;
+        }
     }
+}
+
+template <int COL>
+__global__ void __launch_bounds__(256) k_bsweep32(const BVol *__restrict__ vols, int nv, long long total,
+                                                  const LoopState *__restrict__ st, const DevParams *__restrict__ par,
+                                                  double *partial)
+{
+    __shared__ double wacc[BWARPS][BMAX];
+    VolumeSums sums{wacc};
+    sums.clear();
+    float acc = 0.f;
+    auto want = [&](int v) { return (COL == 0 ? st[v].mode != 0 : st[v].mode == 2) && !st[v].stop; };
+    walk_targets<COL>(
+        vols, nv, total, want,
+        [&](int v, const BVol &V, const Geo &g, const Split &sp, const TileCoord &tc, int p, long long s) {
+            const int ds = st[v].dsrc;
+            const float *src;
+            float *dst;
+            const float *oth;
+            if (COL == 0) {
+                src = ds ? V.b.dR[1] : V.b.dR[0];
+                dst = ds ? V.b.dR[0] : V.b.dR[1];
+                oth = V.b.dB;
+            } else {
+                src = V.b.dB;
+                dst = V.b.dB;
+                oth = ds ? V.b.dR[1] : V.b.dR[0];
+            }
+            const long long Hy = sp.Hs, Hz = Hy * g.jM, Hw = Hz * g.kM;
+            const Sweep32Out o = sweep32_target(g, sp, tc, p, s, Hy, Hz, Hw, src, oth, V.b.coef32[COL],
+                                                V.b.r32[COL], (float)par[v].omega);
+            acc = fmaf(o.r, o.r, acc);
+            dst[s] = o.u;
+        },
+        [&](int v) {
+            sums.add(v, (double)acc);
+            acc = 0.f;
+        });
+    sums.write(nv, partial, want);
 }
 
 __global__ void k_binit(LoopState *st, int nv, int z)
@@ -156,7 +309,7 @@ __global__ void k_binit(LoopState *st, int nv, int z)
 
 // every volume's stopping test (as k_ctrl64 does for one volume)
 __global__ void k_bctrl(const double *__restrict__ pred, const double *__restrict__ pblack, int grid, int nv,
-                        const BParams *__restrict__ par, LoopState *st, cudaGraphConditionalHandle h, int use_cond)
+                        const DevParams *__restrict__ par, LoopState *st, cudaGraphConditionalHandle h, int use_cond)
 {
     __shared__ int any;
     if (threadIdx.x == 0)
@@ -172,28 +325,38 @@ __global__ void k_bctrl(const double *__restrict__ pred, const double *__restric
         }
         a = block_sum(a);
         c = block_sum(c);
-        if (threadIdx.x == 0) {
-            const double om1 = 1.0 - par[v].omega;
-            const double R = (a + om1 * om1 * c) * par[v].h4;
-            const int z = st[v].z;
-            st[v].bodies += 1;
-            if (z == 1)
-                st[v].R_first = R;
-            st[v].R = R;
-            if (fabs(R - par[v].tol) <= par[v].near_band)
-                st[v].near = 1;
-            const bool fin = isfinite(R);
-            const bool stop = !fin || !(R > par[v].tol) || z >= par[v].maxit;
-            if (!fin)
-                st[v].status = SS4D_ERR_NONFINITE;
-            if (stop) {
-                st[v].stop = 1;
-                st[v].final_red = z & 1;
-            } else {
-                st[v].z = z + 1;
-                any = 1;
+        if (threadIdx.x == 0 && !ctrl64_update(&st[v], a, c, &par[v]))
+            any = 1;
+        __syncthreads();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && use_cond)
+        cudaGraphSetConditional(h, any ? 1u : 0u);
+}
+
+// every volume's mixed-form controller step (k_ctrl_mixed per volume)
+__global__ void k_bctrl_mixed(const double *__restrict__ pred, const double *__restrict__ pblack, int grid, int nv,
+                              const DevParams *__restrict__ par, LoopState *st, cudaGraphConditionalHandle h,
+                              int use_cond)
+{
+    __shared__ int any;
+    if (threadIdx.x == 0)
+        any = 0;
+    __syncthreads();
+    for (int v = 0; v < nv; ++v) {
+        if (st[v].stop)
+            continue;
+        const int mode = st[v].mode;
+        double a = 0.0, c = 0.0;
+        if (mode != 1)
+            for (int t = threadIdx.x; t < grid; t += blockDim.x) {
+                a += pred[(long long)v * grid + t];
+                c += pblack[(long long)v * grid + t];
             }
-        }
+        a = block_sum(a);
+        c = block_sum(c);
+        if (threadIdx.x == 0 && !ctrl_mixed_update(&st[v], a, c, &par[v]))
+            any = 1;
         __syncthreads();
     }
     __syncthreads();
@@ -221,25 +384,28 @@ struct ss4d_batch {
     BVol h_vols[BMAX];
     BVol *d_vols;
     LoopState *d_st, *h_st;
-    BParams *d_par, *h_par;
+    DevParams *d_par, *h_par;
     double *d_partial;
     int grid;
     long long total;
     int dirty;
     cudaStream_t stream, cap;
-    cudaGraph_t graph;
-    cudaGraphExec_t exec;
+    cudaGraph_t graph[2]; // per form: plain FP64, mixed
+    cudaGraphExec_t exec[2];
     int use_graph, graph_failed;
+    int mixed;
 };
 
 static void bfree_graph(ss4d_batch *b)
 {
-    if (b->exec)
-        cudaGraphExecDestroy(b->exec);
-    if (b->graph)
-        cudaGraphDestroy(b->graph);
-    b->exec = nullptr;
-    b->graph = nullptr;
+    for (int f = 0; f < 2; ++f) {
+        if (b->exec[f])
+            cudaGraphExecDestroy(b->exec[f]);
+        if (b->graph[f])
+            cudaGraphDestroy(b->graph[f]);
+        b->exec[f] = nullptr;
+        b->graph[f] = nullptr;
+    }
 }
 
 extern "C" ss4d_status ss4d_batch_destroy(ss4d_batch *b)
@@ -321,13 +487,13 @@ extern "C" ss4d_status ss4d_batch_create(int n, const ss4d_dims *dims, void *str
     if (e == cudaSuccess)
         e = cudaMalloc((void **)&b->d_st, sizeof(LoopState) * n);
     if (e == cudaSuccess)
-        e = cudaMalloc((void **)&b->d_par, sizeof(BParams) * n);
+        e = cudaMalloc((void **)&b->d_par, sizeof(DevParams) * n);
     if (e == cudaSuccess)
         e = cudaMalloc((void **)&b->d_partial, sizeof(double) * 2 * (size_t)n * b->grid);
     if (e == cudaSuccess)
         e = cudaMallocHost((void **)&b->h_st, sizeof(LoopState) * n);
     if (e == cudaSuccess)
-        e = cudaMallocHost((void **)&b->h_par, sizeof(BParams) * n);
+        e = cudaMallocHost((void **)&b->h_par, sizeof(DevParams) * n);
     if (e == cudaSuccess)
         e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -344,6 +510,26 @@ extern "C" ss4d_status ss4d_batch_set_graph(ss4d_batch *b, int enable)
     if (!b)
         return bfail(SS4D_ERR_INVALID, "invalid argument: batch is NULL");
     b->use_graph = enable ? 1 : 0;
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_batch_set_arith(ss4d_batch *b, ss4d_arith arith)
+{
+    if (!b || (arith != SS4D_ARITH_FP64 && arith != SS4D_ARITH_MIXED))
+        return bfail(SS4D_ERR_INVALID, "invalid argument: batches run the FP64 or the mixed form");
+    for (int v = 0; v < b->n; ++v)
+        BCKS(ss4d_solver_set_arith(b->vol[v], arith));
+    b->mixed = arith == SS4D_ARITH_MIXED;
+    b->dirty = 1; // the mixed form's buffers enter the descriptions
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_batch_set_extrapolation(ss4d_batch *b, int order)
+{
+    if (!b)
+        return bfail(SS4D_ERR_INVALID, "invalid argument: batch is NULL");
+    for (int v = 0; v < b->n; ++v)
+        BCKS(ss4d_solver_set_extrapolation(b->vol[v], order));
     return SS4D_OK;
 }
 
@@ -396,19 +582,46 @@ extern "C" ss4d_status ss4d_batch_autotune(ss4d_batch *b, const ss4d_params *p, 
     return SS4D_OK;
 }
 
+static double *bpart(ss4d_batch *b, int colour)
+{
+    return b->d_partial + (colour ? (size_t)b->n * b->grid : 0);
+}
+
 static void launch_bsweep(ss4d_batch *b, int colour, cudaStream_t st)
 {
     if (colour == 0)
-        k_bsweep64<0><<<b->grid, 256, 0, st>>>(b->d_vols, b->n, b->total, b->d_st, b->d_partial);
+        k_bsweep64<0><<<b->grid, 256, 0, st>>>(b->d_vols, b->n, b->total, b->d_st, bpart(b, 0));
     else
-        k_bsweep64<1><<<b->grid, 256, 0, st>>>(b->d_vols, b->n, b->total, b->d_st,
-                                               b->d_partial + (size_t)b->n * b->grid);
+        k_bsweep64<1><<<b->grid, 256, 0, st>>>(b->d_vols, b->n, b->total, b->d_st, bpart(b, 1));
 }
 
 static void launch_bctrl(ss4d_batch *b, unsigned long long h, int use_cond, cudaStream_t st)
 {
-    k_bctrl<<<1, 256, 0, st>>>(b->d_partial, b->d_partial + (size_t)b->n * b->grid, b->grid, b->n, b->d_par,
-                               b->d_st, (cudaGraphConditionalHandle)h, use_cond);
+    k_bctrl<<<1, 256, 0, st>>>(bpart(b, 0), bpart(b, 1), b->grid, b->n, b->d_par, b->d_st,
+                               (cudaGraphConditionalHandle)h, use_cond);
+}
+
+// one loop body of the plain form: black half-sweep, red half-sweep, test
+static void launch_body64(ss4d_batch *b, unsigned long long h, int use_cond, cudaStream_t st)
+{
+    launch_bsweep(b, 1, st);
+    launch_bsweep(b, 0, st);
+    launch_bctrl(b, h, use_cond, st);
+}
+
+// one loop body of the mixed form, as the single-volume one: refinement pass
+// (volumes in mode 0), zeroed corrections (mode 1), FP32 black sweep (mode 2)
+// and red sweep (modes 1 and 2), every volume's controller step
+static void launch_body_mixed(ss4d_batch *b, unsigned long long h, int use_cond, cudaStream_t st)
+{
+    k_bapply_black<<<b->grid, 256, 0, st>>>(b->d_vols, b->n, b->total, b->d_st);
+    k_brefine<0><<<b->grid, 256, 0, st>>>(b->d_vols, b->n, b->total, b->d_st, bpart(b, 0));
+    k_brefine<1><<<b->grid, 256, 0, st>>>(b->d_vols, b->n, b->total, b->d_st, bpart(b, 1));
+    k_bzero_delta<<<1024, 256, 0, st>>>(b->d_vols, b->n, b->d_st);
+    k_bsweep32<1><<<b->grid, 256, 0, st>>>(b->d_vols, b->n, b->total, b->d_st, b->d_par, bpart(b, 1));
+    k_bsweep32<0><<<b->grid, 256, 0, st>>>(b->d_vols, b->n, b->total, b->d_st, b->d_par, bpart(b, 0));
+    k_bctrl_mixed<<<1, 256, 0, st>>>(bpart(b, 0), bpart(b, 1), b->grid, b->n, b->d_par, b->d_st,
+                                     (cudaGraphConditionalHandle)h, use_cond);
 }
 
 static ss4d_status bbuild_graph(ss4d_batch *b)
@@ -431,21 +644,23 @@ static ss4d_status bbuild_graph(ss4d_batch *b)
         e = cudaStreamBeginCaptureToGraph(b->cap, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                           cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        launch_bsweep(b, 1, b->cap);
-        launch_bsweep(b, 0, b->cap);
-        launch_bctrl(b, (unsigned long long)h, 1, b->cap);
+        if (b->mixed)
+            launch_body_mixed(b, (unsigned long long)h, 1, b->cap);
+        else
+            launch_body64(b, (unsigned long long)h, 1, b->cap);
         cudaGraph_t body = nullptr;
         e = cudaStreamEndCapture(b->cap, &body);
     }
+    const int f = b->mixed;
     if (e == cudaSuccess)
-        e = cudaGraphInstantiate(&b->exec, graph, 0);
+        e = cudaGraphInstantiate(&b->exec[f], graph, 0);
     if (e != cudaSuccess) {
         cudaGetLastError();
         cudaGraphDestroy(graph);
-        b->exec = nullptr;
+        b->exec[f] = nullptr;
         return bfail(SS4D_ERR_CUDA, "batch graph: %s", cudaGetErrorString(e));
     }
-    b->graph = graph;
+    b->graph[f] = graph;
     return SS4D_OK;
 }
 
@@ -462,6 +677,7 @@ extern "C" ss4d_status ss4d_batch_seg_time_step(ss4d_batch *b, const ss4d_params
     BCK(cudaEventRecord(e0, b->stream));
     for (int v = 0; v < b->n; ++v) {
         BCKS(solver_prepare_step(b->vol[v], &p[v], d_u[v], d_g + 8 * v));
+        b->h_par[v].c = p[v].tau / (p[v].h * p[v].h);
         b->h_par[v].omega = p[v].omega_c;
         b->h_par[v].h4 = p[v].h * p[v].h * p[v].h * p[v].h;
         b->h_par[v].tol = p[v].gsTol;
@@ -472,18 +688,20 @@ extern "C" ss4d_status ss4d_batch_seg_time_step(ss4d_batch *b, const ss4d_params
         BCKS(bdescribe(b));
     for (int v = 0; v < b->n; ++v) // after the volumes are described
         b->h_par[v].near_band = fabs(p[v].gsTol) * (double)b->h_vols[v].g.nint * 0x1p-53;
-    BCK(cudaMemcpyAsync(b->d_par, b->h_par, sizeof(BParams) * b->n, cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaMemcpyAsync(b->d_par, b->h_par, sizeof(DevParams) * b->n, cudaMemcpyHostToDevice, b->stream));
     const int ib = (b->n + 63) / 64;
-    k_binit<<<ib, 64, 0, b->stream>>>(b->d_st, b->n, 0);
-    launch_bsweep(b, 0, b->stream);
-    k_binit<<<ib, 64, 0, b->stream>>>(b->d_st, b->n, 1);
+    k_binit<<<ib, 64, 0, b->stream>>>(b->d_st, b->n, 0); // mixed: mode 0, refine first
+    if (!b->mixed) {
+        launch_bsweep(b, 0, b->stream); // the first red half-sweep
+        k_binit<<<ib, 64, 0, b->stream>>>(b->d_st, b->n, 1);
+    }
     BCK(cudaGetLastError());
     bool graphed = false;
     if (b->use_graph && !b->graph_failed) {
-        if (!b->exec && bbuild_graph(b) != SS4D_OK)
+        if (!b->exec[b->mixed] && bbuild_graph(b) != SS4D_OK)
             b->graph_failed = 1;
-        if (b->exec) {
-            BCK(cudaGraphLaunch(b->exec, b->stream));
+        if (b->exec[b->mixed]) {
+            BCK(cudaGraphLaunch(b->exec[b->mixed], b->stream));
             graphed = true;
         }
     }
@@ -491,10 +709,14 @@ extern "C" ss4d_status ss4d_batch_seg_time_step(ss4d_batch *b, const ss4d_params
         int maxit = 0;
         for (int v = 0; v < b->n; ++v)
             maxit = p[v].maxNoGSIteration > maxit ? p[v].maxNoGSIteration : maxit;
-        for (int guard = 0; guard < maxit + 8; ++guard) {
-            launch_bsweep(b, 1, b->stream);
-            launch_bsweep(b, 0, b->stream);
-            launch_bctrl(b, 0, 0, b->stream);
+        // a mixed body advances a volume by at most one inner iteration, and
+        // every round adds a start and a refinement body
+        const int guard_max = b->mixed ? 4 * (maxit + 4) + 16 : maxit + 8;
+        for (int guard = 0; guard < guard_max; ++guard) {
+            if (b->mixed)
+                launch_body_mixed(b, 0, 0, b->stream);
+            else
+                launch_body64(b, 0, 0, b->stream);
             BCK(cudaGetLastError());
             BCK(cudaMemcpyAsync(b->h_st, b->d_st, sizeof(LoopState) * b->n, cudaMemcpyDeviceToHost, b->stream));
             BCK(cudaStreamSynchronize(b->stream));
@@ -521,6 +743,7 @@ extern "C" ss4d_status ss4d_batch_seg_time_step(ss4d_batch *b, const ss4d_params
             stats[v].iterations = L.z;
             stats[v].residual = L.R;
             stats[v].first_residual = L.R_first;
+            stats[v].refinements = b->mixed ? L.refinements : 0;
             stats[v].status = L.status;
             stats[v].near_tolerance = L.near;
             stats[v].ms = ms;

@@ -339,25 +339,7 @@ __global__ void k_ctrl64(SplitBufs b, int nparts, const DevParams *__restrict__ 
     a = block_sum(a);
     c = block_sum(c);
     if (threadIdx.x == 0) {
-        const double om1 = 1.0 - dp->omega;
-        const double R = (a + om1 * om1 * c) * dp->h4;
-        const int z = st->z;
-        st->bodies += 1;
-        if (z == 1)
-            st->R_first = R;
-        st->R = R;
-        if (fabs(R - dp->tol) <= dp->near_band)
-            st->near = 1;
-        const bool fin = isfinite(R);
-        const bool stop = !fin || !(R > dp->tol) || z >= dp->maxit;
-        if (!fin)
-            st->status = SS4D_ERR_NONFINITE;
-        if (stop) {
-            st->stop = 1;
-            st->final_red = z & 1; // red buffer holding the values of iteration z
-        } else {
-            st->z = z + 1;
-        }
+        const bool stop = ctrl64_update(st, a, c, dp);
         if (use_cond)
             cudaGraphSetConditional(h, stop ? 0u : 1u);
     }
@@ -416,21 +398,11 @@ __global__ void __launch_bounds__(256) k_refine(Geo g, Split sp, SweepCfg cfg, S
         if (i > g.nx)
             continue;
         const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * Hy + tc.xi + sp.A;
-        const long long nb[8] = {s - p + 1, s - p, s + Hy, s - Hy, s + Hz, s - Hz, s + Hw, s - Hw};
-        const double u0 = COL == 0 ? own[s] + f2d_bits(down[s]) : own[s];
-        const double *cv = cf + coef_at(tile_coef_index(g, sp, tc), 0, 10);
-        double S = ld_stream(pv + s); // prev + sum_f c a_f u_f
-#pragma unroll
-        for (int f = 0; f < 8; ++f)
-            S = fma(ld_stream(cv + 32 * f), oth[nb[f]], S);
-        const double diag = ld_stream(cv + 256);
-        const double r = fma(diag, u0, -S);
-        acc = fma(r, r, acc);
+        const RefineOut o = refine_target<COL>(g, sp, tc, p, s, Hy, Hz, Hw, own, down, oth, cf, pv);
+        acc = fma(o.r, o.r, acc);
         if (COL == 0)
-            own[s] = u0;
-        // r = A u - b here; the correction d with A d = b - A u moves u to the
-        // solution, so the FP32 sweeps get the negated residual
-        rr[s] = d2f_bits(-r);
+            own[s] = o.u;
+        rr[s] = d2f_bits(-o.r);
     }
     acc = block_sum(acc);
     if (threadIdx.x == 0)
@@ -485,22 +457,9 @@ __global__ void __launch_bounds__(256) k_sweep32(Geo g, Split sp, SweepCfg cfg, 
         if (i > g.nx)
             continue;
         const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * Hy + tc.xi + sp.A;
-        const float u0 = src[s];
-        const float *cv = cf + 8 * tile_coef_index(g, sp, tc);
-        const float4 c03 = ld_stream4(cv), c47 = ld_stream4(cv + 4);
-        const float a0 = c03.x, a1 = c03.y, a2 = c03.z, a3 = c03.w, a4 = c47.x, a5 = c47.y, a6 = c47.z, a7 = c47.w;
-        float S = a0 * ld_ro(oth + s - p + 1);
-        S = fmaf(a1, ld_ro(oth + s - p), S);
-        S = fmaf(a2, ld_ro(oth + s + Hy), S);
-        S = fmaf(a3, ld_ro(oth + s - Hy), S);
-        S = fmaf(a4, ld_ro(oth + s + Hz), S);
-        S = fmaf(a5, ld_ro(oth + s - Hz), S);
-        S = fmaf(a6, ld_ro(oth + s + Hw), S);
-        S = fmaf(a7, ld_ro(oth + s - Hw), S);
-        const float diag = 1.f + (((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7)));
-        const float r = fmaf(diag, u0, -(S + ld_stream(rhs + s)));
-        acc = fmaf(r, r, acc);
-        dst[s] = fmaf(-omega / diag, r, u0);
+        const Sweep32Out o = sweep32_target(g, sp, tc, p, s, Hy, Hz, Hw, src, oth, cf, rhs, omega);
+        acc = fmaf(o.r, o.r, acc);
+        dst[s] = o.u;
     }
     const double tot = block_sum((double)acc);
     if (threadIdx.x == 0)
@@ -528,48 +487,7 @@ __global__ void k_ctrl_mixed(SplitBufs b, int nparts, const DevParams *__restric
     c = block_sum(c);
     if (threadIdx.x != 0)
         return;
-    st->bodies += 1;
-    bool stop = false;
-    if (mode == 0) {
-        const double R = (a + c) * dp->h4;
-        if (st->refinements == 0)
-            st->R_first = R;
-        st->refinements += 1;
-        st->R = R;
-        if (fabs(R - dp->tol) <= dp->near_band)
-            st->near = 1;
-        const bool fin = isfinite(R);
-        if (!fin)
-            st->status = SS4D_ERR_NONFINITE;
-        if (!fin || !(R > dp->tol) || st->z >= dp->maxit) {
-            stop = true;
-        } else {
-            st->mode = 1;
-            // aim the round at the tolerance, but not below what FP32
-            // corrections can resolve relative to the current residual
-            st->target = fmax(0.5 * dp->tol, 1e-11 * R);
-        }
-    } else if (mode == 1) {
-        st->mode = 2;
-        st->dsrc ^= 1;
-        st->round_z = 0;
-        st->keep = 0;
-    } else {
-        const double om1 = 1.0 - dp->omega;
-        const double Rd = (a + om1 * om1 * c) * dp->h4;
-        st->Rd = Rd;
-        st->z += 1;
-        st->round_z += 1;
-        if (!isfinite(Rd) || !(Rd > st->target) || st->z >= dp->maxit) {
-            st->mode = 0; // refine with the red correction of this iteration
-        } else {
-            st->dsrc ^= 1;
-        }
-    }
-    if (stop) {
-        st->stop = 1;
-        st->final_red = 0;
-    }
+    const bool stop = ctrl_mixed_update(st, a, c, dp);
     if (use_cond)
         cudaGraphSetConditional(h, stop ? 0u : 1u);
 }

@@ -146,4 +146,149 @@ __device__ __forceinline__ double sweep64_target(const Geo &g, const Split &sp, 
     return r;
 }
 
+// ---------------------------------------------------------------------------
+// mixed form: FP64 refinement and FP32 correction sweeps (single-volume
+// kernels in ss4d_kernels_fast.cu, batched ones in ss4d_batch.cu)
+
+// Refinement at a target of colour COL (Hy, Hz, Hw: the split strides of
+// j, k, l): the red pass first adds the red correction (down) to u; then
+// r = diag*u - (prev + sum_f c a_f u_f) against the other colour, whose
+// correction is already in place.  Returns r and the target's u; the caller
+// stores u (red pass) and -r into r32, the right-hand side of the next
+// correction equation (r = A u - b here; the correction d with A d = b - A u
+// moves u to the solution).
+struct RefineOut {
+    double r, u;
+};
+template <int COL>
+__device__ __forceinline__ RefineOut refine_target(const Geo &g, const Split &sp, const TileCoord &tc, int p,
+                                                   long long s, long long Hy, long long Hz, long long Hw,
+                                                   const double *own, const float *__restrict__ down,
+                                                   const double *__restrict__ oth, const double *__restrict__ cf,
+                                                   const double *__restrict__ pv)
+{
+    const long long nb[8] = {s - p + 1, s - p, s + Hy, s - Hy, s + Hz, s - Hz, s + Hw, s - Hw};
+    const double u0 = COL == 0 ? own[s] + f2d_bits(down[s]) : own[s];
+    const double *cv = cf + coef_at(tile_coef_index(g, sp, tc), 0, 10);
+    double S = ld_stream(pv + s); // prev + sum_f c a_f u_f
+#pragma unroll
+    for (int f = 0; f < 8; ++f)
+        S = fma(ld_stream(cv + 32 * f), oth[nb[f]], S);
+    const double diag = ld_stream(cv + 256);
+    return RefineOut{fma(diag, u0, -S), u0};
+}
+
+// One FP32 SOR update of the correction at a target (diag = 1 + sum c a_f,
+// formed from the record): returns the pre-update residual of the correction
+// equation and the updated value, which the caller stores.
+struct Sweep32Out {
+    float r, u;
+};
+__device__ __forceinline__ Sweep32Out sweep32_target(const Geo &g, const Split &sp, const TileCoord &tc, int p,
+                                                     long long s, long long Hy, long long Hz, long long Hw,
+                                                     const float *src, const float *__restrict__ oth,
+                                                     const float *__restrict__ cf, const float *__restrict__ rhs,
+                                                     float omega)
+{
+    const float u0 = src[s];
+    const float *cv = cf + 8 * tile_coef_index(g, sp, tc);
+    const float4 c03 = ld_stream4(cv), c47 = ld_stream4(cv + 4);
+    const float a0 = c03.x, a1 = c03.y, a2 = c03.z, a3 = c03.w, a4 = c47.x, a5 = c47.y, a6 = c47.z, a7 = c47.w;
+    float S = a0 * ld_ro(oth + s - p + 1);
+    S = fmaf(a1, ld_ro(oth + s - p), S);
+    S = fmaf(a2, ld_ro(oth + s + Hy), S);
+    S = fmaf(a3, ld_ro(oth + s - Hy), S);
+    S = fmaf(a4, ld_ro(oth + s + Hz), S);
+    S = fmaf(a5, ld_ro(oth + s - Hz), S);
+    S = fmaf(a6, ld_ro(oth + s + Hw), S);
+    S = fmaf(a7, ld_ro(oth + s - Hw), S);
+    const float diag = 1.f + (((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7)));
+    const float r = fmaf(diag, u0, -(S + ld_stream(rhs + s)));
+    return Sweep32Out{r, fmaf(-omega / diag, r, u0)};
+}
+
+// ---------------------------------------------------------------------------
+// stopping tests, one volume: a and c are the summed red and black partials
+// of the body that just ran.  Both return true when the loop stops.
+
+// plain FP64 form: R after iteration z.  A body is the black half-sweep of
+// iteration z and the red one of z + 1, both summing pre-update residuals:
+// the red ones are those of iteration z's values; an SOR update scales a
+// black target's residual by (1 - omega), so the black sums are scaled by
+// (1 - omega)^2.
+__device__ inline bool ctrl64_update(LoopState *st, double a, double c, const DevParams *dp)
+{
+    const double om1 = 1.0 - dp->omega;
+    const double R = (a + om1 * om1 * c) * dp->h4;
+    const int z = st->z;
+    st->bodies += 1;
+    if (z == 1)
+        st->R_first = R;
+    st->R = R;
+    if (fabs(R - dp->tol) <= dp->near_band)
+        st->near = 1;
+    const bool fin = isfinite(R);
+    const bool stop = !fin || !(R > dp->tol) || z >= dp->maxit;
+    if (!fin)
+        st->status = SS4D_ERR_NONFINITE;
+    if (stop) {
+        st->stop = 1;
+        st->final_red = z & 1; // red buffer holding the values of iteration z
+    } else {
+        st->z = z + 1;
+    }
+    return stop;
+}
+
+// mixed form: mode 0 (refinement: the FP64 residual test), 1 (a round has
+// started), 2 (an inner iteration: the correction equation's residual
+// against the round's target)
+__device__ inline bool ctrl_mixed_update(LoopState *st, double a, double c, const DevParams *dp)
+{
+    const int mode = st->mode;
+    st->bodies += 1;
+    bool stop = false;
+    if (mode == 0) {
+        const double R = (a + c) * dp->h4;
+        if (st->refinements == 0)
+            st->R_first = R;
+        st->refinements += 1;
+        st->R = R;
+        if (fabs(R - dp->tol) <= dp->near_band)
+            st->near = 1;
+        const bool fin = isfinite(R);
+        if (!fin)
+            st->status = SS4D_ERR_NONFINITE;
+        if (!fin || !(R > dp->tol) || st->z >= dp->maxit) {
+            stop = true;
+        } else {
+            st->mode = 1;
+            // aim the round at the tolerance, but not below what FP32
+            // corrections can resolve relative to the current residual
+            st->target = fmax(0.5 * dp->tol, 1e-11 * R);
+        }
+    } else if (mode == 1) {
+        st->mode = 2;
+        st->dsrc ^= 1;
+        st->round_z = 0;
+        st->keep = 0;
+    } else {
+        const double om1 = 1.0 - dp->omega;
+        const double Rd = (a + om1 * om1 * c) * dp->h4;
+        st->Rd = Rd;
+        st->z += 1;
+        st->round_z += 1;
+        if (!isfinite(Rd) || !(Rd > st->target) || st->z >= dp->maxit) {
+            st->mode = 0; // refine with the red correction of this iteration
+        } else {
+            st->dsrc ^= 1;
+        }
+    }
+    if (stop) {
+        st->stop = 1;
+        st->final_red = 0;
+    }
+    return stop;
+}
+
 } // namespace ss4d

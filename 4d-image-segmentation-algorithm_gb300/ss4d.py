@@ -155,6 +155,8 @@ def lib() -> C.CDLL:
         "ss4d_batch_create": ([C.c_int, C.POINTER(Dims), vp, C.POINTER(vp)], st),
         "ss4d_batch_destroy": ([vp], st),
         "ss4d_batch_set_graph": ([vp, C.c_int], st),
+        "ss4d_batch_set_arith": ([vp, C.c_int], st),
+        "ss4d_batch_set_extrapolation": ([vp, C.c_int], st),
         "ss4d_batch_set_shape": ([vp, C.c_int, C.c_int, C.c_int], st),
         "ss4d_batch_autotune": ([vp, C.POINTER(Params), C.POINTER(vp), C.POINTER(vp), C.POINTER(C.c_int),
                                  C.POINTER(C.c_int)], st),
@@ -490,7 +492,8 @@ class Solver:
 
 class Batch:
     """ss4d_batch: many volumes (uneven sizes, own parameters) stepped together
-    in the plain FP64 form, one persistent launch per half-sweep for all."""
+    in the plain FP64 form (or the mixed form, set_arith), one persistent launch
+    per loop kernel for all."""
 
     def __init__(self, dims_list, stream: int | None = None):
         self.L = lib()
@@ -522,6 +525,12 @@ class Batch:
 
     def set_shape(self, v: int, xt: int, k_block: int):
         _check(self.L.ss4d_batch_set_shape(self.h, v, xt, k_block), "batch_set_shape")
+
+    def set_arith(self, arith: str):
+        _check(self.L.ss4d_batch_set_arith(self.h, ARITH[arith]), "batch_set_arith")
+
+    def set_extrapolation(self, order: int):
+        _check(self.L.ss4d_batch_set_extrapolation(self.h, order), "batch_set_extrapolation")
 
     @staticmethod
     def _args(params, us, gs):

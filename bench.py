@@ -560,7 +560,11 @@ def run_batch(args):
     """16 independent volumes, sizes U[64..192] x U[64..192] x U[48..96] x
     U[8..24] per axis, single-ellipsoid scenes with per-volume K in
     [500, 2000] and tau in [0.25, 1], stepped together (one persistent launch
-    per half-sweep, per-volume convergence, autotuned tile shapes)."""
+    per loop kernel, per-volume convergence, autotuned tile shapes), in the
+    forms of --forms among fp64, mixed and extrap (mixed with the cubic
+    extrapolated start), each from the same start; `value` is the FP64 form's
+    (or the first form's) aggregate voxel-updates/s, every form's numbers are
+    in `forms`."""
     import numpy as np
     import torch
 
@@ -570,7 +574,7 @@ def run_batch(args):
     sizes = [(int(rng.integers(64, 193)), int(rng.integers(64, 193)), int(rng.integers(48, 97)),
               int(rng.integers(8, 25))) for _ in range(16)]
     dev = torch.device("cuda", 0)
-    params, us, gs = [], [], []
+    params, u0s, gs = [], [], []
     for v, (nx, ny, nz, nt) in enumerate(sizes):
         p = ss4d.scene_params(K=float(rng.uniform(500, 2000)), tau=float(rng.uniform(0.25, 1.0)))
         i0h, u0h = ss4d.scene(1, nx, ny, nz, nt, seed=args.seed + 100 + v, threads=os.cpu_count() or 1)
@@ -580,30 +584,62 @@ def run_batch(args):
             S.edge_detector(p, i0, None, g)
             S.synchronize()
         params.append(p)
-        us.append(torch.from_numpy(u0h).to(dev))
+        u0s.append(torch.from_numpy(u0h).to(dev))
         gs.append(g)
-    B = ss4d.Batch([(nx + 2, ny + 2, nz + 2, nt + 2) for nx, ny, nz, nt in sizes])
-    shapes = B.autotune(params, us, gs)
-    for _ in range(args.warmup):
-        B.seg_time_step(params, us, gs)
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    its = []
-    for _ in range(args.steps):
-        its.append([s["iterations"] for s in B.seg_time_step(params, us, gs)])
-    torch.cuda.synchronize(dev)
-    sec = time.perf_counter() - t0
+    dims = [(nx + 2, ny + 2, nz + 2, nt + 2) for nx, ny, nz, nt in sizes]
     vox = [nx * ny * nz * nt for nx, ny, nz, nt in sizes]
-    updates = sum(v * z for step in its for v, z in zip(vox, step))
-    B.close()
-    print(json.dumps({"metric": "aggregate voxel-updates/s, 16 uneven volumes (batched persistent launch)",
-                      "value": updates / sec, "unit": "voxel-updates/s", "n_gpus": 1, "steps": args.steps,
-                      "warmup": args.warmup, "ms_per_step": sec * 1e3 / args.steps, "higher_is_better": True,
-                      "dtype": "f64", "data": "synthetic", "impl": "ours",
-                      "config": {"workload": "16 volumes U[64..192]x U[64..192]x U[48..96]x U[8..24], kind-1 "
-                                             "scenes, K~U[500,2000], tau~U[0.25,1], gsTol 1e-6",
-                                 "sizes": sizes, "voxels": sum(vox)},
-                      "autotuned_shapes": shapes, "iterations_per_volume": its}))
+    forms = [f for f in args.forms.split(",") if f in ("fp64", "mixed", "extrap")] or ["fp64"]
+    stream = torch.cuda.current_stream(dev)
+    shapes = None
+    results = {}
+    for form in forms:
+        us = [u.clone() for u in u0s]
+        B = ss4d.Batch(dims, stream=stream.cuda_stream)
+        B.set_graph(not args.no_graph)
+        if form != "fp64":
+            B.set_arith("mixed")
+        if form == "extrap":
+            B.set_extrapolation(EXTRAP_ORDER)
+        if shapes is None:
+            shapes = B.autotune(params, us, gs)
+        else:
+            for v, (xt, kb) in enumerate(shapes):
+                B.set_shape(v, xt, kb)
+        for _ in range(args.warmup):
+            B.seg_time_step(params, us, gs)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        stats = [B.seg_time_step(params, us, gs) for _ in range(args.steps)]
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1)
+        B.close()
+        its = [[s["iterations"] for s in step] for step in stats]
+        updates = sum(vv * z for step in its for vv, z in zip(vox, step))
+        results[form] = {"ms_per_step": ms / args.steps, "voxel_updates_per_s": updates / (ms / 1e3),
+                         "volume_steps_per_s": len(sizes) * args.steps / (ms / 1e3),
+                         "iterations_per_volume": its,
+                         "refinements_per_volume": [[s["refinements"] for s in step] for step in stats],
+                         "max_residual": max(s["residual"] for step in stats for s in step),
+                         "tolerance_met": all(s["residual"] <= p.gsTol or s["iterations"] >= p.maxNoGSIteration
+                                              for step in stats for s, p in zip(step, params))}
+    head = "fp64" if "fp64" in results else forms[0]
+    r = results[head]
+    line = {"metric": "aggregate voxel-updates/s, 16 uneven volumes (batched persistent launch)",
+            "value": r["voxel_updates_per_s"], "unit": "voxel-updates/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+            "dtype": "f64", "data": "synthetic", "impl": "ours",
+            "config": {"workload": "16 volumes U[64..192]x U[64..192]x U[48..96]x U[8..24], kind-1 "
+                                   "scenes, K~U[500,2000], tau~U[0.25,1], gsTol 1e-6", "form": head,
+                       "sizes": sizes, "voxels": sum(vox)},
+            "autotuned_shapes": shapes, "iterations_per_volume": r["iterations_per_volume"],
+            "forms": results}
+    if "fp64" in results:
+        for f in results:
+            if f != "fp64":
+                line[f"{f}_step_speedup_over_fp64"] = results["fp64"]["ms_per_step"] / results[f]["ms_per_step"]
+    print(json.dumps(line))
 
 
 def main():

@@ -326,19 +326,29 @@ ss4d_status ss4d_mcf_exact_solution(ss4d_solver *s, double h, double t, double *
 
 /* ---- batched volumes --------------------------------------------------- */
 /* Many independent volumes, of different sizes and parameters, advanced
- * together in the plain FP64 form.  Every half-sweep of all volumes is ONE
- * persistent launch over the concatenated tiles of the volumes, and the SOR
- * loop is one CUDA graph; each volume keeps its own stopping test
- * (sum r^2 h^4 <= its gsTol, or its maxNoGSIteration) and once it has stopped
- * its tiles return at once.  The reference runs one volume per process, so
- * these entry points have no counterpart there; per volume the arithmetic is
- * that of ss4d_seg_time_step in SS4D_ARITH_FP64 without the rescale (no
- * centres, Mmask == 1).  At most SS4D_BATCH_MAX_VOLUMES volumes. */
+ * together in the plain FP64 form (default) or the mixed form
+ * (ss4d_batch_set_arith).  Every loop kernel (a half-sweep; in the mixed form
+ * also the refinement passes) runs ONE persistent launch over the
+ * concatenated tiles of all volumes, and the SOR loop is one CUDA graph; each
+ * volume keeps its own stopping test (sum r^2 h^4 <= its gsTol, or its
+ * maxNoGSIteration) and once it has stopped its tiles return at once.  The
+ * reference runs one volume per process, so these entry points have no
+ * counterpart there; per volume the arithmetic is that of ss4d_seg_time_step
+ * in the same form without the rescale (no centres, Mmask == 1).  At most
+ * SS4D_BATCH_MAX_VOLUMES volumes. */
 #define SS4D_BATCH_MAX_VOLUMES 64
 typedef struct ss4d_batch ss4d_batch;
 ss4d_status ss4d_batch_create(int n, const ss4d_dims *dims, void *stream, ss4d_batch **out);
 ss4d_status ss4d_batch_destroy(ss4d_batch *b);
 ss4d_status ss4d_batch_set_graph(ss4d_batch *b, int enable);
+/* Arithmetic form of the batched steps: SS4D_ARITH_FP64 (the default) or
+ * SS4D_ARITH_MIXED, each volume as ss4d_seg_time_step does it in that form
+ * (mixed: float-float assembly, FP32 correction sweeps, FP64 refinement and
+ * the FP64 stop test), every loop kernel one launch for all volumes. */
+ss4d_status ss4d_batch_set_arith(ss4d_batch *b, ss4d_arith arith);
+/* Mixed form: start every volume's step from the extrapolation of order
+ * 0..3 of its earlier steps (ss4d_solver_set_extrapolation per volume). */
+ss4d_status ss4d_batch_set_extrapolation(ss4d_batch *b, int order);
 /* Tile shape of volume v: xt threads along x (power of two, 8..256; 0 =
  * automatic) and k-block depth k_block (>= 1).  Results do not depend on it. */
 ss4d_status ss4d_batch_set_shape(ss4d_batch *b, int v, int xt, int k_block);

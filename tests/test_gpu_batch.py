@@ -71,3 +71,64 @@ def test_batch_autotuned_shapes_do_not_change_results(ss4d, oracle, cuda):
     assert out[0][1] == out[1][1]
     for a, b in zip(out[0][0], out[1][0]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("extrap", [0, 3])
+def test_mixed_batch_matches_single_volume_mixed_solves(ss4d, oracle, cuda, extrap):
+    """The mixed form batched (refinement passes and FP32 sweeps of all volumes
+    in one launch each, every volume in its own phase) gives each volume what
+    its own mixed-form solver gives it, step after step, with and without the
+    extrapolated start: the same counts, the same u, the FP64 tolerance met."""
+    torch = cuda
+    sizes = [(20, 16, 12, 5), (33, 9, 14, 7), (12, 24, 10, 3)]
+    vols = _volumes(ss4d, oracle, sizes, seed=11)
+    steps = 5
+    want = []
+    for (p, u0, g), dims in zip(vols, sizes):
+        u = _dev(torch, u0)
+        gd = [_dev(torch, a) for a in g]
+        with ss4d.Solver.for_interior(*dims, arith="mixed") as S:
+            S.set_extrapolation(extrap)
+            rec = []
+            for _ in range(steps):
+                st = S.seg_time_step(p, u, None, gd)
+                rec.append((st["iterations"], st["refinements"], u.cpu().numpy()))
+        want.append(rec)
+    us = [_dev(torch, u0) for _, u0, _ in vols]
+    gs = [[_dev(torch, a) for a in g] for _, _, g in vols]
+    params = [p for p, _, _ in vols]
+    with ss4d.Batch([(d[0] + 2, d[1] + 2, d[2] + 2, d[3] + 2) for d in sizes]) as B:
+        B.set_arith("mixed")
+        B.set_extrapolation(extrap)
+        for step in range(steps):
+            stats = B.seg_time_step(params, us, gs)
+            for v, st in enumerate(stats):
+                its, refs, u_want = want[v][step]
+                assert st["residual"] <= params[v].gsTol, (v, step)
+                assert (st["iterations"], st["refinements"]) == (its, refs), (v, step)
+                assert np.array_equal(us[v].cpu().numpy(), u_want), (v, step)
+
+
+def test_batch_switches_forms(ss4d, oracle, cuda):
+    """One batch run in the FP64 form, then the mixed form, then FP64 again:
+    each form's graph and buffers stay valid, and FP64 steps after the mixed
+    ones equal FP64 steps from the same u."""
+    torch = cuda
+    sizes = [(16, 12, 10, 4), (10, 18, 8, 5)]
+    vols = _volumes(ss4d, oracle, sizes, seed=13)
+    params = [p for p, _, _ in vols]
+    gs = [[_dev(torch, a) for a in g] for _, _, g in vols]
+    dims = [(d[0] + 2, d[1] + 2, d[2] + 2, d[3] + 2) for d in sizes]
+    us = [_dev(torch, u0) for _, u0, _ in vols]
+    with ss4d.Batch(dims) as B:
+        B.seg_time_step(params, us, gs)
+        B.set_arith("mixed")
+        st = B.seg_time_step(params, us, gs)
+        assert all(s["residual"] <= p.gsTol and s["refinements"] >= 1 for s, p in zip(st, params))
+        mid = [u.clone() for u in us]
+        B.set_arith("fp64")
+        B.seg_time_step(params, us, gs)
+    with ss4d.Batch(dims) as B2:
+        B2.seg_time_step(params, mid, gs)
+    for a, b in zip(us, mid):
+        assert np.array_equal(a.cpu().numpy(), b.cpu().numpy())

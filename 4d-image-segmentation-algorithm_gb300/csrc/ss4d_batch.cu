@@ -68,6 +68,18 @@ ss4d_status bfail(ss4d_status st, const char *fmt, ...)
 // ---------------------------------------------------------------------------
 // kernels
 
+// The grid-stride tile index that jumps a block from volume v to its first
+// tile of volume v + 1 (the loop's t += gridDim.x lands on it): a volume the
+// kernel does not work on costs a block one step, not one per tile.
+__device__ __forceinline__ long long skip_to_next_volume(const BVol *__restrict__ vols, int v, long long total)
+{
+    const long long n0 = vols[v + 1].tile0, G = gridDim.x;
+    long long off = ((long long)blockIdx.x - n0) % G;
+    if (off < 0)
+        off += G;
+    return n0 + off - G;
+}
+
 // Walks the block's tiles of all volumes (grid-stride over the concatenated
 // tile lists).  For every target of a volume that want(v) admits it calls
 // body(v, V, g, sp, tc, p, s); when the block moves on from volume v it calls
@@ -85,8 +97,12 @@ __device__ __forceinline__ void walk_targets(const BVol *__restrict__ vols, int 
                 ++v;
             while (v + 1 < nv && t >= vols[v + 1].tile0);
         }
-        if (!want(v))
-            continue; // the whole block skips: v is uniform
+        if (!want(v)) { // the whole block skips: v is uniform
+            if (v + 1 >= nv)
+                break;
+            t = skip_to_next_volume(vols, v, total);
+            continue;
+        }
         const BVol &V = vols[v];
         const Geo g = V.g;
         const Split sp = V.sp;
@@ -159,7 +175,8 @@ __global__ void __launch_bounds__(256) k_bsweep64(const BVol *__restrict__ vols,
             while (v + 1 < nv && t >= vols[v + 1].tile0);
         }
         if (st[v].stop)
-            continue; // the whole block skips: v is uniform
+            continue; // the whole block skips: v is uniform (a jump to the next
+                      // volume, as walk_targets does, measured 4 % slower here)
         const BVol &V = vols[v];
         const Geo g = V.g;
         const Split sp = V.sp;

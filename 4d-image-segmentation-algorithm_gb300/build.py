@@ -37,6 +37,7 @@ CUDA_UNITS = {
     "ss4d_ws.cu": [],
     "ss4d_nn.cu": [],
     "ss4d_assemble_ff.cu": [],
+    "ss4d_front_ff.cu": [],
 }
 C_UNITS = {"ss4d_scene.c": ["-fopenmp"], "ss4d_vtk.c": []}
 

@@ -101,6 +101,7 @@ struct ss4d_solver {
     double *h_scalar; // pinned mirror
     // natural-layout scratch
     double *d_scratch;
+    float2 *d_ff;      // mixed form's edge detector: 3 float-float volumes (image, thresholded image, prev)
     double *d_coef_nat; // 8 arrays (reference arithmetic)
     // split form
     SplitBufs sb;
@@ -305,7 +306,7 @@ extern "C" ss4d_status ss4d_solver_destroy(ss4d_solver *s)
     void *dev[] = {s->d_partial, s->d_scalar, s->d_state, s->d_params, s->d_scratch, s->d_coef_nat,
                    s->sb.R[0], s->sb.P[0], s->sb.coef[0], s->sb.coef32[0], s->sb.dR[0], s->sb.r32[0], s->sb.fn[0],
                    s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz, s->ws_x0, s->ws_y,
-                   s->hist[0], s->hist[1], s->hist[2], s->hist[3], s->sb.fd[0]};
+                   s->hist[0], s->hist[1], s->hist[2], s->hist[3], s->sb.fd[0], s->d_ff};
     for (void *p : dev)
         if (p)
             cudaFree(p);
@@ -393,6 +394,13 @@ static ss4d_status ensure_scratch(ss4d_solver *s)
 {
     if (!s->d_scratch)
         CKS(dmalloc(s, (void **)&s->d_scratch, sizeof(double) * s->geo.n));
+    return SS4D_OK;
+}
+
+static ss4d_status ensure_ff_front(ss4d_solver *s)
+{
+    if (!s->d_ff)
+        CKS(dmalloc(s, (void **)&s->d_ff, sizeof(float2) * 3 * s->geo.n));
     return SS4D_OK;
 }
 
@@ -950,6 +958,59 @@ extern "C" ss4d_status ss4d_reflect(ss4d_solver *s, double *d_img)
     return last_launch();
 }
 
+// The mixed form's presmoothing: the same SOR on float-float copies of the
+// image (slot 0 or 1 of d_ff) and of its input (slot 2), written back to
+// the image's interior at the end; the float-float result stays in its slot
+// for the g faces.  prev (the reference's prev_u) receives the input as in
+// the FP64 forms.
+static ss4d_status presmooth_ff(ss4d_solver *s, const ss4d_params *p, double *d_img, double *prev, int slot,
+                                ss4d_step_stats *stats)
+{
+    CKS(ensure_ff_front(s));
+    const Geo &g = s->geo;
+    float2 *v = s->d_ff + (size_t)slot * g.n, *pf = s->d_ff + 2 * (size_t)g.n;
+    CK(cudaEventRecord(s->ev0, s->stream));
+    CK(cudaMemcpyAsync(prev, d_img, sizeof(double) * g.n, cudaMemcpyDeviceToDevice, s->stream));
+    launch_reflect(g, d_img, s->stream);
+    launch_to_ff(g, d_img, v, s->stream);
+    launch_to_ff(g, prev, pf, s->stream);
+    s->launches += 6;
+    const double c = p->sigma / (p->h * p->h), h4 = p->h * p->h * p->h * p->h;
+    const long long nb = front_resid_blocks(g);
+    // the residual's squares are summed in FP32 per thread: a test within
+    // 1e-6 of gsTol is reported as near the tolerance
+    const double band = fabs(p->gsTol) * 1e-6;
+    double R = 0.0, R1 = 0.0;
+    int z = 0, near = 0;
+    do {
+        z = z + 1;
+        launch_presmooth_half_ff(g, v, pf, c, p->omega_sigma, 0, s->stream);
+        launch_presmooth_half_ff(g, v, pf, c, p->omega_sigma, 1, s->stream);
+        launch_presmooth_resid_ff(g, v, pf, c, h4, s->d_partial, s->stream);
+        s->launches += 3 + launch_reduce_sum(s->d_partial, nb, s->d_scalar, s->stream);
+        CKS(last_launch());
+        CKS(read_scalar(s, 0, &R));
+        if (z == 1)
+            R1 = R;
+        near |= fabs(R - p->gsTol) <= band;
+    } while (R > p->gsTol && z < p->maxNoGSIteration_sigma);
+    launch_from_ff(g, v, d_img, s->stream);
+    s->launches += 1;
+    CKS(last_launch());
+    CK(cudaEventRecord(s->ev1, s->stream));
+    CK(cudaEventSynchronize(s->ev1));
+    if (stats) {
+        memset(stats, 0, sizeof *stats);
+        stats->iterations = z;
+        stats->residual = R;
+        stats->first_residual = R1;
+        stats->near_tolerance = near;
+        cudaEventElapsedTime(&stats->ms, s->ev0, s->ev1);
+        stats->status = isfinite(R) ? SS4D_OK : SS4D_ERR_NONFINITE;
+    }
+    return SS4D_OK;
+}
+
 extern "C" ss4d_status ss4d_presmooth_step(ss4d_solver *s, const ss4d_params *p, double *d_img, double *d_scratch,
                                            ss4d_step_stats *stats)
 {
@@ -960,6 +1021,8 @@ extern "C" ss4d_status ss4d_presmooth_step(ss4d_solver *s, const ss4d_params *p,
         CKS(ensure_scratch(s));
         prev = s->d_scratch;
     }
+    if (s->arith == SS4D_ARITH_MIXED)
+        return presmooth_ff(s, p, d_img, prev, 0, stats);
     const Geo &g = s->geo;
     CK(cudaEventRecord(s->ev0, s->stream));
     CK(cudaMemcpyAsync(prev, d_img, sizeof(double) * g.n, cudaMemcpyDeviceToDevice, s->stream));
@@ -1032,6 +1095,22 @@ extern "C" ss4d_status ss4d_edge_detector(ss4d_solver *s, const ss4d_params *p, 
     for (int f = 0; f < 8; ++f) {
         REQ(d_g[f], "a g array is NULL");
         go.p[f] = d_g[f];
+    }
+    if (s->arith == SS4D_ARITH_MIXED) {
+        // float-float presmoothing of both images, g faces from the
+        // float-float results
+        double *prev = d_scratch;
+        if (!prev) {
+            CKS(ensure_scratch(s));
+            prev = s->d_scratch;
+        }
+        CKS(presmooth_ff(s, p, d_i0, prev, 0, nullptr));
+        if (d_i0_thr)
+            CKS(presmooth_ff(s, p, d_i0_thr, prev, 1, nullptr));
+        launch_gfaces_ff(s->geo, s->d_ff, d_i0_thr ? s->d_ff + s->geo.n : nullptr, go, p->h, p->K, p->theta_img,
+                         p->rho_thr, s->stream);
+        s->launches += 1;
+        return last_launch();
     }
     CKS(ss4d_presmooth_step(s, p, d_i0, d_scratch, nullptr));
     if (d_i0_thr)

@@ -135,6 +135,22 @@ void launch_pack(const Geo &g, const Split &s, const double *u, const double *pr
 // mixed form: the same coefficient records from float-float arithmetic (3 kernels)
 void launch_assemble_ff(const Geo &g, const Split &s, const double *u, CPtrs8 gin, int has_g, const ss4d_params &p,
                         SplitBufs b, int sm_count, cudaStream_t st);
+
+// the mixed form's edge detector in float-float arithmetic (ss4d_front_ff.cu);
+// float2 arrays hold (high, low) pairs in the natural layout
+struct FFc {
+    float h, l; // a constant split on the host
+};
+FFc split_ff(double v);
+void launch_to_ff(const Geo &g, const double *a, float2 *out, cudaStream_t st);
+void launch_from_ff(const Geo &g, const float2 *v, double *out, cudaStream_t st); // interior only
+void launch_presmooth_half_ff(const Geo &g, float2 *v, const float2 *prev, double c, double omega, int colour,
+                              cudaStream_t st);
+long long front_resid_blocks(const Geo &g); // partials of launch_presmooth_resid_ff
+void launch_presmooth_resid_ff(const Geo &g, const float2 *v, const float2 *prev, double c, double h4,
+                               double *partial, cudaStream_t st);
+void launch_gfaces_ff(const Geo &g, const float2 *i0, const float2 *ithr, GPtrs8 gout, double h, double K,
+                      double theta, double rho, cudaStream_t st);
 void launch_pack_coef(const Geo &g, const Split &s, CPtrs8 a, const ss4d_params &p, SplitBufs b, int want32,
                       cudaStream_t st);
 // terms/keep/hist: the mixed form's extrapolated start (k_unpack); hist = {h1 red, h1 black, h2 red, h2 black}

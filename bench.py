@@ -319,7 +319,7 @@ def frontend_balls(nx, ny, nz, nt, seed, per_frame=5, radius=8.0):
              float(rng.integers(lo, nz - lo + 1))) for l in range(1, nt + 1) for _ in range(per_frame)]
 
 
-def run_frontend(args, ctx):
+def run_frontend(args, ctx, arith="fp64"):
     """The reference main's work around the time loop (segmentation4D.c:
     1380-1393: local thresholding, edge detector on both images, initial
     function, rescale; frame conversion for reading and writing; the explicit
@@ -328,8 +328,10 @@ def run_frontend(args, ctx):
     0.5).  Each component: one untimed call, then the median of 3 calls timed
     with CUDA events on the launching stream (inputs restored between calls,
     outside the timed region); algorithmic bytes per call and the fraction of
-    the measured copy bandwidth.  The C oracle times the same sequence on a
-    two-frame sample of the volume on all host cores."""
+    the measured copy bandwidth, in the arithmetic form `arith` (fp64: the
+    reference's FP64 rounding; mixed: the edge detector in float-float).  The
+    C oracle times the same sequence on a two-frame sample of the volume on
+    all host cores (with arith == "fp64" only)."""
     import numpy as np
     import torch
 
@@ -353,7 +355,7 @@ def run_frontend(args, ctx):
     scratch = torch.empty_like(i0)
     out = {}
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ss4d.Solver(*shape[::-1], arith="fp64", stream=stream.cuda_stream) as S:
+    with ss4d.Solver(*shape[::-1], arith=arith, stream=stream.cuda_stream) as S:
 
         def measure(name, setup, fn, bytes_per_call, note):
             """bytes_per_call: a number, or a function of fn's last result"""
@@ -410,6 +412,11 @@ def run_frontend(args, ctx):
     torch.cuda.empty_cache()
     total = sum(v["ms"] for k, v in out.items() if k in ("local_threshold", "edge_detector", "initial_function",
                                                           "rescale"))
+    res = {"workload": f"{nx}x{ny}x{nz}x{nt}, {len(balls)} balls of radius {R:g} (5 per frame)", "arith": arith,
+           "peak": hbm, "peak_source": how, "components": out, "main_front_end_ms": total,
+           "gpu_ms_per_frame": total / nt}
+    if arith != "fp64":
+        return res
 
     # the oracle on a two-frame sample: the same front-end sequence
     ntc = 2
@@ -425,12 +432,9 @@ def run_frontend(args, ctx):
     oracle.generate_segm(R, cu0, cmm, cb)
     oracle.rescale(R, cu0, cmm, cb)
     cpu_ms = (time.perf_counter() - t0) * 1e3
-    return {"workload": f"{nx}x{ny}x{nz}x{nt}, {len(balls)} balls of radius {R:g} (5 per frame)",
-            "peak": hbm, "peak_source": how, "components": out,
-            "main_front_end_ms": total,
-            "cpu": {"ms": cpu_ms, "frames": ntc, "ms_per_frame": cpu_ms / ntc, "cores": threads, "kind": "port",
-                    "sequence": "local threshold, edge detector, initial function, rescale"},
-            "gpu_ms_per_frame": total / nt}
+    res["cpu"] = {"ms": cpu_ms, "frames": ntc, "ms_per_frame": cpu_ms / ntc, "cores": threads, "kind": "port",
+                  "sequence": "local threshold, edge detector, initial function, rescale"}
+    return res
 
 
 def run_e2e(args, form, ctx):
@@ -697,7 +701,8 @@ def main():
         except Exception as ex:  # reported, not hidden
             line["e2e"] = {"value": None, "unit": "time-steps/s", "error": repr(ex)}
     if rank == 0 and world == 1 and not args.no_frontend:
-        line["frontend"] = run_frontend(args, ctx)
+        line["frontend"] = run_frontend(args, ctx, "fp64")
+        line["frontend_mixed"] = run_frontend(args, ctx, "mixed")
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args)
     if dist:

@@ -181,7 +181,10 @@ ss4d_status ss4d_reflect(ss4d_solver *s, double *d_img);
 /* _presmoothStep_ (segmentation4D.c:337-409): one implicit heat step
  * (I - sigma*Laplace) v = img solved in place by red-black SOR with omega_sigma;
  * d_scratch receives the copy of the input that the reference keeps in its
- * global prev_u (may be NULL: the handle then uses its own). */
+ * global prev_u (may be NULL: the handle then uses its own).  The reference
+ * and FP64 forms keep the reference's FP64 rounding bit for bit; the mixed
+ * form iterates in float-float arithmetic (about 48 significant bits, within
+ * 1e-13 of it), as does its ss4d_edge_detector. */
 ss4d_status ss4d_presmooth_step(ss4d_solver *s, const ss4d_params *p, double *d_img,
                                 double *d_scratch, ss4d_step_stats *stats);
 

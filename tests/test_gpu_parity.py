@@ -405,3 +405,32 @@ def test_allocation_failure_is_reported_and_the_context_survives(ss4d, cuda):
         u = dev(torch, d["u0"])
         st = S.seg_time_step(p, u, None, g)
     assert st["iterations"] == d["its"][0]
+
+
+@pytest.mark.parametrize("fixture", ["seg_small.npz", "seg_balls.npz"])
+def test_mixed_edge_detector_is_close_to_reference(ss4d, cuda, fixture):
+    """The mixed form runs the edge detector in float-float arithmetic
+    (about 48 significant bits on the FP32 pipe): the smoothed images within
+    1e-13 and the g faces within 1e-12 of the reference's FP64 values, the
+    same presmoothing iteration counts, and the reference's prev_u copy."""
+    torch = cuda
+    d = load_golden(fixture)
+    p = params_from_golden(ss4d, d)
+    shape = d["i0_in"].shape
+    i0 = dev(torch, d["i0_in"])
+    thr = dev(torch, d["thr_in"])
+    g = zeros8(torch, shape)
+    with ss4d.Solver(*shape[::-1], arith="mixed") as S:
+        S.edge_detector(p, i0, thr, g)
+        one = dev(torch, d["i0_in"])
+        prev = torch.zeros_like(one)
+        st = S.presmooth_step(p, one, prev)
+        S.synchronize()
+    assert rel_err(host(i0), d["i0_smooth"]) <= 1e-13
+    assert rel_err(host(thr), d["thr_smooth"]) <= 1e-13
+    for f in range(8):
+        assert rel_err(host(g[f]), d[f"g{f}"]) <= 1e-12, f"g face {f}"
+    if "presmooth_its" in d:  # the fixtures that recorded the reference's counts
+        assert st["iterations"] == d["presmooth_its"][0]
+    assert np.array_equal(host(prev), d["i0_in"])
+    assert rel_err(host(one), d["i0_smooth"]) <= 1e-13

@@ -1085,6 +1085,83 @@ extern "C" ss4d_status ss4d_presmooth_explicit(ss4d_solver *s, const ss4d_params
     return last_launch();
 }
 
+// taps of ss4d_gaussian_smooth: w_m = exp(-m^2 / (2 sigma^2)) / sum over
+// |m| <= R = ceil(3 sigma), the sum formed as w_0 + 2 w_1 + 2 w_2 + ... (the
+// doubling is exact, so a multiply-add gives the same sum)
+static ss4d_status gauss_weights(double sigma, GaussWeights *W)
+{
+    const double r = ceil(3.0 * sigma);
+    REQ(r <= SS4D_GAUSS_MAX_RADIUS, "a Gaussian radius ceil(3 sigma) exceeds SS4D_GAUSS_MAX_RADIUS");
+    W->R = (int)r;
+    double sum = 0.0;
+    for (int m = 0; m <= W->R; ++m) {
+        W->w[m] = exp(-(double)(m * m) / (2.0 * sigma * sigma));
+        sum += (m ? 2.0 : 1.0) * W->w[m];
+    }
+    for (int m = 0; m <= W->R; ++m)
+        W->w[m] = W->w[m] / sum;
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_gaussian_smooth(ss4d_solver *s, const double sigma[4], double *d_img, double *d_scratch)
+{
+    REQ(s && sigma && d_img, "NULL argument");
+    GaussWeights W[4];
+    for (int a = 0; a < 4; ++a) {
+        REQ(isfinite(sigma[a]) && sigma[a] >= 0.0, "sigma must be finite and >= 0");
+        if (sigma[a] > 0.0)
+            CKS(gauss_weights(sigma[a], &W[a]));
+    }
+    double *tmp = d_scratch;
+    if (!tmp) {
+        CKS(ensure_scratch(s));
+        tmp = s->d_scratch;
+    }
+    const Geo &g = s->geo;
+    double *src = d_img, *dst = tmp;
+    for (int a = 0; a < 4; ++a) {
+        if (sigma[a] == 0.0)
+            continue;
+        launch_gauss_axis(g, a, src, dst, W[a], s->stream);
+        s->launches += 1;
+        double *t = src;
+        src = dst;
+        dst = t;
+    }
+    if (src != d_img)
+        CK(cudaMemcpyAsync(d_img, src, sizeof(double) * g.n, cudaMemcpyDeviceToDevice, s->stream));
+    launch_reflect(g, d_img, s->stream);
+    s->launches += 4;
+    return last_launch();
+}
+
+extern "C" ss4d_status ss4d_gfaces(ss4d_solver *s, const ss4d_params *p, const double *d_i0, const double *d_i0_thr,
+                                   double *const d_g[8])
+{
+    REQ(s && d_i0 && d_g, "NULL argument");
+    CKS(check_params(p));
+    REQ(d_i0_thr || p->rho_thr == 0.0, "i0_thr may only be NULL when rho_thr == 0");
+    GPtrs8 go;
+    for (int f = 0; f < 8; ++f) {
+        REQ(d_g[f], "a g array is NULL");
+        go.p[f] = d_g[f];
+    }
+    const Geo &g = s->geo;
+    if (s->arith == SS4D_ARITH_MIXED) {
+        CKS(ensure_ff_front(s));
+        launch_to_ff(g, d_i0, s->d_ff, s->stream);
+        if (d_i0_thr)
+            launch_to_ff(g, d_i0_thr, s->d_ff + g.n, s->stream);
+        launch_gfaces_ff(g, s->d_ff, d_i0_thr ? s->d_ff + g.n : nullptr, go, p->h, p->K, p->theta_img, p->rho_thr,
+                         s->stream);
+        s->launches += d_i0_thr ? 3 : 2;
+    } else {
+        launch_gfaces(g, d_i0, d_i0_thr, go, p->h, p->K, p->theta_img, p->rho_thr, s->stream);
+        s->launches += 1;
+    }
+    return last_launch();
+}
+
 extern "C" ss4d_status ss4d_edge_detector(ss4d_solver *s, const ss4d_params *p, double *d_i0, double *d_i0_thr,
                                           double *d_scratch, double *const d_g[8])
 {

@@ -20,6 +20,13 @@ void launch_reflect(const Geo &g, double *u, cudaStream_t st);
 void launch_presmooth_half(const Geo &g, double *v, const double *prev, double c, double omega, int colour,
                            cudaStream_t st);
 void launch_presmooth_explicit(const Geo &g, double *v, const double *prev, double coeff, cudaStream_t st);
+// normalised Gaussian taps w[0..R] of one axis (ss4d_gaussian_smooth)
+struct GaussWeights {
+    double w[SS4D_GAUSS_MAX_RADIUS + 1];
+    int R;
+};
+void launch_gauss_axis(const Geo &g, int axis, const double *in, double *out, const GaussWeights &W,
+                       cudaStream_t st);
 void launch_presmooth_resid(const Geo &g, const double *v, const double *prev, double c, double h4, double *partial,
                             cudaStream_t st);
 void launch_gfaces(const Geo &g, const double *i0, const double *ithr, GPtrs8 gout, double h, double K, double theta,

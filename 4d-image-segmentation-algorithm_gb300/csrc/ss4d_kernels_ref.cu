@@ -201,6 +201,45 @@ __global__ void k_presmooth_explicit(Geo g, double *v, const double *prev, doubl
 }
 
 // ---------------------------------------------------------------------------
+// separable Gaussian along one axis (an option beside the reference's
+// implicit presmoothing, which is not a Gaussian): out = sum_{m=-R..R}
+// w[|m|] in(c + m) in order of m, the coordinate mirrored about the volume's
+// faces as the reference's reflection does (ghost 0 = voxel 1:
+// x < 1 -> 1 - x, x > n -> 2n + 1 - x); interior voxels only
+
+__device__ inline int gauss_mirror(int x, int n)
+{
+    // each two reflections move x by 2n towards [1, n]: |x| <= R + n needs
+    // fewer than 2 R / n + 2 steps (R <= SS4D_GAUSS_MAX_RADIUS)
+    for (int q = 0; q < 4 * SS4D_GAUSS_MAX_RADIUS + 4; ++q) {
+        if (x < 1)
+            x = 1 - x;
+        else if (x > n)
+            x = 2 * n + 1 - x;
+        else
+            break;
+    }
+    return x;
+}
+
+template <int AXIS>
+__global__ void k_gauss_axis(Geo g, const double *__restrict__ in, double *__restrict__ out, GaussWeights W)
+{
+    int i, j, k, l;
+    if (!interior_ijkl(g, i, j, k, l))
+        return;
+    const int c[4] = {i, j, k, l};
+    const int n[4] = {g.nx, g.ny, g.nz, g.nt};
+    const long long st[4] = {1, g.sy, g.sz, g.sw};
+    const long long o = nat_index(g, i, j, k, l);
+    const long long base = o - (long long)c[AXIS] * st[AXIS];
+    double acc = 0.0;
+    for (int m = -W.R; m <= W.R; ++m)
+        acc = acc + W.w[m < 0 ? -m : m] * in[base + (long long)gauss_mirror(c[AXIS] + m, n[AXIS]) * st[AXIS]];
+    out[o] = acc;
+}
+
+// ---------------------------------------------------------------------------
 // face gradients (segmentation4D.c:455-548, :594-821): normal component
 // (v[nb]-v[c])/h, tangential ((v[nb+a]+v[c+a]) - (v[nb-a]+v[c-a]))/(4h),
 // squares summed in x, y, z, w order.
@@ -815,6 +854,21 @@ void launch_presmooth_resid(const Geo &g, const double *v, const double *prev, d
     dim3 gr, bl;
     resid_cfg(g, gr, bl);
     k_presmooth_resid<<<gr, bl, 0, st>>>(g, v, prev, c, 1 + c * 8, h4, partial);
+}
+
+void launch_gauss_axis(const Geo &g, int axis, const double *in, double *out, const GaussWeights &W,
+                       cudaStream_t st)
+{
+    dim3 gr, bl;
+    interior_cfg(g, gr, bl);
+    if (axis == 0)
+        k_gauss_axis<0><<<gr, bl, 0, st>>>(g, in, out, W);
+    else if (axis == 1)
+        k_gauss_axis<1><<<gr, bl, 0, st>>>(g, in, out, W);
+    else if (axis == 2)
+        k_gauss_axis<2><<<gr, bl, 0, st>>>(g, in, out, W);
+    else
+        k_gauss_axis<3><<<gr, bl, 0, st>>>(g, in, out, W);
 }
 
 void launch_presmooth_explicit(const Geo &g, double *v, const double *prev, double coeff, cudaStream_t st)

@@ -148,6 +148,8 @@ def lib() -> C.CDLL:
         "ss4d_copy_to_host": ([vp, vp, vp, C.c_size_t], st),
         "ss4d_copy_to_device_side": ([vp, vp, vp, C.c_size_t], st),
         "ss4d_presmooth_explicit": ([vp, C.POINTER(Params), C.c_int, vp, vp], st),
+        "ss4d_gaussian_smooth": ([vp, dp, vp, vp], st),
+        "ss4d_gfaces": ([vp, C.POINTER(Params), vp, vp, P8], st),
         "ss4d_join_side": ([vp], st),
         "ss4d_copy_device": ([vp, vp, vp, C.c_size_t], st),
         "ss4d_synchronize": ([vp], st),
@@ -377,6 +379,15 @@ class Solver:
         """_presmoothStepEXP_ on img; scratch (optional) receives the reference's prev_u"""
         _check(self.L.ss4d_presmooth_explicit(self.h, C.byref(p), int(steps), _ptr(img), _ptr(scratch)),
                "presmooth_explicit")
+
+    def gaussian_smooth(self, sigma, img, scratch=None):
+        """separable Gaussian, sigma per axis (x, y, z, t), in place on img"""
+        s = (C.c_double * 4)(*[float(x) for x in sigma])
+        _check(self.L.ss4d_gaussian_smooth(self.h, s, _ptr(img), _ptr(scratch)), "gaussian_smooth")
+
+    def gfaces(self, p: Params, i0, i0_thr, g8):
+        """the 8 face g values from images already smoothed"""
+        _check(self.L.ss4d_gfaces(self.h, C.byref(p), _ptr(i0), _ptr(i0_thr), _p8(g8)), "gfaces")
 
     def edge_detector(self, p: Params, i0, i0_thr, g8, scratch=None):
         _check(self.L.ss4d_edge_detector(self.h, C.byref(p), _ptr(i0), _ptr(i0_thr), _ptr(scratch), _p8(g8)),

@@ -199,6 +199,26 @@ ss4d_status ss4d_presmooth_step(ss4d_solver *s, const ss4d_params *p, double *d_
 ss4d_status ss4d_presmooth_explicit(ss4d_solver *s, const ss4d_params *p, int timeStepsNum,
                                     double *d_img, double *d_scratch);
 
+/* A true Gaussian G_sigma, an option beside the reference's "G_sigma"
+ * (the implicit heat step of ss4d_presmooth_step; no counterpart in the
+ * reference): d_img is convolved axis by axis (x, y, z, t) with the
+ * normalised taps w_m = exp(-m^2 / (2 sigma_a^2)) / sum, |m| <= R_a =
+ * ceil(3 sigma_a) (sigma_a == 0 leaves axis a alone), over the interior
+ * voxels, the volume mirrored about its faces as the reference's reflection
+ * mirrors it (ghost 0 = voxel 1); then the ghost layer is set by that
+ * reflection.  Each tap sum runs in order of m, every product and sum
+ * rounded separately, in FP64 in every arithmetic form.  R_a must not
+ * exceed SS4D_GAUSS_MAX_RADIUS.  d_scratch (NULL = internal) is overwritten. */
+#define SS4D_GAUSS_MAX_RADIUS 32
+ss4d_status ss4d_gaussian_smooth(ss4d_solver *s, const double sigma[4], double *d_img, double *d_scratch);
+
+/* The edge detector's second half (segmentation4D.c:594-821, _gFunction_
+ * :67-70): the 8 face g values from images already smoothed (by
+ * ss4d_gaussian_smooth, for instance), in the handle's arithmetic form as
+ * ss4d_edge_detector computes them.  d_i0_thr may be NULL when rho_thr == 0. */
+ss4d_status ss4d_gfaces(ss4d_solver *s, const ss4d_params *p, const double *d_i0, const double *d_i0_thr,
+                        double *const d_g[8]);
+
 /* _gf_inputImage_plus_thresholdedImage_ (segmentation4D.c:582-823): presmooth
  * d_i0 and d_i0_thr in place, then the 8 face values of the edge detector
  * g_f = 1/(1 + K (theta_img |grad I0|_f^2 + rho_thr |grad Ithr|_f^2)) into

@@ -108,6 +108,14 @@ def presmooth_explicit(p, steps: int, v: np.ndarray, scratch: np.ndarray | None 
     return scratch
 
 
+def gaussian(sigma, v: np.ndarray, scratch: np.ndarray | None = None) -> int:
+    """separable Gaussian with sigma per axis (x, y, z, t) in place on v"""
+    d = _dims(v.shape)
+    scratch = np.zeros_like(v) if scratch is None else scratch
+    s = (C.c_double * 4)(*[float(x) for x in sigma])
+    return lib().or_gaussian(C.byref(d), s, C.c_void_p(_d(v)), C.c_void_p(_d(scratch)))
+
+
 def gfaces(p, i0: np.ndarray, ithr: np.ndarray):
     d = _dims(i0.shape)
     g = new_like(i0, 8)

@@ -302,6 +302,64 @@ void or_presmooth_explicit(const ss4d_dims *d, const ss4d_params *p, int steps, 
     }
 }
 
+/* A true Gaussian beside the reference's implicit presmoothing (no
+ * counterpart in the reference): per axis with sigma > 0, taps w_m =
+ * exp(-m^2 / (2 sigma^2)) / (w_0 + 2 w_1 + ... ), |m| <= ceil(3 sigma), the
+ * sum over m = -R..R in order, coordinates mirrored about the volume's faces
+ * (x < 1 -> 1 - x, x > n -> 2n + 1 - x, as the reference's reflection
+ * copies voxel 1 into ghost 0); then the ghost layer by reflection.
+ * Returns -1 when a radius exceeds 32. */
+static int mirror_idx(int x, int n)
+{
+    while (x < 1 || x > n)
+        x = x < 1 ? 1 - x : 2 * n + 1 - x;
+    return x;
+}
+
+int or_gaussian(const ss4d_dims *d, const double sigma[4], double *v, double *scratch)
+{
+    geo_t g = geo_of(d);
+    const ptrdiff_t st[4] = {g.sx, g.sy, g.sz, g.sw};
+    const int n[4] = {g.iM - 2, g.jM - 2, g.kM - 2, g.lM - 2};
+    double *src = v, *dst = scratch;
+    for (int a = 0; a < 4; ++a) {
+        if (!(sigma[a] > 0.0))
+            continue;
+        const double r = ceil(3.0 * sigma[a]);
+        if (r > 32)
+            return -1;
+        const int R = (int)r;
+        double w[33], sum = 0.0;
+        for (int m = 0; m <= R; ++m) {
+            w[m] = exp(-(double)(m * m) / (2.0 * sigma[a] * sigma[a]));
+            sum += (m ? 2.0 : 1.0) * w[m];
+        }
+        for (int m = 0; m <= R; ++m)
+            w[m] = w[m] / sum;
+        int l;
+#pragma omp parallel for schedule(static)
+        for (l = 1; l <= g.lM - 2; l++)
+            for (int k = 1; k <= g.kM - 2; k++)
+                for (int j = 1; j <= g.jM - 2; j++)
+                    for (int i = 1; i <= g.iM - 2; i++) {
+                        const int c[4] = {i, j, k, l};
+                        const ptrdiff_t o = at(&g, i, j, k, l);
+                        const ptrdiff_t base = o - (ptrdiff_t)c[a] * st[a];
+                        double acc = 0.0;
+                        for (int m = -R; m <= R; ++m)
+                            acc = acc + w[m < 0 ? -m : m] * src[base + (ptrdiff_t)mirror_idx(c[a] + m, n[a]) * st[a]];
+                        dst[o] = acc;
+                    }
+        double *t = src;
+        src = dst;
+        dst = t;
+    }
+    if (src != v)
+        or_copy(d, src, v);
+    or_reflect(d, v);
+    return 0;
+}
+
 /* ---------------------------------------------------------------------- */
 /* edge detector                                                            */
 

@@ -263,9 +263,12 @@ __device__ inline bool ctrl_mixed_update(LoopState *st, double a, double c, cons
             stop = true;
         } else {
             st->mode = 1;
-            // aim the round at the tolerance, but not below what FP32
-            // corrections can resolve relative to the current residual
-            st->target = fmax(0.5 * dp->tol, 1e-11 * R);
+            // aim the round just under the tolerance (the FP32 correction
+            // residual tracks the FP64 one after refinement to about 1e-5
+            // relative; a round that falls short only costs another round),
+            // but not below what FP32 corrections can resolve relative to
+            // the current residual
+            st->target = fmax(0.9 * dp->tol, 1e-11 * R);
         }
     } else if (mode == 1) {
         st->mode = 2;

@@ -392,6 +392,8 @@ def run_frontend(args, ctx, arith="fp64"):
         out["presmooth_implicit"]["iterations"] = z
         measure("presmooth_explicit", restore((img, i0)), lambda: S.presmooth_explicit(p, 1, img, scratch),
                 32.0 * n_int, "copy 16 B + read prev 8 B + write u 8 B per voxel")
+        measure("gaussian_sigma1_xyz", restore((img, i0)), lambda: S.gaussian_smooth((1.0, 1.0, 1.0, 0.0), img, scratch),
+                64.0 * n_int, "3 axis passes (read 8 B + write 8 B per voxel each) + copy back 16 B per voxel")
         measure("max4d", lambda: None, lambda: S.max4d(i0), 8.0 * n_pad, "8 B read per voxel")
         measure("local_threshold", restore((thr, u0)), lambda: S.local_threshold(0.85, 0.15, R, i0, thr, balls),
                 8.0 * n_pad + 24.0 * box * len(balls), "max4d pass + per ball box: min/max read, threshold read "

@@ -132,3 +132,28 @@ def test_batch_switches_forms(ss4d, oracle, cuda):
         B2.seg_time_step(params, mid, gs)
     for a, b in zip(us, mid):
         assert np.array_equal(a.cpu().numpy(), b.cpu().numpy())
+
+
+@pytest.mark.parametrize("arith", ["fp64", "mixed"])
+def test_batch_with_minimal_and_ragged_volumes(ss4d, oracle, cuda, arith):
+    """Volumes with a single interior voxel, odd and one-voxel extents next to
+    an ordinary one, batched: each gets what its own solver gives it."""
+    torch = cuda
+    sizes = [(1, 1, 1, 1), (3, 2, 5, 2), (17, 4, 3, 6), (2, 9, 1, 3)]
+    vols = _volumes(ss4d, oracle, sizes, seed=17)
+    want = []
+    for (p, u0, g), dims in zip(vols, sizes):
+        u = _dev(torch, u0)
+        gd = [_dev(torch, a) for a in g]
+        with ss4d.Solver.for_interior(*dims, arith=arith) as S:
+            z = [S.seg_time_step(p, u, None, gd)["iterations"] for _ in range(2)]
+        want.append((z, u.cpu().numpy()))
+    us = [_dev(torch, u0) for _, u0, _ in vols]
+    gs = [[_dev(torch, a) for a in g] for _, _, g in vols]
+    params = [p for p, _, _ in vols]
+    with ss4d.Batch([(d[0] + 2, d[1] + 2, d[2] + 2, d[3] + 2) for d in sizes]) as B:
+        B.set_arith(arith)
+        got = [[s["iterations"] for s in B.seg_time_step(params, us, gs)] for _ in range(2)]
+    for v in range(len(sizes)):
+        assert [got[0][v], got[1][v]] == want[v][0], v
+        assert np.array_equal(us[v].cpu().numpy(), want[v][1]), v

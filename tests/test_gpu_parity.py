@@ -471,3 +471,20 @@ def test_gaussian_smooth_refuses_wide_taps(ss4d, cuda):
         with pytest.raises(ss4d.SS4DError) as ei:
             S.gaussian_smooth((11.0, 0.0, 0.0, 0.0), torch.zeros((5, 8, 8, 8), dtype=torch.float64, device="cuda"))
         assert ei.value.status == 1
+
+
+def test_gaussian_smooth_with_taps_wider_than_the_volume(ss4d, oracle, cuda):
+    """A radius of 3 taps on extents of 1, 2 and 3 voxels: the mirrored
+    coordinates fold more than once, bit for bit as the oracle folds them."""
+    torch = cuda
+    rng = np.random.default_rng(6)
+    shape = (5, 3, 4, 3)  # interior t 3, z 1, y 2, x 1
+    a = rng.random(shape)
+    sigma = (1.0, 1.0, 1.0, 1.0)
+    want = a.copy()
+    assert oracle.gaussian(sigma, want) == 0
+    with ss4d.Solver(*shape[::-1]) as S:
+        da = dev(torch, a)
+        S.gaussian_smooth(sigma, da)
+        S.synchronize()
+    assert np.array_equal(host(da), want)

@@ -203,9 +203,11 @@ __global__ void k_presmooth_explicit(Geo g, double *v, const double *prev, doubl
 // ---------------------------------------------------------------------------
 // separable Gaussian along one axis (an option beside the reference's
 // implicit presmoothing, which is not a Gaussian): out = sum_{m=-R..R}
-// w[|m|] in(c + m) in order of m, the coordinate mirrored about the volume's
-// faces as the reference's reflection does (ghost 0 = voxel 1:
-// x < 1 -> 1 - x, x > n -> 2n + 1 - x); interior voxels only
+// w[|m|] in(c + m) in order of m, each term added by a fused multiply-add
+// (explicit fma: one rounding, the same on the host, whatever --fmad says),
+// the coordinate mirrored about the volume's faces as the reference's
+// reflection does (ghost 0 = voxel 1: x < 1 -> 1 - x, x > n -> 2n + 1 - x);
+// interior voxels only
 
 __device__ inline int gauss_mirror(int x, int n)
 {
@@ -235,7 +237,7 @@ __global__ void k_gauss_axis(Geo g, const double *__restrict__ in, double *__res
     const long long base = o - (long long)c[AXIS] * st[AXIS];
     double acc = 0.0;
     for (int m = -W.R; m <= W.R; ++m)
-        acc = acc + W.w[m < 0 ? -m : m] * in[base + (long long)gauss_mirror(c[AXIS] + m, n[AXIS]) * st[AXIS]];
+        acc = fma(W.w[m < 0 ? -m : m], in[base + (long long)gauss_mirror(c[AXIS] + m, n[AXIS]) * st[AXIS]], acc);
     out[o] = acc;
 }
 

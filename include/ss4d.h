@@ -206,8 +206,8 @@ ss4d_status ss4d_presmooth_explicit(ss4d_solver *s, const ss4d_params *p, int ti
  * ceil(3 sigma_a) (sigma_a == 0 leaves axis a alone), over the interior
  * voxels, the volume mirrored about its faces as the reference's reflection
  * mirrors it (ghost 0 = voxel 1); then the ghost layer is set by that
- * reflection.  Each tap sum runs in order of m, every product and sum
- * rounded separately, in FP64 in every arithmetic form.  R_a must not
+ * reflection.  Each tap sum runs in order of m, a fused multiply-add per
+ * tap, in FP64 in every arithmetic form.  R_a must not
  * exceed SS4D_GAUSS_MAX_RADIUS.  d_scratch (NULL = internal) is overwritten. */
 #define SS4D_GAUSS_MAX_RADIUS 32
 ss4d_status ss4d_gaussian_smooth(ss4d_solver *s, const double sigma[4], double *d_img, double *d_scratch);

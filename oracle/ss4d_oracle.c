@@ -305,7 +305,8 @@ void or_presmooth_explicit(const ss4d_dims *d, const ss4d_params *p, int steps, 
 /* A true Gaussian beside the reference's implicit presmoothing (no
  * counterpart in the reference): per axis with sigma > 0, taps w_m =
  * exp(-m^2 / (2 sigma^2)) / (w_0 + 2 w_1 + ... ), |m| <= ceil(3 sigma), the
- * sum over m = -R..R in order, coordinates mirrored about the volume's faces
+ * sum over m = -R..R in order, each term by fma() (correctly rounded, as the
+ * GPU's), coordinates mirrored about the volume's faces
  * (x < 1 -> 1 - x, x > n -> 2n + 1 - x, as the reference's reflection
  * copies voxel 1 into ghost 0); then the ghost layer by reflection.
  * Returns -1 when a radius exceeds 32. */
@@ -347,7 +348,7 @@ int or_gaussian(const ss4d_dims *d, const double sigma[4], double *v, double *sc
                         const ptrdiff_t base = o - (ptrdiff_t)c[a] * st[a];
                         double acc = 0.0;
                         for (int m = -R; m <= R; ++m)
-                            acc = acc + w[m < 0 ? -m : m] * src[base + (ptrdiff_t)mirror_idx(c[a] + m, n[a]) * st[a]];
+                            acc = fma(w[m < 0 ? -m : m], src[base + (ptrdiff_t)mirror_idx(c[a] + m, n[a]) * st[a]], acc);
                         dst[o] = acc;
                     }
         double *t = src;

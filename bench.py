@@ -441,8 +441,9 @@ def run_frontend(args, ctx, arith="fp64"):
 
 def run_e2e(args, form, ctx):
     """The same steps through the reference-named layer (libss4d_seg.so) with
-    host arrays: every _segTimeStep_() uploads u and Mmask and downloads u and
-    prev_u (page-locked host memory), as a reference driver would call it."""
+    host arrays, as a reference driver calls it: every _segTimeStep_() uploads
+    u and Mmask and downloads u (page-locked host memory; Mmask beside the
+    solve, prev_u <- u copied on the host meanwhile)."""
     import ctypes as C
 
     import numpy as np

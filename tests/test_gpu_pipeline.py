@@ -86,3 +86,65 @@ def test_reference_main_sequence_on_files(ss4d, cuda, tmp_path, arith):
         L._deallocateMem_()
         os.environ.pop("SS4D_ARITH", None)
         os.environ.pop("SS4D_EXTRAPOLATE", None)
+
+
+def test_reference_named_layer_mixed_extrapolated_steps_equal_native(ss4d, cuda):
+    """The path of the end-to-end measurement: _segTimeStep_() of the
+    reference-named layer with SS4D_ARITH=mixed and SS4D_EXTRAPOLATE=3 on host
+    arrays (Mmask uploaded beside the solve, prev_u copied on the host) gives,
+    step after step, the u, prev_u and iteration counts of the native mixed
+    solver with the cubic extrapolated start on the same g."""
+    torch = cuda
+    nx, ny, nz, nt = 40, 36, 24, 6
+    p = ss4d.scene_params(maxNoOfTimeSteps=6)
+    i0h, u0h = ss4d.scene(3, nx, ny, nz, nt, seed=5)
+    shape = i0h.shape
+    lM, kM, jM, iM = shape
+    n = int(np.prod(shape))
+    os.environ["SS4D_ARITH"] = "mixed"
+    os.environ["SS4D_EXTRAPOLATE"] = "3"
+    L = C.CDLL(ss4d.SEG_PATH, mode=os.RTLD_LOCAL)
+    for nm, v in (("iMax", iM), ("jMax", jM), ("kMax", kM), ("lMax", lM), ("maxNoGSIteration", p.maxNoGSIteration),
+                  ("maxNoOfTimeSteps", p.maxNoOfTimeSteps)):
+        C.c_int.in_dll(L, nm).value = int(v)
+    for nm in ("K", "eps2", "tau", "h", "omega_c", "gsTol", "segTol", "sigma", "omega_sigma",
+               "maxNoGSIteration_sigma", "theta_img", "rho_thr", "ballRadius"):
+        C.c_double.in_dll(L, nm).value = float(getattr(p, nm))
+    noc = (C.c_int * lM)()
+    C.c_void_p.in_dll(L, "no_of_centers").value = C.addressof(noc)
+    for fn in ("_allocateMem_", "_deallocateMem_", "_segTimeStep_", "_gf_inputImage_plus_thresholdedImage_",
+               "ss4d_compat_sync_host", "ss4d_compat_last_stats"):
+        getattr(L, fn).restype = C.c_bool
+    assert L._allocateMem_()
+    try:
+        def arr(name):
+            addr = C.c_void_p.in_dll(L, name).value
+            return np.ctypeslib.as_array((C.c_double * n).from_address(addr)).reshape(shape)
+
+        i0, u, prev, mm = arr("i0"), arr("u"), arr("prev_u"), arr("Mmask")
+        i0[...] = i0h
+        mm[...] = 1.0
+        assert L._gf_inputImage_plus_thresholdedImage_(C.c_void_p(i0.ctypes.data), C.c_void_p(u.ctypes.data))
+        assert L.ss4d_compat_sync_host()
+        g_host = [arr(nm).copy() for nm in ("g_e", "g_w", "g_n", "g_s", "g_t", "g_b", "g_fw", "g_bw")]
+        u[...] = u0h
+        got = []
+        for _ in range(5):
+            before = u.copy()
+            assert L._segTimeStep_()
+            st = ss4d.StepStats()
+            assert L.ss4d_compat_last_stats(C.byref(st))
+            assert np.array_equal(prev, before)
+            got.append((st.iterations, u.copy()))
+    finally:
+        L._deallocateMem_()
+        os.environ.pop("SS4D_ARITH", None)
+        os.environ.pop("SS4D_EXTRAPOLATE", None)
+    g = [torch.from_numpy(a).cuda() for a in g_host]
+    ud = torch.from_numpy(u0h).cuda()
+    with ss4d.Solver(*shape[::-1], arith="mixed") as S:
+        S.set_extrapolation(3)
+        for its, u_got in got:
+            st = S.seg_time_step(p, ud, None, g)
+            assert st["iterations"] == its
+            assert np.array_equal(ud.cpu().numpy(), u_got)

@@ -660,7 +660,9 @@ bool _segTimeStep_(void)
     ss4d_balls B = {bb.nb, bb.l, bb.x, bb.y, bb.z};
     /* the step without its rescale, then the rescale (per-ball, Mmask) once
      * Mmask has arrived: the same operations in the same order */
-    st = ss4d_seg_time_step(g_solver, &p, g_dev[A_U], g_dev[A_PREV], dg, NULL, NULL, &g_last);
+    /* the device copy of prev_u serves only a strict caller's coefficient
+     * refresh below (every other call uploads the host prev_u it reads) */
+    st = ss4d_seg_time_step(g_solver, &p, g_dev[A_U], g_strict ? g_dev[A_PREV] : NULL, dg, NULL, NULL, &g_last);
     if (st == SS4D_OK)
         st = ss4d_join_side(g_solver);
     if (st == SS4D_OK)

@@ -148,3 +148,52 @@ def test_reference_named_layer_mixed_extrapolated_steps_equal_native(ss4d, cuda)
             st = S.seg_time_step(p, ud, None, g)
             assert st["iterations"] == its
             assert np.array_equal(ud.cpu().numpy(), u_got)
+
+
+@pytest.mark.parametrize("arith", ["reference", "fp64"])
+def test_strict_layer_refreshes_g_and_coefficients(ss4d, cuda, arith):
+    """SS4D_COMPAT_STRICT=1: the host copies of the edge detector's g faces
+    and of the step's coefficients e..bw are those of the reference after
+    _gf_inputImage_plus_thresholdedImage_ and after _segTimeStep_."""
+    d = load_golden("seg_small.npz")
+    params = dict(zip((str(n) for n in d["param_names"]), d["params"]))
+    shape = d["u0"].shape
+    lM, kM, jM, iM = shape
+    n = int(np.prod(shape))
+    os.environ["SS4D_ARITH"] = arith
+    os.environ["SS4D_COMPAT_STRICT"] = "1"
+    L = C.CDLL(ss4d.SEG_PATH, mode=os.RTLD_LOCAL)
+    for nm, v in (("iMax", iM), ("jMax", jM), ("kMax", kM), ("lMax", lM),
+                  ("maxNoGSIteration", params["maxNoGSIteration"]), ("maxNoOfTimeSteps", params["maxNoOfTimeSteps"])):
+        C.c_int.in_dll(L, nm).value = int(v)
+    for nm in ("K", "eps2", "tau", "h", "omega_c", "gsTol", "segTol", "sigma", "omega_sigma",
+               "maxNoGSIteration_sigma", "theta_img", "rho_thr", "ballRadius"):
+        C.c_double.in_dll(L, nm).value = float(params[nm])
+    noc = (C.c_int * lM)()
+    C.c_void_p.in_dll(L, "no_of_centers").value = C.addressof(noc)
+    for fn in ("_allocateMem_", "_deallocateMem_", "_segTimeStep_", "_gf_inputImage_plus_thresholdedImage_"):
+        getattr(L, fn).restype = C.c_bool
+    assert L._allocateMem_()
+    try:
+        def arr(name):
+            addr = C.c_void_p.in_dll(L, name).value
+            return np.ctypeslib.as_array((C.c_double * n).from_address(addr)).reshape(shape)
+
+        i0, u, mm = arr("i0"), arr("u"), arr("Mmask")
+        i0[...] = d["i0_in"]
+        u[...] = d["thr_in"]
+        mm[...] = 1.0
+        assert L._gf_inputImage_plus_thresholdedImage_(C.c_void_p(i0.ctypes.data), C.c_void_p(u.ctypes.data))
+        for f, nm in enumerate(("g_e", "g_w", "g_n", "g_s", "g_t", "g_b", "g_fw", "g_bw")):
+            assert np.array_equal(arr(nm), d[f"g{f}"]), nm
+        u[...] = d["u0"]
+        C.c_int.in_dll(L, "numberOfTimeStep").value = 1
+        assert L._segTimeStep_()
+        for f, nm in enumerate(("e", "w", "n", "s", "t", "b", "fw", "bw")):
+            inner = (slice(1, -1),) * 4
+            assert rel_err(arr(nm)[inner], d[f"coef{f}"][inner]) <= 4e-16, nm
+        assert rel_err(u, d["u_steps"][0]) <= (1e-13 if arith == "reference" else 1e-10)
+    finally:
+        L._deallocateMem_()
+        os.environ.pop("SS4D_ARITH", None)
+        os.environ.pop("SS4D_COMPAT_STRICT", None)

@@ -71,7 +71,7 @@ ss4d_status bfail(ss4d_status st, const char *fmt, ...)
 // The grid-stride tile index that jumps a block from volume v to its first
 // tile of volume v + 1 (the loop's t += gridDim.x lands on it): a volume the
 // kernel does not work on costs a block one step, not one per tile.
-__device__ __forceinline__ long long skip_to_next_volume(const BVol *__restrict__ vols, int v, long long total)
+__device__ __forceinline__ long long skip_to_next_volume(const BVol *__restrict__ vols, int v)
 {
     const long long n0 = vols[v + 1].tile0, G = gridDim.x;
     long long off = ((long long)blockIdx.x - n0) % G;
@@ -100,7 +100,7 @@ __device__ __forceinline__ void walk_targets(const BVol *__restrict__ vols, int 
         if (!want(v)) { // the whole block skips: v is uniform
             if (v + 1 >= nv)
                 break;
-            t = skip_to_next_volume(vols, v, total);
+            t = skip_to_next_volume(vols, v);
             continue;
         }
         const BVol &V = vols[v];

@@ -108,7 +108,7 @@ def build(verbose: bool = False, force: bool = False) -> dict:
     libdir = _cuda_lib_dir(nvcc)
     if force or _stale(LIB, objs):
         _run([nvcc] + GENCODE + ["-shared", "-o", LIB] + objs +
-             ["-cudart", "shared", "-Xcompiler", "-fopenmp", "-Xlinker", f"-rpath,{libdir}", "-lgomp"],
+             ["-cudart", "shared", "-Xcompiler", "-fopenmp", "-Xlinker", f"-rpath,{libdir}", "-lgomp", "-lpthread"],
              os.path.join(BUILD, "link.log"))
     for lib, src in ((LIB_SEG, "ss4d_compat_seg.c"), (LIB_MCF, "ss4d_compat_mcf.c")):
         srcp = os.path.join(CSRC, src)

@@ -9,6 +9,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <thread>
 #include <vector>
 
 #include "ss4d_kernels.cuh"
@@ -86,8 +87,9 @@ struct ss4d_solver {
     ss4d_arith arith;
     cudaStream_t stream;
     cudaStream_t cap;
-    cudaStream_t side;   // ss4d_copy_to_device_side
+    cudaStream_t side;   // ss4d_copy_to_device_side, the chunked copies of ss4d_seg_time_step_host
     cudaEvent_t side_ev; // the last side copy
+    cudaEvent_t chunk_ev[SS4D_HOST_CHUNKS], mask_ev;
     int device;
     int sm_count;
     int use_graph;
@@ -243,6 +245,9 @@ extern "C" ss4d_status ss4d_solver_create(const ss4d_dims *dims, ss4d_arith arit
     FAIL_IF(cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking));
     FAIL_IF(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
     FAIL_IF(cudaEventCreateWithFlags(&s->side_ev, cudaEventDisableTiming));
+    for (int c = 0; c < SS4D_HOST_CHUNKS; ++c)
+        FAIL_IF(cudaEventCreateWithFlags(&s->chunk_ev[c], cudaEventDisableTiming));
+    FAIL_IF(cudaEventCreateWithFlags(&s->mask_ev, cudaEventDisableTiming));
     FAIL_IF(cudaEventCreate(&s->ev0));
     FAIL_IF(cudaEventCreate(&s->ev1));
     FAIL_IF(cudaEventCreate(&s->tev0));
@@ -332,6 +337,11 @@ extern "C" ss4d_status ss4d_solver_destroy(ss4d_solver *s)
     }
     if (s->side_ev)
         cudaEventDestroy(s->side_ev);
+    for (int c = 0; c < SS4D_HOST_CHUNKS; ++c)
+        if (s->chunk_ev[c])
+            cudaEventDestroy(s->chunk_ev[c]);
+    if (s->mask_ev)
+        cudaEventDestroy(s->mask_ev);
     free(s);
     return SS4D_OK;
 }
@@ -1220,20 +1230,37 @@ extern "C" ss4d_status ss4d_gs_coefficients(ss4d_solver *s, const ss4d_params *p
 // segmentation steps with extrapolation it also keeps the next step's start
 // correction: an extrapolation from this step's change and up to order-1
 // earlier ones
-static ss4d_status unpack_step(ss4d_solver *s, const LoopState *d_state, double *d_u, int mixed)
+struct UnpackPlan {
+    int save, terms, keep;
+};
+
+// the extrapolation terms and history depth of this step's unpack
+static ss4d_status unpack_plan(ss4d_solver *s, int mixed, UnpackPlan *u)
 {
-    const int save = mixed && s->extrap && s->have_g && !s->ws_net;
-    int terms = 0, keep = 0;
-    if (save) {
-        keep = s->extrap - 1;
-        for (int q = 0; q < 2 * keep; ++q)
+    u->save = mixed && s->extrap && s->have_g && !s->ws_net;
+    u->terms = u->keep = 0;
+    if (u->save) {
+        u->keep = s->extrap - 1;
+        for (int q = 0; q < 2 * u->keep; ++q)
             if (!s->hist[q])
                 CKS(dmalloc(s, (void **)&s->hist[q], sizeof(float) * s->sp.cs));
-        terms = s->have_dprev + 1 < s->extrap ? s->have_dprev + 1 : s->extrap;
+        u->terms = s->have_dprev + 1 < s->extrap ? s->have_dprev + 1 : s->extrap;
     }
+    return SS4D_OK;
+}
+
+static void unpack_done(ss4d_solver *s, const UnpackPlan &u)
+{
+    s->have_dprev = u.save ? (s->have_dprev < 3 ? s->have_dprev + 1 : 3) : 0;
+}
+
+static ss4d_status unpack_step(ss4d_solver *s, const LoopState *d_state, double *d_u, int mixed)
+{
+    UnpackPlan u;
+    CKS(unpack_plan(s, mixed, &u));
     timed(s, SS4D_K_PACK, true,
-          [&] { launch_unpack(s->geo, s->sp, s->sb, d_state, d_u, s->stream, terms, keep, s->hist); });
-    s->have_dprev = save ? (s->have_dprev < 3 ? s->have_dprev + 1 : 3) : 0;
+          [&] { launch_unpack(s->geo, s->sp, s->sb, d_state, d_u, s->stream, u.terms, u.keep, s->hist); });
+    unpack_done(s, u);
     s->launches += 1;
     return last_launch();
 }
@@ -1331,6 +1358,149 @@ extern "C" ss4d_status ss4d_seg_time_step(ss4d_solver *s, const ss4d_params *p, 
     }
     if (st == SS4D_OK)
         st = rescale_impl(s, p, d_u, d_Mmask, balls);
+    CK(cudaEventRecord(s->ev1, s->stream));
+    CK(cudaEventSynchronize(s->ev1));
+    if (stats)
+        cudaEventElapsedTime(&stats->ms, s->ev0, s->ev1);
+    return st;
+}
+
+// ---------------------------------------------------------------------------
+// a time step on host arrays, the copies overlapped with the step's work
+
+// prev <- u on host threads (the reference's copy at the start of a step)
+struct HostCopy {
+    std::vector<std::thread> th;
+    void start(double *dst, const double *src, size_t n)
+    {
+        if (!dst)
+            return;
+        const int T = 8;
+        const size_t per = (n + T - 1) / T;
+        for (int t = 0; t < T; ++t) {
+            const size_t a = per * t < n ? per * t : n, e = a + per < n ? a + per : n;
+            if (e > a)
+                th.emplace_back([=] { memcpy(dst + a, src + a, sizeof(double) * (e - a)); });
+        }
+    }
+    void join()
+    {
+        for (auto &t : th)
+            t.join();
+        th.clear();
+    }
+    ~HostCopy() { join(); }
+};
+
+extern "C" ss4d_status ss4d_seg_time_step_host(ss4d_solver *s, const ss4d_params *p, double *h_u, double *d_u,
+                                               double *h_prev, const double *h_Mmask, double *d_Mmask,
+                                               const double *const d_g[8], const ss4d_balls *balls,
+                                               ss4d_step_stats *stats)
+{
+    REQ(s && h_u && d_u && d_g, "NULL argument");
+    REQ(!h_Mmask || d_Mmask, "h_Mmask needs d_Mmask");
+    CKS(check_params(p));
+    const Geo &g = s->geo;
+    const size_t frame = (size_t)g.sw, all = (size_t)g.n;
+    HostCopy hc;
+    hc.start(h_prev, h_u, all);
+    if (s->arith == SS4D_ARITH_REFERENCE || s->timing) {
+        // the plain sequence (the reference form has no split layout to
+        // overlap; per-kernel timing wants the kernels in their own order)
+        CK(cudaMemcpyAsync(d_u, h_u, sizeof(double) * all, cudaMemcpyHostToDevice, s->stream));
+        if (h_Mmask)
+            CK(cudaMemcpyAsync(d_Mmask, h_Mmask, sizeof(double) * all, cudaMemcpyHostToDevice, s->stream));
+        CKS(ss4d_seg_time_step(s, p, d_u, nullptr, d_g, h_Mmask ? d_Mmask : nullptr, balls, stats));
+        hc.join();
+        CK(cudaMemcpyAsync(h_u, d_u, sizeof(double) * all, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        return SS4D_OK;
+    }
+    CPtrs8 gi;
+    for (int f = 0; f < 8; ++f) {
+        REQ(d_g[f], "a g array is NULL");
+        gi.p[f] = d_g[f];
+    }
+    if (stats)
+        memset(stats, 0, sizeof *stats);
+    const int mixed = s->arith == SS4D_ARITH_MIXED;
+    CKS(ensure_split(s, mixed));
+    // the centre tables now: they are read only by the rescale, and a copy
+    // from pageable memory later could wait for the loop
+    int have_balls = 0;
+    CKS(upload_balls(s, balls, p->ballRadius, &have_balls));
+    CK(cudaEventRecord(s->ev0, s->stream));
+    // u goes up in chunks of padded frames on the side stream, after the
+    // work already queued on the handle's stream (d_u may be in use there)
+    const int C = g.lM < SS4D_HOST_CHUNKS ? g.lM : SS4D_HOST_CHUNKS;
+    int F[SS4D_HOST_CHUNKS + 1];
+    for (int c = 0; c <= C; ++c)
+        F[c] = (int)((long long)c * g.lM / C);
+    CK(cudaEventRecord(s->side_ev, s->stream));
+    CK(cudaStreamWaitEvent(s->side, s->side_ev, 0));
+    for (int c = 0; c < C; ++c) {
+        CK(cudaMemcpyAsync(d_u + F[c] * frame, h_u + F[c] * frame, sizeof(double) * frame * (F[c + 1] - F[c]),
+                           cudaMemcpyHostToDevice, s->side));
+        CK(cudaEventRecord(s->chunk_ev[c], s->side));
+    }
+    if (h_Mmask) { // needed by the rescale only
+        CK(cudaMemcpyAsync(d_Mmask, h_Mmask, sizeof(double) * all, cudaMemcpyHostToDevice, s->side));
+        CK(cudaEventRecord(s->mask_ev, s->side));
+    }
+    // a chunk's first differences read the next frame: its chunk too
+    for (int c = 0; c < C; ++c) {
+        CK(cudaStreamWaitEvent(s->stream, s->chunk_ev[c], 0));
+        if (c + 1 < C)
+            CK(cudaStreamWaitEvent(s->stream, s->chunk_ev[c + 1], 0));
+        if (mixed)
+            launch_fdiff_range(g, d_u, s->sb, F[c], F[c + 1], s->sm_count, s->stream);
+        launch_pack_range(g, s->sp, d_u, d_u, s->sb, F[c], F[c + 1], s->stream);
+        s->launches += mixed ? 2 : 1;
+    }
+    if (mixed) {
+        launch_assemble_ff_faces(g, s->sp, gi, 1, *p, s->sb, s->stream);
+        s->launches += 2;
+    } else {
+        launch_assemble(g, s->sp, d_u, gi, 1, *p, s->sb, 0, s->stream);
+        s->launches += 2;
+    }
+    CKS(last_launch());
+    s->cur_g = gi;
+    s->have_g = 1;
+    CKS(run_split_loop(s, p, mixed));
+    // the unpack and the rescale per chunk of interior frames, each chunk's
+    // download on the side stream as soon as it is done
+    UnpackPlan up;
+    CKS(unpack_plan(s, mixed, &up));
+    if (h_Mmask)
+        CK(cudaStreamWaitEvent(s->stream, s->mask_ev, 0));
+    hc.join(); // prev has its copy of u before any chunk of u comes down
+    const int nt = g.lM - 2, Ci = nt < SS4D_HOST_CHUNKS ? nt : SS4D_HOST_CHUNKS;
+    for (int c = 0; c < Ci; ++c) {
+        const int a = 1 + (int)((long long)c * nt / Ci), e = 1 + (int)((long long)(c + 1) * nt / Ci);
+        launch_unpack_range(g, s->sp, s->sb, s->d_state, d_u, s->stream, up.terms, up.keep, s->hist, a, e);
+        s->launches += 1;
+        if (have_balls) {
+            launch_rescale_balls_range(g, d_u, s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz,
+                                       p->ballRadius, a, e, s->stream);
+            s->launches += 1;
+        }
+        if (h_Mmask) {
+            launch_mask_zero_range(g, d_u, d_Mmask, a, e, s->stream);
+            s->launches += 1;
+        }
+        CK(cudaEventRecord(s->chunk_ev[c], s->stream));
+        CK(cudaStreamWaitEvent(s->side, s->chunk_ev[c], 0));
+        CK(cudaMemcpyAsync(h_u + a * frame, d_u + a * frame, sizeof(double) * frame * (e - a), cudaMemcpyDeviceToHost,
+                           s->side));
+    }
+    CKS(last_launch());
+    unpack_done(s, up);
+    s->have_g = 0;
+    ss4d_status st = finish_stats(s, stats, mixed);
+    count_graph_launches(s, mixed);
+    CK(cudaEventRecord(s->side_ev, s->side));
+    CK(cudaStreamWaitEvent(s->stream, s->side_ev, 0));
     CK(cudaEventRecord(s->ev1, s->stream));
     CK(cudaEventSynchronize(s->ev1));
     if (stats)

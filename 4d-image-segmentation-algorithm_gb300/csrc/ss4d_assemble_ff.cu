@@ -47,10 +47,12 @@ struct FFConst {
 };
 
 // forward differences of every voxel that has a neighbour along the axis
-__global__ void __launch_bounds__(256) k_fdiff(Geo g, const double *__restrict__ u, SplitBufs b)
+// voxels [o0, o1) (whole frames)
+__global__ void __launch_bounds__(256) k_fdiff(Geo g, const double *__restrict__ u, SplitBufs b, long long o0,
+                                               long long o1)
 {
     const long long st[4] = {1, g.sy, g.sz, g.sw};
-    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < g.n;
+    for (long long o = o0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; o < o1;
          o += (long long)gridDim.x * blockDim.x) {
         int i, j, k, l;
         nat_coords(g, (unsigned)o, i, j, k, l);
@@ -172,8 +174,20 @@ int max_blocks_fdiff()
     return a > 0 ? a : 1;
 }
 
+void launch_fdiff_range(const Geo &g, const double *u, SplitBufs b, int l0, int l1, int sm_count, cudaStream_t st)
+{
+    k_fdiff<<<sm_count * max_blocks_fdiff(), 256, 0, st>>>(g, u, b, (long long)l0 * g.sw, (long long)l1 * g.sw);
+}
+
 void launch_assemble_ff(const Geo &g, const Split &s, const double *u, CPtrs8 gin, int has_g, const ss4d_params &p,
                         SplitBufs b, int sm_count, cudaStream_t st)
+{
+    launch_fdiff_range(g, u, b, 0, g.lM, sm_count, st);
+    launch_assemble_ff_faces(g, s, gin, has_g, p, b, st);
+}
+
+void launch_assemble_ff_faces(const Geo &g, const Split &s, CPtrs8 gin, int has_g, const ss4d_params &p, SplitBufs b,
+                              cudaStream_t st)
 {
     FFConst K;
     split_host(1.0 / (p.h * p.h), K.ih2h, K.ih2l);
@@ -182,7 +196,6 @@ void launch_assemble_ff(const Geo &g, const Split &s, const double *u, CPtrs8 gi
     split_host(p.tau / (p.h * p.h), K.ch, K.cl);
     int e1 = 0, e2 = 0;
     K.pow2 = K.ih2l == 0.f && K.iq2l == 0.f && frexp((double)K.ih2h, &e1) == 0.5 && frexp((double)K.iq2h, &e2) == 0.5;
-    k_fdiff<<<sm_count * max_blocks_fdiff(), 256, 0, st>>>(g, u, b);
     {
         const int bx = g.nx + 1 >= 128 ? 128 : (g.nx + 1 >= 64 ? 64 : 32);
         const int by = 256 / bx;

@@ -8,7 +8,6 @@
  * run the device path of include/ss4d.h.
  */
 #include <ctype.h>
-#include <pthread.h>
 #include <stdbool.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -593,96 +592,47 @@ bool _gs_coefficients_(void)
     return st == SS4D_OK && sync_if_strict(A_E, A_BW) && finish();
 }
 
-/* prev_u <- u on the host, in chunks on helper threads, while the GPU works:
- * the reference's own copy at the start of a step (segmentation4D.c:224),
- * which spares downloading the device copy afterwards */
-#define HOST_COPY_THREADS 8
-typedef struct {
-    char *dst;
-    const char *src;
-    size_t n;
-    pthread_t th;
-    int started;
-} chunk_t;
-
-static void *chunk_copy(void *a)
-{
-    chunk_t *c = (chunk_t *)a;
-    memcpy(c->dst, c->src, c->n);
-    return NULL;
-}
-
-static void host_copy_start(chunk_t *ch, void *dst, const void *src, size_t bytes)
-{
-    const size_t per = (bytes / HOST_COPY_THREADS + 63) & ~(size_t)63;
-    for (int t = 0; t < HOST_COPY_THREADS; ++t) {
-        const size_t off = per * t < bytes ? per * t : bytes;
-        const size_t end = off + per < bytes ? off + per : bytes;
-        ch[t].dst = (char *)dst + off;
-        ch[t].src = (const char *)src + off;
-        ch[t].n = end - off;
-        ch[t].started = ch[t].n && pthread_create(&ch[t].th, NULL, chunk_copy, &ch[t]) == 0;
-        if (ch[t].n && !ch[t].started)
-            memcpy(ch[t].dst, ch[t].src, ch[t].n); /* no thread: copy here */
-    }
-}
-
-static void host_copy_join(chunk_t *ch)
-{
-    for (int t = 0; t < HOST_COPY_THREADS; ++t)
-        if (ch[t].started)
-            pthread_join(ch[t].th, NULL);
-}
-
 bool _segTimeStep_(void)
 {
     if (!g_solver)
         return false;
-    /* u is needed at once; Mmask only by the rescale after the solve, so its
-     * upload runs beside the solve on the side stream */
-    if (!up(u, g_dev[A_U]))
-        return false;
-    ss4d_status st = ss4d_copy_to_device_side(g_solver, g_dev[A_MASK], Mmask, g_bytes);
-    report("upload", st);
-    if (st != SS4D_OK)
-        return false;
-    chunk_t ch[HOST_COPY_THREADS];
-    host_copy_start(ch, prev_u, u, g_bytes);
     ss4d_params p = params_from_globals();
     const double *dg[8];
     for (int f = 0; f < 8; ++f)
         dg[f] = g_dev[A_GE + f];
     balls_t bb;
-    if (!balls_make(&bb)) {
-        host_copy_join(ch);
+    if (!balls_make(&bb))
+        return false;
+    ss4d_balls B = {bb.nb, bb.l, bb.x, bb.y, bb.z};
+    ss4d_status st;
+    if (!g_strict) {
+        /* prev_u <- u as the reference's step begins (segmentation4D.c:224),
+         * u up and down in frame chunks overlapped with the step's first and
+         * last kernels, Mmask up beside the solve */
+        st = ss4d_seg_time_step_host(g_solver, &p, u, g_dev[A_U], prev_u, Mmask, g_dev[A_MASK], dg, &B, &g_last);
+        balls_free(&bb);
+        report("segmentation time step", st);
+        return st == SS4D_OK && finish();
+    }
+    /* strict: the plain sequence, which also leaves prev_u on the device for
+     * the refresh of the reference-layout coefficients */
+    if (!up(u, g_dev[A_U]) || !up(Mmask, g_dev[A_MASK])) {
+        balls_free(&bb);
         return false;
     }
-    ss4d_balls B = {bb.nb, bb.l, bb.x, bb.y, bb.z};
-    /* the step without its rescale, then the rescale (per-ball, Mmask) once
-     * Mmask has arrived: the same operations in the same order */
-    /* the device copy of prev_u serves only a strict caller's coefficient
-     * refresh below (every other call uploads the host prev_u it reads) */
-    st = ss4d_seg_time_step(g_solver, &p, g_dev[A_U], g_strict ? g_dev[A_PREV] : NULL, dg, NULL, NULL, &g_last);
-    if (st == SS4D_OK)
-        st = ss4d_join_side(g_solver);
-    if (st == SS4D_OK)
-        st = ss4d_rescale_to_zero_one(g_solver, &p, g_dev[A_U], g_dev[A_MASK], &B);
+    st = ss4d_seg_time_step(g_solver, &p, g_dev[A_U], g_dev[A_PREV], dg, g_dev[A_MASK], &B, &g_last);
     balls_free(&bb);
-    host_copy_join(ch);
     report("segmentation time step", st);
     if (st != SS4D_OK)
         return false;
-    if (g_strict) {
-        /* the fast forms keep their coefficients in a split layout; refresh
-         * the reference-layout arrays for a strict caller */
-        double *dc[8];
-        for (int f = 0; f < 8; ++f)
-            dc[f] = g_dev[A_E + f];
-        st = ss4d_gs_coefficients(g_solver, &p, g_dev[A_PREV], dg, dc);
-        if (st != SS4D_OK || !sync_if_strict(A_E, A_BW))
-            return false;
-    }
-    return down(u, g_dev[A_U]) && finish();
+    double *dc[8];
+    for (int f = 0; f < 8; ++f)
+        dc[f] = g_dev[A_E + f];
+    st = ss4d_gs_coefficients(g_solver, &p, g_dev[A_PREV], dg, dc);
+    report("coefficients", st);
+    if (st != SS4D_OK || !sync_if_strict(A_E, A_BW))
+        return false;
+    return down(u, g_dev[A_U]) && down(prev_u, g_dev[A_PREV]) && finish();
 }
 
 double _l2norm_(double *a, double *bb)

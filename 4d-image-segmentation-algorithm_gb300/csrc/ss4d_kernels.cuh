@@ -142,6 +142,21 @@ void launch_pack(const Geo &g, const Split &s, const double *u, const double *pr
 // mixed form: the same coefficient records from float-float arithmetic (3 kernels)
 void launch_assemble_ff(const Geo &g, const Split &s, const double *u, CPtrs8 gin, int has_g, const ss4d_params &p,
                         SplitBufs b, int sm_count, cudaStream_t st);
+// the same in parts: first differences of padded frames [l0, l1), then the
+// faces and voxel coefficients (after the differences of every frame)
+void launch_fdiff_range(const Geo &g, const double *u, SplitBufs b, int l0, int l1, int sm_count, cudaStream_t st);
+void launch_assemble_ff_faces(const Geo &g, const Split &s, CPtrs8 gin, int has_g, const ss4d_params &p, SplitBufs b,
+                              cudaStream_t st);
+// frame ranges: padded frames [l0, l1) for the pack, interior frames
+// [l0, l1) (1 <= l0 < l1 <= lMax-1) for the unpack and the rescale
+void launch_pack_range(const Geo &g, const Split &s, const double *u, const double *prev, SplitBufs b, int l0, int l1,
+                       cudaStream_t st);
+void launch_unpack_range(const Geo &g, const Split &s, SplitBufs b, const LoopState *state, double *u, cudaStream_t st,
+                         int terms, int keep, float *const *hist, int l0, int l1);
+void launch_mask_zero_range(const Geo &g, double *v, const double *Mmask, int l0, int l1, cudaStream_t st);
+void launch_rescale_balls_range(const Geo &g, double *v, const int *frame_first, const int *frame_count,
+                                const double *bx, const double *by, const double *bz, double R, int l0, int l1,
+                                cudaStream_t st);
 
 // the mixed form's edge detector in float-float arithmetic (ss4d_front_ff.cu);
 // float2 arrays hold (high, low) pairs in the natural layout

@@ -184,11 +184,12 @@ __global__ void __launch_bounds__(256) k_pack_coef(Geo g, Split sp, CPtrs8 a, do
 // (i = 2m, 2m + 1) of one row: they have opposite colours and land in
 // columns m + A - 1 and m + A of their colour arrays.
 __global__ void __launch_bounds__(256) k_pack(Geo g, Split sp, const double *__restrict__ u,
-                                              const double *__restrict__ prev, SplitBufs b, FastDiv fpairs)
+                                              const double *__restrict__ prev, SplitBufs b, FastDiv fpairs,
+                                              unsigned q0, unsigned q1)
 {
+    // q: rows x pairs, below 2^31; [q0, q1) covers whole frames
     const unsigned npairs = fpairs.d;
-    const unsigned total = (unsigned)(g.n / g.iM) * npairs; // rows x pairs, below 2^31
-    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+    for (unsigned q = q0 + blockIdx.x * blockDim.x + threadIdx.x; q < q1; q += gridDim.x * blockDim.x) {
         const unsigned row = fdiv(q, fpairs);
         const int m = (int)(q - row * npairs);
         // row = (l kM + k) jM + j
@@ -228,11 +229,11 @@ struct History {
 };
 
 __global__ void k_unpack(Geo g, Split sp, SplitBufs b, const LoopState *__restrict__ st, double *u, int terms,
-                         int keep, History hs)
+                         int keep, History hs, int l_off)
 {
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = 1 + blockIdx.z % g.nz, l = 1 + blockIdx.z / g.nz;
+    const int k = 1 + blockIdx.z % g.nz, l = 1 + l_off + blockIdx.z / g.nz;
     if (i > g.nx || j > g.ny)
         return;
     const int col = (i + j + k + l) & 1;
@@ -587,7 +588,15 @@ void launch_assemble(const Geo &g, const Split &s, const double *u, CPtrs8 gin, 
 
 void launch_pack(const Geo &g, const Split &s, const double *u, const double *prev, SplitBufs b, cudaStream_t st)
 {
-    k_pack<<<4096, 256, 0, st>>>(g, s, u, prev, b, make_fastdiv((unsigned)((g.iM + 1) / 2)));
+    launch_pack_range(g, s, u, prev, b, 0, g.lM, st);
+}
+
+void launch_pack_range(const Geo &g, const Split &s, const double *u, const double *prev, SplitBufs b, int l0, int l1,
+                       cudaStream_t st)
+{
+    const unsigned npairs = (unsigned)((g.iM + 1) / 2), per_frame = (unsigned)(g.jM * g.kM) * npairs;
+    k_pack<<<4096, 256, 0, st>>>(g, s, u, prev, b, make_fastdiv(npairs), per_frame * (unsigned)l0,
+                                 per_frame * (unsigned)l1);
 }
 
 void launch_pack_coef(const Geo &g, const Split &s, CPtrs8 a, const ss4d_params &p, SplitBufs b, int want32,
@@ -602,14 +611,21 @@ void launch_pack_coef(const Geo &g, const Split &s, CPtrs8 a, const ss4d_params 
 void launch_unpack(const Geo &g, const Split &s, SplitBufs b, const LoopState *state, double *u, cudaStream_t st,
                    int terms, int keep, float *const *hist)
 {
+    launch_unpack_range(g, s, b, state, u, st, terms, keep, hist, 1, g.lM - 1);
+}
+
+void launch_unpack_range(const Geo &g, const Split &s, SplitBufs b, const LoopState *state, double *u, cudaStream_t st,
+                         int terms, int keep, float *const *hist, int l0, int l1)
+{
     dim3 gr, bl;
     interior_grid(g, gr, bl);
+    gr.z = g.nz * (l1 - l0);
     History hs;
     for (int c = 0; c < 2; ++c) {
         hs.h1[c] = hist ? hist[c] : nullptr;
         hs.h2[c] = hist ? hist[2 + c] : nullptr;
     }
-    k_unpack<<<gr, bl, 0, st>>>(g, s, b, state, u, terms, keep, hs);
+    k_unpack<<<gr, bl, 0, st>>>(g, s, b, state, u, terms, keep, hs, l0 - 1);
 }
 
 void launch_loop_init(LoopState *state, int mode, cudaStream_t st)

@@ -512,9 +512,9 @@ __global__ void k_mcf_field(Geo g, double *u, double h, double t, int ghosts_onl
 // ball's min/max sees the values the earlier balls rescaled.
 
 __global__ void k_rescale_balls(Geo g, double *v, const int *frame_first, const int *frame_count, const double *bx,
-                                const double *by, const double *bz, double R)
+                                const double *by, const double *bz, double R, int l0)
 {
-    const int l = 1 + blockIdx.x;
+    const int l = l0 + blockIdx.x;
     const int first = frame_first[l], count = frame_count[l];
     for (int c = 0; c < count; ++c) {
         const double cx = bx[first + c], cy = by[first + c], cz = bz[first + c];
@@ -714,11 +714,12 @@ __global__ void k_frame_to_bytes(Geo g, const double *img, int l, int mode, uint
     bytes[q] = out;
 }
 
-__global__ void k_mask_zero(Geo g, double *v, const double *Mmask)
+__global__ void k_mask_zero(Geo g, double *v, const double *Mmask, int l_off)
 {
     int i, j, k, l;
     if (!interior_ijkl(g, i, j, k, l))
         return;
+    l += l_off;
     const long long o = nat_index(g, i, j, k, l);
     if (Mmask[o] == 0)
         v[o] = 0;
@@ -966,14 +967,27 @@ void launch_mcf_field(const Geo &g, double *u, double h, double t, int ghosts_on
 void launch_rescale_balls(const Geo &g, double *v, const int *frame_first, const int *frame_count, const double *bx,
                           const double *by, const double *bz, double R, cudaStream_t st)
 {
-    k_rescale_balls<<<g.nt, 256, 0, st>>>(g, v, frame_first, frame_count, bx, by, bz, R);
+    launch_rescale_balls_range(g, v, frame_first, frame_count, bx, by, bz, R, 1, g.lM - 1, st);
+}
+
+void launch_rescale_balls_range(const Geo &g, double *v, const int *frame_first, const int *frame_count,
+                                const double *bx, const double *by, const double *bz, double R, int l0, int l1,
+                                cudaStream_t st)
+{
+    k_rescale_balls<<<l1 - l0, 256, 0, st>>>(g, v, frame_first, frame_count, bx, by, bz, R, l0);
 }
 
 void launch_mask_zero(const Geo &g, double *v, const double *Mmask, cudaStream_t st)
 {
+    launch_mask_zero_range(g, v, Mmask, 1, g.lM - 1, st);
+}
+
+void launch_mask_zero_range(const Geo &g, double *v, const double *Mmask, int l0, int l1, cudaStream_t st)
+{
     dim3 gr, bl;
     interior_cfg(g, gr, bl);
-    k_mask_zero<<<gr, bl, 0, st>>>(g, v, Mmask);
+    gr.z = g.nz * (l1 - l0);
+    k_mask_zero<<<gr, bl, 0, st>>>(g, v, Mmask, l0 - 1);
 }
 
 void launch_ball_min_max(const Geo &g, const double *v, int l, double cx, double cy, double cz, double R, double *out2,

@@ -149,6 +149,8 @@ def lib() -> C.CDLL:
         "ss4d_copy_to_device_side": ([vp, vp, vp, C.c_size_t], st),
         "ss4d_presmooth_explicit": ([vp, C.POINTER(Params), C.c_int, vp, vp], st),
         "ss4d_gaussian_smooth": ([vp, dp, vp, vp], st),
+        "ss4d_seg_time_step_host": ([vp, C.POINTER(Params), vp, vp, vp, vp, vp, P8, C.POINTER(Balls),
+                                     C.POINTER(StepStats)], st),
         "ss4d_gfaces": ([vp, C.POINTER(Params), vp, vp, P8], st),
         "ss4d_join_side": ([vp], st),
         "ss4d_copy_device": ([vp, vp, vp, C.c_size_t], st),
@@ -379,6 +381,21 @@ class Solver:
         """_presmoothStepEXP_ on img; scratch (optional) receives the reference's prev_u"""
         _check(self.L.ss4d_presmooth_explicit(self.h, C.byref(p), int(steps), _ptr(img), _ptr(scratch)),
                "presmooth_explicit")
+
+    def seg_time_step_host(self, p: Params, h_u, d_u, g8, h_prev=None, h_mmask=None, d_mmask=None,
+                           balls=None) -> dict:
+        """ss4d_seg_time_step_host: h_u, h_prev, h_mmask are page-locked host
+        buffers (numpy views of ss4d_host_alloc memory), d_u / d_mmask their
+        device mirrors"""
+        B, keep = _balls(balls)
+        st = StepStats()
+        _check(self.L.ss4d_seg_time_step_host(self.h, C.byref(p), h_u.ctypes.data, _ptr(d_u),
+                                              h_prev.ctypes.data if h_prev is not None else None,
+                                              h_mmask.ctypes.data if h_mmask is not None else None, _ptr(d_mmask),
+                                              _p8(g8), C.byref(B) if B is not None else None, C.byref(st)),
+               "seg_time_step_host")
+        del keep
+        return st.as_dict()
 
     def gaussian_smooth(self, sigma, img, scratch=None):
         """separable Gaussian, sigma per axis (x, y, z, t), in place on img"""

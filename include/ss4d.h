@@ -249,6 +249,23 @@ ss4d_status ss4d_seg_time_step(ss4d_solver *s, const ss4d_params *p, double *d_u
                                const double *d_Mmask, const ss4d_balls *balls,
                                ss4d_step_stats *stats);
 
+/* ss4d_seg_time_step on HOST arrays, as a reference driver calls
+ * _segTimeStep_: h_u (page-locked, read and written), d_u its device
+ * mirror; h_prev (page-locked, may be NULL) receives the step's input u on
+ * host threads, as the reference's step begins (segmentation4D.c:224);
+ * h_Mmask (page-locked, NULL = all ones) goes up into d_Mmask beside the
+ * solve, since only the final rescale reads it.  In the FP64 and mixed forms
+ * u goes up in SS4D_HOST_CHUNKS chunks of frames on the handle's side stream
+ * while the first kernels of the step (first differences, pack) start on the
+ * chunks that have arrived, and comes down in chunks as the unpack and the
+ * rescale finish them; the results equal ss4d_seg_time_step's.  Returns when
+ * h_u holds the result. */
+#define SS4D_HOST_CHUNKS 4
+ss4d_status ss4d_seg_time_step_host(ss4d_solver *s, const ss4d_params *p, double *h_u, double *d_u,
+                                    double *h_prev, const double *h_Mmask, double *d_Mmask,
+                                    const double *const d_g[8], const ss4d_balls *balls,
+                                    ss4d_step_stats *stats);
+
 /* _mcfTimeStep (mcf_4D.c:102-205): prev_u <- u, coefficients (g == 1), exact
  * Dirichlet ghosts at t = tau*numberOfTimeStep, SOR solve. */
 ss4d_status ss4d_mcf_time_step(ss4d_solver *s, const ss4d_params *p, int numberOfTimeStep,

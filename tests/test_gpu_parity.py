@@ -488,3 +488,56 @@ def test_gaussian_smooth_with_taps_wider_than_the_volume(ss4d, oracle, cuda):
         S.gaussian_smooth(sigma, da)
         S.synchronize()
     assert np.array_equal(host(da), want)
+
+
+def _pinned(ss4d, shape):
+    """a page-locked host array (ss4d_host_alloc) and its release"""
+    import ctypes as Cm
+
+    L = ss4d.lib()
+    n = int(np.prod(shape))
+    ptr = Cm.c_void_p()
+    assert L.ss4d_host_alloc(8 * n, Cm.byref(ptr)) == 0
+    a = np.ctypeslib.as_array((Cm.c_double * n).from_address(ptr.value)).reshape(shape)
+    return a, (lambda: L.ss4d_host_free(ptr))
+
+
+@pytest.mark.parametrize("form", ["fp64", "mixed", "extrap"])
+@pytest.mark.parametrize("nt", [1, 3, 6])
+def test_host_array_step_equals_device_step(ss4d, oracle, cuda, form, nt):
+    """ss4d_seg_time_step_host (u up and down in frame chunks overlapped with
+    the step's first and last kernels, Mmask beside the solve, prev_u copied
+    on the host) gives, step after step, the u of ss4d_seg_time_step on device
+    arrays with the same Mmask and balls, and prev_u = the step's input."""
+    torch = cuda
+    nx, ny, nz = 20, 18, 14
+    p = ss4d.scene_params(ballRadius=3.0)
+    i0h, u0h = ss4d.scene(1, nx, ny, nz, nt, seed=8)
+    shape = i0h.shape
+    g = [dev(torch, a) for a in oracle.gfaces(p, i0h, np.zeros_like(i0h))]
+    rng = np.random.default_rng(2)
+    mask = (rng.random(shape) > 0.1).astype(np.float64)
+    balls = [(l, 10.0, 9.0, 7.0) for l in range(1, nt + 1)] + [(l, 6.0, 12.0, 8.0) for l in range(1, nt + 1, 2)]
+    balls.sort(key=lambda b: b[0])
+    arith = "fp64" if form == "fp64" else "mixed"
+    hu, free_u = _pinned(ss4d, shape)
+    hp, free_p = _pinned(ss4d, shape)
+    hm, free_m = _pinned(ss4d, shape)
+    try:
+        hu[...] = u0h
+        hm[...] = mask
+        du, dm = torch.zeros_like(g[0]), torch.zeros_like(g[0])
+        ref_u, ref_m = dev(torch, u0h), dev(torch, mask)
+        with ss4d.Solver(*shape[::-1], arith=arith) as A, ss4d.Solver(*shape[::-1], arith=arith) as B:
+            A.set_extrapolation(3 if form == "extrap" else 0)
+            B.set_extrapolation(3 if form == "extrap" else 0)
+            for _ in range(3):
+                before = hu.copy()
+                sa = A.seg_time_step_host(p, hu, du, g, h_prev=hp, h_mmask=hm, d_mmask=dm, balls=balls)
+                sb = B.seg_time_step(p, ref_u, None, g, ref_m, balls)
+                B.synchronize()
+                assert sa["iterations"] == sb["iterations"] and sa["status"] == 0
+                assert np.array_equal(hu, host(ref_u))
+                assert np.array_equal(hp, before)
+    finally:
+        free_u(), free_p(), free_m()

@@ -1447,20 +1447,31 @@ extern "C" ss4d_status ss4d_seg_time_step_host(ss4d_solver *s, const ss4d_params
         CK(cudaMemcpyAsync(d_Mmask, h_Mmask, sizeof(double) * all, cudaMemcpyHostToDevice, s->side));
         CK(cudaEventRecord(s->mask_ev, s->side));
     }
-    // a chunk's first differences read the next frame: its chunk too
+    // stage c, once chunks c and c + 1 are up (a first difference reads the
+    // next frame): the pack and, in the mixed form, the first differences of
+    // chunk c's frames and the faces and coefficients whose inputs are then
+    // complete (faces of frame l read the differences of l-1 .. l+1, the
+    // coefficients of l the faces of l-1 and l); the last stage does the rest
+    int fh = 0, vh = 1; // next frame of faces / of coefficients
     for (int c = 0; c < C; ++c) {
         CK(cudaStreamWaitEvent(s->stream, s->chunk_ev[c], 0));
         if (c + 1 < C)
             CK(cudaStreamWaitEvent(s->stream, s->chunk_ev[c + 1], 0));
-        if (mixed)
+        if (mixed) {
             launch_fdiff_range(g, d_u, s->sb, F[c], F[c + 1], s->sm_count, s->stream);
+            const bool last = c + 1 == C;
+            int fe = last ? g.nt + 1 : F[c + 1] - 1;
+            fe = fe < fh ? fh : (fe > g.nt + 1 ? g.nt + 1 : fe);
+            const int ve = fe < vh ? vh : fe;
+            launch_assemble_ff_faces_range(g, s->sp, gi, 1, *p, s->sb, fh, fe, vh, ve, s->stream);
+            s->launches += 1 + (fe > fh) + (ve > vh);
+            fh = fe;
+            vh = ve;
+        }
         launch_pack_range(g, s->sp, d_u, d_u, s->sb, F[c], F[c + 1], s->stream);
-        s->launches += mixed ? 2 : 1;
+        s->launches += 1;
     }
-    if (mixed) {
-        launch_assemble_ff_faces(g, s->sp, gi, 1, *p, s->sb, s->stream);
-        s->launches += 2;
-    } else {
+    if (!mixed) {
         launch_assemble(g, s->sp, d_u, gi, 1, *p, s->sb, 0, s->stream);
         s->launches += 2;
     }

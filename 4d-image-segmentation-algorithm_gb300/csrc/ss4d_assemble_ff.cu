@@ -66,11 +66,11 @@ __global__ void __launch_bounds__(256) k_fdiff(Geo g, const double *__restrict__
 }
 
 // faces of voxels v with every index in [0, n_a], as k_faces
-__global__ void __launch_bounds__(256) k_faces_ff(Geo g, CPtrs8 gin, int has_g, FFConst K, SplitBufs b)
+__global__ void __launch_bounds__(256) k_faces_ff(Geo g, CPtrs8 gin, int has_g, FFConst K, SplitBufs b, int l_off)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z % (g.nz + 1), l = blockIdx.z / (g.nz + 1);
+    const int k = blockIdx.z % (g.nz + 1), l = l_off + blockIdx.z / (g.nz + 1);
     if (i > g.nx || j > g.ny)
         return;
     const int idx[4] = {i, j, k, l};
@@ -118,11 +118,11 @@ __global__ void __launch_bounds__(256) k_faces_ff(Geo g, CPtrs8 gin, int has_g, 
     }
 }
 
-__global__ void __launch_bounds__(256) k_voxel_coef_ff(Geo g, Split sp, FFConst K, SplitBufs b)
+__global__ void __launch_bounds__(256) k_voxel_coef_ff(Geo g, Split sp, FFConst K, SplitBufs b, int l_off)
 {
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = 1 + blockIdx.z % g.nz, l = 1 + blockIdx.z / g.nz;
+    const int k = 1 + blockIdx.z % g.nz, l = 1 + l_off + blockIdx.z / g.nz;
     if (i > g.nx || j > g.ny)
         return;
     const long long o = nat_index(g, i, j, k, l);
@@ -189,6 +189,12 @@ void launch_assemble_ff(const Geo &g, const Split &s, const double *u, CPtrs8 gi
 void launch_assemble_ff_faces(const Geo &g, const Split &s, CPtrs8 gin, int has_g, const ss4d_params &p, SplitBufs b,
                               cudaStream_t st)
 {
+    launch_assemble_ff_faces_range(g, s, gin, has_g, p, b, 0, g.nt + 1, 1, g.nt + 1, st);
+}
+
+void launch_assemble_ff_faces_range(const Geo &g, const Split &s, CPtrs8 gin, int has_g, const ss4d_params &p,
+                                    SplitBufs b, int f0, int f1, int v0, int v1, cudaStream_t st)
+{
     FFConst K;
     split_host(1.0 / (p.h * p.h), K.ih2h, K.ih2l);
     split_host(1.0 / (16.0 * p.h * p.h), K.iq2h, K.iq2l);
@@ -200,15 +206,17 @@ void launch_assemble_ff_faces(const Geo &g, const Split &s, CPtrs8 gin, int has_
         const int bx = g.nx + 1 >= 128 ? 128 : (g.nx + 1 >= 64 ? 64 : 32);
         const int by = 256 / bx;
         dim3 bl(bx, by, 1);
-        dim3 gr((g.nx + 1 + bx - 1) / bx, (g.ny + 1 + by - 1) / by, (g.nz + 1) * (g.nt + 1));
-        k_faces_ff<<<gr, bl, 0, st>>>(g, gin, has_g, K, b);
+        dim3 gr((g.nx + 1 + bx - 1) / bx, (g.ny + 1 + by - 1) / by, (g.nz + 1) * (f1 - f0));
+        if (f1 > f0)
+            k_faces_ff<<<gr, bl, 0, st>>>(g, gin, has_g, K, b, f0);
     }
     {
         const int bx = g.nx >= 128 ? 128 : (g.nx >= 64 ? 64 : 32);
         const int by = 256 / bx;
         dim3 bl(bx, by, 1);
-        dim3 gr((g.nx + bx - 1) / bx, (g.ny + by - 1) / by, g.nz * g.nt);
-        k_voxel_coef_ff<<<gr, bl, 0, st>>>(g, s, K, b);
+        dim3 gr((g.nx + bx - 1) / bx, (g.ny + by - 1) / by, g.nz * (v1 - v0));
+        if (v1 > v0)
+            k_voxel_coef_ff<<<gr, bl, 0, st>>>(g, s, K, b, v0 - 1);
     }
 }
 

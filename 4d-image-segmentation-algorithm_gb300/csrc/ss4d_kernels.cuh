@@ -147,6 +147,12 @@ void launch_assemble_ff(const Geo &g, const Split &s, const double *u, CPtrs8 gi
 void launch_fdiff_range(const Geo &g, const double *u, SplitBufs b, int l0, int l1, int sm_count, cudaStream_t st);
 void launch_assemble_ff_faces(const Geo &g, const Split &s, CPtrs8 gin, int has_g, const ss4d_params &p, SplitBufs b,
                               cudaStream_t st);
+// faces of the frames [f0, f1) of the extended box (0 .. nt; they need the
+// first differences of frames f0-1 .. f1) and coefficients of the interior
+// frames [v0, v1) (they need the faces of frames v0-1 .. v1-1); empty ranges
+// launch nothing
+void launch_assemble_ff_faces_range(const Geo &g, const Split &s, CPtrs8 gin, int has_g, const ss4d_params &p,
+                                    SplitBufs b, int f0, int f1, int v0, int v1, cudaStream_t st);
 // frame ranges: padded frames [l0, l1) for the pack, interior frames
 // [l0, l1) (1 <= l0 < l1 <= lMax-1) for the unpack and the rescale
 void launch_pack_range(const Geo &g, const Split &s, const double *u, const double *prev, SplitBufs b, int l0, int l1,

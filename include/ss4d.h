@@ -256,11 +256,11 @@ ss4d_status ss4d_seg_time_step(ss4d_solver *s, const ss4d_params *p, double *d_u
  * h_Mmask (page-locked, NULL = all ones) goes up into d_Mmask beside the
  * solve, since only the final rescale reads it.  In the FP64 and mixed forms
  * u goes up in SS4D_HOST_CHUNKS chunks of frames on the handle's side stream
- * while the first kernels of the step (first differences, pack) start on the
- * chunks that have arrived, and comes down in chunks as the unpack and the
- * rescale finish them; the results equal ss4d_seg_time_step's.  Returns when
- * h_u holds the result. */
-#define SS4D_HOST_CHUNKS 4
+ * while the step's first kernels (the pack; in the mixed form the whole
+ * coefficient assembly) work on the frames that have arrived, and comes down
+ * in chunks as the unpack and the rescale finish them; the results equal
+ * ss4d_seg_time_step's.  Returns when h_u holds the result. */
+#define SS4D_HOST_CHUNKS 8
 ss4d_status ss4d_seg_time_step_host(ss4d_solver *s, const ss4d_params *p, double *h_u, double *d_u,
                                     double *h_prev, const double *h_Mmask, double *d_Mmask,
                                     const double *const d_g[8], const ss4d_balls *balls,

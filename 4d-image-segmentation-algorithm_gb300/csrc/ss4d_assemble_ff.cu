@@ -65,57 +65,174 @@ __global__ void __launch_bounds__(256) k_fdiff(Geo g, const double *__restrict__
     }
 }
 
-// faces of voxels v with every index in [0, n_a], as k_faces
-__global__ void __launch_bounds__(256) k_faces_ff(Geo g, CPtrs8 gin, int has_g, FFConst K, SplitBufs b, int l_off)
+// --- faces ------------------------------------------------------------------
+// A block takes a tile of FTX x FTY voxels (i, j) of one (k, l) plane.  The
+// central differences D_a of every voxel are formed once, by its own thread,
+// and the i- and j-faces read those of their upper neighbour from shared
+// memory (the tile plus one column and one row of halo); the k- and l-faces
+// form them at v + e_k and v + e_l.  Each quantity is computed with the same
+// operations in the same order as a per-face evaluation would.  Offsets are
+// 32-bit (padded volumes below 2^31 voxels).
+constexpr int FTX = 32, FTY = 8;
+
+__device__ __forceinline__ ff ldf(const float2 *__restrict__ p, unsigned x)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z % (g.nz + 1), l = l_off + blockIdx.z / (g.nz + 1);
-    if (i > g.nx || j > g.ny)
-        return;
-    const int idx[4] = {i, j, k, l};
-    const long long o = nat_index(g, i, j, k, l);
-    const long long st[4] = {1, g.sy, g.sz, g.sw};
-    const ff ih2 = ff_make(K.ih2h, K.ih2l), iq2 = ff_make(K.iq2h, K.iq2l), eps2 = ff_make(K.eps2h, K.eps2l);
-    // central differences at v along the axes where v is interior (each is
-    // added once more below, so left unnormalised)
-    ff D[4];
+    const float2 v = __ldg(p + x);
+    return ff_make(v.x, v.y);
+}
+
+// D_a(x) = F_a(x) + F_a(x - e_a), unnormalised (it is added again)
+__device__ __forceinline__ ff cdiff(const float2 *__restrict__ fa, unsigned x, unsigned sa)
+{
+    return ff_add_nr(ldf(fa, x), ldf(fa, x - sa));
+}
+
+// the face between v and v + e_D: Dv, Dn the central differences at v and
+// v + e_D along the axes a != D, cn = F_D(v), gv its g; writes
+// fn = |grad u|_eps and fq = g / |grad u|_eps at v
+template <int D>
+__device__ __forceinline__ void face_ff(const FFConst &K, const ff Dv[4], const ff Dn[4], ff cn, ff gv,
+                                        const SplitBufs &b, unsigned o)
+{
+    ff tt = ff_make(0.f, 0.f); // sum of squares: positive terms, renormalised once
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        if (a == D)
+            continue;
+        const ff t = ff_add(Dn[a], Dv[a]); // may cancel: renormalised before squaring
+        const float p = t.h * t.h;
+        tt = ff_add_nr(tt, ff_make(p, fmaf(2.f * t.h, t.l, fmaf(t.h, t.h, -p))));
+    }
+    tt = ff_norm(tt);
+    const ff cn2 = ff_sqr(cn);
+    const ff a1 = K.pow2 ? ff_make(cn2.h * K.ih2h, cn2.l * K.ih2h) : ff_mul(cn2, ff_make(K.ih2h, K.ih2l));
+    const ff a2 = K.pow2 ? ff_make(tt.h * K.iq2h, tt.l * K.iq2h) : ff_mul(tt, ff_make(K.iq2h, K.iq2l));
+    const ff s2 = ff_add(ff_add_nr(a1, a2), ff_make(K.eps2h, K.eps2l));
+    const ff y = ff_rsqrt(s2);
+    const ff r = ff_mul(s2, y), q = ff_mul(gv, y);
+    __stcs(reinterpret_cast<float2 *>(b.fn[D]) + o, make_float2(r.h, r.l));
+    __stcs(reinterpret_cast<float2 *>(b.fq[D]) + o, make_float2(q.h, q.l));
+}
+
+// g of the face between v and v + e_D: stored at v (g_e, g_n, ...) where v is
+// interior along D, else at v + e_D (g_w, g_s, ...)
+template <int D, int UPPER>
+__device__ __forceinline__ ff face_g(const CPtrs8 &gin, int has_g, unsigned x)
+{
+    return has_g ? ff_from_d(__ldg(gin.p[2 * D + UPPER] + x)) : ff_make(1.f, 0.f);
+}
+
+// the single face along D of a voxel v whose index along D is 0 (and >= 1
+// along the others): the face between the ghost v and v + e_D
+template <int D>
+__device__ __forceinline__ void boundary_face(const FFConst &K, const CPtrs8 &gin, int has_g, const SplitBufs &b,
+                                              const float2 *const F[4], const unsigned st[4], unsigned o,
+                                              const ff Dn[4])
+{
+    ff Dv[4];
 #pragma unroll
     for (int a = 0; a < 4; ++a)
-        D[a] = idx[a] >= 1 ? ff_add_nr(ld_ff(b.fd[a], o), ld_ff(b.fd[a], o - st[a])) : ff_make(0.f, 0.f);
+        Dv[a] = a == D ? ff_make(0.f, 0.f) : cdiff(F[a], o, st[a]);
+    face_ff<D>(K, Dv, Dn, ldf(F[D], o), face_g<D, 1>(gin, has_g, o + st[D]), b, o);
+}
+
+// the faces of every voxel v with all indices in [0, n_a] whose faces
+// between v and v + e_d have v and v + e_d in the extended box: all four for
+// interior v, the one along a where v's index along a is 0 (and none where
+// two indices are); frames l_off .. l_off + gridDim.z / (nz + 1) - 1
+__global__ void __launch_bounds__(FTX *FTY) k_faces_ff(Geo g, CPtrs8 gin, int has_g, FFConst K, SplitBufs b,
+                                                        int l_off)
+{
+    __shared__ float2 sD[4][FTY + 1][FTX + 1];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i0 = 1 + blockIdx.x * FTX, j0 = 1 + blockIdx.y * FTY;
+    const int i = i0 + tx, j = j0 + ty;
+    const int k = blockIdx.z % (g.nz + 1), l = l_off + blockIdx.z / (g.nz + 1);
+    const unsigned st[4] = {1u, (unsigned)g.sy, (unsigned)g.sz, (unsigned)g.sw};
+    const float2 *const F[4] = {reinterpret_cast<const float2 *>(b.fd[0]), reinterpret_cast<const float2 *>(b.fd[1]),
+                                reinterpret_cast<const float2 *>(b.fd[2]), reinterpret_cast<const float2 *>(b.fd[3])};
+    const unsigned o = (((unsigned)l * g.kM + k) * g.jM + j) * g.iM + i;
+    if (k == 0 || l == 0) { // ghost plane or frame: its one face along k or l
+        if (k == l || i > g.nx || j > g.ny)
+            return;
+        ff Dn[4];
+        if (k == 0) {
 #pragma unroll
-    for (int d = 0; d < 4; ++d) {
-        bool ok = true;
+            for (int a = 0; a < 4; ++a)
+                Dn[a] = a == 2 ? ff_make(0.f, 0.f) : cdiff(F[a], o + st[2], st[a]);
+            boundary_face<2>(K, gin, has_g, b, F, st, o, Dn);
+        } else {
 #pragma unroll
-        for (int a = 0; a < 4; ++a)
-            if (a != d && idx[a] < 1)
-                ok = false;
-        if (!ok)
-            continue;
-        const long long nb = o + st[d];
-        const ff cn = ld_ff(b.fd[d], o);
-        ff tt = ff_make(0.f, 0.f); // sum of squares: positive terms, renormalised once
+            for (int a = 0; a < 4; ++a)
+                Dn[a] = a == 3 ? ff_make(0.f, 0.f) : cdiff(F[a], o + st[3], st[a]);
+            boundary_face<3>(K, gin, has_g, b, F, st, o, Dn);
+        }
+        return;
+    }
+    // central differences of the tile (ghost column / row included) ...
+    ff Dv[4];
+    if (i <= g.nx + 1 && j <= g.ny + 1) {
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
-            if (a == d)
-                continue;
-            const ff Dnb = ff_add_nr(ld_ff(b.fd[a], nb), ld_ff(b.fd[a], nb - st[a]));
-            const ff t = ff_add(Dnb, D[a]); // may cancel: renormalised before squaring
-            const float p = t.h * t.h;
-            tt = ff_add_nr(tt, ff_make(p, fmaf(2.f * t.h, t.l, fmaf(t.h, t.h, -p))));
+            Dv[a] = cdiff(F[a], o, st[a]);
+            sD[a][ty][tx] = make_float2(Dv[a].h, Dv[a].l);
         }
-        tt = ff_norm(tt);
-        const ff cn2 = ff_sqr(cn);
-        const ff a1 = K.pow2 ? ff_make(cn2.h * K.ih2h, cn2.l * K.ih2h) : ff_mul(cn2, ih2);
-        const ff a2 = K.pow2 ? ff_make(tt.h * K.iq2h, tt.l * K.iq2h) : ff_mul(tt, iq2);
-        const ff s2 = ff_add(ff_add_nr(a1, a2), eps2);
-        const ff y = ff_rsqrt(s2);
-        ff gv = ff_make(1.f, 0.f);
-        if (has_g)
-            gv = ff_from_d(idx[d] >= 1 ? __ldg(gin.p[2 * d] + o) : __ldg(gin.p[2 * d + 1] + nb));
-        st_ff(b.fn[d], o, ff_mul(s2, y));
-        st_ff(b.fq[d], o, ff_mul(gv, y));
     }
+    // ... and of its halo: row j0 + FTY (for the j-faces of the tile's last
+    // row) and column i0 + FTX (for the i-faces of its last column), where
+    // those faces exist
+    if (ty == 0) {
+        if (i <= g.nx && j0 + FTY <= g.ny + 1) {
+            const unsigned oh = o + FTY * st[1];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+                if (a != 1) {
+                    const ff d = cdiff(F[a], oh, st[a]);
+                    sD[a][FTY][tx] = make_float2(d.h, d.l);
+                }
+        }
+    } else if (ty == 1 && tx < FTY) {
+        if (i0 + FTX <= g.nx + 1 && j0 + tx <= g.ny) {
+            const unsigned oh = (((unsigned)l * g.kM + k) * g.jM + (j0 + tx)) * g.iM + (i0 + FTX);
+#pragma unroll
+            for (int a = 1; a < 4; ++a) {
+                const ff d = cdiff(F[a], oh, st[a]);
+                sD[a][tx][FTX] = make_float2(d.h, d.l);
+            }
+        }
+    }
+    __syncthreads();
+    if (i > g.nx || j > g.ny)
+        return;
+    ff Dn[4];
+    // i-face and j-face: the upper neighbour's differences from the tile
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const float2 v = sD[a][ty][tx + 1];
+        Dn[a] = ff_make(v.x, v.y);
+    }
+    face_ff<0>(K, Dv, Dn, ldf(F[0], o), face_g<0, 0>(gin, has_g, o), b, o);
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const float2 v = sD[a][ty + 1][tx];
+        Dn[a] = ff_make(v.x, v.y);
+    }
+    face_ff<1>(K, Dv, Dn, ldf(F[1], o), face_g<1, 0>(gin, has_g, o), b, o);
+    // k-face and l-face: the differences at v + e_k and v + e_l
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+        Dn[a] = a == 2 ? ff_make(0.f, 0.f) : cdiff(F[a], o + st[2], st[a]);
+    face_ff<2>(K, Dv, Dn, ldf(F[2], o), face_g<2, 0>(gin, has_g, o), b, o);
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+        Dn[a] = a == 3 ? ff_make(0.f, 0.f) : cdiff(F[a], o + st[3], st[a]);
+    face_ff<3>(K, Dv, Dn, ldf(F[3], o), face_g<3, 0>(gin, has_g, o), b, o);
+    // the faces between the ghosts i = 0 / j = 0 and the first voxel: the
+    // thread of that voxel (its differences are the upper side's)
+    if (i == 1)
+        boundary_face<0>(K, gin, has_g, b, F, st, o - 1, Dv);
+    if (j == 1)
+        boundary_face<1>(K, gin, has_g, b, F, st, o - st[1], Dv);
 }
 
 __global__ void __launch_bounds__(256) k_voxel_coef_ff(Geo g, Split sp, FFConst K, SplitBufs b, int l_off)
@@ -202,13 +319,9 @@ void launch_assemble_ff_faces_range(const Geo &g, const Split &s, CPtrs8 gin, in
     split_host(p.tau / (p.h * p.h), K.ch, K.cl);
     int e1 = 0, e2 = 0;
     K.pow2 = K.ih2l == 0.f && K.iq2l == 0.f && frexp((double)K.ih2h, &e1) == 0.5 && frexp((double)K.iq2h, &e2) == 0.5;
-    {
-        const int bx = g.nx + 1 >= 128 ? 128 : (g.nx + 1 >= 64 ? 64 : 32);
-        const int by = 256 / bx;
-        dim3 bl(bx, by, 1);
-        dim3 gr((g.nx + 1 + bx - 1) / bx, (g.ny + 1 + by - 1) / by, (g.nz + 1) * (f1 - f0));
-        if (f1 > f0)
-            k_faces_ff<<<gr, bl, 0, st>>>(g, gin, has_g, K, b, f0);
+    if (f1 > f0) {
+        dim3 gr((g.nx + FTX - 1) / FTX, (g.ny + FTY - 1) / FTY, (g.nz + 1) * (f1 - f0));
+        k_faces_ff<<<gr, dim3(FTX, FTY, 1), 0, st>>>(g, gin, has_g, K, b, f0);
     }
     {
         const int bx = g.nx >= 128 ? 128 : (g.nx >= 64 ? 64 : 32);

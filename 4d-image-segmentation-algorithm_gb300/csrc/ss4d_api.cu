@@ -651,11 +651,20 @@ static ss4d_status finish_stats(ss4d_solver *s, ss4d_step_stats *stats, int mixe
 }
 
 // coefficient assembly from u into the split records: FP64 (plain form,
-// FP64 throughout) or float-float (mixed form, FP32 records for its sweeps)
-static void assemble(ss4d_solver *s, const ss4d_params *p, const double *d_u, CPtrs8 gi, int has_g, int mixed)
+// FP64 throughout) or float-float (mixed form, FP32 records for its sweeps).
+// With pack, the mixed form also makes the split copies of u (prev = u) in
+// its first-difference kernel: packed_by_assembly() says whether that
+// replaces the caller's launch_pack.
+static bool packed_by_assembly(int mixed)
+{
+    return mixed != 0;
+}
+
+static void assemble(ss4d_solver *s, const ss4d_params *p, const double *d_u, CPtrs8 gi, int has_g, int mixed,
+                     int pack = 0)
 {
     if (mixed) {
-        launch_assemble_ff(s->geo, s->sp, d_u, gi, has_g, *p, s->sb, s->sm_count, s->stream);
+        launch_assemble_ff(s->geo, s->sp, d_u, gi, has_g, *p, s->sb, pack, s->sm_count, s->stream);
         s->launches += 3;
     } else {
         launch_assemble(s->geo, s->sp, d_u, gi, has_g, *p, s->sb, 0, s->stream);
@@ -727,9 +736,7 @@ extern "C" ss4d_status ss4d_ws_features(ss4d_solver *s, const ss4d_params *p, do
     CKS(ensure_split(s, 1));
     s->have_dprev = 0; // the corrections are overwritten below
     const Split &sp = s->sp;
-    assemble(s, p, d_u, gi, 1, 1);
-    launch_pack(s->geo, sp, d_u, d_u, s->sb, s->stream);
-    s->launches += 1;
+    assemble(s, p, d_u, gi, 1, 1, 1);
     CKS(upload_params(s, p));
     const size_t fb = sizeof(float) * sp.cs;
     CK(cudaMemsetAsync(s->sb.dR[0], 0, fb, s->stream));
@@ -1265,13 +1272,16 @@ static ss4d_status unpack_step(ss4d_solver *s, const LoopState *d_state, double 
     return last_launch();
 }
 
+// packed: the split copies of u and prev are made already
 static ss4d_status split_solve(ss4d_solver *s, const ss4d_params *p, double *d_u, const double *d_prev,
-                               ss4d_step_stats *stats)
+                               ss4d_step_stats *stats, bool packed = false)
 {
     const int mixed = s->arith == SS4D_ARITH_MIXED;
-    timed(s, SS4D_K_PACK, true, [&] { launch_pack(s->geo, s->sp, d_u, d_prev, s->sb, s->stream); });
-    s->launches += 1;
-    CKS(last_launch());
+    if (!packed) {
+        timed(s, SS4D_K_PACK, true, [&] { launch_pack(s->geo, s->sp, d_u, d_prev, s->sb, s->stream); });
+        s->launches += 1;
+        CKS(last_launch());
+    }
     CKS(run_split_loop(s, p, mixed));
     CKS(unpack_step(s, s->d_state, d_u, mixed));
     ss4d_status st = finish_stats(s, stats, mixed);
@@ -1349,11 +1359,11 @@ extern "C" ss4d_status ss4d_seg_time_step(ss4d_solver *s, const ss4d_params *p, 
         CKS(ensure_split(s, mixed));
         if (d_prev_u)
             CK(cudaMemcpyAsync(d_prev_u, d_u, sizeof(double) * g.n, cudaMemcpyDeviceToDevice, s->stream));
-        timed(s, SS4D_K_ASSEMBLE, true, [&] { assemble(s, p, d_u, gi, 1, mixed); });
+        timed(s, SS4D_K_ASSEMBLE, true, [&] { assemble(s, p, d_u, gi, 1, mixed, 1); });
         CKS(last_launch());
         s->cur_g = gi;
         s->have_g = 1;
-        st = split_solve(s, p, d_u, d_u, stats);
+        st = split_solve(s, p, d_u, d_u, stats, packed_by_assembly(mixed));
         s->have_g = 0;
     }
     if (st == SS4D_OK)
@@ -1448,8 +1458,9 @@ extern "C" ss4d_status ss4d_seg_time_step_host(ss4d_solver *s, const ss4d_params
         CK(cudaEventRecord(s->mask_ev, s->side));
     }
     // stage c, once chunks c and c + 1 are up (a first difference reads the
-    // next frame): the pack and, in the mixed form, the first differences of
-    // chunk c's frames and the faces and coefficients whose inputs are then
+    // next frame): the pack of chunk c's frames and, in the mixed form (whose
+    // first-difference kernel makes the pack's copies), their first
+    // differences and the faces and coefficients whose inputs are then
     // complete (faces of frame l read the differences of l-1 .. l+1, the
     // coefficients of l the faces of l-1 and l); the last stage does the rest
     int fh = 0, vh = 1; // next frame of faces / of coefficients
@@ -1458,7 +1469,7 @@ extern "C" ss4d_status ss4d_seg_time_step_host(ss4d_solver *s, const ss4d_params
         if (c + 1 < C)
             CK(cudaStreamWaitEvent(s->stream, s->chunk_ev[c + 1], 0));
         if (mixed) {
-            launch_fdiff_range(g, d_u, s->sb, F[c], F[c + 1], s->sm_count, s->stream);
+            launch_fdiff_pack_range(g, s->sp, d_u, s->sb, F[c], F[c + 1], s->sm_count, s->stream);
             const bool last = c + 1 == C;
             int fe = last ? g.nt + 1 : F[c + 1] - 1;
             fe = fe < fh ? fh : (fe > g.nt + 1 ? g.nt + 1 : fe);
@@ -1467,9 +1478,10 @@ extern "C" ss4d_status ss4d_seg_time_step_host(ss4d_solver *s, const ss4d_params
             s->launches += 1 + (fe > fh) + (ve > vh);
             fh = fe;
             vh = ve;
+        } else {
+            launch_pack_range(g, s->sp, d_u, d_u, s->sb, F[c], F[c + 1], s->stream);
+            s->launches += 1;
         }
-        launch_pack_range(g, s->sp, d_u, d_u, s->sb, F[c], F[c + 1], s->stream);
-        s->launches += 1;
     }
     if (!mixed) {
         launch_assemble(g, s->sp, d_u, gi, 1, *p, s->sb, 0, s->stream);
@@ -1833,10 +1845,12 @@ ss4d_status ss4d::solver_prepare_step(ss4d_solver *s, const ss4d_params *p, doub
     }
     const int mixed = s->arith == SS4D_ARITH_MIXED;
     CKS(ensure_split(s, mixed));
-    timed(s, SS4D_K_ASSEMBLE, true, [&] { assemble(s, p, d_u, gi, 1, mixed); });
+    timed(s, SS4D_K_ASSEMBLE, true, [&] { assemble(s, p, d_u, gi, 1, mixed, 1); });
     CKS(last_launch());
-    timed(s, SS4D_K_PACK, true, [&] { launch_pack(s->geo, s->sp, d_u, d_u, s->sb, s->stream); });
-    s->launches += 1;
+    if (!packed_by_assembly(mixed)) {
+        timed(s, SS4D_K_PACK, true, [&] { launch_pack(s->geo, s->sp, d_u, d_u, s->sb, s->stream); });
+        s->launches += 1;
+    }
     if (mixed) {
         s->have_g = 1; // a segmentation step: its change feeds the extrapolation
         CKS(clear_corrections(s));

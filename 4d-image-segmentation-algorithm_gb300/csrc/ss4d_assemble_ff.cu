@@ -47,9 +47,14 @@ struct FFConst {
 };
 
 // forward differences of every voxel that has a neighbour along the axis
-// voxels [o0, o1) (whole frames)
-__global__ void __launch_bounds__(256) k_fdiff(Geo g, const double *__restrict__ u, SplitBufs b, long long o0,
-                                               long long o1)
+// voxels [o0, o1) (whole frames).  With PACK also the split copies of u that
+// k_pack makes when prev is u (red voxels into both red buffers, black ones
+// into the black buffer, every voxel into prev of its colour): this kernel
+// is bound by its FP64 subtractions, and the copy rides along on the
+// memory bandwidth it leaves, reading u once for both.
+template <int PACK>
+__global__ void __launch_bounds__(256) k_fdiff(Geo g, Split sp, const double *__restrict__ u, SplitBufs b,
+                                               long long o0, long long o1)
 {
     const long long st[4] = {1, g.sy, g.sz, g.sw};
     for (long long o = o0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; o < o1;
@@ -62,6 +67,17 @@ __global__ void __launch_bounds__(256) k_fdiff(Geo g, const double *__restrict__
 #pragma unroll
         for (int a = 0; a < 4; ++a)
             st_ff(b.fd[a], o, idx[a] < top[a] ? ff_from_d(u[o + st[a]] - uc) : ff_make(0.f, 0.f));
+        if (PACK) {
+            const long long s = (((long long)l * g.kM + k) * g.jM + j) * sp.Hs + ((i + 1) >> 1) + sp.A - 1;
+            if (((i + j + k + l) & 1) == 0) {
+                b.R[0][s] = uc;
+                b.R[1][s] = uc;
+                b.P[0][s] = uc;
+            } else {
+                b.Bk[s] = uc;
+                b.P[1][s] = uc;
+            }
+        }
     }
 }
 
@@ -284,22 +300,33 @@ static void split_host(double v, float &h, float &l)
     l = (float)(v - (double)h);
 }
 
-int max_blocks_fdiff()
+template <int PACK> static int max_blocks_fdiff()
 {
     int a = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_fdiff, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_fdiff<PACK>, 256, 0);
     return a > 0 ? a : 1;
 }
 
 void launch_fdiff_range(const Geo &g, const double *u, SplitBufs b, int l0, int l1, int sm_count, cudaStream_t st)
 {
-    k_fdiff<<<sm_count * max_blocks_fdiff(), 256, 0, st>>>(g, u, b, (long long)l0 * g.sw, (long long)l1 * g.sw);
+    k_fdiff<0><<<sm_count * max_blocks_fdiff<0>(), 256, 0, st>>>(g, Split{}, u, b, (long long)l0 * g.sw,
+                                                                  (long long)l1 * g.sw);
+}
+
+void launch_fdiff_pack_range(const Geo &g, const Split &s, const double *u, SplitBufs b, int l0, int l1, int sm_count,
+                             cudaStream_t st)
+{
+    k_fdiff<1><<<sm_count * max_blocks_fdiff<1>(), 256, 0, st>>>(g, s, u, b, (long long)l0 * g.sw,
+                                                                  (long long)l1 * g.sw);
 }
 
 void launch_assemble_ff(const Geo &g, const Split &s, const double *u, CPtrs8 gin, int has_g, const ss4d_params &p,
-                        SplitBufs b, int sm_count, cudaStream_t st)
+                        SplitBufs b, int pack, int sm_count, cudaStream_t st)
 {
-    launch_fdiff_range(g, u, b, 0, g.lM, sm_count, st);
+    if (pack)
+        launch_fdiff_pack_range(g, s, u, b, 0, g.lM, sm_count, st);
+    else
+        launch_fdiff_range(g, u, b, 0, g.lM, sm_count, st);
     launch_assemble_ff_faces(g, s, gin, has_g, p, b, st);
 }
 

@@ -139,12 +139,17 @@ SweepCfg make_sweep_cfg(const Geo &g, const Split &s, int sm_count, int kb);
 void launch_assemble(const Geo &g, const Split &s, const double *u, CPtrs8 gin, int has_g, const ss4d_params &p,
                      SplitBufs b, int want32, cudaStream_t st);
 void launch_pack(const Geo &g, const Split &s, const double *u, const double *prev, SplitBufs b, cudaStream_t st);
-// mixed form: the same coefficient records from float-float arithmetic (3 kernels)
+// mixed form: the same coefficient records from float-float arithmetic (3
+// kernels); with pack the first of them also makes launch_pack's copies of u
+// with prev = u
 void launch_assemble_ff(const Geo &g, const Split &s, const double *u, CPtrs8 gin, int has_g, const ss4d_params &p,
-                        SplitBufs b, int sm_count, cudaStream_t st);
+                        SplitBufs b, int pack, int sm_count, cudaStream_t st);
 // the same in parts: first differences of padded frames [l0, l1), then the
 // faces and voxel coefficients (after the differences of every frame)
 void launch_fdiff_range(const Geo &g, const double *u, SplitBufs b, int l0, int l1, int sm_count, cudaStream_t st);
+// the same plus launch_pack_range's copies of those frames with prev = u
+void launch_fdiff_pack_range(const Geo &g, const Split &s, const double *u, SplitBufs b, int l0, int l1, int sm_count,
+                             cudaStream_t st);
 void launch_assemble_ff_faces(const Geo &g, const Split &s, CPtrs8 gin, int has_g, const ss4d_params &p, SplitBufs b,
                               cudaStream_t st);
 // faces of the frames [f0, f1) of the extended box (0 .. nt; they need the

@@ -238,14 +238,23 @@ __global__ void k_unpack(Geo g, Split sp, SplitBufs b, const LoopState *__restri
         return;
     const int col = (i + j + k + l) & 1;
     const long long s = (((long long)l * g.kM + k) * g.jM + j) * sp.Hs + ((i + 1) >> 1) + sp.A - 1;
+    // every load before the first store (which could alias them for the
+    // compiler): one round trip to memory, not two
+    float *h1 = pick(hs.h1, col), *h2 = pick(hs.h2, col);
+    double pv = 0.0;
+    float p1 = 0.f, p2 = 0.f;
+    if (terms > 0) {
+        pv = pick(b.P, col)[s];
+        if (terms >= 2)
+            p1 = h1[s];
+        if (terms >= 3)
+            p2 = h2[s];
+    }
     const int fr = st->final_red;
     const double v = col == 0 ? pick(b.R, fr)[s] : b.Bk[s];
     u[nat_index(g, i, j, k, l)] = v;
     if (terms > 0) {
-        const float d = d2f_bits(v - pick(b.P, col)[s]);
-        float *h1 = pick(hs.h1, col), *h2 = pick(hs.h2, col);
-        const float p1 = terms >= 2 ? h1[s] : 0.f;
-        const float p2 = terms >= 3 ? h2[s] : 0.f;
+        const float d = d2f_bits(v - pv);
         float guess = d;
         if (terms == 2)
             guess = fmaf(2.f, d, -p1);

@@ -156,8 +156,11 @@ __device__ __forceinline__ void boundary_face(const FFConst &K, const CPtrs8 &gi
 // between v and v + e_d have v and v + e_d in the extended box: all four for
 // interior v, the one along a where v's index along a is 0 (and none where
 // two indices are); frames l_off .. l_off + gridDim.z / (nz + 1) - 1
-__global__ void __launch_bounds__(FTX *FTY) k_faces_ff(Geo g, CPtrs8 gin, int has_g, FFConst K, SplitBufs b,
-                                                        int l_off)
+// Bound by the latency of its global loads: 8 blocks per SM (32 registers,
+// a few bytes of spill) ran 6.28 ms at 256^2 x 128 x 20 against 6.93 ms
+// at 5 blocks (48 registers) and 6.74 ms at 6.
+__global__ void __launch_bounds__(FTX *FTY, 8) k_faces_ff(Geo g, CPtrs8 gin, int has_g, FFConst K, SplitBufs b,
+                                                           int l_off)
 {
     __shared__ float2 sD[4][FTY + 1][FTX + 1];
     const int tx = threadIdx.x, ty = threadIdx.y;
@@ -251,7 +254,9 @@ __global__ void __launch_bounds__(FTX *FTY) k_faces_ff(Geo g, CPtrs8 gin, int ha
         boundary_face<1>(K, gin, has_g, b, F, st, o - st[1], Dv);
 }
 
-__global__ void __launch_bounds__(256) k_voxel_coef_ff(Geo g, Split sp, FFConst K, SplitBufs b, int l_off)
+// Memory-bound, its warps waiting on loads: 8 blocks per SM (32 registers)
+// rather than 7 took the assembly from 13.5 to 13.0 ms at 256^2 x 128 x 20.
+__global__ void __launch_bounds__(256, 8) k_voxel_coef_ff(Geo g, Split sp, FFConst K, SplitBufs b, int l_off)
 {
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;

@@ -241,7 +241,10 @@ extern "C" ss4d_status ss4d_solver_create(const ss4d_dims *dims, ss4d_arith arit
     } while (0)
     FAIL_IF(cudaGetDevice(&s->device));
     FAIL_IF(cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device));
-    s->cfg = make_sweep_cfg(s->geo, s->sp, s->sm_count, 4);
+    // k blocks of one plane: at 256^2 x 128 x 20 the FP32 half-sweep took
+    // 0.693 ms against 0.714 ms with blocks of 4 planes, the FP64 one 1.685
+    // against 1.751 ms (a refinement kernel 2.023 against 1.996 ms)
+    s->cfg = make_sweep_cfg(s->geo, s->sp, s->sm_count, 1);
     FAIL_IF(cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking));
     FAIL_IF(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
     FAIL_IF(cudaEventCreateWithFlags(&s->side_ev, cudaEventDisableTiming));

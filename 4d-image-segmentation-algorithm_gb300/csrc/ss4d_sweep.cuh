@@ -82,8 +82,9 @@ struct TileCoord {
 
 // Tile order: x chunk fastest, then j group, then k inside a k block, then
 // frame l, then k block.  Consecutive tiles (which a persistent grid works on
-// at the same time) thus cover a few k planes of all frames, so the
-// neighbouring-plane reads of the other colour hit in L2.
+// at the same time) thus cover a few k planes (one with the default block
+// depth of 1) of all frames, so the neighbouring-plane reads of the other
+// colour hit in L2.
 __device__ __forceinline__ TileCoord tile_coord(const Geo &g, const SweepCfg &cfg, long long t, int tx, int ty)
 {
     TileCoord c;

@@ -133,6 +133,7 @@ struct ss4d_solver {
     // mixed form: start from an extrapolation in time (ss4d_solver_set_extrapolation)
     int extrap;      // 0 off, else the extrapolation order 1..3
     int have_dprev;  // steps in a row whose change was kept: dR[0] / dB hold the next start correction
+    int pre_next;    // the next mixed loop's first refinement pass was formed by the assembly
     float *hist[4];  // earlier steps' changes (split layout): h1 red, h1 black, h2 red, h2 black
     double inner_omega; // mixed form: relaxation factor of the FP32 sweeps (0: omega_c)
     // per-kernel timing (ss4d_solver_set_timing)
@@ -473,6 +474,11 @@ static ss4d_status ensure_split(ss4d_solver *s, int mixed)
         CKS(dmalloc(s, (void **)&fd, sizeof(double) * 4 * (size_t)s->geo.n));
         for (int d = 0; d < 4; ++d)
             s->sb.fd[d] = fd + (size_t)d * s->geo.n;
+        double *rp = nullptr; // the first refinement pass's residual, per colour (split layout)
+        CKS(dmalloc(s, (void **)&rp, sizeof(double) * 2 * cs));
+        CK(cudaMemsetAsync(rp, 0, sizeof(double) * 2 * cs, s->stream));
+        s->sb.rpre[0] = rp;
+        s->sb.rpre[1] = rp + cs;
         s->have_mixed = 1;
         free_graphs(s); // kernel arguments changed
     }
@@ -664,10 +670,10 @@ static bool packed_by_assembly(int mixed)
 }
 
 static void assemble(ss4d_solver *s, const ss4d_params *p, const double *d_u, CPtrs8 gi, int has_g, int mixed,
-                     int pack = 0)
+                     int pack = 0, int pre = 0)
 {
     if (mixed) {
-        launch_assemble_ff(s->geo, s->sp, d_u, gi, has_g, *p, s->sb, pack, s->sm_count, s->stream);
+        launch_assemble_ff(s->geo, s->sp, d_u, gi, has_g, *p, s->sb, pack, s->sm_count, s->stream, pre);
         s->launches += 3;
     } else {
         launch_assemble(s->geo, s->sp, d_u, gi, has_g, *p, s->sb, 0, s->stream);
@@ -763,6 +769,22 @@ static bool extrapolating(const ss4d_solver *s)
     return s->arith == SS4D_ARITH_MIXED && s->extrap && s->have_dprev && s->have_g && !s->ws_net;
 }
 
+// A mixed segmentation step (not with the learned warm start, which runs
+// its own first pass before its prediction) has the assembly form its first
+// refinement pass: the first-difference kernel adds the start correction to
+// the split copies of u with the pass's FP64 addition, the coefficient
+// kernel evaluates the pass's FP64 residual with the pass's operations on
+// the same values, and the pass only reads that residual (LoopState.pre).
+// The step's results are those of the pass run in full.  Returns 0 (not
+// this step), 1 (start correction zero) or 2 (the extrapolation that
+// extrapolating() will find in dR[0] / dB).
+static int pre_form(const ss4d_solver *s, int mixed)
+{
+    if (!mixed || s->ws_net)
+        return 0;
+    return s->extrap && s->have_dprev ? 2 : 1;
+}
+
 // the mixed loop's start correction: zero, or the extrapolation the previous
 // step's unpack left in dR[0] / dB (applied by the first refinement pass)
 static ss4d_status clear_corrections(ss4d_solver *s)
@@ -796,6 +818,8 @@ extern "C" ss4d_status ss4d_solver_set_extrapolation(ss4d_solver *s, int order)
 // the loop on the split buffers; u/prev already packed, coefficients assembled
 static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixed)
 {
+    const int pre = mixed ? s->pre_next : 0; // consumed by this loop only
+    s->pre_next = 0;
     const Geo &g = s->geo;
     const Split &sp = s->sp;
     const SweepCfg &cfg = s->cfg;
@@ -808,8 +832,9 @@ static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixe
         s->launches += 3;
     } else {
         // the first refinement pass adds the correction in dR[0] / dB to u
+        // (or the assembly did, and formed the pass's residual: pre_next)
         CKS(clear_corrections(s));
-        launch_loop_init(s->d_state, 0, s->stream);
+        launch_loop_init(s->d_state, 0, s->stream, pre);
         s->launches += 1;
         if (s->ws_net && s->have_g)
             CKS(warm_start_prologue(s));
@@ -1362,10 +1387,12 @@ extern "C" ss4d_status ss4d_seg_time_step(ss4d_solver *s, const ss4d_params *p, 
         CKS(ensure_split(s, mixed));
         if (d_prev_u)
             CK(cudaMemcpyAsync(d_prev_u, d_u, sizeof(double) * g.n, cudaMemcpyDeviceToDevice, s->stream));
-        timed(s, SS4D_K_ASSEMBLE, true, [&] { assemble(s, p, d_u, gi, 1, mixed, 1); });
+        const int pre = pre_form(s, mixed);
+        timed(s, SS4D_K_ASSEMBLE, true, [&] { assemble(s, p, d_u, gi, 1, mixed, 1, pre); });
         CKS(last_launch());
         s->cur_g = gi;
         s->have_g = 1;
+        s->pre_next = pre != 0;
         st = split_solve(s, p, d_u, d_u, stats, packed_by_assembly(mixed));
         s->have_g = 0;
     }
@@ -1467,17 +1494,18 @@ extern "C" ss4d_status ss4d_seg_time_step_host(ss4d_solver *s, const ss4d_params
     // complete (faces of frame l read the differences of l-1 .. l+1, the
     // coefficients of l the faces of l-1 and l); the last stage does the rest
     int fh = 0, vh = 1; // next frame of faces / of coefficients
+    const int pre = pre_form(s, mixed);
     for (int c = 0; c < C; ++c) {
         CK(cudaStreamWaitEvent(s->stream, s->chunk_ev[c], 0));
         if (c + 1 < C)
             CK(cudaStreamWaitEvent(s->stream, s->chunk_ev[c + 1], 0));
         if (mixed) {
-            launch_fdiff_pack_range(g, s->sp, d_u, s->sb, F[c], F[c + 1], s->sm_count, s->stream);
+            launch_fdiff_pack_range(g, s->sp, d_u, s->sb, F[c], F[c + 1], s->sm_count, s->stream, pre);
             const bool last = c + 1 == C;
             int fe = last ? g.nt + 1 : F[c + 1] - 1;
             fe = fe < fh ? fh : (fe > g.nt + 1 ? g.nt + 1 : fe);
             const int ve = fe < vh ? vh : fe;
-            launch_assemble_ff_faces_range(g, s->sp, gi, 1, *p, s->sb, fh, fe, vh, ve, s->stream);
+            launch_assemble_ff_faces_range(g, s->sp, gi, 1, *p, s->sb, fh, fe, vh, ve, s->stream, pre);
             s->launches += 1 + (fe > fh) + (ve > vh);
             fh = fe;
             vh = ve;
@@ -1493,6 +1521,7 @@ extern "C" ss4d_status ss4d_seg_time_step_host(ss4d_solver *s, const ss4d_params
     CKS(last_launch());
     s->cur_g = gi;
     s->have_g = 1;
+    s->pre_next = pre != 0;
     CKS(run_split_loop(s, p, mixed));
     // the unpack and the rescale per chunk of interior frames, each chunk's
     // download on the side stream as soon as it is done

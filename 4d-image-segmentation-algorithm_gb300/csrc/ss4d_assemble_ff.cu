@@ -51,10 +51,13 @@ struct FFConst {
 // k_pack makes when prev is u (red voxels into both red buffers, black ones
 // into the black buffer, every voxel into prev of its colour): this kernel
 // is bound by its FP64 subtractions, and the copy rides along on the
-// memory bandwidth it leaves, reading u once for both.
+// memory bandwidth it leaves, reading u once for both.  PACK 2 also adds the
+// first refinement pass's start correction to the interior of the u copies
+// the pass would update (red: R[0], black: Bk) with the pass's own FP64
+// addition: the correction in dR[0] / dB (withd) or zero.
 template <int PACK>
 __global__ void __launch_bounds__(256) k_fdiff(Geo g, Split sp, const double *__restrict__ u, SplitBufs b,
-                                               long long o0, long long o1)
+                                               long long o0, long long o1, int withd)
 {
     const long long st[4] = {1, g.sy, g.sz, g.sw};
     for (long long o = o0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; o < o1;
@@ -69,12 +72,17 @@ __global__ void __launch_bounds__(256) k_fdiff(Geo g, Split sp, const double *__
             st_ff(b.fd[a], o, idx[a] < top[a] ? ff_from_d(u[o + st[a]] - uc) : ff_make(0.f, 0.f));
         if (PACK) {
             const long long s = (((long long)l * g.kM + k) * g.jM + j) * sp.Hs + ((i + 1) >> 1) + sp.A - 1;
-            if (((i + j + k + l) & 1) == 0) {
-                b.R[0][s] = uc;
+            const bool red = ((i + j + k + l) & 1) == 0;
+            double u0 = uc;
+            if (PACK == 2 && i >= 1 && i <= g.nx && j >= 1 && j <= g.ny && k >= 1 && k <= g.nz && l >= 1 &&
+                l <= g.nt)
+                u0 = uc + (withd ? f2d_bits(red ? b.dR[0][s] : b.dB[s]) : 0.0);
+            if (red) {
+                b.R[0][s] = u0;
                 b.R[1][s] = uc;
                 b.P[0][s] = uc;
             } else {
-                b.Bk[s] = uc;
+                b.Bk[s] = u0;
                 b.P[1][s] = uc;
             }
         }
@@ -256,7 +264,13 @@ __global__ void __launch_bounds__(FTX *FTY, 8) k_faces_ff(Geo g, CPtrs8 gin, int
 
 // Memory-bound, its warps waiting on loads: 8 blocks per SM (32 registers)
 // rather than 7 took the assembly from 13.5 to 13.0 ms at 256^2 x 128 x 20.
-__global__ void __launch_bounds__(256, 8) k_voxel_coef_ff(Geo g, Split sp, FFConst K, SplitBufs b, int l_off)
+// With PRE it also forms the first refinement pass's FP64 residual at the
+// target exactly as k_refine forms it (prev, then the products of the eight
+// coefficients just written with the other colour's u in record order, then
+// diag u0, with the same fused multiply-adds) on the split copies of u whose
+// start correction the first-difference kernel added, into rpre.
+template <int PRE>
+__global__ void __launch_bounds__(256, PRE ? 6 : 8) k_voxel_coef_ff(Geo g, Split sp, FFConst K, SplitBufs b, int l_off)
 {
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
@@ -281,17 +295,30 @@ __global__ void __launch_bounds__(256, 8) k_voxel_coef_ff(Geo g, Split sp, FFCon
     double *cf = pick(b.coef, col);
     float *cf32 = pick(b.coef32, col);
     const long long t = coef_index(g, sp, i, j, k, l);
+    // split index of the target and its neighbours (row phase p = i & 1)
+    const long long Hy = sp.Hs, Hz = Hy * g.jM, Hw = Hz * g.kM;
+    const long long sx = (((long long)l * g.kM + k) * g.jM + j) * Hy + ((i + 1) >> 1) + sp.A - 1;
+    const int p = i & 1;
+    const long long nb[8] = {sx - p + 1, sx - p, sx + Hy, sx - Hy, sx + Hz, sx - Hz, sx + Hw, sx - Hw};
+    const double *__restrict__ oth = col == 0 ? b.Bk : b.R[0];
+    double S = PRE ? __ldg(pick(b.P, col) + sx) : 0.0;
     ff diag = ff_make(1.f, 0.f);
     float a32[8];
 #pragma unroll
     for (int f = 0; f < 8; ++f) {
         const ff a = ff_mul(cv, q[f]);
         diag = ff_add_nr(diag, a); // positive terms: renormalised after the loop
-        __stcs(cf + coef_at(t, f, 10), ff_to_d(a));
+        const double ad = ff_to_d(a);
+        __stcs(cf + coef_at(t, f, 10), ad);
         a32[f] = a.h;
+        if (PRE)
+            S = fma(ad, __ldg(oth + nb[f]), S);
     }
     diag = ff_norm(diag);
-    __stcs(cf + coef_at(t, 8, 10), ff_to_d(diag));
+    const double dd = ff_to_d(diag);
+    __stcs(cf + coef_at(t, 8, 10), dd);
+    if (PRE)
+        pick(b.rpre, col)[sx] = fma(dd, __ldg((col == 0 ? b.R[0] : b.Bk) + sx), -S);
     // component 9 (omega/diag) serves only the FP64 sweep, whose form always
     // assembles its own records: not written here
     float4 *f4 = reinterpret_cast<float4 *>(cf32 + 8 * t);
@@ -315,34 +342,38 @@ template <int PACK> static int max_blocks_fdiff()
 void launch_fdiff_range(const Geo &g, const double *u, SplitBufs b, int l0, int l1, int sm_count, cudaStream_t st)
 {
     k_fdiff<0><<<sm_count * max_blocks_fdiff<0>(), 256, 0, st>>>(g, Split{}, u, b, (long long)l0 * g.sw,
-                                                                  (long long)l1 * g.sw);
+                                                                  (long long)l1 * g.sw, 0);
 }
 
 void launch_fdiff_pack_range(const Geo &g, const Split &s, const double *u, SplitBufs b, int l0, int l1, int sm_count,
-                             cudaStream_t st)
+                             cudaStream_t st, int pre)
 {
-    k_fdiff<1><<<sm_count * max_blocks_fdiff<1>(), 256, 0, st>>>(g, s, u, b, (long long)l0 * g.sw,
-                                                                  (long long)l1 * g.sw);
+    if (pre)
+        k_fdiff<2><<<sm_count * max_blocks_fdiff<2>(), 256, 0, st>>>(g, s, u, b, (long long)l0 * g.sw,
+                                                                      (long long)l1 * g.sw, pre == 2);
+    else
+        k_fdiff<1><<<sm_count * max_blocks_fdiff<1>(), 256, 0, st>>>(g, s, u, b, (long long)l0 * g.sw,
+                                                                      (long long)l1 * g.sw, 0);
 }
 
 void launch_assemble_ff(const Geo &g, const Split &s, const double *u, CPtrs8 gin, int has_g, const ss4d_params &p,
-                        SplitBufs b, int pack, int sm_count, cudaStream_t st)
+                        SplitBufs b, int pack, int sm_count, cudaStream_t st, int pre)
 {
     if (pack)
-        launch_fdiff_pack_range(g, s, u, b, 0, g.lM, sm_count, st);
+        launch_fdiff_pack_range(g, s, u, b, 0, g.lM, sm_count, st, pre);
     else
         launch_fdiff_range(g, u, b, 0, g.lM, sm_count, st);
-    launch_assemble_ff_faces(g, s, gin, has_g, p, b, st);
+    launch_assemble_ff_faces(g, s, gin, has_g, p, b, st, pack ? pre : 0);
 }
 
 void launch_assemble_ff_faces(const Geo &g, const Split &s, CPtrs8 gin, int has_g, const ss4d_params &p, SplitBufs b,
-                              cudaStream_t st)
+                              cudaStream_t st, int pre)
 {
-    launch_assemble_ff_faces_range(g, s, gin, has_g, p, b, 0, g.nt + 1, 1, g.nt + 1, st);
+    launch_assemble_ff_faces_range(g, s, gin, has_g, p, b, 0, g.nt + 1, 1, g.nt + 1, st, pre);
 }
 
 void launch_assemble_ff_faces_range(const Geo &g, const Split &s, CPtrs8 gin, int has_g, const ss4d_params &p,
-                                    SplitBufs b, int f0, int f1, int v0, int v1, cudaStream_t st)
+                                    SplitBufs b, int f0, int f1, int v0, int v1, cudaStream_t st, int pre)
 {
     FFConst K;
     split_host(1.0 / (p.h * p.h), K.ih2h, K.ih2l);
@@ -360,8 +391,10 @@ void launch_assemble_ff_faces_range(const Geo &g, const Split &s, CPtrs8 gin, in
         const int by = 256 / bx;
         dim3 bl(bx, by, 1);
         dim3 gr((g.nx + bx - 1) / bx, (g.ny + by - 1) / by, g.nz * (v1 - v0));
-        if (v1 > v0)
-            k_voxel_coef_ff<<<gr, bl, 0, st>>>(g, s, K, b, v0 - 1);
+        if (v1 > v0 && pre)
+            k_voxel_coef_ff<1><<<gr, bl, 0, st>>>(g, s, K, b, v0 - 1);
+        else if (v1 > v0)
+            k_voxel_coef_ff<0><<<gr, bl, 0, st>>>(g, s, K, b, v0 - 1);
     }
 }
 

@@ -80,6 +80,8 @@ struct LoopState {
     int keep;        // mixed form: the next round starts from the correction already in place
     int warm;        // mixed form: this step's first correction came from the learned predictor
     int near;        // 1 once a stop test saw |R - tol| <= near_band
+    int pre;         // mixed form: the next refinement pass's residual is in rpre (formed by the
+                     // assembly, which also applied the start correction); cleared by that pass
     double R;        // last FP64 residual (sum r^2 h^4)
     double R_first;  // FP64 residual after iteration 1 (fast) / initial (mixed)
     double Rd;       // mixed form: last FP32 correction residual
@@ -119,6 +121,9 @@ struct SplitBufs {
     // mixed form's float-float assembly (ss4d_assemble_ff.cu): per voxel v and
     // axis a the forward difference u(v + e_a) - u(v) as two floats
     double *fd[4];
+    // mixed form, first refinement pass of a segmentation step: its FP64
+    // residual per target, formed by the coefficient kernel (split layout)
+    double *rpre[2];
 };
 
 struct SweepCfg {
@@ -143,21 +148,26 @@ void launch_pack(const Geo &g, const Split &s, const double *u, const double *pr
 // kernels); with pack the first of them also makes launch_pack's copies of u
 // with prev = u
 void launch_assemble_ff(const Geo &g, const Split &s, const double *u, CPtrs8 gin, int has_g, const ss4d_params &p,
-                        SplitBufs b, int pack, int sm_count, cudaStream_t st);
+                        SplitBufs b, int pack, int sm_count, cudaStream_t st, int pre = 0);
 // the same in parts: first differences of padded frames [l0, l1), then the
 // faces and voxel coefficients (after the differences of every frame)
 void launch_fdiff_range(const Geo &g, const double *u, SplitBufs b, int l0, int l1, int sm_count, cudaStream_t st);
-// the same plus launch_pack_range's copies of those frames with prev = u
+// the same plus launch_pack_range's copies of those frames with prev = u;
+// with pre > 0 the interior of the u copies also receives the first
+// refinement pass's start correction (pre 2: the one in dR[0] / dB; pre 1:
+// zero, added as the pass adds it)
 void launch_fdiff_pack_range(const Geo &g, const Split &s, const double *u, SplitBufs b, int l0, int l1, int sm_count,
-                             cudaStream_t st);
+                             cudaStream_t st, int pre = 0);
 void launch_assemble_ff_faces(const Geo &g, const Split &s, CPtrs8 gin, int has_g, const ss4d_params &p, SplitBufs b,
-                              cudaStream_t st);
+                              cudaStream_t st, int pre = 0);
 // faces of the frames [f0, f1) of the extended box (0 .. nt; they need the
 // first differences of frames f0-1 .. f1) and coefficients of the interior
 // frames [v0, v1) (they need the faces of frames v0-1 .. v1-1); empty ranges
-// launch nothing
+// launch nothing.  With pre the coefficient kernel also forms the first
+// refinement pass's residual into rpre (it needs the corrected split copies
+// of u of frames v0-1 .. v1)
 void launch_assemble_ff_faces_range(const Geo &g, const Split &s, CPtrs8 gin, int has_g, const ss4d_params &p,
-                                    SplitBufs b, int f0, int f1, int v0, int v1, cudaStream_t st);
+                                    SplitBufs b, int f0, int f1, int v0, int v1, cudaStream_t st, int pre = 0);
 // frame ranges: padded frames [l0, l1) for the pack, interior frames
 // [l0, l1) (1 <= l0 < l1 <= lMax-1) for the unpack and the rescale
 void launch_pack_range(const Geo &g, const Split &s, const double *u, const double *prev, SplitBufs b, int l0, int l1,
@@ -189,7 +199,7 @@ void launch_pack_coef(const Geo &g, const Split &s, CPtrs8 a, const ss4d_params 
 // terms/keep/hist: the mixed form's extrapolated start (k_unpack); hist = {h1 red, h1 black, h2 red, h2 black}
 void launch_unpack(const Geo &g, const Split &s, SplitBufs b, const LoopState *state, double *u, cudaStream_t st,
                    int terms = 0, int keep = 0, float *const *hist = nullptr);
-void launch_loop_init(LoopState *state, int mode, cudaStream_t st);
+void launch_loop_init(LoopState *state, int mode, cudaStream_t st, int pre = 0);
 void launch_sweep64(const Geo &g, const Split &s, const SweepCfg &cfg, int colour, SplitBufs b, const DevParams *dp,
                     LoopState *state, cudaStream_t st);
 void launch_advance(LoopState *state, cudaStream_t st);

@@ -271,8 +271,9 @@ __global__ void k_unpack(Geo g, Split sp, SplitBufs b, const LoopState *__restri
     }
 }
 
-__global__ void k_loop_init(LoopState *st, int mode)
+__global__ void k_loop_init(LoopState *st, int mode, int pre)
 {
+    st->pre = pre;
     st->z = 0;
     st->stop = 0;
     st->status = 0;
@@ -368,7 +369,7 @@ __global__ void k_ctrl64(SplitBufs b, int nparts, const DevParams *__restrict__ 
 __global__ void __launch_bounds__(256) k_apply_black(Geo g, Split sp, SweepCfg cfg, SplitBufs b,
                                                      const LoopState *__restrict__ st)
 {
-    if (st->mode != 0 || st->stop)
+    if (st->mode != 0 || st->stop || st->pre) // pre: the first-difference kernel added it
         return;
     const int tx = threadIdx.x & (cfg.XT - 1), ty = threadIdx.x / cfg.XT;
     for (long long t = blockIdx.x; t < cfg.ntiles; t += gridDim.x) {
@@ -398,6 +399,11 @@ __global__ void __launch_bounds__(256) k_refine(Geo g, Split sp, SweepCfg cfg, S
     float *__restrict__ rr = b.r32[COL];
     const long long Hy = sp.Hs, Hz = Hy * g.jM, Hw = Hz * g.kM;
     const int tx = threadIdx.x & (cfg.XT - 1), ty = threadIdx.x / cfg.XT;
+    // pre: the first pass of a step whose residual the coefficient kernel
+    // formed (with the same operations on the same values) and whose
+    // correction the first-difference kernel added; only read here
+    const bool pre = st->pre;
+    const double *__restrict__ rp = b.rpre[COL];
     double acc = 0.0;
     for (long long t = blockIdx.x; t < cfg.ntiles; t += gridDim.x) {
         const TileCoord tc = tile_coord(g, cfg, t, tx, ty);
@@ -408,11 +414,17 @@ __global__ void __launch_bounds__(256) k_refine(Geo g, Split sp, SweepCfg cfg, S
         if (i > g.nx)
             continue;
         const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * Hy + tc.xi + sp.A;
-        const RefineOut o = refine_target<COL>(g, sp, tc, p, s, Hy, Hz, Hw, own, down, oth, cf, pv);
-        acc = fma(o.r, o.r, acc);
-        if (COL == 0)
-            own[s] = o.u;
-        rr[s] = d2f_bits(-o.r);
+        double r;
+        if (pre) {
+            r = ld_stream(rp + s);
+        } else {
+            const RefineOut o = refine_target<COL>(g, sp, tc, p, s, Hy, Hz, Hw, own, down, oth, cf, pv);
+            r = o.r;
+            if (COL == 0)
+                own[s] = o.u;
+        }
+        acc = fma(r, r, acc);
+        rr[s] = d2f_bits(-r);
     }
     acc = block_sum(acc);
     if (threadIdx.x == 0)
@@ -637,9 +649,9 @@ void launch_unpack_range(const Geo &g, const Split &s, SplitBufs b, const LoopSt
     k_unpack<<<gr, bl, 0, st>>>(g, s, b, state, u, terms, keep, hs, l0 - 1);
 }
 
-void launch_loop_init(LoopState *state, int mode, cudaStream_t st)
+void launch_loop_init(LoopState *state, int mode, cudaStream_t st, int pre)
 {
-    k_loop_init<<<1, 1, 0, st>>>(state, mode);
+    k_loop_init<<<1, 1, 0, st>>>(state, mode, pre);
 }
 
 void launch_advance(LoopState *state, cudaStream_t st)

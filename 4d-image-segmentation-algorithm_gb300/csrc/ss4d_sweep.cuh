@@ -250,6 +250,7 @@ __device__ inline bool ctrl_mixed_update(LoopState *st, double a, double c, cons
     st->bodies += 1;
     bool stop = false;
     if (mode == 0) {
+        st->pre = 0; // later passes form their own residual
         const double R = (a + c) * dp->h4;
         if (st->refinements == 0)
             st->R_first = R;

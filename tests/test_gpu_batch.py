@@ -78,7 +78,11 @@ def test_mixed_batch_matches_single_volume_mixed_solves(ss4d, oracle, cuda, extr
     """The mixed form batched (refinement passes and FP32 sweeps of all volumes
     in one launch each, every volume in its own phase) gives each volume what
     its own mixed-form solver gives it, step after step, with and without the
-    extrapolated start: the same counts, the same u, the FP64 tolerance met."""
+    extrapolated start: the same counts, the same u, the FP64 tolerance met.
+    The single-volume solver has its assembly form each step's first
+    refinement pass (start correction and FP64 residual) while the batch runs
+    that pass in full, so this also pins the two forms of the pass to the
+    same bits."""
     torch = cuda
     sizes = [(20, 16, 12, 5), (33, 9, 14, 7), (12, 24, 10, 3)]
     vols = _volumes(ss4d, oracle, sizes, seed=11)

@@ -786,7 +786,8 @@ static int pre_form(const ss4d_solver *s, int mixed)
 }
 
 // the mixed loop's start correction: zero, or the extrapolation the previous
-// step's unpack left in dR[0] / dB (applied by the first refinement pass)
+// step's unpack left in dR[0] / dB (applied by the first refinement pass, or
+// by the first-difference kernel when the assembly formed that pass)
 static ss4d_status clear_corrections(ss4d_solver *s)
 {
     const size_t fb = sizeof(float) * s->sp.cs;

@@ -221,8 +221,8 @@ __global__ void __launch_bounds__(256) k_pack(Geo g, Split sp, const double *__r
 // step's start correction, extrapolated in time from this step's change
 // d = u - prev (FP32) and the changes of earlier steps h1, h2 (per colour):
 // terms 1: d, 2: 2 d - h1, 3: 3 d - 3 h1 + h2, written into the interior of
-// dR[0] / dB, where the next step's first refinement pass adds it to
-// u^{n+1}.  The history then shifts: h2 <- h1 (keep >= 2), h1 <- d (keep >= 1).
+// dR[0] / dB, where the next step's first refinement pass (or, when the
+// assembly forms that pass, its first-difference kernel) adds it to u^{n+1}.  The history then shifts: h2 <- h1 (keep >= 2), h1 <- d (keep >= 1).
 struct History {
     float *h1[2]; // per colour
     float *h2[2];

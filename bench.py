@@ -41,12 +41,14 @@ WORKLOAD = ("segmentation time steps, 256x256x128x20 multi-object drifting scene
 BYTES_FP64_ITER = 88.0  # read u, prev, 8 coefficients; write u
 BYTES_FP32_ITER = 44.0  # the same arrays in FP32
 # DRAM bytes per target voxel of one half-sweep launch (dram__bytes_read.sum +
-# dram__bytes_write.sum from ncu on one launch at 128x128x64x8, 4,194,304
-# targets; the summary and command are in profiles/), scaled by the targets
-# of a launch at the benchmarked size
+# dram__bytes_write.sum from ncu; the summaries and commands are in
+# profiles/), scaled by the targets of a launch at the benchmarked size:
+# k_sweep32 from two launches at 256x256x128x20 (83,886,080 targets; a
+# one-pass capture), k_sweep64 from one launch at 128x128x64x8 (4,194,304)
 EXTRAP_ORDER = 3  # the extrap form's order (ss4d_solver_set_extrapolation)
-TRAFFIC_PER_TARGET = {"k_sweep32": 49.7, "k_sweep64": 118.6}
-TRAFFIC_SOURCE = "profiles/sweep_refine_assembly_conv_kernels_128x128x64x8.md"
+TRAFFIC_PER_TARGET = {"k_sweep32": 51.6, "k_sweep64": 118.6}
+TRAFFIC_SOURCE = {"k_sweep32": "profiles/sweep32_dram_traffic_256x256x128x20.md",
+                  "k_sweep64": "profiles/sweep_refine_assembly_conv_kernels_128x128x64x8.md"}
 
 
 def parse_args():
@@ -282,7 +284,7 @@ def run_ours(args, rank, world, dist):
         return {"bound": "hbm", "kernel": kern, "achieved": ach,
                 "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "peak_source": how,
                 "traffic": TRAFFIC_PER_TARGET[kern] * (n_int / 2.0),
-                "traffic_source": f"{TRAFFIC_SOURCE}, {TRAFFIC_PER_TARGET[kern]} B/target x targets per launch",
+                "traffic_source": f"{TRAFFIC_SOURCE[kern]}, {TRAFFIC_PER_TARGET[kern]} B/target x targets per launch",
                 "avg_launch_ms": avg, "launches": n, "bytes_per_launch": per_launch,
                 "share_of_step_kernel_time": (ms / tot) if tot else None,
                 "kernel_ms": {k: v[0] for k, v in kt.items()}}

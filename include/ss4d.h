@@ -260,7 +260,7 @@ ss4d_status ss4d_seg_time_step(ss4d_solver *s, const ss4d_params *p, double *d_u
  * coefficient assembly) work on the frames that have arrived, and comes down
  * in chunks as the unpack and the rescale finish them; the results equal
  * ss4d_seg_time_step's.  Returns when h_u holds the result. */
-#define SS4D_HOST_CHUNKS 8
+#define SS4D_HOST_CHUNKS 16
 ss4d_status ss4d_seg_time_step_host(ss4d_solver *s, const ss4d_params *p, double *h_u, double *d_u,
                                     double *h_prev, const double *h_Mmask, double *d_Mmask,
                                     const double *const d_g[8], const ss4d_balls *balls,

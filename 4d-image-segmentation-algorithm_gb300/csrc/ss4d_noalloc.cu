@@ -11,9 +11,10 @@
 // SS4D_NOALLOC_MAX_FRAMES frames (32 KB); every device that loads the library
 // keeps it until the process exits.
 //
-// Sharing: every call writes the whole table region it uses (all lMax frame
-// counts, so frames without centres read zero) before its kernels run, in
-// stream order.  Calls whose GPU work overlaps race on the array.
+// Sharing: every call writes the whole table region it uses (its centres and
+// all lMax frame counts, so frames without centres read zero) before its
+// kernels run, in stream order, and copies only that region (3n + lMax
+// doubles).  Calls whose GPU work overlaps race on the array.
 #include <cuda_runtime.h>
 
 #include <math.h>
@@ -26,8 +27,9 @@
 
 using namespace ss4d;
 
-// layout: cx[MAX_BALLS] cy[MAX_BALLS] cz[MAX_BALLS] | frame_first[MAX_FRAMES] frame_count[MAX_FRAMES] (ints)
-static_assert(SS4D_NOALLOC_MAX_FRAMES % 2 == 0, "frame tables fill whole doubles");
+// A call with n centres and lMax frames uses the first 3n + lMax doubles:
+// cx[n] cy[n] cz[n] | frame_first[lMax] frame_count[lMax] (ints, two per double),
+// packed so that one copy of exactly that many bytes stages them.
 #define NOALLOC_DOUBLES (3 * SS4D_NOALLOC_MAX_BALLS + SS4D_NOALLOC_MAX_FRAMES)
 
 static __device__ __align__(256) double g_rescale_scratch[NOALLOC_DOUBLES];
@@ -103,9 +105,10 @@ extern "C" ss4d_status ss4d_rescale_to_zero_one_noalloc(const ss4d_dims *dims, c
         // host staging on the stack: pageable, so the copy below has read it
         // by the time cudaMemcpyAsync returns
         double stage[NOALLOC_DOUBLES];
-        int *first = (int *)(stage + 3 * SS4D_NOALLOC_MAX_BALLS);
-        int *count = first + SS4D_NOALLOC_MAX_FRAMES;
-        memset(first, 0, sizeof(int) * 2 * SS4D_NOALLOC_MAX_FRAMES);
+        const size_t used = 3 * (size_t)nb + (size_t)g.lM;  // doubles this call stages
+        int *first = (int *)(stage + 3 * nb);
+        int *count = first + g.lM;
+        memset(first, 0, sizeof(int) * 2 * (size_t)g.lM);
         int prev_l = -1;
         for (int i = 0; i < nb; ++i) {
             const int l = balls->l[i];
@@ -125,21 +128,20 @@ extern "C" ss4d_status ss4d_rescale_to_zero_one_noalloc(const ss4d_dims *dims, c
                 return fail(SS4D_ERR_INVALID,
                             "invalid argument: a ball's box leaves the array (the reference would read out of bounds)");
             stage[i] = cx;
-            stage[SS4D_NOALLOC_MAX_BALLS + i] = cy;
-            stage[2 * SS4D_NOALLOC_MAX_BALLS + i] = cz;
+            stage[nb + i] = cy;
+            stage[2 * nb + i] = cz;
         }
         double *scratch = nullptr;
         ss4d_status s0 = scratch_address(&scratch);
         if (s0 != SS4D_OK)
             return s0;
-        cudaError_t e = cudaMemcpyAsync(scratch, stage, sizeof stage, cudaMemcpyHostToDevice, st);
+        cudaError_t e = cudaMemcpyAsync(scratch, stage, used * sizeof(double), cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) {
             cudaGetLastError();
             return fail(SS4D_ERR_CUDA, "staging the centre table failed: %s", cudaGetErrorString(e));
         }
-        const int *d_first = (const int *)(scratch + 3 * SS4D_NOALLOC_MAX_BALLS);
-        launch_rescale_balls(g, d_img, d_first, d_first + SS4D_NOALLOC_MAX_FRAMES, scratch,
-                             scratch + SS4D_NOALLOC_MAX_BALLS, scratch + 2 * SS4D_NOALLOC_MAX_BALLS, R, st);
+        const int *d_first = (const int *)(scratch + 3 * nb);
+        launch_rescale_balls(g, d_img, d_first, d_first + g.lM, scratch, scratch + nb, scratch + 2 * nb, R, st);
     }
     if (d_Mmask)
         launch_mask_zero(g, d_img, d_Mmask, st);

@@ -279,7 +279,23 @@ def _balls(balls):
 def rescale_to_zero_one_noalloc(dims: tuple, p: Params, img, mmask=None, balls=None, stream: int | None = None):
     """ss4d_rescale_to_zero_one_noalloc: the per-step rescale for callers that
     cannot allocate device memory (no handle; fixed internal table of at most
-    SS4D_NOALLOC_MAX_BALLS centres and frames).  dims = (iMax, jMax, kMax, lMax)."""
+    SS4D_NOALLOC_MAX_BALLS centres and frames).  dims = (iMax, jMax, kMax, lMax).
+
+    No handle checks the arrays against dims here, so this wrapper does:
+    img (and mmask, if given) must be contiguous float64 CUDA tensors of shape
+    (lMax, kMax, jMax, iMax); anything else raises ValueError before the call."""
+    want = tuple(int(x) for x in dims)[::-1]
+    for name, a in (("img", img), ("mmask", mmask)):
+        if a is None and name == "mmask":
+            continue
+        if not (hasattr(a, "is_cuda") and a.is_cuda):
+            raise ValueError(f"{name} must be a CUDA tensor (device memory)")
+        if str(a.dtype) != "torch.float64":
+            raise ValueError(f"{name} must be float64, not {a.dtype}")
+        if not a.is_contiguous():
+            raise ValueError(f"{name} must be contiguous")
+        if tuple(a.shape) != want:
+            raise ValueError(f"{name} has shape {tuple(a.shape)}; dims {tuple(dims)} need {want}")
     B, keep = _balls(balls)
     d = Dims(*dims)
     _check(lib().ss4d_rescale_to_zero_one_noalloc(C.byref(d), C.byref(p), _ptr(img), _ptr(mmask),

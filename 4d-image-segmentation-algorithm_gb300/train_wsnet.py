@@ -176,7 +176,9 @@ def main():
         e = ev[f"kind{kind}"]
         print(f"eval kind {kind}: cold its {e['cold']['iterations']} warm its {e['warm']['iterations']} "
               f"kept {e['warm']['warm_started']} max rel diff {e['max_rel_diff']:.2e}")
-    meta = {"args": vars(args), "train": summary, "eval": ev, "param_count": int(params.size)}
+    rec = dict(vars(args))
+    rec["out"] = os.path.basename(args.out)  # the record names the file, not where it was written
+    meta = {"args": rec, "train": summary, "eval": ev, "param_count": int(params.size)}
     with open(os.path.splitext(args.out)[0] + ".json", "w") as fh:
         json.dump(meta, fh, indent=1)
 

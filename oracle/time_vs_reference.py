@@ -1,6 +1,6 @@
 """Speed of the C oracle against the compiled reference on this host (TEST
 INFRASTRUCTURE: it needs the reference's own build in oracle/_ref/, made by
-``make -C oracle ref`` where the reference checkout exists, so it runs only on
+``make -C oracle ref`` with SS4D_REFERENCE_DIR naming the reference checkout, so it runs only on
 the build host; the GPU machine has no reference sources).
 
 The benchmark's CPU baseline on the GPU machine is the oracle (a restatement of

@@ -2,7 +2,8 @@
 
 The reference's segmentation4D.c and mcf_4D.c are compiled from their own,
 unmodified sources into oracle/_ref/ (``make -C oracle ref``; needs the
-reference checkout, so this script runs only where it is present).  This
+reference checkout, named by the environment variable SS4D_REFERENCE_DIR, so
+this script runs only where it is present).  This
 script drives them through their global variables and functions exactly as
 their main() does, captures what they print (iteration counts, residuals),
 and stores inputs and outputs as .npz files:
@@ -29,7 +30,8 @@ and stores inputs and outputs as .npz files:
                   thresholding into a non-zero image, initial function on a
                   non-zero u with overlapping balls, Mmask
 
-Usage:  python tests/golden/make_golden.py [fixture ...]   (from the repository root;
+Usage:  SS4D_REFERENCE_DIR=<checkout> python tests/golden/make_golden.py [fixture ...]
+        (from the repository root;
         names are the functions below, all of them by default)
 """
 from __future__ import annotations

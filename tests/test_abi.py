@@ -101,3 +101,35 @@ def test_scene_generator_is_seeded_and_thread_independent(ss4d):
         i0, u0 = ss4d.scene(kind, 20, 18, 16, 5, seed=5)
         assert np.isfinite(i0).all() and np.isfinite(u0).all()
         assert i0[1:-1, 1:-1, 1:-1, 1:-1].max() > 0.5  # objects brighter than the background
+
+
+def test_noalloc_wrapper_rejects_arrays_it_cannot_check(ss4d):
+    """The allocation-free rescale takes no handle, so nothing on the C side
+    knows the array behind the pointer: the Python wrapper refuses host
+    arrays, other dtypes, non-contiguous views and shapes that differ from
+    dims before the call is made."""
+    torch = pytest.importorskip("torch")
+    p = ss4d.scene_params()
+    dims = (6, 5, 4, 3)
+    with pytest.raises(ValueError, match="CUDA"):
+        ss4d.rescale_to_zero_one_noalloc(dims, p, np.zeros((3, 4, 5, 6)))
+    with pytest.raises(ValueError, match="CUDA"):
+        ss4d.rescale_to_zero_one_noalloc(dims, p, torch.zeros((3, 4, 5, 6), dtype=torch.float64))
+
+    class FakeCuda:
+        """stands in for a device tensor: only the attributes the checks read"""
+
+        def __init__(self, shape, dtype="torch.float64", contiguous=True):
+            self.shape, self.dtype, self._c, self.is_cuda = shape, dtype, contiguous, True
+
+        def is_contiguous(self):
+            return self._c
+
+    with pytest.raises(ValueError, match="float64"):
+        ss4d.rescale_to_zero_one_noalloc(dims, p, FakeCuda((3, 4, 5, 6), dtype="torch.float32"))
+    with pytest.raises(ValueError, match="contiguous"):
+        ss4d.rescale_to_zero_one_noalloc(dims, p, FakeCuda((3, 4, 5, 6), contiguous=False))
+    with pytest.raises(ValueError, match="shape"):
+        ss4d.rescale_to_zero_one_noalloc(dims, p, FakeCuda((3, 4, 6, 5)))
+    with pytest.raises(ValueError, match="mmask"):
+        ss4d.rescale_to_zero_one_noalloc(dims, p, FakeCuda((3, 4, 5, 6)), np.ones((3, 4, 5, 6)))

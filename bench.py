@@ -41,14 +41,21 @@ WORKLOAD = ("segmentation time steps, 256x256x128x20 multi-object drifting scene
 BYTES_FP64_ITER = 88.0  # read u, prev, 8 coefficients; write u
 BYTES_FP32_ITER = 44.0  # the same arrays in FP32
 # DRAM bytes per target voxel of one half-sweep launch (dram__bytes_read.sum +
-# dram__bytes_write.sum from ncu; the summaries and commands are in
-# profiles/), scaled by the targets of a launch at the benchmarked size:
-# k_sweep32 from two launches at 256x256x128x20 (83,886,080 targets; a
-# one-pass capture), k_sweep64 from one launch at 128x128x64x8 (4,194,304)
+# dram__bytes_write.sum from ncu), scaled by the targets of a launch at the
+# benchmarked size: k_sweep32 from two launches at 256x256x128x20
+# (83,886,080 targets; a one-pass capture), k_sweep64 from one launch at
+# 128x128x64x8 (4,194,304 targets)
 EXTRAP_ORDER = 3  # the extrap form's order (ss4d_solver_set_extrapolation)
 TRAFFIC_PER_TARGET = {"k_sweep32": 51.6, "k_sweep64": 118.6}
-TRAFFIC_SOURCE = {"k_sweep32": "profiles/sweep32_dram_traffic_256x256x128x20.md",
-                  "k_sweep64": "profiles/sweep_refine_assembly_conv_kernels_128x128x64x8.md"}
+TRAFFIC_SOURCE = {"k_sweep32": "ncu capture of two launches at 256x256x128x20",
+                  "k_sweep64": "ncu capture of one launch at 128x128x64x8"}
+# the form the metric names: FP32 sweeps with FP64 refinement started from
+# the learned warm start
+NAMED_FORM = "learned"
+FORM_LABEL = {"fp64": "plain FP64 sweeps", "mixed": "mixed (FP32 sweeps, FP64 residual/refinement)",
+              "extrap": "mixed + cubic extrapolated start (no network)",
+              "learned": "mixed + learned warm start (the metric's named form)",
+              "extrap_w": "mixed + extrapolated start, FP32 sweeps relaxed by --inner-omega (reported only)"}
 
 
 def parse_args():
@@ -76,6 +83,9 @@ def parse_args():
                     help="batch: 16 uneven volumes in one persistent launch per half-sweep (reports "
                          "voxel-updates/s; not the headline metric)")
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--steps100", type=int, default=100,
+                    help="every form also runs on from the timed window to this many time steps from u0 (the "
+                         "headline configuration's 100 steps) and reports their average rate (0: skip)")
     return ap.parse_args()
 
 
@@ -206,13 +216,28 @@ def run_ours(args, rank, world, dist):
 
     results = {}
     finals = {}
+    first_fp64 = None  # u after the plain FP64 form's first step (parity against the oracle's step)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def timed_step(u):
+        """one time step, its device time (CUDA events on the stream)"""
+        ev[0].record(stream)
+        st = S.seg_time_step(p, u, None, g)
+        ev[1].record(stream)
+        ev[1].synchronize()
+        return st, ev[0].elapsed_time(ev[1])
+
     for form in forms:
         use_form(form)
         u = u0.clone()
         its = []
-        for _ in range(args.warmup):
-            st = S.seg_time_step(p, u, None, g)
+        per_step = []  # (ms, iterations) of every step from u0
+        for n in range(args.warmup):
+            st, ms1 = timed_step(u)
+            per_step.append((ms1, st["iterations"]))
             its.append(st["iterations"])
+            if form == "fp64" and n == 0 and rank == 0:
+                first_fp64 = (u.cpu().numpy(), st)
         launches0 = S.launch_count()
         if dist:
             dist.barrier()
@@ -231,6 +256,13 @@ def run_ours(args, rank, world, dist):
         clocks = clk.stop()
         ms = slowest_rank_ms(ms, dist, dev)
         launches = S.launch_count() - launches0
+        # the timed steps' own times are not taken apart: their mean stands in
+        per_step += [(ms / args.steps, s["iterations"]) for s in steps]
+        while len(per_step) < args.steps100:
+            st, ms1 = timed_step(u)
+            per_step.append((ms1, st["iterations"]))
+            if not (st["residual"] <= p.gsTol or st["iterations"] >= p.maxNoGSIteration):
+                steps.append(st)  # counted against `converged`
         ok = all(s["residual"] <= p.gsTol or s["iterations"] >= p.maxNoGSIteration for s in steps)
         results[form] = {
             "steps_per_s": replica_steps_per_s(args.steps, world, ms),
@@ -244,6 +276,16 @@ def run_ours(args, rank, world, dist):
             "launches": launches,
             "clocks": clocks,
         }
+        if args.steps100 > 0:
+            head = per_step[:args.steps100]
+            tot = sum(m for m, _ in head)
+            ok100 = all(s["residual"] <= p.gsTol or s["iterations"] >= p.maxNoGSIteration for s in steps)
+            results[form]["steps100"] = {
+                "steps": len(head), "steps_per_s": len(head) / (tot / 1e3), "ms_per_step": tot / len(head),
+                "iterations_mean": statistics.mean(z for _, z in head),
+                "iterations_first_last": [head[0][1], head[-1][1]], "converged": ok100,
+                "how": f"steps 1..{len(head)} from u0: per-step CUDA events outside the timed window, the timed "
+                       f"window's mean inside it"}
         finals[form] = u
 
     # per-kernel device time (CUDA events on the launching stream), one more
@@ -284,7 +326,8 @@ def run_ours(args, rank, world, dist):
         return {"bound": "hbm", "kernel": kern, "achieved": ach,
                 "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "peak_source": how,
                 "traffic": TRAFFIC_PER_TARGET[kern] * (n_int / 2.0),
-                "traffic_source": f"{TRAFFIC_SOURCE[kern]}, {TRAFFIC_PER_TARGET[kern]} B/target x targets per launch",
+                "traffic_source": f"{TRAFFIC_SOURCE[kern]}: {TRAFFIC_PER_TARGET[kern]} DRAM B/target x targets per "
+                                  f"launch",
                 "avg_launch_ms": avg, "launches": n, "bytes_per_launch": per_launch,
                 "share_of_step_kernel_time": (ms / tot) if tot else None,
                 "kernel_ms": {k: v[0] for k, v in kt.items()}}
@@ -307,7 +350,7 @@ def run_ours(args, rank, world, dist):
     S.close()
     if net is not None:
         net.close()
-    return results, roofline, err, (shape, n_pad, n_int, p, i0h, u0h)
+    return results, roofline, err, (shape, n_pad, n_int, p, i0h, u0h, first_fp64)
 
 
 def frontend_balls(nx, ny, nz, nt, seed, per_frame=5, radius=8.0):
@@ -340,7 +383,7 @@ def run_frontend(args, ctx, arith="fp64"):
     import oracle
     import ss4d
 
-    shape, n_pad, n_int, p0, i0h, u0h = ctx
+    shape, n_pad, n_int, p0, i0h, u0h, _ = ctx
     nx, ny, nz, nt = args.size
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     stream = torch.cuda.current_stream(dev)
@@ -452,7 +495,7 @@ def run_e2e(args, form, ctx):
 
     import ss4d
 
-    shape, n_pad, n_int, p, i0h, u0h = ctx
+    shape, n_pad, n_int, p, i0h, u0h, _ = ctx
     os.environ["SS4D_ARITH"] = "mixed" if form == "extrap" else form
     os.environ["SS4D_EXTRAPOLATE"] = str(EXTRAP_ORDER) if form == "extrap" else "0"
     L = C.CDLL(ss4d.SEG_PATH, mode=os.RTLD_LOCAL)
@@ -510,9 +553,30 @@ def cpu_kind():
     return "port"
 
 
-def cpu_steps(size, seed, warmup, steps, threads):
+def cpu_model() -> str:
+    """the host CPU's model name (lscpu, else /proc/cpuinfo)"""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as fh:
+            for ln in fh:
+                if ln.lower().startswith("model name"):
+                    return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
+def cpu_steps(size, seed, warmup, steps, threads, keep_u=False):
     """Time `steps` segmentation time steps of the oracle (after `warmup`)
-    on `threads` cores; returns (seconds per step, iterations)."""
+    on `threads` cores (the edge detector before them on every core,
+    untimed); returns (seconds per step, iterations, u or None)."""
     import numpy as np
 
     import oracle
@@ -520,10 +584,11 @@ def cpu_steps(size, seed, warmup, steps, threads):
 
     nx, ny, nz, nt = size
     p = ss4d.scene_params()
-    i0, u = ss4d.scene(3, nx, ny, nz, nt, seed=seed, threads=threads)
-    oracle.set_threads(threads)
+    i0, u = ss4d.scene(3, nx, ny, nz, nt, seed=seed, threads=os.cpu_count() or 1)
+    oracle.set_threads(os.cpu_count() or 1)
     g, _, _ = oracle.edge_detector(p, i0, np.zeros_like(i0))
     del i0
+    oracle.set_threads(threads)
     prev = np.zeros_like(u)
     mm = np.ones_like(u)
     coef = oracle.new_like(u, 8)
@@ -534,16 +599,97 @@ def cpu_steps(size, seed, warmup, steps, threads):
     for _ in range(steps):
         z, _ = oracle.seg_time_step(p, u, prev, g, coef=coef, mmask=mm)
         its.append(z)
-    return (time.perf_counter() - t0) / max(1, steps), its
+    sec = (time.perf_counter() - t0) / max(1, steps)
+    return sec, its, (u if keep_u else None)
 
 
-def cpu_baseline(args):
+def cpu_baseline(args, first_fp64=None):
+    """The oracle on the host cores: one full time step of the benchmarked
+    volume on every core (compared with the GPU's plain FP64 first step from
+    the same u0), and the reference's serial path (one core) on a two-frame
+    sample of the same scene."""
+    import numpy as np
+
     threads = os.cpu_count() or 1
-    sec, its = cpu_steps(args.size, args.seed, 0, 1, threads)
-    return {"value": 1.0 / sec, "unit": "time-steps/s", "cores": threads, "kind": "port",
-            "sample": f"1 time step of the same {args.size[0]}x{args.size[1]}x{args.size[2]}x{args.size[3]} workload "
-                      f"({its[0]} SOR iterations), C oracle restating segmentation4D.c with OpenMP over frames "
-                      f"as mcf_4D_openmp.c does, {threads} threads"}
+    sec, its, u = cpu_steps(args.size, args.seed, 0, 1, threads, keep_u=first_fp64 is not None)
+    nx, ny, nz, nt = args.size
+    n_int = nx * ny * nz * nt
+    out = {"value": 1.0 / sec, "unit": "time-steps/s", "cores": threads, "kind": "port",
+           "cpu_model": cpu_model(),
+           "sample": f"1 time step of the same {nx}x{ny}x{nz}x{nt} workload ({its[0]} SOR iterations), C oracle "
+                     f"restating segmentation4D.c with OpenMP over frames as mcf_4D_openmp.c does, {threads} threads",
+           "ns_per_voxel_iteration": sec / (n_int * its[0]) * 1e9}
+    if first_fp64 is not None:
+        got, st = first_fp64
+        inner = (slice(1, -1),) * 4
+        same = st["iterations"] == its[0]
+        err = float(np.abs(got[inner] - u[inner]).max() / np.abs(u[inner]).max()) if same else None
+        out["parity_config3"] = {
+            "what": "u after the first time step from u0: GPU plain FP64 form vs the oracle (its red-black SOR "
+                    "restates segmentation4D.c:228-309)",
+            "iterations_gpu": st["iterations"], "iterations_oracle": its[0], "max_rel_diff_u": err,
+            "near_tolerance": bool(st["near_tolerance"]), "bar": 1e-10,
+            "pass": bool(same and err is not None and err <= 1e-10)}
+    del u
+    # serial: the reference's segmentation is single-threaded
+    ns = 2
+    sec1, its1, _ = cpu_steps((nx, ny, nz, ns), args.seed, 0, 1, 1)
+    ns_vi = sec1 / (nx * ny * nz * ns * its1[0]) * 1e9
+    out["serial"] = {"value": 1.0 / (ns_vi * 1e-9 * n_int * its[0]), "unit": "time-steps/s", "cores": 1,
+                     "kind": "port", "ns_per_voxel_iteration": ns_vi,
+                     "sample": f"1 time step of a {nx}x{ny}x{nz}x{ns} volume of the same generator ({its1[0]} SOR "
+                               f"iterations, {sec1:.1f} s) on one core; value = its time per voxel-iteration x the "
+                               f"full volume's voxels x its {its[0]} iterations"}
+    return out
+
+
+def run_mcf(args):
+    """The MCF known-answer step (mcf_4D.c:102-205; OpenMP variant
+    mcf_4D_openmp.c:102-205) at the reference's OpenMP size, 80^4 interior
+    voxels: the oracle on every host core (OpenMP over frames) against the
+    GPU's plain FP64 form, the same steps from the exact solution at t = 0."""
+    import numpy as np
+    import torch
+
+    import oracle
+    import ss4d
+
+    n, steps = 80, 2
+    p = ss4d.mcf_params(n, steps)
+    shape = (n + 2,) * 4
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    u = oracle.mcf_exact(p.h, 0.0, shape)
+    prev = np.zeros_like(u)
+    coef = oracle.new_like(u, 8)
+    t0 = time.perf_counter()
+    its = [oracle.mcf_time_step(p, k, u, prev, coef=coef)[0] for k in range(1, steps + 1)]
+    sec = (time.perf_counter() - t0) / steps
+    want = u
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ss4d.Solver(*shape, arith="fp64", stream=stream.cuda_stream) as S:
+        ug = torch.zeros(shape, dtype=torch.float64, device=dev)
+        pg = torch.zeros_like(ug)
+        S.mcf_exact_solution(p.h, 0.0, ug)
+        S.mcf_time_step(p, 1, ug.clone(), pg)  # untimed: graph set-up
+        S.mcf_exact_solution(p.h, 0.0, ug)
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        gits = [S.mcf_time_step(p, k, ug, pg)["iterations"] for k in range(1, steps + 1)]
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        gms = e0.elapsed_time(e1) / steps
+        err = float((ug.cpu() - torch.from_numpy(want)).abs().max() / np.abs(want).max())
+    vox = n ** 4
+    return {"workload": f"MCF known-answer steps at {n}^4 interior voxels (tau = eps2 = h^2), {steps} steps from "
+                        f"the exact solution",
+            "cpu": {"steps_per_s": 1.0 / sec, "cores": threads, "kind": "port", "cpu_model": cpu_model(),
+                    "iterations": its, "ns_per_voxel_iteration": sec / (vox * statistics.mean(its)) * 1e9,
+                    "what": "C oracle restating mcf_4D.c's step, OpenMP over frames as mcf_4D_openmp.c"},
+            "gpu_fp64": {"steps_per_s": 1e3 / gms, "ms_per_step": gms, "iterations": gits,
+                         "max_rel_diff_u_vs_oracle": err}}
 
 
 def run_reference(args):
@@ -551,7 +697,7 @@ def run_reference(args):
     if rank != 0:
         return None
     threads = os.cpu_count() or 1
-    sec, its = cpu_steps(args.size, args.seed, args.warmup, args.steps, threads)
+    sec, its, _ = cpu_steps(args.size, args.seed, args.warmup, args.steps, threads)
     v = 1.0 / sec
     kind = "port"  # the compiled reference needs its sources, which only the build host has
     return {"metric": METRIC, "value": v, "unit": "time-steps/s", "n_gpus": args.gpus, "steps": args.steps,
@@ -560,6 +706,7 @@ def run_reference(args):
             "config": {"workload": WORKLOAD, "nx": args.size[0], "ny": args.size[1], "nz": args.size[2],
                        "nt": args.size[3], "parallelism": "host cores", "l2": "working set >> L2"},
             "cpu_baseline": {"value": v, "unit": "time-steps/s", "cores": threads, "kind": kind,
+                             "cpu_model": cpu_model(),
                              "sample": f"{args.steps} full time steps after {args.warmup} warm-up steps, "
                                        f"SOR iterations {its}"},
             "e2e": {"value": v, "unit": "time-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -684,15 +831,25 @@ def main():
                       "extrap": "f32 sweeps + f64 residual/refinement",
                       "learned": "f32 sweeps + f64 residual/refinement, bf16 warm-start network"}[head],
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "form": head, "nx": args.size[0], "ny": args.size[1],
+            "config": {"workload": WORKLOAD, "form": head, "form_label": FORM_LABEL.get(head, head),
+                       "is_named_form": head == NAMED_FORM, "nx": args.size[0], "ny": args.size[1],
                        "nz": args.size[2], "nt": args.size[3], "parallelism": f"replicas x{world}",
                        "l2": "inputs >> L2 (about 25 GB working set), no flush"},
             "roofline": roofline(head), "gpu_launches": r["launches"], "clocks": r["clocks"],
             "forms": {f: {k: v for k, v in results[f].items() if k != "clocks"} for f in forms}}
+    if NAMED_FORM in results:
+        nf = results[NAMED_FORM]
+        line["named_form"] = {"form": NAMED_FORM, "label": FORM_LABEL[NAMED_FORM], "steps_per_s": nf["steps_per_s"],
+                              "over_fp64": (nf["steps_per_s"] / results["fp64"]["steps_per_s"]
+                                            if "fp64" in results else None),
+                              "steps100_per_s": nf.get("steps100", {}).get("steps_per_s")}
     if "fp64" in results:
         for f in ("mixed", "extrap", "extrap_w", "learned"):
             if f in results:
                 line[f"{f}_over_fp64"] = results[f]["steps_per_s"] / results["fp64"]["steps_per_s"]
+        if args.steps100 > 0:
+            line["steps100_over_fp64"] = {f: results[f]["steps100"]["steps_per_s"] /
+                                          results["fp64"]["steps100"]["steps_per_s"] for f in forms}
         line["roofline_fp64"] = roofline("fp64")
         line["error_vs_fp64"] = err
     for f in ("mixed", "extrap", "learned"):
@@ -709,7 +866,10 @@ def main():
         line["frontend"] = run_frontend(args, ctx, "fp64")
         line["frontend_mixed"] = run_frontend(args, ctx, "mixed")
     if rank == 0 and world == 1 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(args)
+        line["cpu_baseline"] = cpu_baseline(args, ctx[6])
+        if "parity_config3" in line["cpu_baseline"]:
+            line["parity_config3"] = line["cpu_baseline"]["parity_config3"]
+        line["mcf_openmp"] = run_mcf(args)
     if dist:
         dist.destroy_process_group()
     if rank == 0:

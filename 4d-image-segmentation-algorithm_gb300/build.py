@@ -39,7 +39,7 @@ CUDA_UNITS = {
     "ss4d_assemble_ff.cu": [],
     "ss4d_front_ff.cu": [],
 }
-C_UNITS = {"ss4d_scene.c": ["-fopenmp"], "ss4d_vtk.c": []}
+C_UNITS = {"ss4d_scene.c": ["-fopenmp"], "ss4d_vtk.c": [], "ss4d_slab.c": []}
 
 LIB = os.path.join(HERE, "libss4d.so")
 LIB_SEG = os.path.join(HERE, "libss4d_seg.so")

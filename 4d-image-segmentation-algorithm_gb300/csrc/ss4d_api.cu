@@ -1918,3 +1918,109 @@ ss4d_status ss4d::solver_time_sweeps(ss4d_solver *s, const ss4d_params *p, int i
     s->launches += 1 + 2LL * iters;
     return SS4D_OK;
 }
+
+// ---------------------------------------------------------------------------
+// one slab of a volume split by frames (ss4d_slab.c runs the loop): the
+// reference-order kernels on the slab's natural layout
+
+namespace {
+struct SlabGpu {
+    ss4d_solver *s;
+    const ss4d_params *p;
+    double *u;
+    const double *prev;
+    CPtrs8 a;
+};
+
+int slab_half_sweep(void *ctx, int colour)
+{
+    SlabGpu *q = static_cast<SlabGpu *>(ctx);
+    launch_sor_half_ref(q->s->geo, q->u, q->prev, q->a, q->p->tau / (q->p->h * q->p->h), q->p->omega_c, colour,
+                        q->s->stream);
+    q->s->launches += 1;
+    return last_launch() != SS4D_OK;
+}
+
+int slab_residual(void *ctx, double *partial)
+{
+    SlabGpu *q = static_cast<SlabGpu *>(ctx);
+    const Geo &g = q->s->geo;
+    const double h2 = q->p->h * q->p->h;
+    launch_sor_resid_ref(g, q->u, q->prev, q->a, q->p->tau / h2, h2 * h2, q->s->d_partial, q->s->stream);
+    q->s->launches += 1 + launch_reduce_sum(q->s->d_partial, resid_blocks(g), q->s->d_scalar, q->s->stream);
+    if (last_launch() != SS4D_OK)
+        return 1;
+    return read_scalar(q->s, 0, partial) != SS4D_OK;
+}
+} // namespace
+
+extern "C" ss4d_status ss4d_slab_sor_solve(ss4d_solver *s, const ss4d_params *p, double *d_u, const double *d_prev_u,
+                                           const double *const d_coef[8], const ss4d_slab_comm *comm,
+                                           long long nint_global, ss4d_step_stats *stats)
+{
+    REQ(s && d_u && d_prev_u && d_coef && comm, "NULL argument");
+    CKS(check_params(p));
+    SlabGpu q{s, p, d_u, d_prev_u, {}};
+    for (int f = 0; f < 8; ++f) {
+        REQ(d_coef[f], "a coefficient array is NULL");
+        q.a.p[f] = d_coef[f];
+    }
+    const Geo &g = s->geo;
+    ss4d_slab_ops ops{&q, slab_half_sweep, slab_residual, d_u, g.sw, g.lM, (void *)s->stream};
+    CK(cudaEventRecord(s->ev0, s->stream));
+    ss4d_status st = ss4d_slab_sor_loop(&ops, comm, p, nint_global, stats);
+    CK(cudaEventRecord(s->ev1, s->stream));
+    CK(cudaEventSynchronize(s->ev1));
+    if (stats)
+        cudaEventElapsedTime(&stats->ms, s->ev0, s->ev1);
+    return st;
+}
+
+extern "C" ss4d_status ss4d_slab_seg_time_step(ss4d_solver *s, const ss4d_params *p, double *d_u, double *d_prev_u,
+                                               const double *const d_g[8], const double *d_Mmask,
+                                               const ss4d_balls *balls, const ss4d_slab_comm *comm,
+                                               long long nint_global, ss4d_step_stats *stats)
+{
+    REQ(s && d_u && d_g && comm && comm->exchange, "NULL argument");
+    CKS(check_params(p));
+    CPtrs8 gi;
+    for (int f = 0; f < 8; ++f) {
+        REQ(d_g[f], "a g array is NULL");
+        gi.p[f] = d_g[f];
+    }
+    const Geo &g = s->geo;
+    double *prev = d_prev_u;
+    if (!prev) {
+        CKS(ensure_scratch(s));
+        prev = s->d_scratch;
+    }
+    CKS(ensure_coef_nat(s));
+    // the coefficients of the slab's first and last frames read u in the
+    // neighbours' frames: bring the ghosts up to date first
+    if (comm->exchange(comm->ctx, d_u, g.sw, g.lM, (void *)s->stream)) {
+        set_err("ss4d_slab_seg_time_step: the ghost-frame exchange failed");
+        return SS4D_ERR_CUDA;
+    }
+    CK(cudaMemcpyAsync(prev, d_u, sizeof(double) * g.n, cudaMemcpyDeviceToDevice, s->stream));
+    GPtrs8 co;
+    const double *ca[8];
+    for (int f = 0; f < 8; ++f) {
+        co.p[f] = s->d_coef_nat + (size_t)f * g.n;
+        ca[f] = co.p[f];
+    }
+    launch_coef_ref(g, d_u, gi, 1, co, p->h, p->eps2, s->stream);
+    s->launches += 1;
+    CKS(last_launch());
+    ss4d_step_stats local;
+    ss4d_status st = ss4d_slab_sor_solve(s, p, d_u, prev, ca, comm, nint_global, stats ? stats : &local);
+    if (st == SS4D_OK)
+        st = rescale_impl(s, p, d_u, d_Mmask, balls);
+    // as the reference's rescale ends (segmentation4D_mpi.c:1256): the ghosts
+    // hold the neighbours' rescaled frames
+    if (st == SS4D_OK && comm->exchange(comm->ctx, d_u, g.sw, g.lM, (void *)s->stream)) {
+        set_err("ss4d_slab_seg_time_step: the ghost-frame exchange failed");
+        return SS4D_ERR_CUDA;
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    return st;
+}

@@ -1,0 +1,410 @@
+// ss4d_conv_tc.cu — the warm-start network's 3x3x3 convolution on the
+// fifth-generation tensor cores: tcgen05.mma with BF16 operands in shared
+// memory, FP32 accumulators in tensor memory (TMEM), input tiles brought in
+// by the tensor memory accelerator (TMA).
+//
+// A convolution over every frame of [F][nz][ny][nx][CIN] BF16 activations
+// (channels last) is an implicit GEMM: D[voxel][cout] = sum over the 27 taps
+// and the input channels of X[voxel + tap][cin] W[tap][cout][cin].  A CTA
+// takes output tiles of 8 (x) by 16 (y) voxels by TZ planes (z) of one
+// frame; each plane is one M = 128 accumulator (row m = x + 8 y) of N
+// output channels.  Its input halo tile, 10 x 18 x (TZ + 2) voxels, arrives
+// in shared memory by one TMA box per group of 8 channels; a box lands as
+// [z][y][x][8 channels], 16 bytes per voxel, which is the canonical K-major
+// layout of the UMMA operands without swizzle: a core matrix is 8
+// consecutive voxels (rows) by 8 channels (16 bytes).  So the A operand of
+// tap (dx, dy, dz) is the halo tile itself, its descriptor starting at voxel
+// (dx, dy, p + dz): rows x + 8 y step 16 bytes within a core matrix and the
+// row stride of the halo (160 bytes) between the 8-row groups, channel
+// groups a plane apart.  No operand is copied per tap.  The weights of all
+// taps stay in shared memory in the same core-matrix layout.
+//
+// Per CTA: one thread issues the TMA loads and the MMAs; the halo tiles and
+// the accumulators are double-buffered, so the loads of tile i+1 and the
+// epilogue of tile i-1 (TMEM -> registers -> bias, ReLU, mask -> global) run
+// while the tensor core works on tile i.  Every wait on an mbarrier is
+// bounded (about a second of clock cycles); one that runs out sets an error
+// flag the host reads, the CTA waits (bounded) for its own loads and MMAs
+// in flight, frees its tensor memory and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ss4d_conv_tc.cuh"
+
+namespace ss4d {
+namespace tc {
+
+// ---- PTX wrappers -----------------------------------------------------------
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+// bounded wait: false when about 2^31 clock cycles passed without the phase
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+{
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > (1LL << 31))
+            return false;
+    return true;
+}
+
+__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap *map, uint32_t bar, int c0, int c1,
+                                            int c2, int c3, int c4)
+{
+    asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%3, %4, %5, %6, %7}], [%2];" ::"r"(dst),
+                 "l"((uint64_t)map), "r"(bar), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t slot, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// D[tmem] (+)= A[smem desc] * B[smem desc]^T, kind::f16 (BF16 in, FP32 accumulate)
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                          uint32_t accumulate)
+{
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "setp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+                 "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+                 : "memory");
+}
+
+// the mbarrier arrives once all tcgen05.mma issued so far by this thread completed
+__device__ __forceinline__ void umma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+// 32 lanes x 32 bit, 16 or 32 consecutive columns into registers
+__device__ __forceinline__ void tmem_ld_x16(uint32_t taddr, uint32_t (&r)[16])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                 "[%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                   "=r"(r[15])
+                 : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// ---- the kernel ---------------------------------------------------------------
+
+template <int CIN, int N>
+__global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUtensorMap tmap, TcArgs a)
+{
+    using C = TcCfg<CIN, N>;
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char *halo0 = smem;
+    unsigned char *wsm = smem + 2 * C::HALO;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(wsm + C::WBYTES); // [0,1] loads, [2,3] MMAs
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 4);
+    int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    // weights: global (already in core-matrix order) -> shared
+    for (int q = tid; q < C::WBYTES / 16; q += blockDim.x)
+        reinterpret_cast<uint4 *>(wsm)[q] = __ldg(reinterpret_cast<const uint4 *>(a.w) + q);
+    if (tid == 0) {
+        for (int b = 0; b < 4; ++b)
+            mbar_init(smem_u32(bars + b), 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // the weights were written by the generic proxy; the MMAs read through the async proxy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (warp == 0)
+        tmem_alloc(smem_u32(tmem_slot), C::TCOLS);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    const int ntx = (a.nx + TX - 1) / TX, nty = (a.ny + TY - 1) / TY, ntz = (a.nz + TZ - 1) / TZ;
+    const long long ntiles = (long long)ntx * nty * ntz * a.nf;
+    const long long first = blockIdx.x;
+    const int my_n = first < ntiles ? (int)((ntiles - 1 - first) / gridDim.x + 1) : 0;
+    auto tile_xyzf = [&](int it, int &x0, int &y0, int &z0, int &f) {
+        long long r = first + (long long)it * gridDim.x;
+        x0 = (int)(r % ntx) * TX;
+        r /= ntx;
+        y0 = (int)(r % nty) * TY;
+        r /= nty;
+        z0 = (int)(r % ntz) * TZ;
+        f = (int)(r / ntz);
+    };
+    auto issue_load = [&](int it) {
+        int x0, y0, z0, f;
+        tile_xyzf(it, x0, y0, z0, f);
+        const int b = it & 1;
+        const uint32_t bar = smem_u32(bars + b);
+        mbar_expect_tx(bar, C::NCG * C::BOX_BYTES);
+        const uint32_t dst = smem_u32(halo0 + b * C::HALO);
+#pragma unroll
+        for (int g = 0; g < C::NCG; ++g)
+            tma_load_5d(dst + g * PLANE, &tmap, bar, 8 * g, x0 - 1, y0 - 1, z0 - 1, f);
+    };
+    // K-major operands without swizzle: LBO = stride of the core matrices
+    // along K, SBO = stride of the 8-row groups along M (N)
+    const uint32_t idesc = (1u << 4)                 // D: FP32
+                           | (1u << 7) | (1u << 10)  // A, B: BF16
+                           | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+    int issued_loads = 0, issued_mma = 0; // of thread 0, for the abort path
+
+    if (tid == 0 && my_n > 0) {
+        issue_load(0);
+        issued_loads = 1;
+    }
+    for (int it = 0; it <= my_n; ++it) {
+        if (tid == 0 && !*abort_flag) {
+            if (it + 1 < my_n) {
+                // the buffer of tile it+1 was read by the MMAs of tile it-1
+                if (it >= 1 && !mbar_wait(smem_u32(bars + 2 + ((it - 1) & 1)), ((it - 1) >> 1) & 1))
+                    *abort_flag = 1;
+                else {
+                    issue_load(it + 1);
+                    issued_loads = it + 2;
+                }
+            }
+            if (it < my_n && !*abort_flag) {
+                if (!mbar_wait(smem_u32(bars + (it & 1)), (it >> 1) & 1)) {
+                    *abort_flag = 1;
+                } else {
+                    tc_fence_after();
+                    const uint32_t hbase = smem_u32(halo0 + (it & 1) * C::HALO);
+                    const uint32_t wbase = smem_u32(wsm);
+                    const uint32_t acc = tmem + (uint32_t)((it & 1) * TZ * N);
+#pragma unroll 1
+                    for (int p = 0; p < TZ; ++p) {
+                        uint32_t accumulate = 0;
+#pragma unroll 1
+                        for (int tap = 0; tap < 27; ++tap) {
+                            const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+                            const uint32_t vox = (uint32_t)(((p + dz) * HY + dy) * HX + dx);
+#pragma unroll
+                            for (int kc = 0; kc < C::KC; ++kc) {
+                                const uint64_t ad = make_desc(hbase + 2 * kc * PLANE + vox * 16, PLANE, HX * 16);
+                                const uint64_t bd =
+                                    make_desc(wbase + (tap * C::KC + kc) * C::WBLK, (N / 8) * 128, 128);
+                                umma_bf16(acc + p * N, ad, bd, idesc, accumulate);
+                                accumulate = 1;
+                            }
+                        }
+                    }
+                    umma_commit(smem_u32(bars + 2 + (it & 1)));
+                    issued_mma = it + 1;
+                }
+            }
+        }
+        __syncwarp();
+        __syncthreads(); // the abort flag as thread 0 left it
+        if (*abort_flag)
+            break;
+        if (it >= 1) {
+            // epilogue of tile it-1: its accumulators -> bias, ReLU, mask -> global
+            const int j = it - 1;
+            if (!mbar_wait(smem_u32(bars + 2 + (j & 1)), (j >> 1) & 1)) {
+                *abort_flag = 1;
+            } else {
+                tc_fence_after();
+                int x0, y0, z0, f;
+                tile_xyzf(j, x0, y0, z0, f);
+                const int m = warp * 32 + lane;
+                const int ox = x0 + (m & 7), oy = y0 + (m >> 3);
+#pragma unroll 1
+                for (int p = 0; p < TZ; ++p) {
+                    const uint32_t col = tmem + (uint32_t)((j & 1) * TZ * N + p * N) + ((uint32_t)(warp * 32) << 16);
+                    float v[N];
+#pragma unroll
+                    for (int h = 0; h < N / 16; ++h) {
+                        uint32_t r[16];
+                        tmem_ld_x16(col + 16 * h, r);
+                        tmem_ld_wait();
+#pragma unroll
+                        for (int e = 0; e < 16; ++e)
+                            v[16 * h + e] = __uint_as_float(r[e]);
+                    }
+                    const int oz = z0 + p;
+                    if (ox < a.nx && oy < a.ny && oz < a.nz)
+                        epilogue_store<N>(a, v, (((size_t)f * a.nz + oz) * a.ny + oy) * a.nx + ox);
+                }
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+        if (*abort_flag)
+            break;
+    }
+    if (*abort_flag) {
+        // wait (bounded) for this CTA's own loads and MMAs in flight before
+        // its shared and tensor memory go away
+        if (tid == 0) {
+            atomicExch(a.err, 1);
+            for (int t = 0; t < issued_loads; ++t)
+                mbar_wait(smem_u32(bars + (t & 1)), (t >> 1) & 1);
+            if (issued_mma > 0)
+                mbar_wait(smem_u32(bars + 2 + ((issued_mma - 1) & 1)), ((issued_mma - 1) >> 1) & 1);
+        }
+        tc_fence_before();
+        __syncthreads();
+    }
+    tc_fence_after();
+    if (warp == 0)
+        tmem_dealloc(tmem, C::TCOLS);
+}
+
+// ---- host side ------------------------------------------------------------------
+
+namespace {
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+template <int CIN, int N> void set_attr_once()
+{
+    static bool done = false;
+    if (!done) {
+        cudaFuncSetAttribute(k_conv_tc<CIN, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcCfg<CIN, N>::SMEM);
+        done = true;
+    }
+}
+} // namespace
+
+// the 5-D map of [nf][nz][ny][nx][CIN] BF16 with boxes of 8 channels x the halo tile
+static bool make_map(CUtensorMap *m, const void *x, int cin, int nx, int ny, int nz, int nf)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+    if (!enc)
+        return false;
+    const cuuint64_t dims[5] = {(cuuint64_t)cin, (cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz, (cuuint64_t)nf};
+    const cuuint64_t row = (cuuint64_t)cin * 2;
+    const cuuint64_t strides[4] = {row, row * nx, row * nx * ny, row * nx * ny * nz};
+    const cuuint32_t box[5] = {8, HX, HY, HZ, 1};
+    const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(x), dims, strides, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int CIN, int N>
+static cudaError_t launch(const void *x, const TcArgs &a, int sm_count, cudaStream_t st)
+{
+    CUtensorMap m;
+    if (!make_map(&m, x, CIN, a.nx, a.ny, a.nz, a.nf))
+        return cudaErrorInvalidValue;
+    set_attr_once<CIN, N>();
+    const long long tiles = tc_tiles(a.nx, a.ny, a.nz, a.nf);
+    const int grid = (int)(tiles < sm_count ? tiles : sm_count);
+    k_conv_tc<CIN, N><<<grid, 128, TcCfg<CIN, N>::SMEM, st>>>(m, a);
+    return cudaGetLastError();
+}
+
+cudaError_t conv_tc(int cin, int n, const void *x, const TcArgs &a, int sm_count, cudaStream_t st)
+{
+    if (cin == 16 && n == 32)
+        return launch<16, 32>(x, a, sm_count, st);
+    if (cin == 32 && n == 32)
+        return launch<32, 32>(x, a, sm_count, st);
+    if (cin == 32 && n == 16)
+        return launch<32, 16>(x, a, sm_count, st);
+    return cudaErrorInvalidValue;
+}
+
+// W[tap][cout][cin] FP32 (master layout, or the data-gradient layout with
+// `reverse`: tap 26 - t and the channel roles swapped) -> B blocks
+// [27][KC][2 K groups][N/8 N groups][8 rows][8 K] BF16, zero beyond cout/cin
+__global__ void k_pack_tc(const float *__restrict__ w, int cout, int cin, int reverse, int cinp, int n,
+                          __nv_bfloat16 *out)
+{
+    const int kc_n = cinp / 16;
+    const int total = 27 * kc_n * 2 * n * 8;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+        int r = q;
+        const int e = r % 8;
+        r /= 8;
+        const int row = r % 8;
+        r /= 8;
+        const int j = r % (n / 8);
+        r /= n / 8;
+        const int h = r % 2;
+        r /= 2;
+        const int kc = r % kc_n;
+        const int tap = r / kc_n;
+        const int co = 8 * j + row, ci = 16 * kc + 8 * h + e;
+        float v = 0.f;
+        if (!reverse) {
+            if (co < cout && ci < cin)
+                v = w[((size_t)tap * cout + co) * cin + ci];
+        } else {
+            // data gradient: output channel co = the forward's input channel,
+            // input channel ci = the forward's output channel
+            if (co < cin && ci < cout)
+                v = w[((size_t)(26 - tap) * cout + ci) * cin + co];
+        }
+        out[q] = __float2bfloat16_rn(v);
+    }
+}
+
+void pack_tc(const float *w, int cout, int cin, int reverse, int cinp, int n, __nv_bfloat16 *out, cudaStream_t st)
+{
+    k_pack_tc<<<64, 256, 0, st>>>(w, cout, cin, reverse, cinp, n, out);
+}
+
+} // namespace tc
+} // namespace ss4d

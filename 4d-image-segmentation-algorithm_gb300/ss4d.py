@@ -92,6 +92,85 @@ _lib = None
 ABI_VERSION = 2  # include/ss4d.h SS4D_ABI_VERSION: the structures above mirror it
 
 
+# t-slab callbacks (include/ss4d.h: ss4d_slab_comm, ss4d_slab_ops)
+EXCHANGE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p)
+ALLREDUCE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double))
+HALF_SWEEP_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int)
+RESIDUAL_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double))
+
+
+class SlabComm(C.Structure):
+    _fields_ = [("ctx", C.c_void_p), ("exchange", EXCHANGE_FN), ("allreduce_sum", ALLREDUCE_FN)]
+
+
+class SlabOps(C.Structure):
+    _fields_ = [("ctx", C.c_void_p), ("half_sweep", HALF_SWEEP_FN), ("residual", RESIDUAL_FN), ("u", C.c_void_p),
+                ("frame_elems", C.c_longlong), ("lMax", C.c_int), ("stream", C.c_void_p)]
+
+
+def _guarded(fn):
+    """a callback that reports a Python exception as a non-zero status"""
+    def call(*a):
+        try:
+            r = fn(*a)
+            return 0 if r is None else int(r)
+        except Exception as ex:  # noqa: BLE001  (surfaced through the library's status)
+            import traceback
+            traceback.print_exc()
+            call.error = ex
+            return 1
+    call.error = None
+    return call
+
+
+def slab_comm(exchange, allreduce_sum):
+    """An ss4d_slab_comm from Python callables:
+    exchange(u_ptr: int, frame_elems: int, lMax: int, stream: int | None) and
+    allreduce_sum(value: float) -> float.  Keep the returned object alive
+    while the library may call it."""
+    def ex(ctx, u, fe, lM, stream):
+        exchange(u, fe, lM, stream)
+
+    def ar(ctx, v):
+        v[0] = float(allreduce_sum(v[0]))
+
+    keep = (EXCHANGE_FN(_guarded(ex)), ALLREDUCE_FN(_guarded(ar)))
+    c = SlabComm(None, keep[0], keep[1])
+    c._keep = keep
+    return c
+
+
+def slab_ops(half_sweep, residual, u_ptr: int, frame_elems: int, lMax: int):
+    """An ss4d_slab_ops from Python callables (host work): half_sweep(colour)
+    and residual() -> float, over the slab array at u_ptr."""
+    def hs(ctx, colour):
+        half_sweep(colour)
+
+    def rs(ctx, out):
+        out[0] = float(residual())
+
+    keep = (HALF_SWEEP_FN(_guarded(hs)), RESIDUAL_FN(_guarded(rs)))
+    o = SlabOps(None, keep[0], keep[1], u_ptr, frame_elems, lMax, None)
+    o._keep = keep
+    return o
+
+
+def slab_partition(nt: int, nranks: int):
+    """[(first, count)] per rank: global interior frames first..first+count-1"""
+    first = (C.c_int * nranks)()
+    count = (C.c_int * nranks)()
+    _check(lib().ss4d_slab_partition(nt, nranks, first, count), "slab_partition")
+    return [(first[r], count[r]) for r in range(nranks)]
+
+
+def slab_sor_loop(ops: SlabOps, comm: SlabComm, p: Params, nint_global: int) -> dict:
+    """ss4d_slab_sor_loop: the slab SOR loop over the given callbacks"""
+    st = StepStats()
+    _check(lib().ss4d_slab_sor_loop(C.byref(ops), C.byref(comm), C.byref(p), nint_global, C.byref(st)),
+           "slab_sor_loop")
+    return st.as_dict()
+
+
 def lib() -> C.CDLL:
     """Load libss4d.so (built by build.py) and declare its signatures."""
     global _lib
@@ -179,6 +258,13 @@ def lib() -> C.CDLL:
         "ss4d_solver_set_warm_start": ([vp, vp, vp], st),
         "ss4d_solver_set_extrapolation": ([vp, C.c_int], st),
         "ss4d_solver_set_inner_omega": ([vp, C.c_double], st),
+        "ss4d_slab_partition": ([C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)], st),
+        "ss4d_slab_sor_loop": ([C.POINTER(SlabOps), C.POINTER(SlabComm), C.POINTER(Params), C.c_longlong,
+                                C.POINTER(StepStats)], st),
+        "ss4d_slab_sor_solve": ([vp, C.POINTER(Params), vp, vp, P8, C.POINTER(SlabComm), C.c_longlong,
+                                 C.POINTER(StepStats)], st),
+        "ss4d_slab_seg_time_step": ([vp, C.POINTER(Params), vp, vp, P8, vp, C.POINTER(Balls), C.POINTER(SlabComm),
+                                     C.c_longlong, C.POINTER(StepStats)], st),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -449,6 +535,25 @@ class Solver:
         _check(self.L.ss4d_ws_features(self.h, C.byref(p), _ptr(u), _p8(g8), _ptr(i0), _ptr(x0), C.byref(sig)),
                "ws_features")
         return sig.value
+
+    def slab_sor_solve(self, p: Params, u, prev, coef8, comm: SlabComm, nint_global: int) -> dict:
+        """ss4d_slab_sor_solve: this handle's volume is one slab of a volume
+        split by frames; comm exchanges ghost frames and sums the residual"""
+        st = StepStats()
+        _check(self.L.ss4d_slab_sor_solve(self.h, C.byref(p), _ptr(u), _ptr(prev), _p8(coef8), C.byref(comm),
+                                          nint_global, C.byref(st)), "slab_sor_solve")
+        return st.as_dict()
+
+    def slab_seg_time_step(self, p: Params, u, prev, g8, comm: SlabComm, nint_global: int, mmask=None,
+                           balls=None) -> dict:
+        """ss4d_slab_seg_time_step: one time step of this slab"""
+        st = StepStats()
+        B, keep = _balls(balls)
+        _check(self.L.ss4d_slab_seg_time_step(self.h, C.byref(p), _ptr(u), _ptr(prev), _p8(g8), _ptr(mmask),
+                                              C.byref(B) if B is not None else None, C.byref(comm), nint_global,
+                                              C.byref(st)), "slab_seg_time_step")
+        del keep
+        return st.as_dict()
 
     def set_warm_start(self, net, i0):
         """Attach a `Wsnet` (None detaches); i0 is the presmoothed image.  The

@@ -441,6 +441,78 @@ ss4d_status ss4d_ws_features(ss4d_solver *s, const ss4d_params *p, double *d_u, 
  * image.  Used by SS4D_ARITH_MIXED segmentation steps. */
 ss4d_status ss4d_solver_set_warm_start(ss4d_solver *s, ss4d_wsnet *n, const double *d_i0);
 
+/* ---- one volume split across ranks by frames (t-slabs) ----------------
+ * The reference's MPI program (segmentation4D_mpi.c) splits the frames of one
+ * volume into slabs, one per process, exchanges one ghost frame with each
+ * neighbour after every half-sweep (_communication_mpi_, :485-526; called at
+ * :330 and :361), sums the residual over all processes every iteration
+ * (MPI_Allreduce, :386) and picks the red voxels by the global index sum
+ * (:307, :338).  Here a rank holds its slab as an ordinary padded volume
+ * (lMax = its frames + 2, frame 0 and lMax-1 the ghosts) and the caller
+ * supplies the communication (NCCL, MPI, ...) as two callbacks; the library
+ * runs the loop.  Slabs are cut by ss4d_slab_partition so that every slab
+ * starts on an even global frame offset: the red voxels of a slab are then
+ * those with (i + j + k + l_local) even, the global red set, on every rank
+ * (the reference's offset N * rank is wrong for uneven slabs). */
+
+/* Cut nt frames into nranks slabs: rank r holds global interior frames
+ * first[r] .. first[r] + count[r] - 1 (1-based).  Every slab but the last has
+ * an even number of frames; SS4D_ERR_INVALID when nt < 2 nranks - 1. */
+ss4d_status ss4d_slab_partition(int nt, int nranks, int *first, int *count);
+
+typedef struct ss4d_slab_comm {
+    void *ctx;
+    /* Exchange the ghost frames of u (lMax frames of frame_elems doubles):
+     * send frame 1 to the rank below and frame lMax-2 to the rank above;
+     * receive the rank below's last interior frame into frame 0 and the rank
+     * above's first into frame lMax-1.  At the volume's ends nothing is sent
+     * or received (those ghosts keep the boundary values).  u is device
+     * memory for the GPU entry points, whose work is queued on `stream` (a
+     * cudaStream_t; NULL for host work): the exchange must come after it in
+     * that stream (an NCCL call on it) or wait for it.  Returns 0 on success. */
+    int (*exchange)(void *ctx, double *u, long long frame_elems, int lMax, void *stream);
+    /* *value <- the sum of *value over all ranks (host memory).  0 on success. */
+    int (*allreduce_sum)(void *ctx, double *value);
+} ss4d_slab_comm;
+
+/* The local work of one slab's SOR loop: a half-sweep of colour 0 (red) or 1
+ * (black) over the slab's interior, and the slab's part of the residual
+ * sum r^2 h^4 over its interior.  Returns 0 on success. */
+typedef struct ss4d_slab_ops {
+    void *ctx;
+    int (*half_sweep)(void *ctx, int colour);
+    int (*residual)(void *ctx, double *partial);
+    double *u;              /* the slab's u, handed to the exchange */
+    long long frame_elems;  /* iMax * jMax * kMax */
+    int lMax;               /* the slab's padded frame count */
+    void *stream;           /* where the ops' work is queued (cudaStream_t; NULL: host) */
+} ss4d_slab_ops;
+
+/* The slab SOR loop of _segTimeStep_mpi_ (segmentation4D_mpi.c:297-387):
+ * repeat { red; exchange; black; exchange; residual; sum over ranks } while
+ * sum > gsTol && z < maxNoGSIteration.  nint_global = the whole volume's
+ * interior voxel count (the near_tolerance band).  Host code only: the ops
+ * decide where the work runs. */
+ss4d_status ss4d_slab_sor_loop(const ss4d_slab_ops *ops, const ss4d_slab_comm *comm, const ss4d_params *p,
+                               long long nint_global, ss4d_step_stats *stats);
+
+/* ss4d_slab_sor_loop on the GPU: the solver's dims are the slab's; d_u,
+ * d_prev_u, d_coef in its natural layout (device).  The half-sweeps and the
+ * residual are the reference-order FP64 kernels (SS4D_ARITH_REFERENCE), so
+ * slab iterates equal the single-volume iterates bit for bit. */
+ss4d_status ss4d_slab_sor_solve(ss4d_solver *s, const ss4d_params *p, double *d_u, const double *d_prev_u,
+                                const double *const d_coef[8], const ss4d_slab_comm *comm, long long nint_global,
+                                ss4d_step_stats *stats);
+
+/* _segTimeStep_mpi_ (segmentation4D_mpi.c:282-397) for one slab: exchange
+ * u's ghost frames, prev_u <- u, coefficients (reference order) from u and
+ * the slab's g faces, ss4d_slab_sor_solve, then the rescale of the slab's
+ * frames (d_Mmask may be NULL; balls with frame indices local to the slab).
+ * d_prev_u may be NULL (the handle's own). */
+ss4d_status ss4d_slab_seg_time_step(ss4d_solver *s, const ss4d_params *p, double *d_u, double *d_prev_u,
+                                    const double *const d_g[8], const double *d_Mmask, const ss4d_balls *balls,
+                                    const ss4d_slab_comm *comm, long long nint_global, ss4d_step_stats *stats);
+
 /* ---- memory helpers (used by the reference-named layer) --------------- */
 /* Device / pinned-host allocations and copies on the handle's stream.  They
  * exist so that C callers without the CUDA headers (ss4d_compat.c) can mirror

@@ -148,6 +148,19 @@ def sor(p, u: np.ndarray, prev: np.ndarray, coef):
     return z, R.value
 
 
+def sor_half(p, u: np.ndarray, prev: np.ndarray, coef, colour: int):
+    """one red (0) or black (1) half-sweep of the SOR loop over u's interior"""
+    lib().or_sor_half(C.byref(_dims(u.shape)), C.byref(p), C.c_void_p(_d(u)), C.c_void_p(_d(prev)), _p8(coef),
+                      C.c_int(colour))
+
+
+def sor_residual(p, u: np.ndarray, prev: np.ndarray, coef) -> float:
+    """the SOR loop's residual sum r^2 h^4 over u's interior"""
+    f = lib().or_sor_residual
+    f.restype = C.c_double
+    return f(C.byref(_dims(u.shape)), C.byref(p), C.c_void_p(_d(u)), C.c_void_p(_d(prev)), _p8(coef))
+
+
 def _balls(balls):
     if not balls:
         return 0, None, None, None, None

@@ -495,6 +495,63 @@ int or_sor(const ss4d_dims *d, const ss4d_params *p, double *u, const double *pr
     return z;
 }
 
+/* One half-sweep of or_sor's loop (the red or the black loop of
+ * segmentation4D.c:234-285, identical in _segTimeStep_mpi_,
+ * segmentation4D_mpi.c:300-359) over the interior of the given array; with
+ * or_sor_residual the pieces a slab of a volume split by frames runs between
+ * its ghost-frame exchanges.  Same evaluation order as or_sor. */
+void or_sor_half(const ss4d_dims *d, const ss4d_params *p, double *u, const double *prev, const double *const a[8],
+                 int colour)
+{
+    geo_t g = geo_of(d);
+    const double c = p->tau / (p->h * p->h);
+    const ptrdiff_t sx = g.sx, sy = g.sy, sz = g.sz, sw = g.sw;
+    const double *E = a[0], *W = a[1], *N = a[2], *S = a[3], *T = a[4], *B = a[5], *FW = a[6], *BW = a[7];
+    int l;
+#pragma omp parallel for schedule(static)
+    for (l = 1; l <= g.lM - 2; l++)
+        for (int k = 1; k <= g.kM - 2; k++)
+            for (int j = 1; j <= g.jM - 2; j++)
+                for (int i = 1; i <= g.iM - 2; i++) {
+                    if ((i + j + k + l) % 2 != colour)
+                        continue;
+                    ptrdiff_t o = at(&g, i, j, k, l);
+                    double gs = (prev[o] + c * ((E[o] * u[o + sx]) + (W[o] * u[o - sx]) + (S[o] * u[o - sy])
+                                                + (N[o] * u[o + sy]) + (B[o] * u[o - sz]) + (T[o] * u[o + sz])
+                                                + (BW[o] * u[o - sw]) + (FW[o] * u[o + sw])))
+                                / (1 + c * (E[o] + W[o] + N[o] + S[o] + T[o] + B[o] + FW[o] + BW[o]));
+                    u[o] = u[o] + p->omega_c * (gs - u[o]);
+                }
+}
+
+/* The residual sum of or_sor's loop (segmentation4D.c:288-308) over the
+ * interior of the given array (summed in (l, k, j, i) order when one thread
+ * runs it). */
+double or_sor_residual(const ss4d_dims *d, const ss4d_params *p, const double *u, const double *prev,
+                       const double *const a[8])
+{
+    geo_t g = geo_of(d);
+    const double c = p->tau / (p->h * p->h);
+    const double h4 = p->h * p->h * p->h * p->h;
+    const ptrdiff_t sx = g.sx, sy = g.sy, sz = g.sz, sw = g.sw;
+    const double *E = a[0], *W = a[1], *N = a[2], *S = a[3], *T = a[4], *B = a[5], *FW = a[6], *BW = a[7];
+    double R = 0.0;
+    int l;
+#pragma omp parallel for schedule(static) reduction(+ : R)
+    for (l = 1; l <= g.lM - 2; l++)
+        for (int k = 1; k <= g.kM - 2; k++)
+            for (int j = 1; j <= g.jM - 2; j++)
+                for (int i = 1; i <= g.iM - 2; i++) {
+                    ptrdiff_t o = at(&g, i, j, k, l);
+                    R += (pow(u[o] * (1 + c * (E[o] + W[o] + N[o] + S[o] + T[o] + B[o] + FW[o] + BW[o]))
+                                  - c * ((E[o] * u[o + sx]) + (W[o] * u[o - sx]) + (S[o] * u[o - sy])
+                                         + (N[o] * u[o + sy]) + (B[o] * u[o - sz]) + (T[o] * u[o + sz])
+                                         + (BW[o] * u[o - sw]) + (FW[o] * u[o + sw]))
+                                  - prev[o], 2) * h4);
+                }
+    return R;
+}
+
 /* ---------------------------------------------------------------------- */
 /* rescale / mask                                                           */
 

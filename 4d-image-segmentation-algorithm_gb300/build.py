@@ -36,6 +36,7 @@ CUDA_UNITS = {
     "ss4d_batch.cu": [],
     "ss4d_ws.cu": [],
     "ss4d_nn.cu": [],
+    "ss4d_conv_tc.cu": [],
     "ss4d_assemble_ff.cu": [],
     "ss4d_front_ff.cu": [],
 }

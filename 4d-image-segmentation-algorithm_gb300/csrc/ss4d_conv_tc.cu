@@ -245,10 +245,17 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
         if (*abort_flag)
             break;
         if (it >= 1) {
-            // epilogue of tile it-1: its accumulators -> bias, ReLU, mask -> global
+            // epilogue of tile it-1: its accumulators -> bias, ReLU, mask -> global.
+            // One lane per warp waits, so that the warp stays converged for
+            // the .sync.aligned tensor-memory loads.
             const int j = it - 1;
-            if (!mbar_wait(smem_u32(bars + 2 + (j & 1)), (j >> 1) & 1)) {
-                *abort_flag = 1;
+            int ok = 0;
+            if (lane == 0)
+                ok = mbar_wait(smem_u32(bars + 2 + (j & 1)), (j >> 1) & 1);
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) {
+                if (lane == 0)
+                    *abort_flag = 1;
             } else {
                 tc_fence_after();
                 int x0, y0, z0, f;
@@ -284,10 +291,14 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
         // its shared and tensor memory go away
         if (tid == 0) {
             atomicExch(a.err, 1);
-            for (int t = 0; t < issued_loads; ++t)
-                mbar_wait(smem_u32(bars + (t & 1)), (t >> 1) & 1);
-            if (issued_mma > 0)
-                mbar_wait(smem_u32(bars + 2 + ((issued_mma - 1) & 1)), ((issued_mma - 1) >> 1) & 1);
+            // the last load and the last MMA batch of each buffer may still be
+            // in flight (earlier phases of its barrier have completed)
+            for (int t = issued_loads - 2; t < issued_loads; ++t)
+                if (t >= 0)
+                    mbar_wait(smem_u32(bars + (t & 1)), (t >> 1) & 1);
+            for (int t = issued_mma - 2; t < issued_mma; ++t)
+                if (t >= 0)
+                    mbar_wait(smem_u32(bars + 2 + (t & 1)), (t >> 1) & 1);
         }
         tc_fence_before();
         __syncthreads();
@@ -349,8 +360,14 @@ static cudaError_t launch(const void *x, const TcArgs &a, int sm_count, cudaStre
     if (!make_map(&m, x, CIN, a.nx, a.ny, a.nz, a.nf))
         return cudaErrorInvalidValue;
     set_attr_once<CIN, N>();
+    static int per_sm = 0;
+    if (!per_sm) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv_tc<CIN, N>, 128, TcCfg<CIN, N>::SMEM);
+        per_sm = per_sm < 1 ? 1 : (per_sm > 2 ? 2 : per_sm); // tensor memory: 2 x TCOLS <= 512 columns
+    }
     const long long tiles = tc_tiles(a.nx, a.ny, a.nz, a.nf);
-    const int grid = (int)(tiles < sm_count ? tiles : sm_count);
+    const long long cap = (long long)sm_count * per_sm;
+    const int grid = (int)(tiles < cap ? tiles : cap);
     k_conv_tc<CIN, N><<<grid, 128, TcCfg<CIN, N>::SMEM, st>>>(m, a);
     return cudaGetLastError();
 }
@@ -399,6 +416,21 @@ __global__ void k_pack_tc(const float *__restrict__ w, int cout, int cin, int re
         }
         out[q] = __float2bfloat16_rn(v);
     }
+}
+
+// after a convolution that gave up a wait: the prediction becomes NaN, which
+// every consumer discards (the warm start's check) or shows (the loss)
+__global__ void k_poison_if_err(const int *__restrict__ err, float *y, long long n)
+{
+    if (!*err)
+        return;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        y[i] = __int_as_float(0x7fc00000);
+}
+
+void poison_if_err(const int *err, float *y, long long n, cudaStream_t st)
+{
+    k_poison_if_err<<<256, 256, 0, st>>>(err, y, n);
 }
 
 void pack_tc(const float *w, int cout, int cin, int reverse, int cinp, int n, __nv_bfloat16 *out, cudaStream_t st)

@@ -3,19 +3,18 @@
 // gradients and its optimiser, as hand-written kernels.
 //
 // Tensors are channels-last: [F][nz][ny][nx][C] with C = 16 or 32 BF16
-// channels (16 input features; 24 hidden channels, the rest zero).  A convolution is an
-// implicit GEMM per frame: M = voxels, N = output channels, K = 27 taps x
-// input channels.  A block loads a 10x10x6 input tile (an 8x8x4 output tile
-// plus a one-voxel halo, zero outside the volume) into shared memory once;
-// every tap is then a shifted view of it, gathered by ldmatrix row addresses
-// and fed to BF16 tensor-core MMAs (m16n8k16, FP32 accumulators).  The data
-// gradient of a layer is the same kernel with the taps reversed and the
-// channel roles swapped; the weight gradient is an FP32 reduction over voxels
-// with a fixed summation order.
+// channels (16 input features; 24 hidden channels, the rest zero).  Every
+// convolution, forward and data gradient, runs on the tcgen05 tensor cores
+// (ss4d_conv_tc.cu): an implicit GEMM per frame, M = voxels, N = output
+// channels, K = 27 taps x input channels.  The data gradient of a layer is
+// the same convolution with the taps reversed and the channel roles swapped;
+// the weight gradient is an FP32 reduction over voxels with a fixed
+// summation order (this file).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "ss4d_conv_tc.cuh"
 #include "ss4d_kernels.cuh"
 
 namespace ss4d {
@@ -25,179 +24,6 @@ constexpr int TX = 8, TY = 8, TZ = 4;
 constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2;
 constexpr int TV = TX * TY * TZ; // 256 output voxels per tile
 constexpr int HV = HX * HY * HZ; // 600 input voxels per tile
-
-struct ConvArgs {
-    const __nv_bfloat16 *x; // [F][nz][ny][nx][CIN]
-    const __nv_bfloat16 *w; // [27][NT*8][CIN]
-    const float *bias;      // [NT*8] or null
-    const __nv_bfloat16 *mask; // [F][..][mstride]: keep output channel c where mask > 0 (or null)
-    __nv_bfloat16 *y;       // [F][..][ystride] or null
-    float *yf;              // [F][..] channel 0 in FP32, or null
-    int nx, ny, nz, nf;
-    int ystride, mstride;
-    int relu;
-};
-
-__device__ __forceinline__ unsigned smem_u32(const void *p)
-{
-    return (unsigned)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void ldsm_x4(unsigned addr, unsigned &r0, unsigned &r1, unsigned &r2, unsigned &r3)
-{
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-                 : "r"(addr));
-}
-
-__device__ __forceinline__ void ldsm_x2(unsigned addr, unsigned &r0, unsigned &r1)
-{
-    asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n" : "=r"(r0), "=r"(r1) : "r"(addr));
-}
-
-__device__ __forceinline__ void mma_bf16(float (&c)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
-                                         unsigned b0, unsigned b1)
-{
-    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-                 "{%0,%1,%2,%3};\n"
-                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-                 : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-__host__ __device__ constexpr int conv_smem_bytes(int cin, int nt)
-{
-    return (HV * (cin + 8) + 27 * nt * 8 * (cin + 8)) * 2;
-}
-
-// One "same" 3x3x3 convolution (zero padding) over every frame.  CIN input
-// channels (16 or 32), NT tiles of 8 output channels.  Persistent blocks loop
-// over 8x8x4 output tiles; the weights stay in shared memory.
-template <int CIN, int NT>
-__global__ void __launch_bounds__(256) k_conv(ConvArgs a)
-{
-    extern __shared__ __align__(16) unsigned char smem[];
-    constexpr int XS = CIN + 8; // padded rows: conflict-free ldmatrix
-    constexpr int NO = NT * 8;
-    __nv_bfloat16 *sx = reinterpret_cast<__nv_bfloat16 *>(smem);
-    __nv_bfloat16 *sw = sx + HV * XS;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-
-    for (int q = tid; q < 27 * NO * (CIN / 8); q += blockDim.x) {
-        const int row = q / (CIN / 8), c8 = q % (CIN / 8);
-        *reinterpret_cast<uint4 *>(sw + row * XS + c8 * 8) =
-            *reinterpret_cast<const uint4 *>(a.w + (size_t)row * CIN + c8 * 8);
-    }
-    const int ntx = (a.nx + TX - 1) / TX, nty = (a.ny + TY - 1) / TY, ntz = (a.nz + TZ - 1) / TZ;
-    const long long ntiles = (long long)ntx * nty * ntz * a.nf;
-    // this lane's ldmatrix rows (output voxels) in the two 16-row m tiles of its warp
-    int hb[2];
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt) {
-        const int m = warp * 32 + mt * 16 + (lane & 15);
-        hb[mt] = ((m / (TX * TY) + 1) * HY + ((m / TX) % TY) + 1) * HX + (m % TX) + 1;
-    }
-    const int kofs = (lane >> 4) * 8;
-
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        long long r = tile;
-        const int tx0 = (int)(r % ntx) * TX;
-        r /= ntx;
-        const int ty0 = (int)(r % nty) * TY;
-        r /= nty;
-        const int tz0 = (int)(r % ntz) * TZ;
-        const int f = (int)(r / ntz);
-        __syncthreads(); // previous tile's reads of sx are done
-        for (int q = tid; q < HV * (CIN / 8); q += blockDim.x) {
-            const int v = q / (CIN / 8), c8 = q % (CIN / 8);
-            const int gx = tx0 + v % HX - 1, gy = ty0 + (v / HX) % HY - 1, gz = tz0 + v / (HX * HY) - 1;
-            uint4 val = make_uint4(0, 0, 0, 0);
-            if (gx >= 0 && gx < a.nx && gy >= 0 && gy < a.ny && gz >= 0 && gz < a.nz)
-                val = *reinterpret_cast<const uint4 *>(
-                    a.x + ((((size_t)f * a.nz + gz) * a.ny + gy) * a.nx + gx) * CIN + c8 * 8);
-            *reinterpret_cast<uint4 *>(sx + v * XS + c8 * 8) = val;
-        }
-        __syncthreads();
-
-        float acc[2][NT][4];
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-            for (int nt = 0; nt < NT; ++nt)
-#pragma unroll
-                for (int e = 0; e < 4; ++e)
-                    acc[mt][nt][e] = 0.f;
-
-        for (int tap = 0; tap < 27; ++tap) {
-            const int toff = ((tap / 9 - 1) * HY + ((tap / 3) % 3 - 1)) * HX + (tap % 3 - 1);
-            const __nv_bfloat16 *wt = sw + tap * NO * XS;
-#pragma unroll
-            for (int kc = 0; kc < CIN / 16; ++kc) {
-                unsigned bfr[NT][2];
-#pragma unroll
-                for (int np = 0; np < NT; np += 2) {
-                    if (np + 1 < NT) {
-                        const int nrow = np * 8 + (lane & 7) + ((lane >> 4) << 3);
-                        const int kk = kc * 16 + ((lane >> 3) & 1) * 8;
-                        ldsm_x4(smem_u32(wt + nrow * XS + kk), bfr[np][0], bfr[np][1], bfr[np + 1][0],
-                                bfr[np + 1][1]);
-                    } else {
-                        const int nrow = np * 8 + (lane & 7);
-                        const int kk = kc * 16 + ((lane >> 3) & 1) * 8;
-                        ldsm_x2(smem_u32(wt + nrow * XS + kk), bfr[np][0], bfr[np][1]);
-                    }
-                }
-#pragma unroll
-                for (int mt = 0; mt < 2; ++mt) {
-                    unsigned a0, a1, a2, a3;
-                    ldsm_x4(smem_u32(sx + (hb[mt] + toff) * XS + kc * 16 + kofs), a0, a1, a2, a3);
-#pragma unroll
-                    for (int nt = 0; nt < NT; ++nt)
-                        mma_bf16(acc[mt][nt], a0, a1, a2, a3, bfr[nt][0], bfr[nt][1]);
-                }
-            }
-        }
-
-        // epilogue: rows lane/4 and lane/4 + 8 of each m tile, columns 2(lane%4), +1
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt) {
-#pragma unroll
-            for (int half = 0; half < 2; ++half) {
-                const int m = warp * 32 + mt * 16 + (lane >> 2) + 8 * half;
-                const int ox = tx0 + m % TX, oy = ty0 + (m / TX) % TY, oz = tz0 + m / (TX * TY);
-                if (ox >= a.nx || oy >= a.ny || oz >= a.nz)
-                    continue;
-                const size_t vox = (((size_t)f * a.nz + oz) * a.ny + oy) * a.nx + ox;
-#pragma unroll
-                for (int nt = 0; nt < NT; ++nt) {
-                    const int c = nt * 8 + 2 * (lane & 3);
-                    float v0 = acc[mt][nt][2 * half], v1 = acc[mt][nt][2 * half + 1];
-                    if (a.bias) {
-                        v0 += a.bias[c];
-                        v1 += a.bias[c + 1];
-                    }
-                    if (a.relu) {
-                        v0 = fmaxf(v0, 0.f);
-                        v1 = fmaxf(v1, 0.f);
-                    }
-                    if (a.mask) {
-                        const __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162 *>(a.mask + vox * a.mstride + c);
-                        if (!(__low2float(mk) > 0.f))
-                            v0 = 0.f;
-                        if (!(__high2float(mk) > 0.f))
-                            v1 = 0.f;
-                    }
-                    if (a.y)
-                        *reinterpret_cast<__nv_bfloat162 *>(a.y + vox * a.ystride + c) = __floats2bfloat162_rn(v0, v1);
-                    if (a.yf && nt == 0 && (lane & 3) == 0)
-                        a.yf[vox] = v0;
-                }
-                if (a.y) // zero the padding channels of the output rows
-                    for (int c = NO + 2 * (lane & 3); c < a.ystride; c += 8)
-                        *reinterpret_cast<__nv_bfloat162 *>(a.y + vox * a.ystride + c) = __floats2bfloat162_rn(0.f, 0.f);
-            }
-        }
-    }
-}
 
 // dW[tap][co][ci] and db[co] summed over the voxels of each block's tiles
 // (FP32); X: [F][..][CIN] (the layer input), dY: [F][..][YS] with COUT used
@@ -345,28 +171,6 @@ __global__ void k_adam(float *p, const float *__restrict__ g, float *m, float *v
     p[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
 }
 
-// master weights W[27][cout][cin_real] -> forward layout [27][nout][cinp] BF16
-// and (when wt != null) the data-gradient layout [27][ninp][coutp]: tap
-// reversed, channels swapped
-__global__ void k_pack_weights(const float *__restrict__ w, int cout, int cin, __nv_bfloat16 *wf, int nout, int cinp,
-                               __nv_bfloat16 *wt, int ninp, int coutp)
-{
-    const int n1 = 27 * nout * cinp;
-    const int n2 = wt ? 27 * ninp * coutp : 0;
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n1 + n2; q += gridDim.x * blockDim.x) {
-        if (q < n1) {
-            const int tap = q / (nout * cinp), r = q % (nout * cinp), co = r / cinp, ci = r % cinp;
-            const float val = (co < cout && ci < cin) ? w[((size_t)tap * cout + co) * cin + ci] : 0.f;
-            wf[q] = __float2bfloat16_rn(val);
-        } else {
-            const int q2 = q - n1;
-            const int tap = q2 / (ninp * coutp), r = q2 % (ninp * coutp), ci = r / coutp, co = r % coutp;
-            const float val = (co < cout && ci < cin) ? w[((size_t)(26 - tap) * cout + co) * cin + ci] : 0.f;
-            wt[q2] = __float2bfloat16_rn(val);
-        }
-    }
-}
-
 // gradient rows of the weight partials -> master layout [27][cout][cin_real] + bias
 __global__ void k_unpack_grad(const float *__restrict__ gsum, int cout, int cinp, int cin, float *gw, float *gb)
 {
@@ -399,17 +203,18 @@ namespace {
 
 struct Layer {
     int cin, cout;   // real channels
-    int cinp, nout;  // padded input channels (kernel CIN), output channels computed (NT*8)
+    int cinp, nout;  // stored input channels (the convolution's CIN), output channels computed (its N)
     int coutp_t;     // channels of this layer's output gradient as a data-gradient input (16 or 32)
     size_t w_off, b_off;
 };
 
-// 16 -> 24 -> 24 -> 24 -> 1
+// 16 -> 24 -> 24 -> 24 -> 1; a tcgen05 MMA with M = 128 computes N = 32 (or
+// 16) output channels, the ones beyond cout with zero weights
 const Layer kLayers[4] = {
-    {16, 24, 16, 24, 32, 0, 0},
-    {24, 24, 32, 24, 32, 0, 0},
-    {24, 24, 32, 24, 32, 0, 0},
-    {24, 1, 32, 8, 16, 0, 0},
+    {16, 24, 16, 32, 32, 0, 0},
+    {24, 24, 32, 32, 32, 0, 0},
+    {24, 24, 32, 32, 32, 0, 0},
+    {24, 1, 32, 16, 16, 0, 0},
 };
 
 ss4d_status nfail(ss4d_status st, const char *fmt, ...)
@@ -440,7 +245,8 @@ struct ss4d_wsnet {
     int sm;
     size_t nparam;
     float *p, *g, *m, *v;          // master parameters, gradients, Adam moments (FP32, flat)
-    __nv_bfloat16 *wf[4], *wt[4];  // packed forward / data-gradient weights
+    __nv_bfloat16 *wf[4], *wt[4];  // forward / data-gradient weights as tcgen05 B operands (tc::pack_tc)
+    int *err;                      // set by a convolution that gave up a bounded wait
     float *bias[4];                // views into p
     // activations and gradients, sized for `cap` voxels
     size_t cap;
@@ -452,6 +258,7 @@ struct ss4d_wsnet {
     float *loss_part;
     float h_loss;
     long long step;
+    int launch_failed;
 };
 
 static size_t layer_offsets(size_t *w_off, size_t *b_off)
@@ -478,7 +285,7 @@ extern "C" ss4d_status ss4d_wsnet_destroy(ss4d_wsnet *n)
         return SS4D_OK;
     cudaStreamSynchronize(n->stream);
     void *ptrs[] = {n->p, n->g, n->m, n->v, n->a[0], n->a[1], n->a[2], n->dz16, n->dz32[0], n->dz32[1], n->y,
-                    n->partial, n->gsum, n->loss_part};
+                    n->partial, n->gsum, n->loss_part, n->err};
     for (void *q : ptrs)
         if (q)
             cudaFree(q);
@@ -497,9 +304,6 @@ static void set_conv_attrs()
     static bool done = false;
     if (done)
         return;
-    cudaFuncSetAttribute(k_conv<16, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, conv_smem_bytes(16, 3));
-    cudaFuncSetAttribute(k_conv<32, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, conv_smem_bytes(32, 3));
-    cudaFuncSetAttribute(k_conv<32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, conv_smem_bytes(32, 1));
     cudaFuncSetAttribute(k_wgrad<16, 24, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, wgrad_smem_bytes(16, 24));
     cudaFuncSetAttribute(k_wgrad<32, 24, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, wgrad_smem_bytes(32, 24));
     cudaFuncSetAttribute(k_wgrad<32, 1, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, wgrad_smem_bytes(32, 1));
@@ -528,11 +332,13 @@ extern "C" ss4d_status ss4d_wsnet_create(void *stream, ss4d_wsnet **out)
     if (e == cudaSuccess)
         e = cudaMalloc((void **)&n->v, n->nparam * 4);
     for (int L = 0; L < 4 && e == cudaSuccess; ++L) {
-        e = cudaMalloc((void **)&n->wf[L], (size_t)27 * kLayers[L].nout * kLayers[L].cinp * 2);
+        e = cudaMalloc((void **)&n->wf[L], tc::packed_tc_elems(kLayers[L].cinp, kLayers[L].nout) * 2);
         if (e == cudaSuccess && L > 0)
-            e = cudaMalloc((void **)&n->wt[L], (size_t)27 * 24 * kLayers[L].coutp_t * 2);
+            e = cudaMalloc((void **)&n->wt[L], tc::packed_tc_elems(kLayers[L].coutp_t, 32) * 2);
         n->bias[L] = n->p + boff[L];
     }
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **)&n->err, sizeof(int));
     if (e == cudaSuccess)
         e = cudaMalloc((void **)&n->gsum, (size_t)(27 * 24 * 32 + 24) * 4);
     if (e == cudaSuccess)
@@ -544,6 +350,7 @@ extern "C" ss4d_status ss4d_wsnet_create(void *stream, ss4d_wsnet **out)
     }
     cudaMemsetAsync(n->m, 0, n->nparam * 4, n->stream);
     cudaMemsetAsync(n->v, 0, n->nparam * 4, n->stream);
+    cudaMemsetAsync(n->err, 0, sizeof(int), n->stream);
     set_conv_attrs();
     *out = n;
     return SS4D_OK;
@@ -563,8 +370,9 @@ static ss4d_status pack_all(ss4d_wsnet *n)
     layer_offsets(woff, boff);
     for (int L = 0; L < 4; ++L) {
         const Layer &l = kLayers[L];
-        k_pack_weights<<<64, 256, 0, n->stream>>>(n->p + woff[L], l.cout, l.cin, n->wf[L], l.nout, l.cinp,
-                                                  L > 0 ? n->wt[L] : nullptr, 24, l.coutp_t);
+        tc::pack_tc(n->p + woff[L], l.cout, l.cin, 0, l.cinp, l.nout, n->wf[L], n->stream);
+        if (L > 0) // data gradient: input = this layer's output gradient, output = its input channels
+            tc::pack_tc(n->p + woff[L], l.cout, l.cin, 1, l.coutp_t, 32, n->wt[L], n->stream);
     }
     NCK(cudaGetLastError());
     return SS4D_OK;
@@ -653,11 +461,13 @@ static int conv_grid(const ss4d_wsnet *n, int nx, int ny, int nz, int nf)
     return (int)(tiles < g ? tiles : g);
 }
 
-static void conv(ss4d_wsnet *n, int cin, int nt, const __nv_bfloat16 *x, const __nv_bfloat16 *w, const float *bias,
-                 const __nv_bfloat16 *mask, __nv_bfloat16 *y, float *yf, int nx, int ny, int nz, int nf, int relu)
+// one convolution on the tensor cores: cin input channels (16 or 32), nout
+// computed output channels (32, or 16 for the output layer), cout of them real
+static void conv(ss4d_wsnet *n, int cin, int nout, int cout, const __nv_bfloat16 *x, const __nv_bfloat16 *w,
+                 const float *bias, const __nv_bfloat16 *mask, __nv_bfloat16 *y, float *yf, int nx, int ny, int nz,
+                 int nf, int relu)
 {
-    ConvArgs a;
-    a.x = x;
+    tc::TcArgs a;
     a.w = w;
     a.bias = bias;
     a.mask = mask;
@@ -667,16 +477,13 @@ static void conv(ss4d_wsnet *n, int cin, int nt, const __nv_bfloat16 *x, const _
     a.ny = ny;
     a.nz = nz;
     a.nf = nf;
+    a.cout = cout;
     a.ystride = 32;
     a.mstride = 32;
     a.relu = relu;
-    const int grid = conv_grid(n, nx, ny, nz, nf);
-    if (cin == 16 && nt == 3)
-        k_conv<16, 3><<<grid, 256, conv_smem_bytes(16, 3), n->stream>>>(a);
-    else if (cin == 32 && nt == 3)
-        k_conv<32, 3><<<grid, 256, conv_smem_bytes(32, 3), n->stream>>>(a);
-    else
-        k_conv<32, 1><<<grid, 256, conv_smem_bytes(32, 1), n->stream>>>(a);
+    a.err = n->err;
+    if (tc::conv_tc(cin, nout, x, a, n->sm, n->stream) != cudaSuccess)
+        n->launch_failed = 1;
 }
 
 // forward over F frames of extents nx, ny, nz; x0 [F][nz][ny][nx][16] BF16.
@@ -687,11 +494,16 @@ static ss4d_status forward(ss4d_wsnet *n, const __nv_bfloat16 *x0, int nx, int n
     const size_t vox = (size_t)nx * ny * nz * nf;
     NCK(ensure_act(n, vox, train) == SS4D_OK ? cudaSuccess : cudaErrorMemoryAllocation);
     __nv_bfloat16 *a1 = n->a[0], *a2 = n->a[1], *a3 = train ? n->a[2] : n->a[0];
-    conv(n, 16, 3, x0, n->wf[0], n->bias[0], nullptr, a1, nullptr, nx, ny, nz, nf, 1);
-    conv(n, 32, 3, a1, n->wf[1], n->bias[1], nullptr, a2, nullptr, nx, ny, nz, nf, 1);
-    conv(n, 32, 3, a2, n->wf[2], n->bias[2], nullptr, a3, nullptr, nx, ny, nz, nf, 1);
-    conv(n, 32, 1, a3, n->wf[3], n->bias[3], nullptr, nullptr, out ? out : n->y, nx, ny, nz, nf, 0);
+    n->launch_failed = 0;
+    conv(n, 16, 32, 24, x0, n->wf[0], n->bias[0], nullptr, a1, nullptr, nx, ny, nz, nf, 1);
+    conv(n, 32, 32, 24, a1, n->wf[1], n->bias[1], nullptr, a2, nullptr, nx, ny, nz, nf, 1);
+    conv(n, 32, 32, 24, a2, n->wf[2], n->bias[2], nullptr, a3, nullptr, nx, ny, nz, nf, 1);
+    float *y = out ? out : n->y;
+    conv(n, 32, 16, 1, a3, n->wf[3], n->bias[3], nullptr, nullptr, y, nx, ny, nz, nf, 0);
+    tc::poison_if_err(n->err, y, (long long)vox, n->stream);
     NCK(cudaGetLastError());
+    if (n->launch_failed)
+        return nfail(SS4D_ERR_CUDA, "a tensor-core convolution could not be launched (tensor map or launch)");
     return SS4D_OK;
 }
 
@@ -745,18 +557,20 @@ extern "C" ss4d_status ss4d_wsnet_train_step(ss4d_wsnet *n, const void *d_x0, co
     // layer 4 (3 -> out): weights and data gradient (masked by a3 > 0)
     if (wgrad<32, 1, 16>(n, n->a[2], n->dz16, nx, ny, nz, nf, 24, n->g + woff[3], n->g + boff[3]) != SS4D_OK)
         return SS4D_ERR_CUDA;
-    conv(n, 16, 3, n->dz16, n->wt[3], nullptr, n->a[2], n->dz32[0], nullptr, nx, ny, nz, nf, 0);
+    conv(n, 16, 32, 24, n->dz16, n->wt[3], nullptr, n->a[2], n->dz32[0], nullptr, nx, ny, nz, nf, 0);
     // layer 3
     if (wgrad<32, 24, 32>(n, n->a[1], n->dz32[0], nx, ny, nz, nf, 24, n->g + woff[2], n->g + boff[2]) != SS4D_OK)
         return SS4D_ERR_CUDA;
-    conv(n, 32, 3, n->dz32[0], n->wt[2], nullptr, n->a[1], n->dz32[1], nullptr, nx, ny, nz, nf, 0);
+    conv(n, 32, 32, 24, n->dz32[0], n->wt[2], nullptr, n->a[1], n->dz32[1], nullptr, nx, ny, nz, nf, 0);
     // layer 2
     if (wgrad<32, 24, 32>(n, n->a[0], n->dz32[1], nx, ny, nz, nf, 24, n->g + woff[1], n->g + boff[1]) != SS4D_OK)
         return SS4D_ERR_CUDA;
-    conv(n, 32, 3, n->dz32[1], n->wt[1], nullptr, n->a[0], n->dz32[0], nullptr, nx, ny, nz, nf, 0);
+    conv(n, 32, 32, 24, n->dz32[1], n->wt[1], nullptr, n->a[0], n->dz32[0], nullptr, nx, ny, nz, nf, 0);
     // layer 1
     if (wgrad<16, 24, 32>(n, x0, n->dz32[0], nx, ny, nz, nf, 16, n->g + woff[0], n->g + boff[0]) != SS4D_OK)
         return SS4D_ERR_CUDA;
+    if (n->launch_failed)
+        return nfail(SS4D_ERR_CUDA, "a tensor-core convolution could not be launched (tensor map or launch)");
     if (d_grad)
         NCK(cudaMemcpyAsync(d_grad, n->g, n->nparam * 4, cudaMemcpyDeviceToDevice, n->stream));
     if (lr > 0.f) {

@@ -126,10 +126,12 @@ struct ss4d_solver {
     // learned warm start (mixed form)
     ss4d_wsnet *ws_net;
     const double *ws_i0;
-    void *ws_x0;   // BF16 features [nt][nz][ny][nx][16]
+    void *ws_x0;   // BF16 features, planar [nt][2][nz][ny][nx][8]
     float *ws_y;   // prediction [nt][nz][ny][nx]
     CPtrs8 cur_g;  // g of the segmentation step in progress
     int have_g;
+    int ws_gate;       // the network runs when the previous mixed step took >= ws_gate FP32 sweeps (0: always)
+    int ws_last_iters; // FP32 sweeps of the previous mixed step (-1: none yet)
     // mixed form: start from an extrapolation in time (ss4d_solver_set_extrapolation)
     int extrap;      // 0 off, else the extrapolation order 1..3
     int have_dprev;  // steps in a row whose change was kept: dR[0] / dB hold the next start correction
@@ -643,6 +645,8 @@ static ss4d_status finish_stats(ss4d_solver *s, ss4d_step_stats *stats, int mixe
     CK(cudaMemcpyAsync(s->h_state, s->d_state, sizeof(LoopState), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     const LoopState &L = *s->h_state;
+    if (mixed)
+        s->ws_last_iters = L.z;
     if (stats) {
         stats->iterations = L.z;
         stats->residual = L.R;
@@ -729,7 +733,23 @@ extern "C" ss4d_status ss4d_solver_set_warm_start(ss4d_solver *s, ss4d_wsnet *n,
     REQ(!n || d_i0, "the warm start needs the presmoothed image");
     s->ws_net = n;
     s->ws_i0 = n ? d_i0 : nullptr;
+    s->ws_last_iters = -1;
     return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_solver_set_warm_start_gate(ss4d_solver *s, int min_iterations)
+{
+    REQ(s, "solver is NULL");
+    REQ(min_iterations >= 0, "the gate is a non-negative iteration count");
+    s->ws_gate = min_iterations;
+    return SS4D_OK;
+}
+
+// this step's solve starts from the network's prediction
+static bool ws_this_step(const ss4d_solver *s, int mixed)
+{
+    return mixed && s->ws_net && s->have_g &&
+           (s->ws_gate <= 0 || s->ws_last_iters < 0 || s->ws_last_iters >= s->ws_gate);
 }
 
 extern "C" ss4d_status ss4d_ws_features(ss4d_solver *s, const ss4d_params *p, double *d_u, const double *const d_g[8],
@@ -766,7 +786,7 @@ extern "C" ss4d_status ss4d_ws_features(ss4d_solver *s, const ss4d_params *p, do
 // a segmentation step of the mixed form that starts from u^n + (u^n - u^{n-1})
 static bool extrapolating(const ss4d_solver *s)
 {
-    return s->arith == SS4D_ARITH_MIXED && s->extrap && s->have_dprev && s->have_g && !s->ws_net;
+    return s->arith == SS4D_ARITH_MIXED && s->extrap && s->have_dprev && s->have_g;
 }
 
 // A mixed segmentation step (not with the learned warm start, which runs
@@ -780,7 +800,7 @@ static bool extrapolating(const ss4d_solver *s)
 // extrapolating() will find in dR[0] / dB).
 static int pre_form(const ss4d_solver *s, int mixed)
 {
-    if (!mixed || s->ws_net)
+    if (!mixed)
         return 0;
     return s->extrap && s->have_dprev ? 2 : 1;
 }
@@ -837,7 +857,7 @@ static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixe
         CKS(clear_corrections(s));
         launch_loop_init(s->d_state, 0, s->stream, pre);
         s->launches += 1;
-        if (s->ws_net && s->have_g)
+        if (ws_this_step(s, mixed))
             CKS(warm_start_prologue(s));
     }
     CKS(last_launch());
@@ -856,7 +876,7 @@ static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixe
     }
     if (!graphed) {
         // host-driven form of the same loop: one small readback per iteration
-        int mode = (mixed && s->ws_net && s->have_g) ? 1 : 0; // the mode the controller left for this body
+        int mode = ws_this_step(s, mixed) ? 1 : 0; // the mode the controller left for this body
         for (int guard = 0; guard < 4 * (p->maxNoGSIteration + 4) + 16; ++guard) {
             if (!mixed) {
                 timed(s, SS4D_K_SWEEP64, true,
@@ -1273,7 +1293,7 @@ struct UnpackPlan {
 // the extrapolation terms and history depth of this step's unpack
 static ss4d_status unpack_plan(ss4d_solver *s, int mixed, UnpackPlan *u)
 {
-    u->save = mixed && s->extrap && s->have_g && !s->ws_net;
+    u->save = mixed && s->extrap && s->have_g;
     u->terms = u->keep = 0;
     if (u->save) {
         u->keep = s->extrap - 1;

@@ -8,24 +8,28 @@
 // and the input channels of X[voxel + tap][cin] W[tap][cout][cin].  A CTA
 // takes output tiles of 8 (x) by 16 (y) voxels by TZ planes (z) of one
 // frame; each plane is one M = 128 accumulator (row m = x + 8 y) of N
-// output channels.  Its input halo tile, 10 x 18 x (TZ + 2) voxels, arrives
-// in shared memory by one TMA box per group of 8 channels; a box lands as
-// [z][y][x][8 channels], 16 bytes per voxel, which is the canonical K-major
-// layout of the UMMA operands without swizzle: a core matrix is 8
-// consecutive voxels (rows) by 8 channels (16 bytes).  So the A operand of
+// output channels.  Activations are channel-group planar in global memory
+// ([F][C/8][nz][ny][nx][8], ss4d_conv_tc.cuh), so the input halo tile,
+// 10 x 18 x (TZ + 2) voxels, arrives in shared memory by one TMA box per
+// group of 8 channels whose rows are 160 contiguous bytes (x and the 8
+// channels merged into one dimension); a box lands as [z][y][x][8 channels],
+// 16 bytes per voxel, which is the canonical K-major layout of the UMMA
+// operands without swizzle: a core matrix is 8 consecutive voxels (rows) by
+// 8 channels (16 bytes).  So the A operand of
 // tap (dx, dy, dz) is the halo tile itself, its descriptor starting at voxel
 // (dx, dy, p + dz): rows x + 8 y step 16 bytes within a core matrix and the
 // row stride of the halo (160 bytes) between the 8-row groups, channel
 // groups a plane apart.  No operand is copied per tap.  The weights of all
 // taps stay in shared memory in the same core-matrix layout.
 //
-// Per CTA: one thread issues the TMA loads and the MMAs; the halo tiles and
-// the accumulators are double-buffered, so the loads of tile i+1 and the
-// epilogue of tile i-1 (TMEM -> registers -> bias, ReLU, mask -> global) run
-// while the tensor core works on tile i.  Every wait on an mbarrier is
-// bounded (about a second of clock cycles); one that runs out sets an error
-// flag the host reads, the CTA waits (bounded) for its own loads and MMAs
-// in flight, frees its tensor memory and returns.
+// Per CTA: one thread of a fifth warp issues the TMA loads and the MMAs, four
+// warps drain the accumulators (TMEM -> registers -> bias, ReLU, mask ->
+// global); STAGES halo tiles and two accumulator buffers are in flight and
+// the roles meet only at mbarriers, so the loads of the next tiles and the
+// epilogue of tile i-1 run while the tensor core works on tile i.  Every wait on an
+// mbarrier is bounded (about a second of clock cycles); one that runs out
+// sets an error flag the host reads, the producer waits (bounded) for its own
+// loads and MMAs in flight, and the CTA frees its tensor memory and returns.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -76,12 +80,12 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
     return true;
 }
 
-__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap *map, uint32_t bar, int c0, int c1,
-                                            int c2, int c3, int c4)
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, uint32_t bar, int c0, int c1,
+                                            int c2, int c3)
 {
-    asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-                 " [%0], [%1, {%3, %4, %5, %6, %7}], [%2];" ::"r"(dst),
-                 "l"((uint64_t)map), "r"(bar), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4)
+    asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%3, %4, %5, %6}], [%2];" ::"r"(dst),
+                 "l"((uint64_t)map), "r"(bar), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
                  : "memory");
 }
 
@@ -133,25 +137,38 @@ __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.
 
 // ---- the kernel ---------------------------------------------------------------
 
+// warp roles: warps 0-3 read the accumulators (a warp reaches only its own 32
+// lanes of tensor memory) and store; lane 0 of warp 4 issues the loads and
+// the MMAs.  Barriers, one phase per use: full[s] (the loads of the tile in
+// halo stage s landed), done[b] (the MMAs of the tile in accumulator buffer
+// b completed: tcgen05.commit), free[b] (the four epilogue warps have read
+// buffer b).  Tile it uses stage it % STAGES and buffer it % 2.
+constexpr int EPI_WARPS = 4, THREADS = 32 * (EPI_WARPS + 1);
+
 template <int CIN, int N>
-__global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUtensorMap tmap, TcArgs a)
+__global__ void __launch_bounds__(THREADS, 1) k_conv_tc(const __grid_constant__ CUtensorMap tmap, TcArgs a)
 {
     using C = TcCfg<CIN, N>;
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     unsigned char *halo0 = smem;
-    unsigned char *wsm = smem + 2 * C::HALO;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(wsm + C::WBYTES); // [0,1] loads, [2,3] MMAs
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 4);
+    unsigned char *wsm = smem + STAGES * C::HALO;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(wsm + C::WBYTES); // full[STAGES], done[2], free[2]
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + STAGES + 4);
     int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t full0 = smem_u32(bars), done0 = smem_u32(bars + STAGES), free0 = smem_u32(bars + STAGES + 2);
 
     // weights: global (already in core-matrix order) -> shared
     for (int q = tid; q < C::WBYTES / 16; q += blockDim.x)
         reinterpret_cast<uint4 *>(wsm)[q] = __ldg(reinterpret_cast<const uint4 *>(a.w) + q);
     if (tid == 0) {
-        for (int b = 0; b < 4; ++b)
-            mbar_init(smem_u32(bars + b), 1);
+        for (int q = 0; q < STAGES; ++q)
+            mbar_init(full0 + 8 * q, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(done0 + 8 * b, 1);
+            mbar_init(free0 + 8 * b, EPI_WARPS);
+        }
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -177,132 +194,130 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
         z0 = (int)(r % ntz) * TZ;
         f = (int)(r / ntz);
     };
-    auto issue_load = [&](int it) {
-        int x0, y0, z0, f;
-        tile_xyzf(it, x0, y0, z0, f);
-        const int b = it & 1;
-        const uint32_t bar = smem_u32(bars + b);
-        mbar_expect_tx(bar, C::NCG * C::BOX_BYTES);
-        const uint32_t dst = smem_u32(halo0 + b * C::HALO);
-#pragma unroll
-        for (int g = 0; g < C::NCG; ++g)
-            tma_load_5d(dst + g * PLANE, &tmap, bar, 8 * g, x0 - 1, y0 - 1, z0 - 1, f);
-    };
-    // K-major operands without swizzle: LBO = stride of the core matrices
-    // along K, SBO = stride of the 8-row groups along M (N)
-    const uint32_t idesc = (1u << 4)                 // D: FP32
-                           | (1u << 7) | (1u << 10)  // A, B: BF16
-                           | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
-    int issued_loads = 0, issued_mma = 0; // of thread 0, for the abort path
 
-    if (tid == 0 && my_n > 0) {
-        issue_load(0);
-        issued_loads = 1;
-    }
-    for (int it = 0; it <= my_n; ++it) {
-        if (tid == 0 && !*abort_flag) {
-            if (it + 1 < my_n) {
-                // the buffer of tile it+1 was read by the MMAs of tile it-1
-                if (it >= 1 && !mbar_wait(smem_u32(bars + 2 + ((it - 1) & 1)), ((it - 1) >> 1) & 1))
-                    *abort_flag = 1;
-                else {
-                    issue_load(it + 1);
-                    issued_loads = it + 2;
-                }
-            }
-            if (it < my_n && !*abort_flag) {
-                if (!mbar_wait(smem_u32(bars + (it & 1)), (it >> 1) & 1)) {
-                    *abort_flag = 1;
-                } else {
-                    tc_fence_after();
-                    const uint32_t hbase = smem_u32(halo0 + (it & 1) * C::HALO);
-                    const uint32_t wbase = smem_u32(wsm);
-                    const uint32_t acc = tmem + (uint32_t)((it & 1) * TZ * N);
-#pragma unroll 1
-                    for (int p = 0; p < TZ; ++p) {
-                        uint32_t accumulate = 0;
-#pragma unroll 1
-                        for (int tap = 0; tap < 27; ++tap) {
-                            const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
-                            const uint32_t vox = (uint32_t)(((p + dz) * HY + dy) * HX + dx);
+    if (warp == EPI_WARPS) {
+        if (lane == 0) {
+            // ---- producer: loads and MMAs ----
+            // K-major operands without swizzle: LBO = stride of the core
+            // matrices along K, SBO = stride of the 8-row groups along M (N)
+            const uint32_t idesc = (1u << 4)                 // D: FP32
+                                   | (1u << 7) | (1u << 10)  // A, B: BF16
+                                   | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+            const uint64_t b0 = make_desc(smem_u32(wsm), (N / 8) * 128, 128);
+            int loads = 0, mmas = 0; // issued
+            auto load = [&](int it) {
+                int x0, y0, z0, f;
+                tile_xyzf(it, x0, y0, z0, f);
+                const int q = it % STAGES;
+                mbar_expect_tx(full0 + 8 * q, C::NCG * C::BOX_BYTES);
+                const uint32_t dst = smem_u32(halo0 + q * C::HALO);
+                // box {x and 8 channels merged: 80, y: 18, z: TZ + 2, plane: 1}
 #pragma unroll
-                            for (int kc = 0; kc < C::KC; ++kc) {
-                                const uint64_t ad = make_desc(hbase + 2 * kc * PLANE + vox * 16, PLANE, HX * 16);
-                                const uint64_t bd =
-                                    make_desc(wbase + (tap * C::KC + kc) * C::WBLK, (N / 8) * 128, 128);
-                                umma_bf16(acc + p * N, ad, bd, idesc, accumulate);
-                                accumulate = 1;
-                            }
-                        }
+                for (int g = 0; g < C::NCG; ++g)
+                    tma_load_4d(dst + g * PLANE, &tmap, full0 + 8 * q, 8 * (x0 - 1), y0 - 1, z0 - 1,
+                                f * C::NCG + g);
+                loads = it + 1;
+            };
+            bool ok = true;
+            for (int it = 0; it < STAGES - 1 && it < my_n; ++it)
+                load(it);
+            for (int it = 0; it < my_n && ok; ++it) {
+                const int q = it % STAGES, b = it & 1;
+                const int nxt = it + STAGES - 1;
+                if (nxt < my_n) {
+                    // its halo stage was read by the MMAs of tile it-1
+                    if (it >= 1 && !mbar_wait(done0 + 8 * ((it - 1) & 1), ((it - 1) >> 1) & 1)) {
+                        ok = false;
+                        break;
                     }
-                    umma_commit(smem_u32(bars + 2 + (it & 1)));
-                    issued_mma = it + 1;
+                    load(nxt);
                 }
+                // this tile's loads, and its accumulator buffer read out (tile it-2)
+                if (!mbar_wait(full0 + 8 * q, (it / STAGES) & 1) ||
+                    (it >= 2 && !mbar_wait(free0 + 8 * b, ((it - 2) >> 1) & 1))) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                // descriptors differ only in their start address (the low 14
+                // bits, in 16-byte units): one base each, plus constants
+                const uint64_t a0 = make_desc(smem_u32(halo0 + q * C::HALO), PLANE, HX * 16);
+                const uint32_t acc = tmem + (uint32_t)(b * TZ * N);
+#pragma unroll
+                for (int p = 0; p < TZ; ++p) {
+#pragma unroll
+                    for (int tap = 0; tap < 27; ++tap) {
+                        const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+                        const uint32_t vox = (uint32_t)(((p + dz) * HY + dy) * HX + dx);
+#pragma unroll
+                        for (int kc = 0; kc < C::KC; ++kc)
+                            umma_bf16(acc + p * N, a0 + ((2 * kc * PLANE + vox * 16) >> 4),
+                                      b0 + (((tap * C::KC + kc) * C::WBLK) >> 4), idesc, tap + kc > 0);
+                    }
+                }
+                umma_commit(done0 + 8 * b);
+                mmas = it + 1;
+            }
+            if (!ok) {
+                *abort_flag = 1;
+                atomicExch(a.err, 1);
+                // the last loads and MMAs of each buffer may still be in
+                // flight (earlier phases of their barriers have completed)
+                for (int t = loads - STAGES; t < loads; ++t)
+                    if (t >= mmas && t >= 0)
+                        mbar_wait(full0 + 8 * (t % STAGES), (t / STAGES) & 1);
+                for (int t = mmas - 2; t < mmas; ++t)
+                    if (t >= 0)
+                        mbar_wait(done0 + 8 * (t & 1), (t >> 1) & 1);
             }
         }
-        __syncwarp();
-        __syncthreads(); // the abort flag as thread 0 left it
-        if (*abort_flag)
-            break;
-        if (it >= 1) {
-            // epilogue of tile it-1: its accumulators -> bias, ReLU, mask -> global.
-            // One lane per warp waits, so that the warp stays converged for
-            // the .sync.aligned tensor-memory loads.
-            const int j = it - 1;
+    } else {
+        // ---- epilogue warps: accumulators -> bias, ReLU, mask -> global ----
+        const int m = warp * 32 + lane;
+        for (int it = 0; it < my_n; ++it) {
+            const int b = it & 1;
+            // one lane waits, so that the warp stays converged for the
+            // .sync.aligned tensor-memory loads
             int ok = 0;
             if (lane == 0)
-                ok = mbar_wait(smem_u32(bars + 2 + (j & 1)), (j >> 1) & 1);
+                ok = mbar_wait(done0 + 8 * b, (it >> 1) & 1);
             ok = __shfl_sync(0xffffffffu, ok, 0);
-            if (!ok) {
+            if (!ok || *(volatile int *)abort_flag) {
                 if (lane == 0)
-                    *abort_flag = 1;
-            } else {
-                tc_fence_after();
-                int x0, y0, z0, f;
-                tile_xyzf(j, x0, y0, z0, f);
-                const int m = warp * 32 + lane;
-                const int ox = x0 + (m & 7), oy = y0 + (m >> 3);
-#pragma unroll 1
-                for (int p = 0; p < TZ; ++p) {
-                    const uint32_t col = tmem + (uint32_t)((j & 1) * TZ * N + p * N) + ((uint32_t)(warp * 32) << 16);
-                    float v[N];
-#pragma unroll
-                    for (int h = 0; h < N / 16; ++h) {
-                        uint32_t r[16];
-                        tmem_ld_x16(col + 16 * h, r);
-                        tmem_ld_wait();
-#pragma unroll
-                        for (int e = 0; e < 16; ++e)
-                            v[16 * h + e] = __uint_as_float(r[e]);
-                    }
-                    const int oz = z0 + p;
-                    if (ox < a.nx && oy < a.ny && oz < a.nz)
-                        epilogue_store<N>(a, v, (((size_t)f * a.nz + oz) * a.ny + oy) * a.nx + ox);
-                }
+                    atomicExch(a.err, 1);
+                break;
             }
+            tc_fence_after();
+            int x0, y0, z0, f;
+            tile_xyzf(it, x0, y0, z0, f);
+            const int ox = x0 + (m & 7), oy = y0 + (m >> 3);
+            const long long vol = (long long)a.nx * a.ny * a.nz;
+#pragma unroll 1
+            for (int p = 0; p < TZ; ++p) {
+                const uint32_t col = tmem + (uint32_t)(b * TZ * N + p * N) + ((uint32_t)(warp * 32) << 16);
+                float v[N];
+#pragma unroll
+                for (int h = 0; h < N / 16; ++h) {
+                    uint32_t r[16];
+                    tmem_ld_x16(col + 16 * h, r);
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int e = 0; e < 16; ++e)
+                        v[16 * h + e] = __uint_as_float(r[e]);
+                }
+                const int oz = z0 + p;
+                if (ox < a.nx && oy < a.ny && oz < a.nz)
+                    epilogue_store<N>(a, v, f, ((long long)oz * a.ny + oy) * a.nx + ox, vol);
+            }
+            // this warp is done with the buffer's tensor memory
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(free0 + 8 * b) : "memory");
         }
-        tc_fence_before();
-        __syncthreads();
-        if (*abort_flag)
-            break;
     }
-    if (*abort_flag) {
-        // wait (bounded) for this CTA's own loads and MMAs in flight before
-        // its shared and tensor memory go away
-        if (tid == 0) {
-            atomicExch(a.err, 1);
-            // the last load and the last MMA batch of each buffer may still be
-            // in flight (earlier phases of its barrier have completed)
-            for (int t = issued_loads - 2; t < issued_loads; ++t)
-                if (t >= 0)
-                    mbar_wait(smem_u32(bars + (t & 1)), (t >> 1) & 1);
-            for (int t = issued_mma - 2; t < issued_mma; ++t)
-                if (t >= 0)
-                    mbar_wait(smem_u32(bars + 2 + (t & 1)), (t >> 1) & 1);
-        }
-        tc_fence_before();
-        __syncthreads();
-    }
+    tc_fence_before();
+    __syncthreads();
     tc_fence_after();
     if (warp == 0)
         tmem_dealloc(tmem, C::TCOLS);
@@ -337,18 +352,19 @@ template <int CIN, int N> void set_attr_once()
 }
 } // namespace
 
-// the 5-D map of [nf][nz][ny][nx][CIN] BF16 with boxes of 8 channels x the halo tile
+// the 4-D map of a planar tensor ([nf * cin/8 planes][nz][ny][nx * 8] BF16,
+// x and the 8 channels of a group merged) with boxes of the halo tile
 static bool make_map(CUtensorMap *m, const void *x, int cin, int nx, int ny, int nz, int nf)
 {
     PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
     if (!enc)
         return false;
-    const cuuint64_t dims[5] = {(cuuint64_t)cin, (cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz, (cuuint64_t)nf};
-    const cuuint64_t row = (cuuint64_t)cin * 2;
-    const cuuint64_t strides[4] = {row, row * nx, row * nx * ny, row * nx * ny * nz};
-    const cuuint32_t box[5] = {8, HX, HY, HZ, 1};
-    const cuuint32_t es[5] = {1, 1, 1, 1, 1};
-    return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(x), dims, strides, box, es,
+    const cuuint64_t dims[4] = {(cuuint64_t)nx * 8, (cuuint64_t)ny, (cuuint64_t)nz, (cuuint64_t)nf * (cin / 8)};
+    const cuuint64_t row = (cuuint64_t)nx * 16; // bytes of one x row of a plane
+    const cuuint64_t strides[3] = {row, row * ny, row * ny * nz};
+    const cuuint32_t box[4] = {HX * 8, HY, HZ, 1};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(x), dims, strides, box, es,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -362,13 +378,13 @@ static cudaError_t launch(const void *x, const TcArgs &a, int sm_count, cudaStre
     set_attr_once<CIN, N>();
     static int per_sm = 0;
     if (!per_sm) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv_tc<CIN, N>, 128, TcCfg<CIN, N>::SMEM);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv_tc<CIN, N>, THREADS, TcCfg<CIN, N>::SMEM);
         per_sm = per_sm < 1 ? 1 : (per_sm > 2 ? 2 : per_sm); // tensor memory: 2 x TCOLS <= 512 columns
     }
     const long long tiles = tc_tiles(a.nx, a.ny, a.nz, a.nf);
     const long long cap = (long long)sm_count * per_sm;
     const int grid = (int)(tiles < cap ? tiles : cap);
-    k_conv_tc<CIN, N><<<grid, 128, TcCfg<CIN, N>::SMEM, st>>>(m, a);
+    k_conv_tc<CIN, N><<<grid, THREADS, TcCfg<CIN, N>::SMEM, st>>>(m, a);
     return cudaGetLastError();
 }
 

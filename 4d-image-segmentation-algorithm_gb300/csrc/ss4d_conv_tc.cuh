@@ -10,9 +10,20 @@
 namespace ss4d {
 namespace tc {
 
+// Activations are stored channel-group planar: a tensor of C channels over
+// F frames of nx*ny*nz voxels is [F][C/8][nz][ny][nx][8] BF16, element
+// (f, c, voxel v of its frame) at ((f * C/8 + c/8) * nx*ny*nz + v) * 8 + c%8:
+// the 8 channels of a group are the 16 bytes of one operand row, and a row
+// of the halo tile (10 voxels) is 160 contiguous bytes for the TMA.
+__host__ __device__ __forceinline__ size_t planar_off(int f, int c, int groups, long long vol, long long v)
+{
+    return (((size_t)f * groups + (c >> 3)) * (size_t)vol + (size_t)v) * 8 + (c & 7);
+}
+
 // output tile: 8 (x) x 16 (y) voxels = one M = 128 accumulator per z plane,
 // TZ planes per tile; its input halo tile is HX x HY x HZ voxels
 constexpr int TX = 8, TY = 16, TZ = 2;
+constexpr int STAGES = 3; // halo tiles in flight
 constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2;
 constexpr int HV = HX * HY * HZ;
 // one 8-channel group of the halo tile, 16 bytes per voxel, each group on a
@@ -27,7 +38,7 @@ template <int CIN, int N> struct TcCfg {
     static constexpr int WBLK = N * 32;                      // one (tap, kc) B operand: 2 K groups x N rows x 16 B
     static constexpr int WBYTES = 27 * KC * WBLK;
     static constexpr int HALO = NCG * PLANE;                 // one halo buffer
-    static constexpr int SMEM = 1024 + 2 * HALO + WBYTES + 64;
+    static constexpr int SMEM = 1024 + STAGES * HALO + WBYTES + 128; // + mbarriers, the TMEM address, a flag
     static constexpr int TCOLS = 2 * TZ * N < 32 ? 32 : 2 * TZ * N; // two accumulator buffers (a power of two here)
     static_assert((TCOLS & (TCOLS - 1)) == 0, "tensor memory is allocated in powers of two columns");
     static_assert(SMEM <= 227 * 1024, "shared memory per CTA");
@@ -36,8 +47,8 @@ template <int CIN, int N> struct TcCfg {
 struct TcArgs {
     const __nv_bfloat16 *w;    // B blocks of the layer (pack_tc)
     const float *bias;         // [cout] or null
-    const __nv_bfloat16 *mask; // [voxel][mstride]: keep channel c where mask > 0 (or null)
-    __nv_bfloat16 *y;          // [voxel][ystride] BF16 output, or null
+    const __nv_bfloat16 *mask; // planar, mstride channels: keep channel c where mask > 0 (or null)
+    __nv_bfloat16 *y;          // planar, ystride channels: BF16 output, or null
     float *yf;                 // [voxel] channel 0 in FP32, or null
     int nx, ny, nz, nf;
     int cout;                  // real output channels; channels cout .. ystride-1 are written as zero
@@ -59,9 +70,10 @@ __host__ __device__ __forceinline__ uint64_t make_desc(uint32_t addr, uint32_t l
            ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
 }
 
-// one voxel's N accumulated channels -> bias, ReLU, mask -> global
+// one voxel's N accumulated channels -> bias, ReLU, mask -> global; voxel vf
+// of frame f, vol voxels per frame
 template <int N>
-__device__ __forceinline__ void epilogue_store(const TcArgs &a, float (&v)[N], size_t vox)
+__device__ __forceinline__ void epilogue_store(const TcArgs &a, float (&v)[N], int f, long long vf, long long vol)
 {
 #pragma unroll
     for (int c = 0; c < N; ++c) {
@@ -73,20 +85,23 @@ __device__ __forceinline__ void epilogue_store(const TcArgs &a, float (&v)[N], s
         v[c] = x;
     }
     if (a.mask) {
-        const __nv_bfloat162 *mk = reinterpret_cast<const __nv_bfloat162 *>(a.mask + vox * a.mstride);
 #pragma unroll
-        for (int c = 0; c < N; c += 2) {
+        for (int c = 0; c < N; c += 8) {
             if (c >= a.mstride)
                 break;
-            const __nv_bfloat162 m2 = mk[c / 2];
-            if (!(__low2float(m2) > 0.f))
-                v[c] = 0.f;
-            if (!(__high2float(m2) > 0.f))
-                v[c + 1] = 0.f;
+            const uint4 q = *reinterpret_cast<const uint4 *>(a.mask + planar_off(f, c, a.mstride / 8, vol, vf));
+            const __nv_bfloat162 *m2 = reinterpret_cast<const __nv_bfloat162 *>(&q);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                if (!(__low2float(m2[e]) > 0.f))
+                    v[c + 2 * e] = 0.f;
+                if (!(__high2float(m2[e]) > 0.f))
+                    v[c + 2 * e + 1] = 0.f;
+            }
         }
     }
     if (a.y) {
-        uint4 *dst = reinterpret_cast<uint4 *>(a.y + vox * a.ystride);
+        const int G = a.ystride / 8;
 #pragma unroll
         for (int c = 0; c < N; c += 8) {
             if (c >= a.ystride)
@@ -98,17 +113,18 @@ __device__ __forceinline__ void epilogue_store(const TcArgs &a, float (&v)[N], s
             q.y = *reinterpret_cast<uint32_t *>(&b1);
             q.z = *reinterpret_cast<uint32_t *>(&b2);
             q.w = *reinterpret_cast<uint32_t *>(&b3);
-            dst[c / 8] = q;
+            *reinterpret_cast<uint4 *>(a.y + planar_off(f, c, G, vol, vf)) = q;
         }
         for (int c = N; c < a.ystride; c += 8) // channels beyond N: zero
-            dst[c / 8] = make_uint4(0, 0, 0, 0);
+            *reinterpret_cast<uint4 *>(a.y + planar_off(f, c, G, vol, vf)) = make_uint4(0, 0, 0, 0);
     }
     if (a.yf)
-        a.yf[vox] = v[0];
+        a.yf[(size_t)f * vol + vf] = v[0];
 }
 
 // launch one convolution (cin 16 or 32 input channels, N 32 or 16 computed
-// output channels) on x [nf][nz][ny][nx][cin] BF16; sm_count CTAs at most
+// output channels) on x (planar, cin channels, nf frames) BF16; persistent
+// CTAs, as many as fit on sm_count SMs
 cudaError_t conv_tc(int cin, int n, const void *x, const TcArgs &a, int sm_count, cudaStream_t st);
 // weights W[27][cout][cin] FP32 -> the B blocks of a (cinp, n) convolution;
 // reverse: the data-gradient weights (taps reversed, channel roles swapped)

@@ -2,8 +2,8 @@
 // (BF16 weights and activations, FP32 accumulation) with its forward, its
 // gradients and its optimiser, as hand-written kernels.
 //
-// Tensors are channels-last: [F][nz][ny][nx][C] with C = 16 or 32 BF16
-// channels (16 input features; 24 hidden channels, the rest zero).  Every
+// Tensors are channel-group planar: [F][C/8][nz][ny][nx][8] with C = 16 or
+// 32 BF16 channels (16 input features; 24 hidden channels, the rest zero).  Every
 // convolution, forward and data gradient, runs on the tcgen05 tensor cores
 // (ss4d_conv_tc.cu): an implicit GEMM per frame, M = voxels, N = output
 // channels, K = 27 taps x input channels.  The data gradient of a layer is
@@ -26,8 +26,8 @@ constexpr int TV = TX * TY * TZ; // 256 output voxels per tile
 constexpr int HV = HX * HY * HZ; // 600 input voxels per tile
 
 // dW[tap][co][ci] and db[co] summed over the voxels of each block's tiles
-// (FP32); X: [F][..][CIN] (the layer input), dY: [F][..][YS] with COUT used
-// channels.  Each block writes its partial sums; k_reduce_cols adds them in
+// (FP32); X: planar, CIN channels (the layer input), dY: planar, YS channels
+// of which COUT are used.  Each block writes its partial sums; k_reduce_cols adds them in
 // block order.
 __host__ __device__ constexpr int wgrad_smem_bytes(int cin, int cout)
 {
@@ -67,7 +67,8 @@ __global__ void __launch_bounds__(256) k_wgrad(const __nv_bfloat16 *__restrict__
             const int gx = tx0 + v % HX - 1, gy = ty0 + (v / HX) % HY - 1, gz = tz0 + v / (HX * HY) - 1;
             float val = 0.f;
             if (gx >= 0 && gx < nx && gy >= 0 && gy < ny && gz >= 0 && gz < nz)
-                val = __bfloat162float(x[((((size_t)f * nz + gz) * ny + gy) * nx + gx) * CIN + c]);
+                val = __bfloat162float(
+                    x[tc::planar_off(f, c, CIN / 8, (long long)nx * ny * nz, ((long long)gz * ny + gy) * nx + gx)]);
             sx[q] = val;
         }
         for (int q = tid; q < TV * COUT; q += blockDim.x) {
@@ -75,7 +76,8 @@ __global__ void __launch_bounds__(256) k_wgrad(const __nv_bfloat16 *__restrict__
             const int ox = tx0 + m % TX, oy = ty0 + (m / TX) % TY, oz = tz0 + m / (TX * TY);
             float val = 0.f;
             if (ox < nx && oy < ny && oz < nz)
-                val = __bfloat162float(dy[((((size_t)f * nz + oz) * ny + oy) * nx + ox) * YS + c]);
+                val = __bfloat162float(
+                    dy[tc::planar_off(f, c, YS / 8, (long long)nx * ny * nz, ((long long)oz * ny + oy) * nx + ox)]);
             sd[q] = val;
         }
         __syncthreads();
@@ -124,7 +126,7 @@ __global__ void k_reduce_cols(const float *__restrict__ in, int rows, int cols, 
 }
 
 // squared error over the voxels at least `margin` from the crop border;
-// dy (channel 0 of 16) = d(mean squared error)/d out
+// dy (channel 0 of 16, planar) = d(mean squared error)/d out
 __global__ void k_mse(const float *__restrict__ out, const float *__restrict__ target, int nx, int ny, int nz, int nf,
                       int margin, float inv_count, __nv_bfloat16 *dy, float *partial)
 {
@@ -145,11 +147,16 @@ __global__ void k_mse(const float *__restrict__ out, const float *__restrict__ t
             acc += d * d;
             g = 2.f * d * inv_count;
         }
-        __nv_bfloat162 *row = reinterpret_cast<__nv_bfloat162 *>(dy + v * 16);
-        row[0] = __floats2bfloat162_rn(g, 0.f);
+        const long long vol = (long long)nx * ny * nz, f = v / vol, vf = v - f * vol;
+        __nv_bfloat162 *g0 = reinterpret_cast<__nv_bfloat162 *>(dy + tc::planar_off((int)f, 0, 2, vol, vf));
+        __nv_bfloat162 *g1 = reinterpret_cast<__nv_bfloat162 *>(dy + tc::planar_off((int)f, 8, 2, vol, vf));
+        g0[0] = __floats2bfloat162_rn(g, 0.f);
 #pragma unroll
-        for (int c = 1; c < 8; ++c)
-            row[c] = __floats2bfloat162_rn(0.f, 0.f);
+        for (int c = 1; c < 4; ++c)
+            g0[c] = __floats2bfloat162_rn(0.f, 0.f);
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            g1[c] = __floats2bfloat162_rn(0.f, 0.f);
     }
     acc = block_sum(acc);
     if (threadIdx.x == 0)
@@ -486,7 +493,7 @@ static void conv(ss4d_wsnet *n, int cin, int nout, int cout, const __nv_bfloat16
         n->launch_failed = 1;
 }
 
-// forward over F frames of extents nx, ny, nz; x0 [F][nz][ny][nx][16] BF16.
+// forward over F frames of extents nx, ny, nz; x0 planar [F][2][nz][ny][nx][8] BF16.
 // With train, a[0..2] keep the three hidden activations for the backward.
 static ss4d_status forward(ss4d_wsnet *n, const __nv_bfloat16 *x0, int nx, int ny, int nz, int nf, bool train,
                            float *out)
@@ -536,7 +543,7 @@ static ss4d_status wgrad(ss4d_wsnet *n, const __nv_bfloat16 *x, const __nv_bfloa
     return SS4D_OK;
 }
 
-// one Adam step on crops: x0 [F][nz][ny][nx][16] BF16 features, target
+// one Adam step on crops: x0 planar [F][2][nz][ny][nx][8] BF16 features, target
 // [F][nz][ny][nx] FP32; the loss is the mean squared error over voxels at
 // least `margin` from the crop borders.  d_grad (nparam floats, may be NULL)
 // receives the gradient; lr == 0 computes loss and gradient without updating.

@@ -11,6 +11,7 @@
 //                14 u^n             15 I0 (the presmoothed image)
 //              with s = sqrt(R_first / (N h^4)) the RMS of r0 and c a_f, diag the
 //              step's own FP64 coefficient records;
+//              stored channel-group planar, [nt][2][nz][ny][nx][8]
 //   (the network maps them to d/s, ss4d_nn.cu)
 //   apply:     the red and black corrections d = s * prediction;
 //   check:     sum over both colours of (r0 - A32 d)^2 h^4, the correction
@@ -20,6 +21,7 @@
 //              the round starts from zero, as without the network.
 #include <cuda_bf16.h>
 
+#include "ss4d_conv_tc.cuh"
 #include "ss4d_sweep.cuh"
 
 namespace ss4d {
@@ -70,10 +72,11 @@ __global__ void __launch_bounds__(256) k_ws_features(Geo g, Split sp, SplitBufs 
 #pragma unroll
     for (int c = 0; c < 8; ++c)
         v[c] = __floats2bfloat162_rn(ch[2 * c], ch[2 * c + 1]);
-    const size_t vox = (((size_t)(l - 1) * g.nz + (k - 1)) * g.ny + (j - 1)) * g.nx + (i - 1);
-    uint4 *dst = reinterpret_cast<uint4 *>(x0 + vox * 16);
-    dst[0] = *reinterpret_cast<uint4 *>(&v[0]);
-    dst[1] = *reinterpret_cast<uint4 *>(&v[4]);
+    // planar: channels 0-7 and 8-15 in the frame's two planes
+    const long long vol = (long long)g.nx * g.ny * g.nz;
+    const long long vf = ((long long)(k - 1) * g.ny + (j - 1)) * g.nx + (i - 1);
+    *reinterpret_cast<uint4 *>(x0 + tc::planar_off(l - 1, 0, 2, vol, vf)) = *reinterpret_cast<uint4 *>(&v[0]);
+    *reinterpret_cast<uint4 *>(x0 + tc::planar_off(l - 1, 8, 2, vol, vf)) = *reinterpret_cast<uint4 *>(&v[4]);
 }
 
 __global__ void __launch_bounds__(256) k_ws_apply(Geo g, Split sp, SplitBufs b, const float *__restrict__ y,

@@ -258,6 +258,7 @@ def lib() -> C.CDLL:
         "ss4d_solver_set_warm_start": ([vp, vp, vp], st),
         "ss4d_solver_set_extrapolation": ([vp, C.c_int], st),
         "ss4d_solver_set_inner_omega": ([vp, C.c_double], st),
+        "ss4d_solver_set_warm_start_gate": ([vp, C.c_int], st),
         "ss4d_slab_partition": ([C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)], st),
         "ss4d_slab_sor_loop": ([C.POINTER(SlabOps), C.POINTER(SlabComm), C.POINTER(Params), C.c_longlong,
                                 C.POINTER(StepStats)], st),
@@ -529,12 +530,16 @@ class Solver:
         return st.as_dict()
 
     def ws_features(self, p: Params, u, g8, i0, x0) -> float:
-        """Warm-start features of the step from u (BF16 [nt][nz][ny][nx][16]
+        """Warm-start features of the step from u (BF16, planar [nt][2][nz][ny][nx][8]
         into x0); returns the RMS s of the step's initial residual."""
         sig = C.c_double(0)
         _check(self.L.ss4d_ws_features(self.h, C.byref(p), _ptr(u), _p8(g8), _ptr(i0), _ptr(x0), C.byref(sig)),
                "ws_features")
         return sig.value
+
+    def set_warm_start_gate(self, min_iterations: int):
+        """run the network only after a mixed step of >= min_iterations FP32 sweeps (0: always)"""
+        _check(self.L.ss4d_solver_set_warm_start_gate(self.h, int(min_iterations)), "set_warm_start_gate")
 
     def slab_sor_solve(self, p: Params, u, prev, coef8, comm: SlabComm, nint_global: int) -> dict:
         """ss4d_slab_sor_solve: this handle's volume is one slab of a volume
@@ -703,12 +708,29 @@ class Batch:
         return [s.as_dict() for s in S]
 
 
+def features_to_planar(x):
+    """[F][nz][ny][nx][C] -> the network's channel-group planar layout
+    [F][C/8][nz][ny][nx][8] (torch tensor or numpy array; a contiguous copy)"""
+    F, nz, ny, nx, C = x.shape
+    y = x.reshape(F, nz, ny, nx, C // 8, 8)
+    y = y.permute(0, 4, 1, 2, 3, 5) if hasattr(y, "permute") else y.transpose(0, 4, 1, 2, 3, 5)
+    return y.contiguous() if hasattr(y, "contiguous") else y.copy()
+
+
+def features_from_planar(x):
+    """[F][G][nz][ny][nx][8] -> [F][nz][ny][nx][8 G]"""
+    F, G, nz, ny, nx, e = x.shape
+    y = x.permute(0, 2, 3, 4, 1, 5) if hasattr(x, "permute") else x.transpose(0, 2, 3, 4, 1, 5)
+    return y.reshape(F, nz, ny, nx, G * e)
+
+
 class Wsnet:
     """ss4d_wsnet: the learned warm start's convolutional network (BF16
     weights/activations, FP32 master parameters and Adam state on the device).
     Parameter vector layout: per layer L = 0..3, weights [27][cout][cin]
     (tap = 9 dz + 3 dy + dx, offsets -1..1, x fastest) then bias [cout];
-    channels 16 -> 24 -> 24 -> 24 -> 1."""
+    channels 16 -> 24 -> 24 -> 24 -> 1.  Features are channel-group planar,
+    [F][2][nz][ny][nx][8] BF16 (features_to_planar)."""
 
     LAYERS = ((16, 24), (24, 24), (24, 24), (24, 1))
 

@@ -48,13 +48,15 @@ def prepare_scene(torch, kind, dims, seed, p):
 
 
 def make_dataset(torch, scenes, dims, steps, crops_per_step, crop, gs_tol, rng, log=print):
-    """Crops of features [N, cz, cy, cx, 16] (BF16) and targets [N, cz, cy, cx]."""
+    """Crops of features [N, 2, cz, cy, cx, 8] (BF16, the network's planar
+    layout: a crop is one frame of the training batch) and targets
+    [N, cz, cy, cx]."""
     nx, ny, nz, nt = dims
     cx, cy, cz = crop
     n = len(scenes) * steps * crops_per_step
-    X = torch.empty((n, cz, cy, cx, 16), dtype=torch.bfloat16, device="cuda")
+    X = torch.empty((n, 2, cz, cy, cx, 8), dtype=torch.bfloat16, device="cuda")
     T = torch.empty((n, cz, cy, cx), dtype=torch.float32, device="cuda")
-    x0 = torch.empty((nt, nz, ny, nx, 16), dtype=torch.bfloat16, device="cuda")
+    x0 = torch.empty((nt, 2, nz, ny, nx, 8), dtype=torch.bfloat16, device="cuda")
     q = 0
     for kind, seed in scenes:
         p = ss4d.scene_params(gsTol=gs_tol)
@@ -73,7 +75,7 @@ def make_dataset(torch, scenes, dims, steps, crops_per_step, crop, gs_tol, rng, 
                     z0 = int(rng.integers(nz - cz + 1))
                     y0 = int(rng.integers(ny - cy + 1))
                     xs = int(rng.integers(nx - cx + 1))
-                    X[q] = x0[f, z0:z0 + cz, y0:y0 + cy, xs:xs + cx]
+                    X[q] = x0[f, :, z0:z0 + cz, y0:y0 + cy, xs:xs + cx]
                     T[q] = d[f, z0:z0 + cz, y0:y0 + cy, xs:xs + cx]
                     q += 1
         log(f"scene kind {kind} seed {seed}: iterations/step {its}")
@@ -85,7 +87,7 @@ def train(torch, net, X, T, iters, batch, lr, rng, val_frac=0.1, log=print):
     perm = rng.permutation(n)
     nval = max(1, int(n * val_frac))
     val, tr = perm[:nval], perm[nval:]
-    cz, cy, cx = X.shape[1:4]
+    cz, cy, cx = X.shape[2:5]
     hist = []
 
     def val_loss():

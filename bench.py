@@ -55,6 +55,7 @@ NAMED_FORM = "learned"
 FORM_LABEL = {"fp64": "plain FP64 sweeps", "mixed": "mixed (FP32 sweeps, FP64 residual/refinement)",
               "extrap": "mixed + cubic extrapolated start (no network)",
               "learned": "mixed + learned warm start (the metric's named form)",
+              "learned_x": "mixed + learned warm start at the extrapolated start (the metric's named form)",
               "extrap_w": "mixed + extrapolated start, FP32 sweeps relaxed by --inner-omega (reported only)"}
 
 
@@ -65,11 +66,16 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--size", type=int, nargs=4, default=[256, 256, 128, 20], metavar=("NX", "NY", "NZ", "NT"))
-    ap.add_argument("--forms", default="fp64,mixed,extrap,learned,extrap_w",
+    ap.add_argument("--forms", default="fp64,mixed,extrap,learned,learned_x,extrap_w",
                     help="fp64: plain FP64 sweeps; mixed: FP32 sweeps + FP64 refinement; extrap: mixed started "
                          "from the cubic extrapolation u^n + 3 d_(n-1) - 3 d_(n-2) + d_(n-3) of the earlier "
                          "changes; learned: mixed started from the warm-start network (weights/wsnet_seg.npy); "
+                         "learned_x: the learned warm start at the extrapolated start (the network predicts the "
+                         "correction the extrapolation leaves), run while it pays (--ws-gate); "
                          "extrap_w: extrap with --inner-omega")
+    ap.add_argument("--ws-gate", type=int, default=0,
+                    help="learned_x: run the network in a step only when the previous step took at least this many "
+                         "FP32 sweeps (0: every step)")
     ap.add_argument("--inner-omega", type=float, default=1.2,
                     help="relaxation factor of the extra form 'extrap_w' (extrap with its FP32 sweeps relaxed by "
                          "this instead of the configured omega 1.8; reported, never the headline)")
@@ -204,14 +210,15 @@ def run_ours(args, rank, world, dist):
 
     forms = [f for f in args.forms.split(",") if f]
     net = None
-    if "learned" in forms:
+    if "learned" in forms or "learned_x" in forms:
         net = ss4d.Wsnet(stream=sh, seed=None)
         net.set_params(np.load(os.path.join(PKG, "weights", "wsnet_seg.npy")))
 
     def use_form(form):
-        S.set_arith("mixed" if form in ("learned", "extrap", "extrap_w") else form)
-        S.set_warm_start(net if form == "learned" else None, i0)
-        S.set_extrapolation(EXTRAP_ORDER if form in ("extrap", "extrap_w") else 0)
+        S.set_arith("mixed" if form in ("learned", "learned_x", "extrap", "extrap_w") else form)
+        S.set_warm_start(net if form in ("learned", "learned_x") else None, i0)
+        S.set_warm_start_gate(args.ws_gate if form == "learned_x" else 0)
+        S.set_extrapolation(EXTRAP_ORDER if form in ("extrap", "extrap_w", "learned_x") else 0)
         S.set_inner_omega(args.inner_omega if form == "extrap_w" else 0.0)
 
     results = {}
@@ -294,7 +301,7 @@ def run_ours(args, rank, world, dist):
     for form in forms:
         use_form(form)
         u = finals[form].clone()
-        if form in ("extrap", "extrap_w"):  # untimed steps rebuild the history
+        if form in ("extrap", "extrap_w", "learned_x"):  # untimed steps rebuild the history
             for _ in range(EXTRAP_ORDER):
                 S.seg_time_step(p, u, None, g)
         S.set_timing(True)
@@ -310,7 +317,7 @@ def run_ours(args, rank, world, dist):
         if form == "mixed":
             ms, n = kt["sweep32"]
             per_unit = BYTES_FP32_ITER
-        elif form in ("learned", "extrap", "extrap_w"):
+        elif form in ("learned", "learned_x", "extrap", "extrap_w"):
             ms, n = kt["sweep32"]
             per_unit = BYTES_FP32_ITER
         else:
@@ -334,7 +341,7 @@ def run_ours(args, rank, world, dist):
 
     # error of the mixed forms against the plain FP64 form after the same steps
     err = {}
-    for form in ("mixed", "extrap", "extrap_w", "learned"):
+    for form in ("mixed", "extrap", "extrap_w", "learned", "learned_x"):
         if "fp64" not in finals or form not in finals:
             continue
         a = finals[form][1:-1, 1:-1, 1:-1, 1:-1]
@@ -821,7 +828,7 @@ def main():
     forms = list(results)
     # headline: the faster of the mixed forms (with and without the learned
     # warm start) among those that converged every step, else plain FP64
-    fast = [f for f in ("mixed", "extrap", "learned") if f in results and results[f]["converged"]]
+    fast = [f for f in ("mixed", "extrap", "learned", "learned_x") if f in results and results[f]["converged"]]
     head = max(fast, key=lambda f: results[f]["steps_per_s"]) if fast else forms[0]
     r = results[head]
     line = {"metric": METRIC, "value": r["steps_per_s"], "unit": "time-steps/s", "n_gpus": world,
@@ -829,7 +836,8 @@ def main():
             "scaling": "weak", "vs_baseline": None,
             "dtype": {"fp64": "f64", "mixed": "f32 sweeps + f64 residual/refinement",
                       "extrap": "f32 sweeps + f64 residual/refinement",
-                      "learned": "f32 sweeps + f64 residual/refinement, bf16 warm-start network"}[head],
+                      "learned": "f32 sweeps + f64 residual/refinement, bf16 warm-start network",
+                      "learned_x": "f32 sweeps + f64 residual/refinement, bf16 warm-start network"}[head],
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "form": head, "form_label": FORM_LABEL.get(head, head),
                        "is_named_form": head == NAMED_FORM, "nx": args.size[0], "ny": args.size[1],
@@ -844,7 +852,7 @@ def main():
                                             if "fp64" in results else None),
                               "steps100_per_s": nf.get("steps100", {}).get("steps_per_s")}
     if "fp64" in results:
-        for f in ("mixed", "extrap", "extrap_w", "learned"):
+        for f in ("mixed", "extrap", "extrap_w", "learned", "learned_x"):
             if f in results:
                 line[f"{f}_over_fp64"] = results[f]["steps_per_s"] / results["fp64"]["steps_per_s"]
         if args.steps100 > 0:
@@ -852,14 +860,15 @@ def main():
                                           results["fp64"]["steps100"]["steps_per_s"] for f in forms}
         line["roofline_fp64"] = roofline("fp64")
         line["error_vs_fp64"] = err
-    for f in ("mixed", "extrap", "learned"):
+    for f in ("mixed", "extrap", "learned", "learned_x"):
         if f in results and f != head:
             line[f"roofline_{f}"] = roofline(f)
     if rank == 0 and world == 1 and not args.no_e2e:
         try:
             # the reference-named layer runs the mixed form without the network
-            line["e2e"] = run_e2e(args, "mixed" if head == "learned" else head, ctx)
-            line["e2e"]["form"] = "mixed" if head == "learned" else head
+            ef = {"learned": "mixed", "learned_x": "extrap"}.get(head, head)
+            line["e2e"] = run_e2e(args, ef, ctx)
+            line["e2e"]["form"] = ef
         except Exception as ex:  # reported, not hidden
             line["e2e"] = {"value": None, "unit": "time-steps/s", "error": repr(ex)}
     if rank == 0 and world == 1 and not args.no_frontend:

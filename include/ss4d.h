@@ -140,10 +140,11 @@ ss4d_status ss4d_solver_set_tiling(ss4d_solver *s, int k_block, int max_grid);
  * + d_{n-3} (lower orders while fewer earlier steps exist), with d_m the
  * change u^{m+1} - u^m of an earlier step on this handle, kept in FP32;
  * 0 (default): off.  The FP64 stop rule is unchanged, so only the iteration
- * count depends on it.  Not applied while a warm-start network is attached;
- * the history is dropped by this call, by ss4d_solver_set_arith and by any
- * other solve on the handle.  No counterpart in the reference (each of its
- * solves starts from u^n). */
+ * count depends on it.  With a warm-start network attached the network
+ * predicts the correction left at the extrapolated start.  The history is
+ * dropped by this call, by ss4d_solver_set_arith and by any other solve on
+ * the handle.  No counterpart in the reference (each of its solves starts
+ * from u^n). */
 ss4d_status ss4d_solver_set_extrapolation(ss4d_solver *s, int order);
 /* Mixed form: relaxation factor of the FP32 sweeps on the correction
  * equation (0, the default: the step's omega_c).  Only the iteration count
@@ -414,8 +415,10 @@ ss4d_status ss4d_batch_seg_time_step(ss4d_batch *b, const ss4d_params *p, double
  * finishes to the unchanged FP64 tolerance.  When the prediction does not
  * lower the correction equation's residual the step starts from zero instead.
  * Training and inference are this library's own kernels.  No counterpart in
- * the reference.  Feature tensors are BF16 [F][nz][ny][nx][16] (interior
- * voxels, F frames); parameters are FP32, per layer weights [27][cout][cin]
+ * the reference.  Feature tensors are BF16 and channel-group planar,
+ * [F][2][nz][ny][nx][8] (interior voxels, F frames; channels 0-7 in the first
+ * plane of a frame, 8-15 in the second), the layout the tensor-core
+ * convolutions load; parameters are FP32, per layer weights [27][cout][cin]
  * (tap = 9 dz + 3 dy + dx) then biases [cout]. */
 typedef struct ss4d_wsnet ss4d_wsnet;
 size_t ss4d_wsnet_param_count(void);
@@ -440,6 +443,12 @@ ss4d_status ss4d_ws_features(ss4d_solver *s, const ss4d_params *p, double *d_u, 
 /* Attach a network (NULL detaches) to a solver; d_i0 is the presmoothed
  * image.  Used by SS4D_ARITH_MIXED segmentation steps. */
 ss4d_status ss4d_solver_set_warm_start(ss4d_solver *s, ss4d_wsnet *n, const double *d_i0);
+/* Run the attached network in a segmentation step only when the handle's
+ * previous mixed step needed at least min_iterations FP32 sweeps (0, the
+ * default: every step).  The network costs about as much as a fixed number
+ * of sweeps; once the extrapolated start leaves fewer than that to save,
+ * the gate keeps it idle.  The first step after attaching always runs it. */
+ss4d_status ss4d_solver_set_warm_start_gate(ss4d_solver *s, int min_iterations);
 
 /* ---- one volume split across ranks by frames (t-slabs) ----------------
  * The reference's MPI program (segmentation4D_mpi.c) splits the frames of one

@@ -22,9 +22,12 @@ def host(t):
 
 
 def random_features(torch, rng, nf, nz, ny, nx):
+    """device features in the network's planar layout, and the same values
+    channels-last on the host for the reference"""
+    import ss4d
     x = rng.standard_normal((nf, nz, ny, nx, 16)).astype(np.float32)
-    xd = torch.from_numpy(x).to(torch.bfloat16).to("cuda")
-    return xd, host(xd.float())
+    xb = torch.from_numpy(x).to(torch.bfloat16)
+    return ss4d.features_to_planar(xb).to("cuda"), host(xb.float())
 
 
 def l2rel(a, b):
@@ -150,14 +153,14 @@ def test_features_match_oracle(ss4d, oracle, cuda):
     want[..., 14] = u0h[inner]
     want[..., 15] = i0h[inner]
 
-    x0 = torch.zeros((nt, nz, ny, nx, 16), dtype=torch.bfloat16, device="cuda")
+    x0 = torch.zeros((nt, 2, nz, ny, nx, 8), dtype=torch.bfloat16, device="cuda")  # planar
     u = dev(torch, u0h)
     with ss4d.Solver.for_interior(*dims, arith="mixed") as S:
         sigma = S.ws_features(p, u, [dev(torch, a) for a in g], dev(torch, i0h), x0)
     torch.cuda.synchronize()
     assert np.array_equal(host(u), u0h)  # features leave u alone
     assert abs(sigma - sigma_want) <= 1e-12 * sigma_want
-    x = host(x0.float())
+    x = host(ss4d.features_from_planar(x0).float())
     assert not x[0, ..., 1].any() and not x[-1, ..., 2].any()  # frames outside 1..nt
     # BF16 storage: at most one unit in the last place (2^-8 relative) apart
     for ch in range(16):

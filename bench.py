@@ -47,6 +47,7 @@ BYTES_FP32_ITER = 44.0  # the same arrays in FP32
 # 128x128x64x8 (4,194,304 targets)
 EXTRAP_ORDER = 3  # the extrap form's order (ss4d_solver_set_extrapolation)
 TRAFFIC_PER_TARGET = {"k_sweep32": 51.6, "k_sweep64": 118.6}
+FP64_INSTR_PER_TARGET = 11.4  # k_sweep64, ncu at 128x128x64x8
 TRAFFIC_SOURCE = {"k_sweep32": "ncu capture of two launches at 256x256x128x20",
                   "k_sweep64": "ncu capture of one launch at 128x128x64x8"}
 # the form the metric names: FP32 sweeps with FP64 refinement started from
@@ -85,9 +86,11 @@ def parse_args():
                     help="skip the timing of the work around the time loop (thresholding, edge detector, ...)")
     ap.add_argument("--no-graph", action="store_true",
                     help="run the sweep loop host-driven instead of as one CUDA graph (same kernels)")
-    ap.add_argument("--workload", choices=["single", "batch"], default="single",
+    ap.add_argument("--workload", choices=["single", "batch", "conv"], default="single",
                     help="batch: 16 uneven volumes in one persistent launch per half-sweep (reports "
-                         "voxel-updates/s; not the headline metric)")
+                         "voxel-updates/s; not the headline metric); conv: the warm-start network's forward "
+                         "(four tensor-core convolutions) on random features of --size (reports TFLOP/s; for "
+                         "profiling)")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--steps100", type=int, default=100,
                     help="every form also runs on from the timed window to this many time steps from u0 (the "
@@ -164,6 +167,29 @@ class Clocks:
 
 # --------------------------------------------------------------------------
 # our arm
+
+def fp64_peak_flops(device) -> float | None:
+    """FP64 FLOP/s of a cuBLAS DGEMM (4096^3, best of 3) on this GPU: the
+    measured ceiling of the FP64 pipe, beside the copy bandwidth"""
+    try:
+        import torch
+        a = torch.randn((4096, 4096), dtype=torch.float64, device=device)
+        b = torch.randn_like(a)
+        torch.matmul(a, b)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        best = None
+        for _ in range(3):
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            torch.cuda.synchronize(device)
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        del a, b
+        return 2.0 * 4096 ** 3 / (best / 1e3)
+    except Exception:
+        return None
+
 
 def slowest_rank_ms(ms: float, dist, device) -> float:
     """The timed region's duration of the slowest rank (ranks = independent
@@ -311,6 +337,7 @@ def run_ours(args, rank, world, dist):
         S.set_timing(False)
         roof[form] = kt
     hbm, how = peaks()
+    fp64_peak = fp64_peak_flops(dev)
 
     def roofline(form):
         kt = roof[form]
@@ -330,6 +357,16 @@ def run_ours(args, rank, world, dist):
         ach = per_launch / (avg / 1e3) / 1e9
         tot = sum(v[0] for v in kt.values())
         kern = "k_sweep64" if form == "fp64" else "k_sweep32"
+        fp64 = None
+        if kern == "k_sweep64" and fp64_peak:
+            # the FP64 pipe: instructions per target from ncu against the
+            # DGEMM rate (one fused multiply-add = two flops)
+            rate = FP64_INSTR_PER_TARGET * (n_int / 2.0) / (avg / 1e3)
+            fp64 = {"instr_per_target": FP64_INSTR_PER_TARGET, "achieved_instr_per_s": rate,
+                    "peak_fma_per_s": fp64_peak / 2.0, "frac": rate / (fp64_peak / 2.0),
+                    "peak_source": "torch float64 matmul 4096^3 on this GPU (cuBLAS DGEMM), best of 3",
+                    "instr_source": "ncu smsp FP64 instructions of one launch at 128x128x64x8 / targets: 8 stencil "
+                                    "FMAs, 2 for the update, 1 for the residual, 0.4 for the black residual scale"}
         return {"bound": "hbm", "kernel": kern, "achieved": ach,
                 "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "peak_source": how,
                 "traffic": TRAFFIC_PER_TARGET[kern] * (n_int / 2.0),
@@ -337,7 +374,7 @@ def run_ours(args, rank, world, dist):
                                   f"launch",
                 "avg_launch_ms": avg, "launches": n, "bytes_per_launch": per_launch,
                 "share_of_step_kernel_time": (ms / tot) if tot else None,
-                "kernel_ms": {k: v[0] for k, v in kt.items()}}
+                "kernel_ms": {k: v[0] for k, v in kt.items()}, "fp64_pipe": fp64}
 
     # error of the mixed forms against the plain FP64 form after the same steps
     err = {}
@@ -805,12 +842,47 @@ def run_batch(args):
     print(json.dumps(line))
 
 
+def run_conv(args):
+    """The warm-start network's forward on random BF16 features of --size
+    (nx ny nz frames): W untimed calls, then K timed with CUDA events; FLOP
+    counted at the network's real widths (16 -> 24 -> 24 -> 24 -> 1)."""
+    import numpy as np
+    import torch
+
+    import ss4d
+
+    nx, ny, nz, nf = args.size
+    net = ss4d.Wsnet(seed=3)
+    x = torch.randn((nf, 2, nz, ny, nx, 8), device="cuda").to(torch.bfloat16)
+    out = torch.empty((nf, nz, ny, nx), device="cuda", dtype=torch.float32)
+    for _ in range(args.warmup):
+        net.forward(x, nx, ny, nz, nf, out)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        net.forward(x, nx, ny, nz, nf, out)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    vox = nx * ny * nz * nf
+    flop = vox * 2 * 27 * (16 * 24 + 24 * 24 + 24 * 24 + 24)
+    net.close()
+    print(json.dumps({"metric": "warm-start network forward", "value": flop / (ms / 1e3) / 1e12, "unit": "TFLOP/s",
+                      "ms_per_forward": ms, "ns_per_voxel": ms / vox * 1e6, "finite": bool(torch.isfinite(out).all()),
+                      "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                      "config": {"workload": f"random features {nx}x{ny}x{nz}x{nf}", "flop_per_voxel": flop // vox}}))
+
+
 def main():
     args = parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if args.workload == "batch":
         run_batch(args)
+        return
+    if args.workload == "conv":
+        run_conv(args)
         return
     if args.impl == "reference":
         line = run_reference(args)

@@ -1887,7 +1887,8 @@ ss4d_status ss4d::solver_set_shape(ss4d_solver *s, int xt, int kb)
     return SS4D_OK;
 }
 
-ss4d_status ss4d::solver_prepare_step(ss4d_solver *s, const ss4d_params *p, double *d_u, const double *const d_g[8])
+ss4d_status ss4d::solver_prepare_step(ss4d_solver *s, const ss4d_params *p, double *d_u, const double *const d_g[8],
+                                      int *pre_out)
 {
     REQ(s && d_u && d_g, "NULL argument");
     CKS(check_params(p));
@@ -1898,7 +1899,10 @@ ss4d_status ss4d::solver_prepare_step(ss4d_solver *s, const ss4d_params *p, doub
     }
     const int mixed = s->arith == SS4D_ARITH_MIXED;
     CKS(ensure_split(s, mixed));
-    timed(s, SS4D_K_ASSEMBLE, true, [&] { assemble(s, p, d_u, gi, 1, mixed, 1); });
+    const int pre = pre_out ? pre_form(s, mixed) : 0;
+    if (pre_out)
+        *pre_out = pre;
+    timed(s, SS4D_K_ASSEMBLE, true, [&] { assemble(s, p, d_u, gi, 1, mixed, 1, pre); });
     CKS(last_launch());
     if (!packed_by_assembly(mixed)) {
         timed(s, SS4D_K_PACK, true, [&] { launch_pack(s->geo, s->sp, d_u, d_u, s->sb, s->stream); });

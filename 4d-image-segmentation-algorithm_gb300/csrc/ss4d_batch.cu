@@ -2,15 +2,19 @@
 // per-volume parameters) in the plain FP64 form or the mixed form.
 //
 // Each volume owns a solver handle for its buffers, its coefficient assembly
-// and its pack/unpack (ss4d_api.cu), extrapolated start included.  What is
-// batched is the SOR loop: one persistent launch per loop kernel walks the
+// (which in the mixed form also forms the step's first refinement pass) and
+// its pack/unpack (ss4d_api.cu), extrapolated start included.  What is
+// batched is the SOR loop: every phase of a loop body walks the
 // concatenated tile lists of all volumes (volume v owns tiles [tile0_v,
 // tile0_{v+1})), every tile with its volume's own tile shape; a tile whose
 // volume has stopped, or (mixed form) is in another phase of its loop, is
 // skipped.  Residual partial sums are kept per (volume, block) in a fixed
-// order, and one controller kernel runs every volume's stopping test (the
-// single-volume state machines of ss4d_sweep.cuh) and keeps the graph's
-// while loop going while any volume is active.
+// order, and one controller runs every volume's stopping test (the
+// single-volume state machines of ss4d_sweep.cuh).  By default the whole
+// loop is one persistent launch (k_bsolve: a co-resident grid, its phases
+// separated by a bounded grid barrier, the controller in block 0);
+// otherwise each phase is a kernel of a CUDA graph's while loop, which the
+// controller keeps going while any volume is active.
 #include <cuda_runtime.h>
 
 #include <math.h>
@@ -158,10 +162,9 @@ struct VolumeSums {
 // Its own loop rather than walk_targets: the walker form of this kernel
 // measured 8 % slower on the 16-volume workload (A/B on one box).
 template <int COL>
-__global__ void __launch_bounds__(256) k_bsweep64(const BVol *__restrict__ vols, int nv, long long total,
-                                                  const LoopState *__restrict__ st, double *partial)
+__device__ __forceinline__ void bsweep64(const BVol *__restrict__ vols, int nv, long long total,
+                                         const LoopState *__restrict__ st, double *partial, double (*wacc)[BMAX])
 {
-    __shared__ double wacc[BWARPS][BMAX];
     VolumeSums sums{wacc};
     sums.clear();
     int v = 0;
@@ -212,25 +215,42 @@ __global__ void __launch_bounds__(256) k_bsweep64(const BVol *__restrict__ vols,
     sums.write(nv, partial, [&](int q) { return !st[q].stop; });
 }
 
+template <int COL>
+__global__ void __launch_bounds__(256) k_bsweep64(const BVol *__restrict__ vols, int nv, long long total,
+                                                  const LoopState *__restrict__ st, double *partial)
+{
+    __shared__ double wacc[BWARPS][BMAX];
+    bsweep64<COL>(vols, nv, total, st, partial, wacc);
+}
+
 // ---- mixed form (the single-volume kernels k_apply_black, k_refine,
 // k_zero_delta, k_sweep32 of ss4d_kernels_fast.cu, per volume in its mode)
 
-__global__ void __launch_bounds__(256) k_bapply_black(const BVol *__restrict__ vols, int nv, long long total,
-                                                      const LoopState *__restrict__ st)
+// (not when the assembly formed the pass: its first-difference kernel added
+// the correction, LoopState.pre)
+__device__ __forceinline__ void bapply_black(const BVol *__restrict__ vols, int nv, long long total,
+                                             const LoopState *__restrict__ st)
 {
     walk_targets<1>(
-        vols, nv, total, [&](int v) { return st[v].mode == 0 && !st[v].stop; },
+        vols, nv, total, [&](int v) { return st[v].mode == 0 && !st[v].stop && !st[v].pre; },
         [&](int, const BVol &V, const Geo &, const Split &, const TileCoord &, int, long long s) {
             V.b.Bk[s] += f2d_bits(V.b.dB[s]);
         },
         [](int) {});
 }
 
-template <int COL>
-__global__ void __launch_bounds__(256) k_brefine(const BVol *__restrict__ vols, int nv, long long total,
-                                                 const LoopState *__restrict__ st, double *partial)
+__global__ void __launch_bounds__(256) k_bapply_black(const BVol *__restrict__ vols, int nv, long long total,
+                                                      const LoopState *__restrict__ st)
 {
-    __shared__ double wacc[BWARPS][BMAX];
+    bapply_black(vols, nv, total, st);
+}
+
+// a volume whose first pass the assembly formed (LoopState.pre) only reads
+// that pass's residual, as k_refine does
+template <int COL>
+__device__ __forceinline__ void brefine(const BVol *__restrict__ vols, int nv, long long total,
+                                        const LoopState *__restrict__ st, double *partial, double (*wacc)[BMAX])
+{
     VolumeSums sums{wacc};
     sums.clear();
     double acc = 0.0;
@@ -242,12 +262,18 @@ __global__ void __launch_bounds__(256) k_brefine(const BVol *__restrict__ vols, 
             const float *down = st[v].dsrc ? V.b.dR[1] : V.b.dR[0];
             const double *oth = COL == 0 ? V.b.Bk : V.b.R[0];
             const long long Hy = sp.Hs, Hz = Hy * g.jM, Hw = Hz * g.kM;
-            const RefineOut o =
-                refine_target<COL>(g, sp, tc, p, s, Hy, Hz, Hw, own, down, oth, V.b.coef[COL], V.b.P[COL]);
-            acc = fma(o.r, o.r, acc);
-            if (COL == 0)
-                own[s] = o.u;
-            V.b.r32[COL][s] = d2f_bits(-o.r);
+            double r;
+            if (st[v].pre) {
+                r = ld_stream(V.b.rpre[COL] + s);
+            } else {
+                const RefineOut o =
+                    refine_target<COL>(g, sp, tc, p, s, Hy, Hz, Hw, own, down, oth, V.b.coef[COL], V.b.P[COL]);
+                r = o.r;
+                if (COL == 0)
+                    own[s] = o.u;
+            }
+            acc = fma(r, r, acc);
+            V.b.r32[COL][s] = d2f_bits(-r);
         },
         [&](int v) {
             sums.add(v, acc);
@@ -256,9 +282,17 @@ __global__ void __launch_bounds__(256) k_brefine(const BVol *__restrict__ vols, 
     sums.write(nv, partial, want);
 }
 
+template <int COL>
+__global__ void __launch_bounds__(256) k_brefine(const BVol *__restrict__ vols, int nv, long long total,
+                                                 const LoopState *__restrict__ st, double *partial)
+{
+    __shared__ double wacc[BWARPS][BMAX];
+    brefine<COL>(vols, nv, total, st, partial, wacc);
+}
+
 // zero the corrections of the volumes that start a round (unless the round
 // keeps the correction in place)
-__global__ void k_bzero_delta(const BVol *__restrict__ vols, int nv, const LoopState *__restrict__ st)
+__device__ __forceinline__ void bzero_delta(const BVol *__restrict__ vols, int nv, const LoopState *__restrict__ st)
 {
     for (int v = 0; v < nv; ++v) {
         if (st[v].mode != 1 || st[v].stop || st[v].keep)
@@ -273,12 +307,16 @@ __global__ void k_bzero_delta(const BVol *__restrict__ vols, int nv, const LoopS
     }
 }
 
-template <int COL>
-__global__ void __launch_bounds__(256) k_bsweep32(const BVol *__restrict__ vols, int nv, long long total,
-                                                  const LoopState *__restrict__ st, const DevParams *__restrict__ par,
-                                                  double *partial)
+__global__ void k_bzero_delta(const BVol *__restrict__ vols, int nv, const LoopState *__restrict__ st)
 {
-    __shared__ double wacc[BWARPS][BMAX];
+    bzero_delta(vols, nv, st);
+}
+
+template <int COL>
+__device__ __forceinline__ void bsweep32(const BVol *__restrict__ vols, int nv, long long total,
+                                         const LoopState *__restrict__ st, const DevParams *__restrict__ par,
+                                         double *partial, double (*wacc)[BMAX])
+{
     VolumeSums sums{wacc};
     sums.clear();
     float acc = 0.f;
@@ -312,21 +350,34 @@ __global__ void __launch_bounds__(256) k_bsweep32(const BVol *__restrict__ vols,
     sums.write(nv, partial, want);
 }
 
-__global__ void k_binit(LoopState *st, int nv, int z)
+template <int COL>
+__global__ void __launch_bounds__(256) k_bsweep32(const BVol *__restrict__ vols, int nv, long long total,
+                                                  const LoopState *__restrict__ st, const DevParams *__restrict__ par,
+                                                  double *partial)
+{
+    __shared__ double wacc[BWARPS][BMAX];
+    bsweep32<COL>(vols, nv, total, st, par, partial, wacc);
+}
+
+// z == 0: a fresh state (mode 0), whose first refinement pass the assembly
+// formed where pre[v] says so (may be null)
+__global__ void k_binit(LoopState *st, int nv, int z, const int *pre)
 {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nv)
         return;
     if (z == 0) {
         memset(&st[v], 0, sizeof(LoopState));
+        st[v].pre = pre ? pre[v] : 0;
     } else {
         st[v].z = z;
     }
 }
 
-// every volume's stopping test (as k_ctrl64 does for one volume)
-__global__ void k_bctrl(const double *__restrict__ pred, const double *__restrict__ pblack, int grid, int nv,
-                        const DevParams *__restrict__ par, LoopState *st, cudaGraphConditionalHandle h, int use_cond)
+// every volume's stopping test (as k_ctrl64 does for one volume); one
+// block; returns (in every thread) whether a volume is still active
+__device__ __forceinline__ int bctrl(const double *__restrict__ pred, const double *__restrict__ pblack, int grid,
+                                     int nv, const DevParams *__restrict__ par, LoopState *st)
 {
     __shared__ int any;
     if (threadIdx.x == 0)
@@ -347,14 +398,20 @@ __global__ void k_bctrl(const double *__restrict__ pred, const double *__restric
         __syncthreads();
     }
     __syncthreads();
+    return any;
+}
+
+__global__ void k_bctrl(const double *__restrict__ pred, const double *__restrict__ pblack, int grid, int nv,
+                        const DevParams *__restrict__ par, LoopState *st, cudaGraphConditionalHandle h, int use_cond)
+{
+    const int any = bctrl(pred, pblack, grid, nv, par, st);
     if (threadIdx.x == 0 && use_cond)
         cudaGraphSetConditional(h, any ? 1u : 0u);
 }
 
 // every volume's mixed-form controller step (k_ctrl_mixed per volume)
-__global__ void k_bctrl_mixed(const double *__restrict__ pred, const double *__restrict__ pblack, int grid, int nv,
-                              const DevParams *__restrict__ par, LoopState *st, cudaGraphConditionalHandle h,
-                              int use_cond)
+__device__ __forceinline__ int bctrl_mixed(const double *__restrict__ pred, const double *__restrict__ pblack,
+                                           int grid, int nv, const DevParams *__restrict__ par, LoopState *st)
 {
     __shared__ int any;
     if (threadIdx.x == 0)
@@ -377,8 +434,125 @@ __global__ void k_bctrl_mixed(const double *__restrict__ pred, const double *__r
         __syncthreads();
     }
     __syncthreads();
+    return any;
+}
+
+__global__ void k_bctrl_mixed(const double *__restrict__ pred, const double *__restrict__ pblack, int grid, int nv,
+                              const DevParams *__restrict__ par, LoopState *st, cudaGraphConditionalHandle h,
+                              int use_cond)
+{
+    const int any = bctrl_mixed(pred, pblack, grid, nv, par, st);
     if (threadIdx.x == 0 && use_cond)
         cudaGraphSetConditional(h, any ? 1u : 0u);
+}
+
+// ---- the whole loop in one launch
+
+// A grid-wide barrier for a co-resident grid (cooperative launch): the last
+// block to arrive resets the count and advances the generation the others
+// wait on.  The wait is bounded (about a second of clock cycles); one that
+// runs out sets err and returns false, and the caller leaves its loop.
+struct GridBar {
+    unsigned count, gen;
+    int err, any;
+};
+
+__device__ __forceinline__ bool grid_sync(GridBar *gb)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = &gb->gen;
+        const unsigned g0 = *gen;
+        __threadfence();
+        if (atomicAdd(&gb->count, 1u) == gridDim.x - 1) {
+            gb->count = 0;
+            __threadfence();
+            atomicAdd(&gb->gen, 1u);
+        } else {
+            const long long t0 = clock64();
+            while (*gen == g0) {
+                if (clock64() - t0 > (1LL << 31)) {
+                    atomicExch(&gb->err, 1);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int *)&gb->err == 0;
+}
+
+// The SOR loop of every volume as one persistent launch: the loop body's
+// phases (those of the graph's body: refinement, zeroed corrections, FP32
+// black and red sweeps, controller; or the FP64 black and red sweeps and the
+// controller) run back to back with a grid barrier between them, until the
+// controller finds no volume active or max_bodies bodies have run.  In the
+// mixed form a phase (and its barrier) is left out when no active volume is
+// in a mode it works on; every block reads the modes at the start of the
+// body, after the controller's barrier, so the choice is the same in all.
+// Six blocks of 256 threads per SM, as the separate kernels run (42
+// registers at most).
+template <int MIXED>
+__global__ void __launch_bounds__(256, 6) k_bsolve(const BVol *__restrict__ vols, int nv, long long total,
+                                                   LoopState *st, const DevParams *__restrict__ par, double *pred,
+                                                   double *pblack, GridBar *gb, int max_bodies)
+{
+    __shared__ double wacc[BWARPS][BMAX];
+    const int grid = gridDim.x;
+    for (int body = 0; body < max_bodies; ++body) {
+        if (MIXED) {
+            int m0 = 0, m1 = 0, m2 = 0; // active volumes in mode 0 (refine), 1 (start a round), 2 (sweep)
+            for (int v = 0; v < nv; ++v) {
+                if (st[v].stop)
+                    continue;
+                const int mode = st[v].mode;
+                m0 |= mode == 0;
+                m1 |= mode == 1;
+                m2 |= mode == 2;
+            }
+            if (m0) {
+                bapply_black(vols, nv, total, st);
+                if (!grid_sync(gb))
+                    return;
+                brefine<0>(vols, nv, total, st, pred, wacc);
+                if (!grid_sync(gb))
+                    return;
+                brefine<1>(vols, nv, total, st, pblack, wacc);
+                if (!grid_sync(gb))
+                    return;
+            }
+            if (m1) {
+                bzero_delta(vols, nv, st);
+                if (!grid_sync(gb))
+                    return;
+            }
+            if (m2) {
+                bsweep32<1>(vols, nv, total, st, par, pblack, wacc);
+                if (!grid_sync(gb))
+                    return;
+            }
+            if (m1 || m2)
+                bsweep32<0>(vols, nv, total, st, par, pred, wacc);
+        } else {
+            bsweep64<1>(vols, nv, total, st, pblack, wacc);
+            if (!grid_sync(gb))
+                return;
+            bsweep64<0>(vols, nv, total, st, pred, wacc);
+        }
+        if (!grid_sync(gb))
+            return;
+        if (blockIdx.x == 0) {
+            const int any = MIXED ? bctrl_mixed(pred, pblack, grid, nv, par, st) : bctrl(pred, pblack, grid, nv, par, st);
+            if (threadIdx.x == 0)
+                *(volatile int *)&gb->any = any;
+        }
+        if (!grid_sync(gb))
+            return;
+        if (*(volatile int *)&gb->any == 0)
+            return;
+    }
 }
 
 int bsweep_blocks_per_sm()
@@ -411,6 +585,10 @@ struct ss4d_batch {
     cudaGraphExec_t exec[2];
     int use_graph, graph_failed;
     int mixed;
+    int *d_pre, *h_pre; // per volume: the assembly formed the step's first refinement pass
+    GridBar *d_bar;     // the persistent loop's grid barrier and its "any volume active" flag
+    int persistent;     // run the loop as one persistent launch (default) or as the graph's while loop
+    int pgrid[2];       // co-resident blocks of k_bsolve<0/1> (0: not yet known)
 };
 
 static void bfree_graph(ss4d_batch *b)
@@ -441,6 +619,12 @@ extern "C" ss4d_status ss4d_batch_destroy(ss4d_batch *b)
         cudaFree(b->d_par);
     if (b->d_partial)
         cudaFree(b->d_partial);
+    if (b->d_pre)
+        cudaFree(b->d_pre);
+    if (b->d_bar)
+        cudaFree(b->d_bar);
+    if (b->h_pre)
+        cudaFreeHost(b->h_pre);
     if (b->h_st)
         cudaFreeHost(b->h_st);
     if (b->h_par)
@@ -485,6 +669,7 @@ extern "C" ss4d_status ss4d_batch_create(int n, const ss4d_dims *dims, void *str
     b->n = n;
     b->stream = (cudaStream_t)stream;
     b->use_graph = 1;
+    b->persistent = 1;
     b->dirty = 1;
     ss4d_status st = SS4D_OK;
     for (int v = 0; v < n && st == SS4D_OK; ++v) {
@@ -512,6 +697,12 @@ extern "C" ss4d_status ss4d_batch_create(int n, const ss4d_dims *dims, void *str
     if (e == cudaSuccess)
         e = cudaMallocHost((void **)&b->h_par, sizeof(DevParams) * n);
     if (e == cudaSuccess)
+        e = cudaMalloc((void **)&b->d_pre, sizeof(int) * n);
+    if (e == cudaSuccess)
+        e = cudaMallocHost((void **)&b->h_pre, sizeof(int) * n);
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **)&b->d_bar, sizeof(GridBar));
+    if (e == cudaSuccess)
         e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -527,6 +718,14 @@ extern "C" ss4d_status ss4d_batch_set_graph(ss4d_batch *b, int enable)
     if (!b)
         return bfail(SS4D_ERR_INVALID, "invalid argument: batch is NULL");
     b->use_graph = enable ? 1 : 0;
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_batch_set_persistent(ss4d_batch *b, int enable)
+{
+    if (!b)
+        return bfail(SS4D_ERR_INVALID, "invalid argument: batch is NULL");
+    b->persistent = enable ? 1 : 0;
     return SS4D_OK;
 }
 
@@ -693,7 +892,7 @@ extern "C" ss4d_status ss4d_batch_seg_time_step(ss4d_batch *b, const ss4d_params
     BCK(cudaEventCreate(&e1));
     BCK(cudaEventRecord(e0, b->stream));
     for (int v = 0; v < b->n; ++v) {
-        BCKS(solver_prepare_step(b->vol[v], &p[v], d_u[v], d_g + 8 * v));
+        BCKS(solver_prepare_step(b->vol[v], &p[v], d_u[v], d_g + 8 * v, &b->h_pre[v]));
         b->h_par[v].c = p[v].tau / (p[v].h * p[v].h);
         b->h_par[v].omega = p[v].omega_c;
         b->h_par[v].h4 = p[v].h * p[v].h * p[v].h * p[v].h;
@@ -706,15 +905,46 @@ extern "C" ss4d_status ss4d_batch_seg_time_step(ss4d_batch *b, const ss4d_params
     for (int v = 0; v < b->n; ++v) // after the volumes are described
         b->h_par[v].near_band = fabs(p[v].gsTol) * (double)b->h_vols[v].g.nint * 0x1p-53;
     BCK(cudaMemcpyAsync(b->d_par, b->h_par, sizeof(DevParams) * b->n, cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaMemcpyAsync(b->d_pre, b->h_pre, sizeof(int) * b->n, cudaMemcpyHostToDevice, b->stream));
     const int ib = (b->n + 63) / 64;
-    k_binit<<<ib, 64, 0, b->stream>>>(b->d_st, b->n, 0); // mixed: mode 0, refine first
+    k_binit<<<ib, 64, 0, b->stream>>>(b->d_st, b->n, 0, b->d_pre); // mixed: mode 0, refine first
     if (!b->mixed) {
         launch_bsweep(b, 0, b->stream); // the first red half-sweep
-        k_binit<<<ib, 64, 0, b->stream>>>(b->d_st, b->n, 1);
+        k_binit<<<ib, 64, 0, b->stream>>>(b->d_st, b->n, 1, nullptr);
     }
     BCK(cudaGetLastError());
-    bool graphed = false;
-    if (b->use_graph && !b->graph_failed) {
+    int maxit = 0;
+    for (int v = 0; v < b->n; ++v)
+        maxit = p[v].maxNoGSIteration > maxit ? p[v].maxNoGSIteration : maxit;
+    // a mixed body advances a volume by at most one inner iteration, and
+    // every round adds a start and a refinement body
+    const int guard_max = b->mixed ? 4 * (maxit + 4) + 16 : maxit + 8;
+    bool graphed = false, persisted = false;
+    if (b->persistent) {
+        const int f = b->mixed;
+        if (!b->pgrid[f]) {
+            int per = 0;
+            BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f ? (const void *)k_bsolve<1> : (const void *)k_bsolve<0>,
+                                                             256, 0));
+            const int cap = per * solver_sm_count(b->vol[0]);
+            b->pgrid[f] = cap < b->grid ? cap : b->grid; // the partial arrays hold b->grid blocks
+        }
+        if (b->pgrid[f] > 0) {
+            BCK(cudaMemsetAsync(b->d_bar, 0, sizeof(GridBar), b->stream));
+            const BVol *vols = b->d_vols;
+            int nv = b->n, mb = guard_max;
+            long long total = b->total;
+            LoopState *st = b->d_st;
+            const DevParams *par = b->d_par;
+            double *pred = bpart(b, 0), *pblack = bpart(b, 1);
+            GridBar *gb = b->d_bar;
+            void *args[] = {(void *)&vols, &nv, &total, &st, (void *)&par, &pred, &pblack, &gb, &mb};
+            BCK(cudaLaunchCooperativeKernel(f ? (const void *)k_bsolve<1> : (const void *)k_bsolve<0>,
+                                            dim3(b->pgrid[f]), dim3(256), args, 0, b->stream));
+            persisted = true;
+        }
+    }
+    if (!persisted && b->use_graph && !b->graph_failed) {
         if (!b->exec[b->mixed] && bbuild_graph(b) != SS4D_OK)
             b->graph_failed = 1;
         if (b->exec[b->mixed]) {
@@ -722,13 +952,7 @@ extern "C" ss4d_status ss4d_batch_seg_time_step(ss4d_batch *b, const ss4d_params
             graphed = true;
         }
     }
-    if (!graphed) {
-        int maxit = 0;
-        for (int v = 0; v < b->n; ++v)
-            maxit = p[v].maxNoGSIteration > maxit ? p[v].maxNoGSIteration : maxit;
-        // a mixed body advances a volume by at most one inner iteration, and
-        // every round adds a start and a refinement body
-        const int guard_max = b->mixed ? 4 * (maxit + 4) + 16 : maxit + 8;
+    if (!graphed && !persisted) {
         for (int guard = 0; guard < guard_max; ++guard) {
             if (b->mixed)
                 launch_body_mixed(b, 0, 0, b->stream);
@@ -748,7 +972,16 @@ extern "C" ss4d_status ss4d_batch_seg_time_step(ss4d_batch *b, const ss4d_params
         BCKS(solver_finish_step(b->vol[v], b->d_st + v, d_u[v]));
     BCK(cudaEventRecord(e1, b->stream));
     BCK(cudaMemcpyAsync(b->h_st, b->d_st, sizeof(LoopState) * b->n, cudaMemcpyDeviceToHost, b->stream));
+    GridBar hb;
+    memset(&hb, 0, sizeof hb);
+    if (persisted)
+        BCK(cudaMemcpyAsync(&hb, b->d_bar, sizeof(GridBar), cudaMemcpyDeviceToHost, b->stream));
     BCK(cudaStreamSynchronize(b->stream));
+    if (hb.err) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return bfail(SS4D_ERR_TIMEOUT, "the persistent batch loop's grid barrier gave up a wait");
+    }
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);

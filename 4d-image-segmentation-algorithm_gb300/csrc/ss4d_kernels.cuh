@@ -240,8 +240,12 @@ struct SolverView {
 SweepCfg make_sweep_cfg_xt(const Geo &g, const Split &s, int sm_count, int kb, int xt);
 ss4d_status solver_view(ss4d_solver *s, SolverView *out);      // allocates the FP64 split buffers
 ss4d_status solver_set_shape(ss4d_solver *s, int xt, int kb);  // tile width (threads along x) and k-block depth
-// assemble the coefficients of u and pack u (= prev) into the split buffers
-ss4d_status solver_prepare_step(ss4d_solver *s, const ss4d_params *p, double *d_u, const double *const d_g[8]);
+// assemble the coefficients of u and pack u (= prev) into the split buffers;
+// with pre_out (mixed form) the assembly also forms the first refinement
+// pass (its start correction added, its residual in rpre) and *pre_out gets
+// the LoopState.pre value the loop must start with (0 without pre_out)
+ss4d_status solver_prepare_step(ss4d_solver *s, const ss4d_params *p, double *d_u, const double *const d_g[8],
+                                int *pre_out = nullptr);
 // unpack the red buffer state->final_red and black into the interior of u
 ss4d_status solver_finish_step(ss4d_solver *s, const LoopState *d_state, double *d_u);
 // device time of `iters` (black + red) FP64 sweep pairs with the current shape

@@ -238,6 +238,7 @@ def lib() -> C.CDLL:
         "ss4d_batch_create": ([C.c_int, C.POINTER(Dims), vp, C.POINTER(vp)], st),
         "ss4d_batch_destroy": ([vp], st),
         "ss4d_batch_set_graph": ([vp, C.c_int], st),
+        "ss4d_batch_set_persistent": ([vp, C.c_int], st),
         "ss4d_batch_set_arith": ([vp, C.c_int], st),
         "ss4d_batch_set_extrapolation": ([vp, C.c_int], st),
         "ss4d_batch_set_shape": ([vp, C.c_int, C.c_int, C.c_int], st),
@@ -676,6 +677,10 @@ class Batch:
 
     def set_graph(self, on: bool):
         _check(self.L.ss4d_batch_set_graph(self.h, 1 if on else 0), "batch_set_graph")
+
+    def set_persistent(self, on: bool):
+        """the SOR loop as one persistent launch (default) or as the graph's while loop"""
+        _check(self.L.ss4d_batch_set_persistent(self.h, 1 if on else 0), "batch_set_persistent")
 
     def set_shape(self, v: int, xt: int, k_block: int):
         _check(self.L.ss4d_batch_set_shape(self.h, v, xt, k_block), "batch_set_shape")

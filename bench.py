@@ -87,10 +87,13 @@ def parse_args():
     ap.add_argument("--no-graph", action="store_true",
                     help="run the sweep loop host-driven instead of as one CUDA graph (same kernels)")
     ap.add_argument("--workload", choices=["single", "batch", "conv"], default="single",
-                    help="batch: 16 uneven volumes in one persistent launch per half-sweep (reports "
+                    help="batch: 16 uneven volumes, the SOR loop of all of them in one launch (reports "
                          "voxel-updates/s; not the headline metric); conv: the warm-start network's forward "
                          "(four tensor-core convolutions) on random features of --size (reports TFLOP/s; for "
                          "profiling)")
+    ap.add_argument("--batch-loop", choices=["persistent", "graph"], default="persistent",
+                    help="batch workload: the SOR loop of all volumes as one persistent launch (default) or as a "
+                         "CUDA graph's while loop of per-phase kernels")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--steps100", type=int, default=100,
                     help="every form also runs on from the timed window to this many time steps from u0 (the "
@@ -796,6 +799,7 @@ def run_batch(args):
         us = [u.clone() for u in u0s]
         B = ss4d.Batch(dims, stream=stream.cuda_stream)
         B.set_graph(not args.no_graph)
+        B.set_persistent(args.batch_loop == "persistent")
         if form != "fp64":
             B.set_arith("mixed")
         if form == "extrap":
@@ -826,12 +830,13 @@ def run_batch(args):
                                               for step in stats for s, p in zip(step, params))}
     head = "fp64" if "fp64" in results else forms[0]
     r = results[head]
-    line = {"metric": "aggregate voxel-updates/s, 16 uneven volumes (batched persistent launch)",
+    line = {"metric": "aggregate voxel-updates/s, 16 uneven volumes (batched, one launch per solve)",
             "value": r["voxel_updates_per_s"], "unit": "voxel-updates/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
             "dtype": "f64", "data": "synthetic", "impl": "ours",
             "config": {"workload": "16 volumes U[64..192]x U[64..192]x U[48..96]x U[8..24], kind-1 "
                                    "scenes, K~U[500,2000], tau~U[0.25,1], gsTol 1e-6", "form": head,
+                       "loop": args.batch_loop,
                        "sizes": sizes, "voxels": sum(vox)},
             "autotuned_shapes": shapes, "iterations_per_volume": r["iterations_per_volume"],
             "forms": results}

@@ -368,11 +368,16 @@ ss4d_status ss4d_mcf_exact_solution(ss4d_solver *s, double h, double t, double *
 /* ---- batched volumes --------------------------------------------------- */
 /* Many independent volumes, of different sizes and parameters, advanced
  * together in the plain FP64 form (default) or the mixed form
- * (ss4d_batch_set_arith).  Every loop kernel (a half-sweep; in the mixed form
- * also the refinement passes) runs ONE persistent launch over the
- * concatenated tiles of all volumes, and the SOR loop is one CUDA graph; each
- * volume keeps its own stopping test (sum r^2 h^4 <= its gsTol, or its
- * maxNoGSIteration) and once it has stopped its tiles return at once.  The
+ * (ss4d_batch_set_arith).  The SOR loop of all volumes is ONE persistent
+ * launch (a co-resident grid whose phases, the half-sweeps and in the mixed
+ * form the refinement passes, walk the concatenated tiles of all volumes,
+ * with a bounded grid barrier between phases: SS4D_ERR_TIMEOUT if one gives
+ * up); ss4d_batch_set_persistent(b, 0) runs the same phases as kernels of a
+ * CUDA graph's while loop instead.  Each volume keeps its own stopping test
+ * (sum r^2 h^4 <= its gsTol, or its maxNoGSIteration) and once it has
+ * stopped its tiles return at once.  In the mixed form each volume's
+ * coefficient assembly also forms its step's first refinement pass, as
+ * ss4d_seg_time_step does.  The
  * reference runs one volume per process, so these entry points have no
  * counterpart there; per volume the arithmetic is that of ss4d_seg_time_step
  * in the same form without the rescale (no centres, Mmask == 1).  At most
@@ -382,6 +387,10 @@ typedef struct ss4d_batch ss4d_batch;
 ss4d_status ss4d_batch_create(int n, const ss4d_dims *dims, void *stream, ss4d_batch **out);
 ss4d_status ss4d_batch_destroy(ss4d_batch *b);
 ss4d_status ss4d_batch_set_graph(ss4d_batch *b, int enable);
+/* 1 (default): the SOR loop as one persistent launch; 0: as the graph's
+ * while loop (or host-driven, with ss4d_batch_set_graph(b, 0)).  Results do
+ * not depend on it except through the residual's summation order. */
+ss4d_status ss4d_batch_set_persistent(ss4d_batch *b, int enable);
 /* Arithmetic form of the batched steps: SS4D_ARITH_FP64 (the default) or
  * SS4D_ARITH_MIXED, each volume as ss4d_seg_time_step does it in that form
  * (mixed: float-float assembly, FP32 correction sweeps, FP64 refinement and

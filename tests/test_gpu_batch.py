@@ -23,8 +23,8 @@ def _volumes(ss4d, oracle, sizes, seed=5):
     return vols
 
 
-@pytest.mark.parametrize("graph", [True, False])
-def test_batch_matches_single_volume_solves(ss4d, oracle, cuda, graph):
+@pytest.mark.parametrize("loop", ["persistent", "graph", "host"])
+def test_batch_matches_single_volume_solves(ss4d, oracle, cuda, loop):
     torch = cuda
     sizes = [(20, 16, 12, 5), (33, 9, 14, 7), (12, 24, 10, 3)]
     vols = _volumes(ss4d, oracle, sizes)
@@ -40,7 +40,8 @@ def test_batch_matches_single_volume_solves(ss4d, oracle, cuda, graph):
     gs = [[_dev(torch, a) for a in g] for _, _, g in vols]
     params = [p for p, _, _ in vols]
     with ss4d.Batch([(d[0] + 2, d[1] + 2, d[2] + 2, d[3] + 2) for d in sizes]) as B:
-        B.set_graph(graph)
+        B.set_persistent(loop == "persistent")
+        B.set_graph(loop == "graph")
         got_its = [[s["iterations"] for s in B.seg_time_step(params, us, gs)] for _ in range(2)]
     for v in range(len(sizes)):
         assert [got_its[0][v], got_its[1][v]] == its[v], v
@@ -73,16 +74,16 @@ def test_batch_autotuned_shapes_do_not_change_results(ss4d, oracle, cuda):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("loop", ["persistent", "graph"])
 @pytest.mark.parametrize("extrap", [0, 3])
-def test_mixed_batch_matches_single_volume_mixed_solves(ss4d, oracle, cuda, extrap):
+def test_mixed_batch_matches_single_volume_mixed_solves(ss4d, oracle, cuda, extrap, loop):
     """The mixed form batched (refinement passes and FP32 sweeps of all volumes
-    in one launch each, every volume in its own phase) gives each volume what
-    its own mixed-form solver gives it, step after step, with and without the
-    extrapolated start: the same counts, the same u, the FP64 tolerance met.
-    The single-volume solver has its assembly form each step's first
-    refinement pass (start correction and FP64 residual) while the batch runs
-    that pass in full, so this also pins the two forms of the pass to the
-    same bits."""
+    in one persistent launch, or as kernels of a graph's while loop, every
+    volume in its own phase) gives each volume what its own mixed-form solver
+    gives it, step after step, with and without the extrapolated start: the
+    same counts, the same u, the FP64 tolerance met.  Both have the assembly
+    form each step's first refinement pass (start correction and FP64
+    residual)."""
     torch = cuda
     sizes = [(20, 16, 12, 5), (33, 9, 14, 7), (12, 24, 10, 3)]
     vols = _volumes(ss4d, oracle, sizes, seed=11)
@@ -104,6 +105,7 @@ def test_mixed_batch_matches_single_volume_mixed_solves(ss4d, oracle, cuda, extr
     with ss4d.Batch([(d[0] + 2, d[1] + 2, d[2] + 2, d[3] + 2) for d in sizes]) as B:
         B.set_arith("mixed")
         B.set_extrapolation(extrap)
+        B.set_persistent(loop == "persistent")
         for step in range(steps):
             stats = B.seg_time_step(params, us, gs)
             for v, st in enumerate(stats):

@@ -8,7 +8,8 @@
 // and the input channels of X[voxel + tap][cin] W[tap][cout][cin].  A CTA
 // takes output tiles of 8 (x) by 16 (y) voxels by TZ planes (z) of one
 // frame; each plane is one M = 128 accumulator (row m = x + 8 y) of N
-// output channels.  Activations are channel-group planar in global memory
+// output channels, the TZ accumulators of a tile side by side in tensor
+// memory, plane p at column (TZ - 1 - p) N.  Activations are channel-group planar in global memory
 // ([F][C/8][nz][ny][nx][8], ss4d_conv_tc.cuh), so the input halo tile,
 // 10 x 18 x (TZ + 2) voxels, arrives in shared memory by one TMA box per
 // group of 8 channels whose rows are 160 contiguous bytes (x and the 8
@@ -16,11 +17,20 @@
 // 16 bytes per voxel, which is the canonical K-major layout of the UMMA
 // operands without swizzle: a core matrix is 8 consecutive voxels (rows) by
 // 8 channels (16 bytes).  So the A operand of
-// tap (dx, dy, dz) is the halo tile itself, its descriptor starting at voxel
-// (dx, dy, p + dz): rows x + 8 y step 16 bytes within a core matrix and the
-// row stride of the halo (160 bytes) between the 8-row groups, channel
-// groups a plane apart.  No operand is copied per tap.  The weights of all
-// taps stay in shared memory in the same core-matrix layout.
+// tap (dx, dy, dz) for output plane p is the halo tile itself, its
+// descriptor starting at voxel (dx, dy, p + dz): rows x + 8 y step 16 bytes
+// within a core matrix and the row stride of the halo (160 bytes) between
+// the 8-row groups, channel groups a plane apart.  No operand is copied per
+// tap.  The view at halo plane hz = p + dz serves the output planes hz,
+// hz - 1 and hz - 2 (dz = 0, 1, 2) alike, so one MMA does them together:
+// the weights of the three dz taps are stacked along N (3N rows per (dy, dx)
+// block in shared memory) and, with the accumulators in descending plane
+// order, the N blocks of taps dz_lo..dz_hi land on the accumulators of
+// planes hz - dz_lo .. hz - dz_hi.  A tile of TZ planes then takes
+// (TZ + 2) x 9 MMAs per K chunk instead of 27 TZ, each reading its A operand
+// from shared memory once for up to three planes.  An accumulate flag is
+// per MMA, not per column, so a first MMA of A = 0 clears all TZ
+// accumulators and every MMA after it accumulates.
 //
 // Per CTA: one thread of a fifth warp issues the TMA loads and the MMAs, four
 // warps drain the accumulators (TMEM -> registers -> bias, ReLU, mask ->
@@ -153,7 +163,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_conv_tc(const __grid_constant__ 
     unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     unsigned char *halo0 = smem;
     unsigned char *wsm = smem + STAGES * C::HALO;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(wsm + C::WBYTES); // full[STAGES], done[2], free[2]
+    unsigned char *zsm = wsm + C::WBYTES;                            // zeros: the clearing MMA's A operand
+    uint64_t *bars = reinterpret_cast<uint64_t *>(zsm + C::ZBYTES); // full[STAGES], done[2], free[2]
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + STAGES + 4);
     int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -162,6 +173,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_conv_tc(const __grid_constant__ 
     // weights: global (already in core-matrix order) -> shared
     for (int q = tid; q < C::WBYTES / 16; q += blockDim.x)
         reinterpret_cast<uint4 *>(wsm)[q] = __ldg(reinterpret_cast<const uint4 *>(a.w) + q);
+    for (int q = tid; q < C::ZBYTES / 16; q += blockDim.x)
+        reinterpret_cast<uint4 *>(zsm)[q] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
         for (int q = 0; q < STAGES; ++q)
             mbar_init(full0 + 8 * q, 1);
@@ -200,10 +213,13 @@ __global__ void __launch_bounds__(THREADS, 1) k_conv_tc(const __grid_constant__ 
             // ---- producer: loads and MMAs ----
             // K-major operands without swizzle: LBO = stride of the core
             // matrices along K, SBO = stride of the 8-row groups along M (N)
-            const uint32_t idesc = (1u << 4)                 // D: FP32
-                                   | (1u << 7) | (1u << 10)  // A, B: BF16
-                                   | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
-            const uint64_t b0 = make_desc(smem_u32(wsm), (N / 8) * 128, 128);
+            // instruction descriptor: D FP32, A and B BF16, M = 128, N = n
+            auto idesc = [](int n) {
+                return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+            };
+            const uint64_t b0 = make_desc(smem_u32(wsm), (3 * N / 8) * 128, 128);
+            // 128 rows x 16 K of zeros (16-row groups 128 B apart, K halves 2 KB apart)
+            const uint64_t zdesc = make_desc(smem_u32(zsm), 16 * 128, 128);
             int loads = 0, mmas = 0; // issued
             auto load = [&](int it) {
                 int x0, y0, z0, f;
@@ -223,15 +239,6 @@ __global__ void __launch_bounds__(THREADS, 1) k_conv_tc(const __grid_constant__ 
                 load(it);
             for (int it = 0; it < my_n && ok; ++it) {
                 const int q = it % STAGES, b = it & 1;
-                const int nxt = it + STAGES - 1;
-                if (nxt < my_n) {
-                    // its halo stage was read by the MMAs of tile it-1
-                    if (it >= 1 && !mbar_wait(done0 + 8 * ((it - 1) & 1), ((it - 1) >> 1) & 1)) {
-                        ok = false;
-                        break;
-                    }
-                    load(nxt);
-                }
                 // this tile's loads, and its accumulator buffer read out (tile it-2)
                 if (!mbar_wait(full0 + 8 * q, (it / STAGES) & 1) ||
                     (it >= 2 && !mbar_wait(free0 + 8 * b, ((it - 2) >> 1) & 1))) {
@@ -243,20 +250,36 @@ __global__ void __launch_bounds__(THREADS, 1) k_conv_tc(const __grid_constant__ 
                 // bits, in 16-byte units): one base each, plus constants
                 const uint64_t a0 = make_desc(smem_u32(halo0 + q * C::HALO), PLANE, HX * 16);
                 const uint32_t acc = tmem + (uint32_t)(b * TZ * N);
+                // clear the TZ accumulators: A = 0 times any B rows (finite weights)
+                umma_bf16(acc, zdesc, b0, idesc(TZ * N), 0);
 #pragma unroll
-                for (int p = 0; p < TZ; ++p) {
+                for (int hz = 0; hz < TZ + 2; ++hz) {
+                    // the dz taps whose output plane hz - dz lies in the tile
+                    const int dz_lo = hz - (TZ - 1) > 0 ? hz - (TZ - 1) : 0, dz_hi = hz < 2 ? hz : 2;
+                    const uint32_t col = (uint32_t)((TZ - 1 - hz + dz_lo) * N);
 #pragma unroll
-                    for (int tap = 0; tap < 27; ++tap) {
-                        const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
-                        const uint32_t vox = (uint32_t)(((p + dz) * HY + dy) * HX + dx);
+                    for (int dd = 0; dd < 9; ++dd) {
+                        const int dy = dd / 3, dx = dd % 3;
+                        const uint32_t vox = (uint32_t)((hz * HY + dy) * HX + dx);
 #pragma unroll
                         for (int kc = 0; kc < C::KC; ++kc)
-                            umma_bf16(acc + p * N, a0 + ((2 * kc * PLANE + vox * 16) >> 4),
-                                      b0 + (((tap * C::KC + kc) * C::WBLK) >> 4), idesc, tap + kc > 0);
+                            umma_bf16(acc + col, a0 + ((2 * kc * PLANE + vox * 16) >> 4),
+                                      b0 + (((dd * C::KC + kc) * C::WBLK + dz_lo * N * 16) >> 4),
+                                      idesc((dz_hi - dz_lo + 1) * N), 1);
                     }
                 }
                 umma_commit(done0 + 8 * b);
                 mmas = it + 1;
+                // the next load goes to the halo stage that tile it-1 read:
+                // wait for its MMAs while this tile's run behind them
+                const int nxt = it + STAGES - 1;
+                if (nxt < my_n) {
+                    if (it >= 1 && !mbar_wait(done0 + 8 * ((it - 1) & 1), ((it - 1) >> 1) & 1)) {
+                        ok = false;
+                        break;
+                    }
+                    load(nxt);
+                }
             }
             if (!ok) {
                 *abort_flag = 1;
@@ -294,7 +317,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_conv_tc(const __grid_constant__ 
             const long long vol = (long long)a.nx * a.ny * a.nz;
 #pragma unroll 1
             for (int p = 0; p < TZ; ++p) {
-                const uint32_t col = tmem + (uint32_t)(b * TZ * N + p * N) + ((uint32_t)(warp * 32) << 16);
+                const uint32_t col = tmem + (uint32_t)(b * TZ * N + (TZ - 1 - p) * N) + ((uint32_t)(warp * 32) << 16);
                 float v[N];
 #pragma unroll
                 for (int h = 0; h < N / 16; ++h) {
@@ -401,25 +424,28 @@ cudaError_t conv_tc(int cin, int n, const void *x, const TcArgs &a, int sm_count
 
 // W[tap][cout][cin] FP32 (master layout, or the data-gradient layout with
 // `reverse`: tap 26 - t and the channel roles swapped) -> B blocks
-// [27][KC][2 K groups][N/8 N groups][8 rows][8 K] BF16, zero beyond cout/cin
+// [9 (dy, dx)][KC][2 K groups][3N/8 N groups][8 rows][8 K] BF16, row
+// dz * N + co of block (dy, dx) holding tap 9 dz + 3 dy + dx; zero beyond
+// cout/cin
 __global__ void k_pack_tc(const float *__restrict__ w, int cout, int cin, int reverse, int cinp, int n,
                           __nv_bfloat16 *out)
 {
     const int kc_n = cinp / 16;
-    const int total = 27 * kc_n * 2 * n * 8;
+    const int total = 9 * kc_n * 2 * 3 * n * 8;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
         int r = q;
         const int e = r % 8;
         r /= 8;
         const int row = r % 8;
         r /= 8;
-        const int j = r % (n / 8);
-        r /= n / 8;
+        const int j = r % (3 * n / 8);
+        r /= 3 * n / 8;
         const int h = r % 2;
         r /= 2;
         const int kc = r % kc_n;
-        const int tap = r / kc_n;
-        const int co = 8 * j + row, ci = 16 * kc + 8 * h + e;
+        const int dd = r / kc_n;
+        const int nr = 8 * j + row, dz = nr / n;
+        const int tap = 9 * dz + dd, co = nr % n, ci = 16 * kc + 8 * h + e;
         float v = 0.f;
         if (!reverse) {
             if (co < cout && ci < cin)

@@ -22,8 +22,8 @@ __host__ __device__ __forceinline__ size_t planar_off(int f, int c, int groups, 
 
 // output tile: 8 (x) x 16 (y) voxels = one M = 128 accumulator per z plane,
 // TZ planes per tile; its input halo tile is HX x HY x HZ voxels
-constexpr int TX = 8, TY = 16, TZ = 2;
-constexpr int STAGES = 3; // halo tiles in flight
+constexpr int TX = 8, TY = 16, TZ = 4;
+constexpr int STAGES = 2; // halo tiles in flight
 constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2;
 constexpr int HV = HX * HY * HZ;
 // one 8-channel group of the halo tile, 16 bytes per voxel, each group on a
@@ -35,11 +35,15 @@ template <int CIN, int N> struct TcCfg {
     static constexpr int NCG = CIN / 8;                      // channel groups (TMA boxes per tile)
     static constexpr int KC = CIN / 16;                      // K chunks of 16 per tap
     static constexpr int BOX_BYTES = HV * 16;                // bytes one box writes
-    static constexpr int WBLK = N * 32;                      // one (tap, kc) B operand: 2 K groups x N rows x 16 B
-    static constexpr int WBYTES = 27 * KC * WBLK;
+    // one (dy, dx, kc) B operand: the three dz taps stacked along N (rows dz*N + co),
+    // 2 K groups x 3N rows x 16 B
+    static constexpr int WBLK = 3 * N * 32;
+    static constexpr int WBYTES = 9 * KC * WBLK;
     static constexpr int HALO = NCG * PLANE;                 // one halo buffer
-    static constexpr int SMEM = 1024 + STAGES * HALO + WBYTES + 128; // + mbarriers, the TMEM address, a flag
+    static constexpr int ZBYTES = 4096;                      // a zero A operand (128 rows x 16 K) for clearing
+    static constexpr int SMEM = 1024 + STAGES * HALO + WBYTES + ZBYTES + 128; // + mbarriers, the TMEM address, a flag
     static constexpr int TCOLS = 2 * TZ * N < 32 ? 32 : 2 * TZ * N; // two accumulator buffers (a power of two here)
+    static_assert(TZ * N <= 256 && 3 * N <= 256, "one MMA covers at most 256 columns");
     static_assert((TCOLS & (TCOLS - 1)) == 0, "tensor memory is allocated in powers of two columns");
     static_assert(SMEM <= 227 * 1024, "shared memory per CTA");
 };
@@ -126,8 +130,9 @@ __device__ __forceinline__ void epilogue_store(const TcArgs &a, float (&v)[N], i
 // output channels) on x (planar, cin channels, nf frames) BF16; persistent
 // CTAs, as many as fit on sm_count SMs
 cudaError_t conv_tc(int cin, int n, const void *x, const TcArgs &a, int sm_count, cudaStream_t st);
-// weights W[27][cout][cin] FP32 -> the B blocks of a (cinp, n) convolution;
-// reverse: the data-gradient weights (taps reversed, channel roles swapped)
+// weights W[27][cout][cin] FP32 -> the B blocks of a (cinp, n) convolution
+// (per (dy, dx, K chunk) the three dz taps stacked along N); reverse: the
+// data-gradient weights (taps reversed, channel roles swapped)
 void pack_tc(const float *w, int cout, int cin, int reverse, int cinp, int n, __nv_bfloat16 *out, cudaStream_t st);
 constexpr size_t packed_tc_elems(int cinp, int n) { return (size_t)27 * (cinp / 16) * 2 * n * 8; }
 // y[0..n) <- NaN when *err is set (a convolution before it gave up a wait)

@@ -286,8 +286,8 @@ ss4d_status ss4d_rescale_to_zero_one(ss4d_solver *s, const ss4d_params *p, doubl
  * library (32 KB per device, kept until the process exits), which limits it
  * to SS4D_NOALLOC_MAX_BALLS centres and lMax <= SS4D_NOALLOC_MAX_FRAMES;
  * larger inputs return SS4D_ERR_INVALID.  The first call on a device looks
- * up that array's device address (cudaGetSymbolAddress); make that first
- * call before any stream capture.  All calls share the one array, so calls
+ * up that array's device address (cudaGetSymbolAddress).  All calls share
+ * the one array, so calls
  * whose GPU work overlaps (different streams, or different host threads
  * without ordering) race on it; issue them in one stream.  `stream` is a
  * cudaStream_t (NULL = legacy default stream); the call is asynchronous. */

@@ -82,6 +82,9 @@ def parse_args():
                          "this instead of the configured omega 1.8; reported, never the headline)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="leave out the short batched-workload measurement (16 uneven volumes, FP64 and mixed + "
+                         "extrapolation, 10 steps after 3) that the default line carries as `batch`")
     ap.add_argument("--no-frontend", action="store_true",
                     help="skip the timing of the work around the time loop (thresholding, edge detector, ...)")
     ap.add_argument("--no-graph", action="store_true",
@@ -760,6 +763,10 @@ def run_reference(args):
 
 
 def run_batch(args):
+    print(json.dumps(batch_line(args, args.steps, args.warmup, args.forms)))
+
+
+def batch_line(args, steps, warmup, forms_arg):
     """16 independent volumes, sizes U[64..192] x U[64..192] x U[48..96] x
     U[8..24] per axis, single-ellipsoid scenes with per-volume K in
     [500, 2000] and tau in [0.25, 1], stepped together (one persistent launch
@@ -791,7 +798,7 @@ def run_batch(args):
         gs.append(g)
     dims = [(nx + 2, ny + 2, nz + 2, nt + 2) for nx, ny, nz, nt in sizes]
     vox = [nx * ny * nz * nt for nx, ny, nz, nt in sizes]
-    forms = [f for f in args.forms.split(",") if f in ("fp64", "mixed", "extrap")] or ["fp64"]
+    forms = [f for f in forms_arg.split(",") if f in ("fp64", "mixed", "extrap")] or ["fp64"]
     stream = torch.cuda.current_stream(dev)
     shapes = None
     results = {}
@@ -809,20 +816,20 @@ def run_batch(args):
         else:
             for v, (xt, kb) in enumerate(shapes):
                 B.set_shape(v, xt, kb)
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             B.seg_time_step(params, us, gs)
         torch.cuda.synchronize(dev)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        stats = [B.seg_time_step(params, us, gs) for _ in range(args.steps)]
+        stats = [B.seg_time_step(params, us, gs) for _ in range(steps)]
         e1.record(stream)
         torch.cuda.synchronize(dev)
         ms = e0.elapsed_time(e1)
         B.close()
         its = [[s["iterations"] for s in step] for step in stats]
         updates = sum(vv * z for step in its for vv, z in zip(vox, step))
-        results[form] = {"ms_per_step": ms / args.steps, "voxel_updates_per_s": updates / (ms / 1e3),
-                         "volume_steps_per_s": len(sizes) * args.steps / (ms / 1e3),
+        results[form] = {"ms_per_step": ms / steps, "voxel_updates_per_s": updates / (ms / 1e3),
+                         "volume_steps_per_s": len(sizes) * steps / (ms / 1e3),
                          "iterations_per_volume": its,
                          "refinements_per_volume": [[s["refinements"] for s in step] for step in stats],
                          "max_residual": max(s["residual"] for step in stats for s in step),
@@ -831,8 +838,8 @@ def run_batch(args):
     head = "fp64" if "fp64" in results else forms[0]
     r = results[head]
     line = {"metric": "aggregate voxel-updates/s, 16 uneven volumes (batched, one launch per solve)",
-            "value": r["voxel_updates_per_s"], "unit": "voxel-updates/s", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+            "value": r["voxel_updates_per_s"], "unit": "voxel-updates/s", "n_gpus": 1, "steps": steps,
+            "warmup": warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
             "dtype": "f64", "data": "synthetic", "impl": "ours",
             "config": {"workload": "16 volumes U[64..192]x U[64..192]x U[48..96]x U[8..24], kind-1 "
                                    "scenes, K~U[500,2000], tau~U[0.25,1], gsTol 1e-6", "form": head,
@@ -844,7 +851,9 @@ def run_batch(args):
         for f in results:
             if f != "fp64":
                 line[f"{f}_step_speedup_over_fp64"] = results["fp64"]["ms_per_step"] / results[f]["ms_per_step"]
-    print(json.dumps(line))
+    del us, u0s, gs
+    torch.cuda.empty_cache()
+    return line
 
 
 def run_conv(args):
@@ -951,6 +960,15 @@ def main():
     if rank == 0 and world == 1 and not args.no_frontend:
         line["frontend"] = run_frontend(args, ctx, "fp64")
         line["frontend_mixed"] = run_frontend(args, ctx, "mixed")
+    if rank == 0 and world == 1 and not args.no_batch:
+        # the batched workload, short: per-volume iteration counts of the last
+        # step only (the full record is `--workload batch`)
+        b = batch_line(args, 10, 3, "fp64,extrap")
+        for f in b["forms"].values():
+            f["iterations_last_step"] = f.pop("iterations_per_volume")[-1]
+            f.pop("refinements_per_volume", None)
+        b.pop("iterations_per_volume", None)
+        line["batch"] = b
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args, ctx[6])
         if "parity_config3" in line["cpu_baseline"]:

@@ -48,7 +48,12 @@ def net(ss4d, cuda):
         yield n
 
 
-@pytest.mark.parametrize("shape", [(2, 5, 11, 13), (1, 4, 8, 8), (3, 1, 2, 3)])
+@pytest.mark.parametrize("shape", [(2, 5, 11, 13), (1, 4, 8, 8), (3, 1, 2, 3),
+                                   # partial tiles along every axis (tiles are 8 x 16 x 4 voxels)
+                                   (2, 7, 35, 21),
+                                   # 512 tiles: several per CTA, so the halo stages and the two
+                                   # accumulator buffers each go round more than once
+                                   (4, 16, 64, 64)])
 def test_forward_matches_torch_reference(ss4d, cuda, net, shape):
     torch = cuda
     nf, nz, ny, nx = shape

@@ -89,6 +89,30 @@ __global__ void __launch_bounds__(256) k_fdiff(Geo g, Split sp, const double *__
     }
 }
 
+// plane pk and frame fl (both from 0) of block z of a grid over P planes of
+// F frames: frame by frame (kb <= 0 or kb >= P), else in blocks of kb
+// planes, the planes of a block for each frame in turn (the last block
+// holds the remaining P mod kb planes)
+__device__ __forceinline__ void plane_frame(int z, int P, int F, int kb, int &pk, int &fl)
+{
+    if (kb <= 0 || kb >= P) {
+        pk = z % P;
+        fl = z / P;
+        return;
+    }
+    const int full = P / kb, blk = kb * F;
+    const int b = z / blk;
+    if (b < full) {
+        const int r = z - b * blk;
+        fl = r / kb;
+        pk = b * kb + r % kb;
+    } else {
+        const int rest = P - full * kb, r = z - full * blk;
+        fl = r / rest;
+        pk = full * kb + r % rest;
+    }
+}
+
 // --- faces ------------------------------------------------------------------
 // A block takes a tile of FTX x FTY voxels (i, j) of one (k, l) plane.  The
 // central differences D_a of every voxel are formed once, by its own thread,
@@ -168,13 +192,15 @@ __device__ __forceinline__ void boundary_face(const FFConst &K, const CPtrs8 &gi
 // a few bytes of spill) ran 6.28 ms at 256^2 x 128 x 20 against 6.93 ms
 // at 5 blocks (48 registers) and 6.74 ms at 6.
 __global__ void __launch_bounds__(FTX *FTY, 8) k_faces_ff(Geo g, CPtrs8 gin, int has_g, FFConst K, SplitBufs b,
-                                                           int l_off)
+                                                           int l_off, int kblock)
 {
     __shared__ float2 sD[4][FTY + 1][FTX + 1];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int i0 = 1 + blockIdx.x * FTX, j0 = 1 + blockIdx.y * FTY;
     const int i = i0 + tx, j = j0 + ty;
-    const int k = blockIdx.z % (g.nz + 1), l = l_off + blockIdx.z / (g.nz + 1);
+    int k, lf;
+    plane_frame(blockIdx.z, g.nz + 1, gridDim.z / (g.nz + 1), kblock, k, lf);
+    const int l = l_off + lf;
     const unsigned st[4] = {1u, (unsigned)g.sy, (unsigned)g.sz, (unsigned)g.sw};
     const float2 *const F[4] = {reinterpret_cast<const float2 *>(b.fd[0]), reinterpret_cast<const float2 *>(b.fd[1]),
                                 reinterpret_cast<const float2 *>(b.fd[2]), reinterpret_cast<const float2 *>(b.fd[3])};
@@ -270,11 +296,14 @@ __global__ void __launch_bounds__(FTX *FTY, 8) k_faces_ff(Geo g, CPtrs8 gin, int
 // diag u0, with the same fused multiply-adds) on the split copies of u whose
 // start correction the first-difference kernel added, into rpre.
 template <int PRE>
-__global__ void __launch_bounds__(256, PRE ? 6 : 8) k_voxel_coef_ff(Geo g, Split sp, FFConst K, SplitBufs b, int l_off)
+__global__ void __launch_bounds__(256, PRE ? 6 : 8) k_voxel_coef_ff(Geo g, Split sp, FFConst K, SplitBufs b, int l_off,
+                                                                    int kblock)
 {
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = 1 + blockIdx.z % g.nz, l = 1 + l_off + blockIdx.z / g.nz;
+    int kk, lf;
+    plane_frame(blockIdx.z, g.nz, gridDim.z / g.nz, kblock, kk, lf);
+    const int k = 1 + kk, l = 1 + l_off + lf;
     if (i > g.nx || j > g.ny)
         return;
     const long long o = nat_index(g, i, j, k, l);
@@ -357,23 +386,23 @@ void launch_fdiff_pack_range(const Geo &g, const Split &s, const double *u, Spli
 }
 
 void launch_assemble_ff(const Geo &g, const Split &s, const double *u, CPtrs8 gin, int has_g, const ss4d_params &p,
-                        SplitBufs b, int pack, int sm_count, cudaStream_t st, int pre)
+                        SplitBufs b, int pack, int sm_count, cudaStream_t st, int pre, int kblock)
 {
     if (pack)
         launch_fdiff_pack_range(g, s, u, b, 0, g.lM, sm_count, st, pre);
     else
         launch_fdiff_range(g, u, b, 0, g.lM, sm_count, st);
-    launch_assemble_ff_faces(g, s, gin, has_g, p, b, st, pack ? pre : 0);
+    launch_assemble_ff_faces(g, s, gin, has_g, p, b, st, pack ? pre : 0, kblock);
 }
 
 void launch_assemble_ff_faces(const Geo &g, const Split &s, CPtrs8 gin, int has_g, const ss4d_params &p, SplitBufs b,
-                              cudaStream_t st, int pre)
+                              cudaStream_t st, int pre, int kblock)
 {
-    launch_assemble_ff_faces_range(g, s, gin, has_g, p, b, 0, g.nt + 1, 1, g.nt + 1, st, pre);
+    launch_assemble_ff_faces_range(g, s, gin, has_g, p, b, 0, g.nt + 1, 1, g.nt + 1, st, pre, kblock);
 }
 
 void launch_assemble_ff_faces_range(const Geo &g, const Split &s, CPtrs8 gin, int has_g, const ss4d_params &p,
-                                    SplitBufs b, int f0, int f1, int v0, int v1, cudaStream_t st, int pre)
+                                    SplitBufs b, int f0, int f1, int v0, int v1, cudaStream_t st, int pre, int kblock)
 {
     FFConst K;
     split_host(1.0 / (p.h * p.h), K.ih2h, K.ih2l);
@@ -384,7 +413,7 @@ void launch_assemble_ff_faces_range(const Geo &g, const Split &s, CPtrs8 gin, in
     K.pow2 = K.ih2l == 0.f && K.iq2l == 0.f && frexp((double)K.ih2h, &e1) == 0.5 && frexp((double)K.iq2h, &e2) == 0.5;
     if (f1 > f0) {
         dim3 gr((g.nx + FTX - 1) / FTX, (g.ny + FTY - 1) / FTY, (g.nz + 1) * (f1 - f0));
-        k_faces_ff<<<gr, dim3(FTX, FTY, 1), 0, st>>>(g, gin, has_g, K, b, f0);
+        k_faces_ff<<<gr, dim3(FTX, FTY, 1), 0, st>>>(g, gin, has_g, K, b, f0, kblock);
     }
     {
         const int bx = g.nx >= 128 ? 128 : (g.nx >= 64 ? 64 : 32);
@@ -392,9 +421,9 @@ void launch_assemble_ff_faces_range(const Geo &g, const Split &s, CPtrs8 gin, in
         dim3 bl(bx, by, 1);
         dim3 gr((g.nx + bx - 1) / bx, (g.ny + by - 1) / by, g.nz * (v1 - v0));
         if (v1 > v0 && pre)
-            k_voxel_coef_ff<1><<<gr, bl, 0, st>>>(g, s, K, b, v0 - 1);
+            k_voxel_coef_ff<1><<<gr, bl, 0, st>>>(g, s, K, b, v0 - 1, kblock);
         else if (v1 > v0)
-            k_voxel_coef_ff<0><<<gr, bl, 0, st>>>(g, s, K, b, v0 - 1);
+            k_voxel_coef_ff<0><<<gr, bl, 0, st>>>(g, s, K, b, v0 - 1, kblock);
     }
 }
 

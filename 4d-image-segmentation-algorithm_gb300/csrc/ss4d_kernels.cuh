@@ -147,8 +147,10 @@ void launch_pack(const Geo &g, const Split &s, const double *u, const double *pr
 // mixed form: the same coefficient records from float-float arithmetic (3
 // kernels); with pack the first of them also makes launch_pack's copies of u
 // with prev = u
+// (kblock: block order of the faces and coefficient kernels, as in
+// launch_assemble_ff_faces_range)
 void launch_assemble_ff(const Geo &g, const Split &s, const double *u, CPtrs8 gin, int has_g, const ss4d_params &p,
-                        SplitBufs b, int pack, int sm_count, cudaStream_t st, int pre = 0);
+                        SplitBufs b, int pack, int sm_count, cudaStream_t st, int pre = 0, int kblock = 0);
 // the same in parts: first differences of padded frames [l0, l1), then the
 // faces and voxel coefficients (after the differences of every frame)
 void launch_fdiff_range(const Geo &g, const double *u, SplitBufs b, int l0, int l1, int sm_count, cudaStream_t st);
@@ -159,15 +161,20 @@ void launch_fdiff_range(const Geo &g, const double *u, SplitBufs b, int l0, int 
 void launch_fdiff_pack_range(const Geo &g, const Split &s, const double *u, SplitBufs b, int l0, int l1, int sm_count,
                              cudaStream_t st, int pre = 0);
 void launch_assemble_ff_faces(const Geo &g, const Split &s, CPtrs8 gin, int has_g, const ss4d_params &p, SplitBufs b,
-                              cudaStream_t st, int pre = 0);
+                              cudaStream_t st, int pre = 0, int kblock = 0);
 // faces of the frames [f0, f1) of the extended box (0 .. nt; they need the
 // first differences of frames f0-1 .. f1) and coefficients of the interior
 // frames [v0, v1) (they need the faces of frames v0-1 .. v1-1); empty ranges
 // launch nothing.  With pre the coefficient kernel also forms the first
 // refinement pass's residual into rpre (it needs the corrected split copies
-// of u of frames v0-1 .. v1)
+// of u of frames v0-1 .. v1).  kblock orders the blocks of both kernels:
+// 0 frame by frame (all planes of a frame, then the next frame), n >= 1 in
+// blocks of n planes (those planes of every frame in turn, then the next n
+// planes), which keeps a frame's neighbours in the next frame and the next
+// plane close in time; results do not depend on it
 void launch_assemble_ff_faces_range(const Geo &g, const Split &s, CPtrs8 gin, int has_g, const ss4d_params &p,
-                                    SplitBufs b, int f0, int f1, int v0, int v1, cudaStream_t st, int pre = 0);
+                                    SplitBufs b, int f0, int f1, int v0, int v1, cudaStream_t st, int pre = 0,
+                                    int kblock = 0);
 // frame ranges: padded frames [l0, l1) for the pack, interior frames
 // [l0, l1) (1 <= l0 < l1 <= lMax-1) for the unpack and the rescale
 void launch_pack_range(const Geo &g, const Split &s, const double *u, const double *prev, SplitBufs b, int l0, int l1,

@@ -193,6 +193,7 @@ def lib() -> C.CDLL:
         "ss4d_solver_workspace_bytes": ([vp, C.POINTER(C.c_size_t)], st),
         "ss4d_solver_set_timing": ([vp, C.c_int], st),
         "ss4d_solver_set_tiling": ([vp, C.c_int, C.c_int], st),
+        "ss4d_solver_set_assembly_order": ([vp, C.c_int], st),
         "ss4d_solver_kernel_time": ([vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong)], st),
         "ss4d_solver_reset_timing": ([vp], st),
         "ss4d_solver_launch_count": ([vp, C.POINTER(C.c_longlong)], st),
@@ -444,6 +445,11 @@ class Solver:
 
     def set_tiling(self, k_block: int, max_grid: int = 0):
         _check(self.L.ss4d_solver_set_tiling(self.h, k_block, max_grid), "set_tiling")
+
+    def set_assembly_order(self, planes: int):
+        """block order of the mixed form's assembly: 0 frame by frame, n >= 1
+        in blocks of n k planes across the frames"""
+        _check(self.L.ss4d_solver_set_assembly_order(self.h, planes), "set_assembly_order")
 
     KERNELS = ("sweep64", "sweep32", "refine", "assemble", "pack", "warm")
 

@@ -80,6 +80,9 @@ def parse_args():
     ap.add_argument("--inner-omega", type=float, default=1.2,
                     help="relaxation factor of the extra form 'extrap_w' (extrap with its FP32 sweeps relaxed by "
                          "this instead of the configured omega 1.8; reported, never the headline)")
+    ap.add_argument("--assembly-order", type=int, default=None, metavar="PLANES",
+                    help="block order of the mixed form's assembly kernels (0 frame by frame, n >= 1 in blocks of "
+                         "n k planes across the frames; default: the library's)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true",
@@ -252,6 +255,8 @@ def run_ours(args, rank, world, dist):
         S.set_warm_start_gate(args.ws_gate if form == "learned_x" else 0)
         S.set_extrapolation(EXTRAP_ORDER if form in ("extrap", "extrap_w", "learned_x") else 0)
         S.set_inner_omega(args.inner_omega if form == "extrap_w" else 0.0)
+        if args.assembly_order is not None:
+            S.set_assembly_order(args.assembly_order)
 
     results = {}
     finals = {}

@@ -134,6 +134,11 @@ ss4d_status ss4d_solver_set_arith(ss4d_solver *s, ss4d_arith arith);
  * in the tile order (>= 1), max_grid caps the persistent grid (0 = as many
  * blocks as fit on the device).  Results do not depend on either. */
 ss4d_status ss4d_solver_set_tiling(ss4d_solver *s, int k_block, int max_grid);
+/* Block order of the mixed form's coefficient assembly (its faces and
+ * coefficient kernels): 0 = frame by frame; planes >= 1 = in blocks of that
+ * many k planes, each block's planes for every frame in turn (default 4).
+ * Results do not depend on it. */
+ss4d_status ss4d_solver_set_assembly_order(ss4d_solver *s, int planes);
 /* Mixed form, segmentation steps: start the solve of step n from an
  * extrapolation in time instead of from u^n.  order 1: u^n + d_{n-1};
  * order 2: u^n + 2 d_{n-1} - d_{n-2}; order 3: u^n + 3 d_{n-1} - 3 d_{n-2}

@@ -102,3 +102,48 @@ def test_inner_omega_changes_only_the_iteration_count(ss4d, oracle, cuda):
     with pytest.raises(ss4d.SS4DError):
         with ss4d.Solver.for_interior(*dims, arith="mixed") as S:
             S.set_inner_omega(2.5)
+
+
+
+@pytest.mark.parametrize("host_arrays", [False, True])
+def test_assembly_order_changes_no_bit(ss4d, cuda, host_arrays):
+    """The mixed form's faces and coefficient kernels may visit the planes
+    frame by frame or in blocks of k planes across the frames: every voxel's
+    arithmetic is the same, so steps must agree bit for bit (with the
+    extrapolated start and the first refinement pass formed by the assembly;
+    on device arrays and through the host-array step, which assembles frame
+    ranges as chunks arrive)."""
+    from test_gpu_parity import _pinned
+
+    torch = cuda
+    nx, ny, nz, nt = 37, 21, 13, 7  # ragged against the 32 x 8 face tiles and every block depth below
+    p = ss4d.scene_params()
+    i0h, u0h = ss4d.scene(1, nx, ny, nz, nt, seed=61)
+    shape = i0h.shape
+    i0 = torch.from_numpy(i0h).cuda()
+    g = [torch.zeros_like(i0) for _ in range(8)]
+    with ss4d.Solver(*shape[::-1], arith="fp64") as S:
+        S.edge_detector(p, i0, None, g)
+    hu, free_u = _pinned(ss4d, shape)
+    hp, free_p = _pinned(ss4d, shape)
+    results = {}
+    try:
+        for order in (0, 1, 3, 5, 14, 100):
+            with ss4d.Solver(*shape[::-1], arith="mixed") as S:  # a fresh extrapolation history each
+                S.set_extrapolation(3)
+                S.set_assembly_order(order)
+                if host_arrays:
+                    hu[...] = u0h
+                    du = torch.zeros_like(i0)
+                    its = [S.seg_time_step_host(p, hu, du, g, h_prev=hp)["iterations"] for _ in range(4)]
+                    results[order] = (hu.copy(), its)
+                else:
+                    u = torch.from_numpy(u0h).cuda()
+                    its = [S.seg_time_step(p, u, None, g)["iterations"] for _ in range(4)]
+                    results[order] = (u.cpu().numpy(), its)
+    finally:
+        free_u(), free_p()
+    want_u, want_its = results[0]
+    for order, (u, its) in results.items():
+        assert its == want_its, (order, its, want_its)
+        assert np.array_equal(u, want_u), order

@@ -588,6 +588,7 @@ struct ss4d_batch {
     int *d_pre, *h_pre; // per volume: the assembly formed the step's first refinement pass
     GridBar *d_bar;     // the persistent loop's grid barrier and its "any volume active" flag
     int persistent;     // run the loop as one persistent launch (default) or as the graph's while loop
+    int withhold_barrier; // test of the timeout path (ss4d_batch_set_test_withhold_barrier)
     int pgrid[2];       // co-resident blocks of k_bsolve<0/1> (0: not yet known)
 };
 
@@ -726,6 +727,14 @@ extern "C" ss4d_status ss4d_batch_set_persistent(ss4d_batch *b, int enable)
     if (!b)
         return bfail(SS4D_ERR_INVALID, "invalid argument: batch is NULL");
     b->persistent = enable ? 1 : 0;
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_batch_set_test_withhold_barrier(ss4d_batch *b, int enable)
+{
+    if (!b)
+        return bfail(SS4D_ERR_INVALID, "invalid argument: batch is NULL");
+    b->withhold_barrier = enable ? 1 : 0;
     return SS4D_OK;
 }
 
@@ -931,6 +940,8 @@ extern "C" ss4d_status ss4d_batch_seg_time_step(ss4d_batch *b, const ss4d_params
         }
         if (b->pgrid[f] > 0) {
             BCK(cudaMemsetAsync(b->d_bar, 0, sizeof(GridBar), b->stream));
+            if (b->withhold_barrier) // the arrival count starts beyond the grid: no arrival completes the barrier
+                BCK(cudaMemsetAsync(&b->d_bar->count, 0x80, sizeof(unsigned), b->stream));
             const BVol *vols = b->d_vols;
             int nv = b->n, mb = guard_max;
             long long total = b->total;

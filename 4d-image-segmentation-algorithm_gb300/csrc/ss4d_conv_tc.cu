@@ -235,7 +235,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_conv_tc(const __grid_constant__ 
                 loads = it + 1;
             };
             bool ok = true;
-            for (int it = 0; it < STAGES - 1 && it < my_n; ++it)
+            // withhold_loads (a test of the timeout path) issues no load:
+            // the first wait below runs out and nothing is left in flight
+            for (int it = 0; it < STAGES - 1 && it < my_n && !a.withhold_loads; ++it)
                 load(it);
             for (int it = 0; it < my_n && ok; ++it) {
                 const int q = it % STAGES, b = it & 1;
@@ -273,7 +275,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_conv_tc(const __grid_constant__ 
                 // the next load goes to the halo stage that tile it-1 read:
                 // wait for its MMAs while this tile's run behind them
                 const int nxt = it + STAGES - 1;
-                if (nxt < my_n) {
+                if (nxt < my_n && !a.withhold_loads) {
                     if (it >= 1 && !mbar_wait(done0 + 8 * ((it - 1) & 1), ((it - 1) >> 1) & 1)) {
                         ok = false;
                         break;

@@ -59,6 +59,7 @@ struct TcArgs {
     int ystride, mstride;
     int relu;
     int *err;                  // set to 1 when a bounded wait ran out
+    int withhold_loads;        // test of the timeout path: issue no halo loads, so every wait runs out
 };
 
 inline long long tc_tiles(int nx, int ny, int nz, int nf)

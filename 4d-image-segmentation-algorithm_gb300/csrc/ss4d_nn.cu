@@ -253,7 +253,8 @@ struct ss4d_wsnet {
     size_t nparam;
     float *p, *g, *m, *v;          // master parameters, gradients, Adam moments (FP32, flat)
     __nv_bfloat16 *wf[4], *wt[4];  // forward / data-gradient weights as tcgen05 B operands (tc::pack_tc)
-    int *err;                      // set by a convolution that gave up a bounded wait
+    int *err;                      // set by a convolution that gave up a bounded wait (reset per forward)
+    int withhold_loads;            // test of the timeout path (ss4d_wsnet_set_test_withhold_loads)
     float *bias[4];                // views into p
     // activations and gradients, sized for `cap` voxels
     size_t cap;
@@ -368,6 +369,26 @@ extern "C" ss4d_status ss4d_wsnet_set_stream(ss4d_wsnet *n, void *stream)
     if (!n)
         return nfail(SS4D_ERR_INVALID, "invalid argument: network is NULL");
     n->stream = (cudaStream_t)stream;
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_wsnet_set_test_withhold_loads(ss4d_wsnet *n, int enable)
+{
+    if (!n)
+        return nfail(SS4D_ERR_INVALID, "invalid argument: network is NULL");
+    n->withhold_loads = enable ? 1 : 0;
+    return SS4D_OK;
+}
+
+extern "C" ss4d_status ss4d_wsnet_check(ss4d_wsnet *n)
+{
+    if (!n)
+        return nfail(SS4D_ERR_INVALID, "invalid argument: network is NULL");
+    int h = 0;
+    NCK(cudaMemcpyAsync(&h, n->err, sizeof(int), cudaMemcpyDeviceToHost, n->stream));
+    NCK(cudaStreamSynchronize(n->stream));
+    if (h)
+        return nfail(SS4D_ERR_TIMEOUT, "a tensor-core convolution gave up a bounded wait; its output was made NaN");
     return SS4D_OK;
 }
 
@@ -489,6 +510,7 @@ static void conv(ss4d_wsnet *n, int cin, int nout, int cout, const __nv_bfloat16
     a.mstride = 32;
     a.relu = relu;
     a.err = n->err;
+    a.withhold_loads = n->withhold_loads;
     if (tc::conv_tc(cin, nout, x, a, n->sm, n->stream) != cudaSuccess)
         n->launch_failed = 1;
 }
@@ -502,6 +524,7 @@ static ss4d_status forward(ss4d_wsnet *n, const __nv_bfloat16 *x0, int nx, int n
     NCK(ensure_act(n, vox, train) == SS4D_OK ? cudaSuccess : cudaErrorMemoryAllocation);
     __nv_bfloat16 *a1 = n->a[0], *a2 = n->a[1], *a3 = train ? n->a[2] : n->a[0];
     n->launch_failed = 0;
+    NCK(cudaMemsetAsync(n->err, 0, sizeof(int), n->stream)); // this forward's waits only
     conv(n, 16, 32, 24, x0, n->wf[0], n->bias[0], nullptr, a1, nullptr, nx, ny, nz, nf, 1);
     conv(n, 32, 32, 24, a1, n->wf[1], n->bias[1], nullptr, a2, nullptr, nx, ny, nz, nf, 1);
     conv(n, 32, 32, 24, a2, n->wf[2], n->bias[2], nullptr, a3, nullptr, nx, ny, nz, nf, 1);

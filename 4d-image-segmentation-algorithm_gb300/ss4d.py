@@ -240,6 +240,7 @@ def lib() -> C.CDLL:
         "ss4d_batch_destroy": ([vp], st),
         "ss4d_batch_set_graph": ([vp, C.c_int], st),
         "ss4d_batch_set_persistent": ([vp, C.c_int], st),
+        "ss4d_batch_set_test_withhold_barrier": ([vp, C.c_int], st),
         "ss4d_batch_set_arith": ([vp, C.c_int], st),
         "ss4d_batch_set_extrapolation": ([vp, C.c_int], st),
         "ss4d_batch_set_shape": ([vp, C.c_int, C.c_int, C.c_int], st),
@@ -254,6 +255,8 @@ def lib() -> C.CDLL:
         "ss4d_wsnet_set_params": ([vp, vp], st),
         "ss4d_wsnet_get_params": ([vp, vp], st),
         "ss4d_wsnet_forward": ([vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp], st),
+        "ss4d_wsnet_check": ([vp], st),
+        "ss4d_wsnet_set_test_withhold_loads": ([vp, C.c_int], st),
         "ss4d_wsnet_train_step": ([vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float,
                                    C.POINTER(C.c_float), vp], st),
         "ss4d_ws_features": ([vp, C.POINTER(Params), vp, P8, vp, vp, dp], st),
@@ -688,6 +691,11 @@ class Batch:
         """the SOR loop as one persistent launch (default) or as the graph's while loop"""
         _check(self.L.ss4d_batch_set_persistent(self.h, 1 if on else 0), "batch_set_persistent")
 
+    def set_test_withhold_barrier(self, on: bool):
+        """test of the timeout path: the persistent loop's grid barrier can
+        never complete, so the next step returns SS4D_ERR_TIMEOUT"""
+        _check(self.L.ss4d_batch_set_test_withhold_barrier(self.h, 1 if on else 0), "batch_set_test_withhold_barrier")
+
     def set_shape(self, v: int, xt: int, k_block: int):
         _check(self.L.ss4d_batch_set_shape(self.h, v, xt, k_block), "batch_set_shape")
 
@@ -792,6 +800,16 @@ class Wsnet:
 
     def forward(self, x0, nx: int, ny: int, nz: int, nf: int, out):
         _check(self.L.ss4d_wsnet_forward(self.h, _ptr(x0), nx, ny, nz, nf, _ptr(out)), "wsnet_forward")
+
+    def check(self):
+        """synchronise; SS4DError (SS4D_ERR_TIMEOUT) if a convolution of the
+        last forward gave up a bounded wait"""
+        _check(self.L.ss4d_wsnet_check(self.h), "wsnet_check")
+
+    def set_test_withhold_loads(self, on: bool):
+        """test of the timeout path: the convolutions issue no loads, so their
+        waits run out and the prediction is NaN"""
+        _check(self.L.ss4d_wsnet_set_test_withhold_loads(self.h, 1 if on else 0), "wsnet_set_test_withhold_loads")
 
     def train_step(self, x0, target, nx: int, ny: int, nz: int, nf: int, margin: int = 0, lr: float = 1e-3,
                    grad=None) -> float:

@@ -396,6 +396,12 @@ ss4d_status ss4d_batch_set_graph(ss4d_batch *b, int enable);
  * while loop (or host-driven, with ss4d_batch_set_graph(b, 0)).  Results do
  * not depend on it except through the residual's summation order. */
 ss4d_status ss4d_batch_set_persistent(ss4d_batch *b, int enable);
+/* Test of the timeout path, no fault: with enable the persistent loop's grid
+ * barrier starts with its arrival count beyond the grid, so no arrival
+ * completes it; every block's first wait runs out after about a second and
+ * the step returns SS4D_ERR_TIMEOUT with the context usable.  The volumes'
+ * states after such a step are undefined. */
+ss4d_status ss4d_batch_set_test_withhold_barrier(ss4d_batch *b, int enable);
 /* Arithmetic form of the batched steps: SS4D_ARITH_FP64 (the default) or
  * SS4D_ARITH_MIXED, each volume as ss4d_seg_time_step does it in that form
  * (mixed: float-float assembly, FP32 correction sweeps, FP64 refinement and
@@ -442,8 +448,17 @@ ss4d_status ss4d_wsnet_set_stream(ss4d_wsnet *n, void *stream);
 ss4d_status ss4d_wsnet_init(ss4d_wsnet *n, uint64_t seed);
 ss4d_status ss4d_wsnet_set_params(ss4d_wsnet *n, const float *h_params);
 ss4d_status ss4d_wsnet_get_params(ss4d_wsnet *n, float *h_params);
-/* prediction [F][nz][ny][nx] FP32 */
+/* prediction [F][nz][ny][nx] FP32; asynchronous on the network's stream.  A
+ * convolution whose bounded wait (about a second) gave up makes the whole
+ * prediction NaN, which the warm start's check discards. */
 ss4d_status ss4d_wsnet_forward(ss4d_wsnet *n, const void *d_x0, int nx, int ny, int nz, int nf, float *d_out);
+/* Synchronise the network's stream; SS4D_ERR_TIMEOUT if a convolution of the
+ * last forward (and any backward after it) gave up a wait, else SS4D_OK. */
+ss4d_status ss4d_wsnet_check(ss4d_wsnet *n);
+/* Test of the timeout path, no fault: with enable the convolutions issue no
+ * halo loads, so each one's waits run out after about a second and its
+ * output is made NaN. */
+ss4d_status ss4d_wsnet_set_test_withhold_loads(ss4d_wsnet *n, int enable);
 /* one Adam step on a batch of crops (frames F of nx*ny*nz voxels): mean
  * squared error against d_target over voxels at least `margin` from a crop's
  * border; lr == 0 only evaluates; d_grad (may be NULL) gets the gradient. */

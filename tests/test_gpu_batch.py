@@ -163,3 +163,37 @@ def test_batch_with_minimal_and_ragged_volumes(ss4d, oracle, cuda, arith):
     for v in range(len(sizes)):
         assert [got[0][v], got[1][v]] == want[v][0], v
         assert np.array_equal(us[v].cpu().numpy(), want[v][1]), v
+
+
+@pytest.mark.parametrize("arith", ["fp64", "mixed"])
+def test_grid_barrier_timeout_is_reported(ss4d, oracle, cuda, arith):
+    """Failure detection without a fault: a grid barrier that no arrival can
+    complete (its arrival count starts beyond the grid) makes every block of
+    the persistent loop give up its wait after about a second; the step
+    returns SS4D_ERR_TIMEOUT, the context stays usable, and the same handle's
+    next step from fresh inputs equals a fresh handle's step bit for bit."""
+    torch = cuda
+    sizes = [(20, 16, 12, 5), (12, 24, 10, 3)]
+    vols = _volumes(ss4d, oracle, sizes, seed=9)
+    params = [p for p, _, _ in vols]
+    gs = [[_dev(torch, a) for a in g] for _, _, g in vols]
+    dims = [(d[0] + 2, d[1] + 2, d[2] + 2, d[3] + 2) for d in sizes]
+    with ss4d.Batch(dims) as B:
+        if arith == "mixed":
+            B.set_arith("mixed")
+        B.set_test_withhold_barrier(True)
+        us = [_dev(torch, u0) for _, u0, _ in vols]
+        with pytest.raises(ss4d.SS4DError) as ei:
+            B.seg_time_step(params, us, gs)
+        assert ei.value.status == 5  # SS4D_ERR_TIMEOUT
+        B.set_test_withhold_barrier(False)
+        us = [_dev(torch, u0) for _, u0, _ in vols]
+        got = [s["iterations"] for s in B.seg_time_step(params, us, gs)]
+    with ss4d.Batch(dims) as F:
+        if arith == "mixed":
+            F.set_arith("mixed")
+        ref = [_dev(torch, u0) for _, u0, _ in vols]
+        want = [s["iterations"] for s in F.seg_time_step(params, ref, gs)]
+    assert got == want
+    for v in range(len(sizes)):
+        assert np.array_equal(us[v].cpu().numpy(), ref[v].cpu().numpy()), v

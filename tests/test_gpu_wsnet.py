@@ -282,3 +282,30 @@ def test_extrapolated_start_meets_the_fp64_tolerance(ss4d, oracle, cuda, graph):
         assert all(st["status"] == 0 and st["residual"] <= p.gsTol for st in cs + xs)
         assert sum(st["iterations"] for st in xs[1:]) < sum(st["iterations"] for st in cs[1:])
         assert rel_err(xu[-1], cu[-1]) <= 1e-4
+
+
+def test_convolution_wait_timeout_is_reported(ss4d, cuda, net):
+    """Failure detection without a fault: with its halo loads withheld, every
+    tensor-core convolution's waits run out after about a second; the
+    prediction is NaN (which the warm start's check discards), the network
+    reports SS4D_ERR_TIMEOUT, and the next forward is exact again."""
+    torch = cuda
+    nf, nz, ny, nx = 1, 4, 16, 16
+    rng = np.random.default_rng(13)
+    xd, _ = random_features(torch, rng, nf, nz, ny, nx)
+    good = torch.full((nf, nz, ny, nx), float("nan"), dtype=torch.float32, device="cuda")
+    net.forward(xd, nx, ny, nz, nf, good)
+    net.check()
+    out = torch.zeros_like(good)
+    net.set_test_withhold_loads(True)
+    try:
+        net.forward(xd, nx, ny, nz, nf, out)
+        with pytest.raises(ss4d.SS4DError) as ei:
+            net.check()
+        assert ei.value.status == 5  # SS4D_ERR_TIMEOUT
+        assert torch.isnan(out).all()
+    finally:
+        net.set_test_withhold_loads(False)
+    net.forward(xd, nx, ny, nz, nf, out)
+    net.check()
+    assert torch.equal(out, good)

@@ -136,11 +136,10 @@ __device__ __forceinline__ ff cdiff(const float2 *__restrict__ fa, unsigned x, u
 }
 
 // the face between v and v + e_D: Dv, Dn the central differences at v and
-// v + e_D along the axes a != D, cn = F_D(v), gv its g; writes
-// fn = |grad u|_eps and fq = g / |grad u|_eps at v
+// v + e_D along the axes a != D, cn = F_D(v), gv its g; gives
+// r = |grad u|_eps and q = g / |grad u|_eps
 template <int D>
-__device__ __forceinline__ void face_ff(const FFConst &K, const ff Dv[4], const ff Dn[4], ff cn, ff gv,
-                                        const SplitBufs &b, unsigned o)
+__device__ __forceinline__ void face_val(const FFConst &K, const ff Dv[4], const ff Dn[4], ff cn, ff gv, ff &r, ff &q)
 {
     ff tt = ff_make(0.f, 0.f); // sum of squares: positive terms, renormalised once
 #pragma unroll
@@ -157,7 +156,17 @@ __device__ __forceinline__ void face_ff(const FFConst &K, const ff Dv[4], const 
     const ff a2 = K.pow2 ? ff_make(tt.h * K.iq2h, tt.l * K.iq2h) : ff_mul(tt, ff_make(K.iq2h, K.iq2l));
     const ff s2 = ff_add(ff_add_nr(a1, a2), ff_make(K.eps2h, K.eps2l));
     const ff y = ff_rsqrt(s2);
-    const ff r = ff_mul(s2, y), q = ff_mul(gv, y);
+    r = ff_mul(s2, y);
+    q = ff_mul(gv, y);
+}
+
+// face_val, written as fn and fq at v
+template <int D>
+__device__ __forceinline__ void face_ff(const FFConst &K, const ff Dv[4], const ff Dn[4], ff cn, ff gv,
+                                        const SplitBufs &b, unsigned o)
+{
+    ff r, q;
+    face_val<D>(K, Dv, Dn, cn, gv, r, q);
     __stcs(reinterpret_cast<float2 *>(b.fn[D]) + o, make_float2(r.h, r.l));
     __stcs(reinterpret_cast<float2 *>(b.fq[D]) + o, make_float2(q.h, q.l));
 }
@@ -295,26 +304,17 @@ __global__ void __launch_bounds__(FTX *FTY, 8) k_faces_ff(Geo g, CPtrs8 gin, int
 // coefficients just written with the other colour's u in record order, then
 // diag u0, with the same fused multiply-adds) on the split copies of u whose
 // start correction the first-difference kernel added, into rpre.
+// The records of interior voxel (i, j, k, l) (and with PRE the first pass's
+// residual) from its 8 faces: fp[d], fm[d] the |grad u|_eps of its faces
+// towards v + e_d and v - e_d, q[2d], q[2d+1] their g / |grad u|_eps
 template <int PRE>
-__global__ void __launch_bounds__(256, PRE ? 6 : 8) k_voxel_coef_ff(Geo g, Split sp, FFConst K, SplitBufs b, int l_off,
-                                                                    int kblock)
+__device__ __forceinline__ void voxel_coef(const Geo &g, const Split &sp, const FFConst &K, const SplitBufs &b, int i,
+                                           int j, int k, int l, const ff fp[4], const ff fm[4], const ff q[8])
 {
-    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    int kk, lf;
-    plane_frame(blockIdx.z, g.nz, gridDim.z / g.nz, kblock, kk, lf);
-    const int k = 1 + kk, l = 1 + l_off + lf;
-    if (i > g.nx || j > g.ny)
-        return;
-    const long long o = nat_index(g, i, j, k, l);
-    const long long st[4] = {1, g.sy, g.sz, g.sw};
-    ff q[8], sum = ff_make(0.f, 0.f);
+    ff sum = ff_make(0.f, 0.f);
 #pragma unroll
-    for (int d = 0; d < 4; ++d) { // positive terms: renormalised once
-        sum = ff_add_nr(sum, ff_add_nr(ld_ff(b.fn[d], o), ld_ff(b.fn[d], o - st[d])));
-        q[2 * d] = ld_ff(b.fq[d], o);
-        q[2 * d + 1] = ld_ff(b.fq[d], o - st[d]);
-    }
+    for (int d = 0; d < 4; ++d) // positive terms: renormalised once
+        sum = ff_add_nr(sum, ff_add_nr(fp[d], fm[d]));
     sum = ff_norm(sum);
     // mean^2 + eps2 with mean = sum / 8 (exact scaling)
     const ff m = ff_make(sum.h * 0.125f, sum.l * 0.125f);
@@ -353,6 +353,30 @@ __global__ void __launch_bounds__(256, PRE ? 6 : 8) k_voxel_coef_ff(Geo g, Split
     float4 *f4 = reinterpret_cast<float4 *>(cf32 + 8 * t);
     __stcs(f4, make_float4(a32[0], a32[1], a32[2], a32[3]));
     __stcs(f4 + 1, make_float4(a32[4], a32[5], a32[6], a32[7]));
+}
+
+template <int PRE>
+__global__ void __launch_bounds__(256, PRE ? 6 : 8) k_voxel_coef_ff(Geo g, Split sp, FFConst K, SplitBufs b, int l_off,
+                                                                    int kblock)
+{
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    int kk, lf;
+    plane_frame(blockIdx.z, g.nz, gridDim.z / g.nz, kblock, kk, lf);
+    const int k = 1 + kk, l = 1 + l_off + lf;
+    if (i > g.nx || j > g.ny)
+        return;
+    const long long o = nat_index(g, i, j, k, l);
+    const long long st[4] = {1, g.sy, g.sz, g.sw};
+    ff fp[4], fm[4], q[8];
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+        fp[d] = ld_ff(b.fn[d], o);
+        fm[d] = ld_ff(b.fn[d], o - st[d]);
+        q[2 * d] = ld_ff(b.fq[d], o);
+        q[2 * d + 1] = ld_ff(b.fq[d], o - st[d]);
+    }
+    voxel_coef<PRE>(g, sp, K, b, i, j, k, l, fp, fm, q);
 }
 
 static void split_host(double v, float &h, float &l)
@@ -401,8 +425,7 @@ void launch_assemble_ff_faces(const Geo &g, const Split &s, CPtrs8 gin, int has_
     launch_assemble_ff_faces_range(g, s, gin, has_g, p, b, 0, g.nt + 1, 1, g.nt + 1, st, pre, kblock);
 }
 
-void launch_assemble_ff_faces_range(const Geo &g, const Split &s, CPtrs8 gin, int has_g, const ss4d_params &p,
-                                    SplitBufs b, int f0, int f1, int v0, int v1, cudaStream_t st, int pre, int kblock)
+static FFConst make_ffconst(const ss4d_params &p)
 {
     FFConst K;
     split_host(1.0 / (p.h * p.h), K.ih2h, K.ih2l);
@@ -411,6 +434,13 @@ void launch_assemble_ff_faces_range(const Geo &g, const Split &s, CPtrs8 gin, in
     split_host(p.tau / (p.h * p.h), K.ch, K.cl);
     int e1 = 0, e2 = 0;
     K.pow2 = K.ih2l == 0.f && K.iq2l == 0.f && frexp((double)K.ih2h, &e1) == 0.5 && frexp((double)K.iq2h, &e2) == 0.5;
+    return K;
+}
+
+void launch_assemble_ff_faces_range(const Geo &g, const Split &s, CPtrs8 gin, int has_g, const ss4d_params &p,
+                                    SplitBufs b, int f0, int f1, int v0, int v1, cudaStream_t st, int pre, int kblock)
+{
+    const FFConst K = make_ffconst(p);
     if (f1 > f0) {
         dim3 gr((g.nx + FTX - 1) / FTX, (g.ny + FTY - 1) / FTY, (g.nz + 1) * (f1 - f0));
         k_faces_ff<<<gr, dim3(FTX, FTY, 1), 0, st>>>(g, gin, has_g, K, b, f0, kblock);

@@ -97,6 +97,10 @@ def parse_args():
                          "voxel-updates/s; not the headline metric); conv: the warm-start network's forward "
                          "(four tensor-core convolutions) on random features of --size (reports TFLOP/s; for "
                          "profiling)")
+    ap.add_argument("--batch-config", choices=["16x_64-192", "48x_24-48"], default="16x_64-192",
+                    help="batch workload: the configuration's 16 volumes, or 48 small ones")
+    ap.add_argument("--batch-sequential", action="store_true",
+                    help="batch workload: also time the same volumes solved one after another")
     ap.add_argument("--batch-loop", choices=["persistent", "graph"], default="persistent",
                     help="batch workload: the SOR loop of all volumes as one persistent launch (default) or as a "
                          "CUDA graph's while loop of per-phase kernels")
@@ -768,26 +772,38 @@ def run_reference(args):
 
 
 def run_batch(args):
-    print(json.dumps(batch_line(args, args.steps, args.warmup, args.forms)))
+    print(json.dumps(batch_line(args, args.steps, args.warmup, args.forms, config=args.batch_config,
+                                sequential=args.batch_sequential)))
 
 
-def batch_line(args, steps, warmup, forms_arg):
-    """16 independent volumes, sizes U[64..192] x U[64..192] x U[48..96] x
-    U[8..24] per axis, single-ellipsoid scenes with per-volume K in
-    [500, 2000] and tau in [0.25, 1], stepped together (one persistent launch
-    per loop kernel, per-volume convergence, autotuned tile shapes), in the
-    forms of --forms among fp64, mixed and extrap (mixed with the cubic
-    extrapolated start), each from the same start; `value` is the FP64 form's
-    (or the first form's) aggregate voxel-updates/s, every form's numbers are
-    in `forms`."""
+BATCH_CONFIGS = {
+    # the configuration's batch: volumes that each fill the GPU on their own
+    "16x_64-192": (16, (64, 193), (64, 193), (48, 97), (8, 25)),
+    # many small volumes, where one volume alone leaves the GPU idle
+    "48x_24-48": (48, (24, 49), (24, 49), (24, 49), (4, 9)),
+}
+
+
+def batch_line(args, steps, warmup, forms_arg, config="16x_64-192", sequential=False):
+    """Independent volumes (BATCH_CONFIGS: 16 of U[64..192] x U[64..192] x
+    U[48..96] x U[8..24] per axis by default), single-ellipsoid scenes with
+    per-volume K in [500, 2000] and tau in [0.25, 1], stepped together (the
+    SOR loop of all volumes in one persistent launch, per-volume convergence,
+    autotuned tile shapes), in the forms of --forms among fp64, mixed and
+    extrap (mixed with the cubic extrapolated start), each from the same
+    start; `value` is the FP64 form's (or the first form's) aggregate
+    voxel-updates/s, every form's numbers are in `forms`.  With sequential,
+    each form is also timed with the same volumes solved one after another
+    by single-volume handles (same steps, same stream)."""
     import numpy as np
     import torch
 
     import ss4d
 
     rng = np.random.default_rng(args.seed)
-    sizes = [(int(rng.integers(64, 193)), int(rng.integers(64, 193)), int(rng.integers(48, 97)),
-              int(rng.integers(8, 25))) for _ in range(16)]
+    nvol, rx, ry, rz, rt = BATCH_CONFIGS[config]
+    sizes = [(int(rng.integers(*rx)), int(rng.integers(*ry)), int(rng.integers(*rz)), int(rng.integers(*rt)))
+             for _ in range(nvol)]
     dev = torch.device("cuda", 0)
     params, u0s, gs = [], [], []
     for v, (nx, ny, nz, nt) in enumerate(sizes):
@@ -840,14 +856,38 @@ def batch_line(args, steps, warmup, forms_arg):
                          "max_residual": max(s["residual"] for step in stats for s in step),
                          "tolerance_met": all(s["residual"] <= p.gsTol or s["iterations"] >= p.maxNoGSIteration
                                               for step in stats for s, p in zip(step, params))}
+        if sequential:
+            us = [u.clone() for u in u0s]
+            handles = [ss4d.Solver(*d, arith="fp64" if form == "fp64" else "mixed", stream=stream.cuda_stream)
+                       for d in dims]
+            for S in handles:
+                S.set_extrapolation(EXTRAP_ORDER if form == "extrap" else 0)
+            for _ in range(warmup):
+                for v, S in enumerate(handles):
+                    S.seg_time_step(params[v], us[v], None, gs[v])
+            torch.cuda.synchronize(dev)
+            e0.record(stream)
+            seq = [[S.seg_time_step(params[v], us[v], None, gs[v])["iterations"] for v, S in enumerate(handles)]
+                   for _ in range(steps)]
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            ms_seq = e0.elapsed_time(e1) / steps
+            for S in handles:
+                S.close()
+            results[form]["sequential"] = {
+                "ms_per_step": ms_seq, "batch_speedup": ms_seq / results[form]["ms_per_step"],
+                "same_iterations": seq == its,
+                "how": "the same volumes from the same start, one single-volume handle each, solved one after "
+                       "another on the same stream"}
     head = "fp64" if "fp64" in results else forms[0]
     r = results[head]
-    line = {"metric": "aggregate voxel-updates/s, 16 uneven volumes (batched, one launch per solve)",
+    line = {"metric": f"aggregate voxel-updates/s, {nvol} uneven volumes (batched, one launch per solve)",
             "value": r["voxel_updates_per_s"], "unit": "voxel-updates/s", "n_gpus": 1, "steps": steps,
             "warmup": warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
             "dtype": "f64", "data": "synthetic", "impl": "ours",
-            "config": {"workload": "16 volumes U[64..192]x U[64..192]x U[48..96]x U[8..24], kind-1 "
-                                   "scenes, K~U[500,2000], tau~U[0.25,1], gsTol 1e-6", "form": head,
+            "config": {"workload": f"{nvol} volumes U[{rx[0]}..{rx[1] - 1}]x U[{ry[0]}..{ry[1] - 1}]x "
+                                   f"U[{rz[0]}..{rz[1] - 1}]x U[{rt[0]}..{rt[1] - 1}], kind-1 scenes, K~U[500,2000], "
+                                   "tau~U[0.25,1], gsTol 1e-6", "form": head,
                        "loop": args.batch_loop,
                        "sizes": sizes, "voxels": sum(vox)},
             "autotuned_shapes": shapes, "iterations_per_volume": r["iterations_per_volume"],
@@ -970,11 +1010,14 @@ def main():
     if rank == 0 and world == 1 and not args.no_batch:
         # the batched workload, short: per-volume iteration counts of the last
         # step only (the full record is `--workload batch`)
-        b = batch_line(args, 10, 3, "fp64,extrap")
-        for f in b["forms"].values():
-            f["iterations_last_step"] = f.pop("iterations_per_volume")[-1]
-            f.pop("refinements_per_volume", None)
-        b.pop("iterations_per_volume", None)
+        b = batch_line(args, 10, 3, "fp64,extrap", sequential=True)
+        small = batch_line(args, 10, 3, "fp64,extrap", config="48x_24-48", sequential=True)
+        for bl in (b, small):
+            for f in bl["forms"].values():
+                f["iterations_last_step"] = f.pop("iterations_per_volume")[-1]
+                f.pop("refinements_per_volume", None)
+            bl.pop("iterations_per_volume", None)
+        b["small_volumes"] = small
         line["batch"] = b
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args, ctx[6])

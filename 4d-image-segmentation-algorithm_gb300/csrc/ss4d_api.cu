@@ -317,7 +317,7 @@ extern "C" ss4d_status ss4d_solver_destroy(ss4d_solver *s)
     free_graphs(s);
     // allocation bases only: R[1], Bk, P[1], coef[1], ... point inside them
     void *dev[] = {s->d_partial, s->d_scalar, s->d_state, s->d_params, s->d_scratch, s->d_coef_nat,
-                   s->sb.R[0], s->sb.P[0], s->sb.coef[0], s->sb.coef32[0], s->sb.dR[0], s->sb.r32[0], s->sb.fn[0],
+                   s->sb.R[0], s->sb.P[0], s->sb.coef[0], s->sb.coefq[0], s->sb.dR[0], s->sb.r32[0], s->sb.fn[0],
                    s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz, s->ws_x0, s->ws_y,
                    s->hist[0], s->hist[1], s->hist[2], s->hist[3], s->sb.fd[0], s->d_ff};
     for (void *p : dev)
@@ -469,14 +469,17 @@ static ss4d_status ensure_split(ss4d_solver *s, int mixed)
     }
     if (mixed && !s->have_mixed) {
         float *c32 = nullptr, *d3 = nullptr, *r2 = nullptr;
-        CKS(dmalloc(s, (void **)&c32, sizeof(float) * 16 * s->sp.ct));
+        // per colour: ct 16-byte fraction records, then (after both) ct scales
+        CKS(dmalloc(s, (void **)&c32, sizeof(float) * 10 * s->sp.ct));
         CKS(dmalloc(s, (void **)&d3, sizeof(float) * 3 * cs));
         CKS(dmalloc(s, (void **)&r2, sizeof(float) * 2 * cs));
-        CK(cudaMemsetAsync(c32, 0, sizeof(float) * 16 * s->sp.ct, s->stream));
+        CK(cudaMemsetAsync(c32, 0, sizeof(float) * 10 * s->sp.ct, s->stream));
         CK(cudaMemsetAsync(d3, 0, sizeof(float) * 3 * cs, s->stream));
         CK(cudaMemsetAsync(r2, 0, sizeof(float) * 2 * cs, s->stream));
-        s->sb.coef32[0] = c32;
-        s->sb.coef32[1] = c32 + 8 * s->sp.ct;
+        s->sb.coefq[0] = reinterpret_cast<uint4 *>(c32);
+        s->sb.coefq[1] = reinterpret_cast<uint4 *>(c32 + 4 * s->sp.ct);
+        s->sb.coefs[0] = c32 + 8 * s->sp.ct;
+        s->sb.coefs[1] = c32 + 9 * s->sp.ct;
         s->sb.dR[0] = d3;
         s->sb.dR[1] = d3 + cs;
         s->sb.dB = d3 + 2 * cs;

@@ -22,7 +22,8 @@
 //                     s2 = |grad u|^2 + eps2, fn = s2 / sqrt(s2), fq = g / sqrt(s2);
 //   k_voxel_coef_ff:  vc = sqrt(mean(fn)^2 + eps2), c a_f = c vc fq_f,
 //                     diag = 1 + sum c a_f; written as FP64 records
-//                     (refinement) and FP32 records (sweeps).
+//                     (refinement) and the FP32 sweeps' records (16-bit
+//                     fractions of sum c a_f and that sum, store_coef16).
 //
 // Relative error of the coefficients: below 1e-12 (1/sqrt from an FP32 seed
 // and one Newton step, about 1.5 (2^-22)^2 each; sums and products to 2^-46).  The mixed form's refinement passes measure the FP64 residual
@@ -322,7 +323,6 @@ __device__ __forceinline__ void voxel_coef(const Geo &g, const Split &sp, const 
     const ff cv = ff_mul(ff_make(K.ch, K.cl), ff_mul(x, ff_rsqrt(x))); // c * vc
     const int col = (i + j + k + l) & 1;
     double *cf = pick(b.coef, col);
-    float *cf32 = pick(b.coef32, col);
     const long long t = coef_index(g, sp, i, j, k, l);
     // split index of the target and its neighbours (row phase p = i & 1)
     const long long Hy = sp.Hs, Hz = Hy * g.jM, Hw = Hz * g.kM;
@@ -350,9 +350,7 @@ __device__ __forceinline__ void voxel_coef(const Geo &g, const Split &sp, const 
         pick(b.rpre, col)[sx] = fma(dd, __ldg((col == 0 ? b.R[0] : b.Bk) + sx), -S);
     // component 9 (omega/diag) serves only the FP64 sweep, whose form always
     // assembles its own records: not written here
-    float4 *f4 = reinterpret_cast<float4 *>(cf32 + 8 * t);
-    __stcs(f4, make_float4(a32[0], a32[1], a32[2], a32[3]));
-    __stcs(f4 + 1, make_float4(a32[4], a32[5], a32[6], a32[7]));
+    store_coef16(pick(b.coefq, col), pick(b.coefs, col), t, a32);
 }
 
 template <int PRE>

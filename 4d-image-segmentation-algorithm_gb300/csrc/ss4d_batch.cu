@@ -338,8 +338,8 @@ __device__ __forceinline__ void bsweep32(const BVol *__restrict__ vols, int nv, 
                 oth = ds ? V.b.dR[1] : V.b.dR[0];
             }
             const long long Hy = sp.Hs, Hz = Hy * g.jM, Hw = Hz * g.kM;
-            const Sweep32Out o = sweep32_target(g, sp, tc, p, s, Hy, Hz, Hw, src, oth, V.b.coef32[COL],
-                                                V.b.r32[COL], (float)par[v].omega);
+            const Sweep32Out o = sweep32_target(g, sp, tc, p, s, Hy, Hz, Hw, src, oth, V.b.coefq[COL],
+                                                V.b.coefs[COL], V.b.r32[COL], (float)par[v].omega);
             acc = fmaf(o.r, o.r, acc);
             dst[s] = o.u;
         },

@@ -109,7 +109,12 @@ struct SplitBufs {
     double *P[2];       // prev (per colour)
     double *coef[2];    // per colour, record t (coef_at(t, f, 10)): f < 8: c*a_f (f = e,w,n,s,t,b,fw,bw),
                         // f = 8: diag, f = 9: omega/diag;  10 * ct doubles
-    float *coef32[2];   // per colour, [8 t + f] = c*a_f in FP32 (mixed form);  8 * ct floats
+    // mixed form, records of the FP32 sweeps, per colour and target t: the
+    // scale s = sum_f c*a_f (coefs[t], FP32) and the fractions c*a_f / s as
+    // eight 16-bit fixed-point numbers (coefq[t], faces in record order);
+    // 20 bytes per target (store_coef16 / load_coef16 in ss4d_sweep.cuh)
+    uint4 *coefq[2];
+    float *coefs[2];
     float *dR[2];       // mixed: red correction, ping-pong
     float *dB;          // mixed: black correction
     float *r32[2];      // mixed: FP64 residual rounded to FP32, per colour

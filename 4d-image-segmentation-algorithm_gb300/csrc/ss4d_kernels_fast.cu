@@ -4,7 +4,8 @@
 // rows (l,k,j) x Hs columns (see Split in ss4d_common.cuh), so a half-sweep
 // streams only the coefficients of its own colour and every warp load is a
 // contiguous run.  The coefficients of a voxel (FP64: 32 records per
-// component-major block, see coef_at; FP32: one interleaved 32-byte record)
+// component-major block, see coef_at; the FP32 sweeps: a 16-byte record of
+// fixed-point fractions and an FP32 scale, see store_coef16 in ss4d_sweep.cuh)
 // are c*a_f for the 8 faces (+x,-x,+y,-y,+z,-z,+w,-w = e,w,n,s,t,b,fw,bw),
 // the diagonal 1 + c*sum a_f and omega/diagonal (c = tau/h^2), so one update is
 //     r = diag*u - sum (c a_f) u_f - prev,   u <- u - (omega/diag) r
@@ -58,9 +59,10 @@ __device__ __forceinline__ double rcp_nr(double x)
 }
 
 // Coefficient record t of one voxel (layout: coef_at in ss4d_common.cuh):
-// FP64 [c a_0..c a_7, diag, omega/diag] and FP32 [c a_0..c a_7].
-__device__ __forceinline__ void store_coef(double *cf, float *cf32, long long t, const double ac[8], double diag,
-                                           double winv, int want32)
+// FP64 [c a_0..c a_7, diag, omega/diag] and, with want32, the FP32 sweeps'
+// compressed record (store_coef16).
+__device__ __forceinline__ void store_coef(double *cf, uint4 *cq, float *cs, long long t, const double ac[8],
+                                           double diag, double winv, int want32)
 {
 #pragma unroll
     for (int f = 0; f < 8; ++f)
@@ -68,11 +70,11 @@ __device__ __forceinline__ void store_coef(double *cf, float *cf32, long long t,
     __stcs(cf + coef_at(t, 8, 10), diag);
     __stcs(cf + coef_at(t, 9, 10), winv);
     if (want32) {
-        // FP32 records stay interleaved (32 B per target, two 16-byte loads):
-        // the FP32 sweep issues fewer, wider loads that way
-        float4 *f4 = reinterpret_cast<float4 *>(cf32 + 8 * t);
-        __stcs(f4, make_float4(d2f_bits(ac[0]), d2f_bits(ac[1]), d2f_bits(ac[2]), d2f_bits(ac[3])));
-        __stcs(f4 + 1, make_float4(d2f_bits(ac[4]), d2f_bits(ac[5]), d2f_bits(ac[6]), d2f_bits(ac[7])));
+        float a[8];
+#pragma unroll
+        for (int f = 0; f < 8; ++f)
+            a[f] = d2f_bits(ac[f]);
+        store_coef16(cq, cs, t, a);
     }
 }
 
@@ -146,18 +148,18 @@ __global__ void __launch_bounds__(256) k_voxel_coef(Geo g, Split sp, double eps2
     const double cv = c * (x * rsqrt_nr(x));           // c * vc
     const int col = (i + j + k + l) & 1;
     double *cf = pick(b.coef, col);
-    float *cf32 = pick(b.coef32, col);
     double ac[8], diag = 1.0;
 #pragma unroll
     for (int f = 0; f < 8; ++f) {
         ac[f] = cv * q[f];
         diag += ac[f];
     }
-    store_coef(cf, cf32, coef_index(g, sp, i, j, k, l), ac, diag, omega * rcp_nr(diag), want32);
+    store_coef(cf, pick(b.coefq, col), pick(b.coefs, col), coef_index(g, sp, i, j, k, l), ac, diag,
+               omega * rcp_nr(diag), want32);
 }
 
 // given natural coefficient arrays e..bw (the reference's layout) -> split
-// FP64 c*a_f, diagonal, omega/diagonal (+ FP32 c*a_f)
+// FP64 c*a_f, diagonal, omega/diagonal (+ the FP32 sweeps' records)
 __global__ void __launch_bounds__(256) k_pack_coef(Geo g, Split sp, CPtrs8 a, double c, double omega, SplitBufs b,
                                                    int want32)
 {
@@ -169,14 +171,14 @@ __global__ void __launch_bounds__(256) k_pack_coef(Geo g, Split sp, CPtrs8 a, do
     const long long o = nat_index(g, i, j, k, l);
     const int col = (i + j + k + l) & 1;
     double *cf = pick(b.coef, col);
-    float *cf32 = pick(b.coef32, col);
     double ac[8], diag = 1.0;
 #pragma unroll
     for (int f = 0; f < 8; ++f) {
         ac[f] = c * a.p[f][o];
         diag += ac[f];
     }
-    store_coef(cf, cf32, coef_index(g, sp, i, j, k, l), ac, diag, omega / diag, want32);
+    store_coef(cf, pick(b.coefq, col), pick(b.coefs, col), coef_index(g, sp, i, j, k, l), ac, diag, omega / diag,
+               want32);
 }
 
 // natural -> split copies of u (both red buffers and black, ghosts
@@ -464,7 +466,8 @@ __global__ void __launch_bounds__(256) k_sweep32(Geo g, Split sp, SweepCfg cfg, 
         dst = b.dB;
         oth = pick(b.dR, ds);
     }
-    const float *__restrict__ cf = b.coef32[COL];
+    const uint4 *__restrict__ cq = b.coefq[COL];
+    const float *__restrict__ cs = b.coefs[COL];
     const float *__restrict__ rhs = b.r32[COL];
     const float omega = (float)dp->omega;
     const long long Hy = sp.Hs, Hz = Hy * g.jM, Hw = Hz * g.kM;
@@ -479,7 +482,7 @@ __global__ void __launch_bounds__(256) k_sweep32(Geo g, Split sp, SweepCfg cfg, 
         if (i > g.nx)
             continue;
         const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * Hy + tc.xi + sp.A;
-        const Sweep32Out o = sweep32_target(g, sp, tc, p, s, Hy, Hz, Hw, src, oth, cf, rhs, omega);
+        const Sweep32Out o = sweep32_target(g, sp, tc, p, s, Hy, Hz, Hw, src, oth, cq, cs, rhs, omega);
         acc = fmaf(o.r, o.r, acc);
         dst[s] = o.u;
     }

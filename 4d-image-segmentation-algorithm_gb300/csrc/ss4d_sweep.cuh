@@ -179,33 +179,94 @@ __device__ __forceinline__ RefineOut refine_target(const Geo &g, const Split &sp
     return RefineOut{fma(diag, u0, -S), u0};
 }
 
-// One FP32 SOR update of the correction at a target (diag = 1 + sum c a_f,
-// formed from the record): returns the pre-update residual of the correction
-// equation and the updated value, which the caller stores.
+// Records of the FP32 correction sweeps.  The sweeps stream their records
+// once per half-sweep and are bound by HBM, so a record is compressed: per
+// target the scale s = sum_f c a_f in FP32 and the eight fractions
+// w_f = c a_f / s in [0, 1] as 16-bit fixed-point numbers q_f (w_f = q_f /
+// 2^16 rounded to nearest, 65535 at most): 20 bytes instead of 32 for eight
+// FP32 values.  A sweep uses c a_f = s q_f / 2^16 and the diagonal
+// 1 + s sum_f q_f / 2^16, so every row keeps the FP64 operator's structure
+// diag - sum_f c a_f = 1: the rounding only moves weight between the target
+// and its neighbours, and changes A d by sum_f da_f (d - d_f) with |da_f| <=
+// 2^-17 s, small where the correction d is smooth.  The FP64 refinement
+// measures the residual with the FP64 records, so the stop rule and the
+// tolerance are those of the FP64 operator.
+__device__ __forceinline__ void store_coef16(uint4 *__restrict__ cq, float *__restrict__ cs, long long t,
+                                             const float a[8])
+{
+    const float s = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+    // the scale of the rounding need not be exact: a sweep forms its
+    // diagonal from the stored fractions themselves
+    const float k = s > 0.f ? __fdividef(65536.f, s) : 0.f;
+    unsigned q[8];
+#pragma unroll
+    for (int f = 0; f < 8; ++f)
+        q[f] = min(__float2uint_rn(a[f] * k), 65535u);
+    __stcs(cq + t, make_uint4(q[0] | (q[1] << 16), q[2] | (q[3] << 16), q[4] | (q[5] << 16), q[6] | (q[7] << 16)));
+    __stcs(cs + t, s);
+}
+
+// q / 2^16 for the low / high 16 bits of x, exactly: the bits under the
+// exponent of 2^23 give 2^23 + q, and (2^23 + q) 2^-16 - 128 rounds nowhere
+__device__ __forceinline__ float q16_lo(unsigned x)
+{
+    return fmaf(__uint_as_float((x & 0xFFFFu) | 0x4B000000u), 0x1p-16f, -128.f);
+}
+__device__ __forceinline__ float q16_hi(unsigned x)
+{
+    return fmaf(__uint_as_float((x >> 16) | 0x4B000000u), 0x1p-16f, -128.f);
+}
+
+// the fractions w[8] and the scale of record t
+__device__ __forceinline__ float load_coef16(const uint4 *__restrict__ cq, const float *__restrict__ cs, long long t,
+                                             float w[8])
+{
+    const uint4 v = __ldcs(cq + t);
+    w[0] = q16_lo(v.x);
+    w[1] = q16_hi(v.x);
+    w[2] = q16_lo(v.y);
+    w[3] = q16_hi(v.y);
+    w[4] = q16_lo(v.z);
+    w[5] = q16_hi(v.z);
+    w[6] = q16_lo(v.w);
+    w[7] = q16_hi(v.w);
+    return __ldcs(cs + t);
+}
+
+// residual of the correction equation at a target: diag u0 - (s sum_f w_f
+// u_f + rhs), diag = 1 + s sum_f w_f; nb[f] the neighbours in record order
+__device__ __forceinline__ float resid32(const float w[8], float sc, const float nb[8], float u0, float rhs,
+                                         float &diag)
+{
+    float T = w[0] * nb[0];
+#pragma unroll
+    for (int f = 1; f < 8; ++f)
+        T = fmaf(w[f], nb[f], T);
+    diag = fmaf(sc, ((w[0] + w[1]) + (w[2] + w[3])) + ((w[4] + w[5]) + (w[6] + w[7])), 1.f);
+    return fmaf(diag, u0, -fmaf(sc, T, rhs));
+}
+
+// One FP32 SOR update of the correction at a target: returns the pre-update
+// residual of the correction equation and the updated value, which the
+// caller stores.
 struct Sweep32Out {
     float r, u;
 };
 __device__ __forceinline__ Sweep32Out sweep32_target(const Geo &g, const Split &sp, const TileCoord &tc, int p,
                                                      long long s, long long Hy, long long Hz, long long Hw,
                                                      const float *src, const float *__restrict__ oth,
-                                                     const float *__restrict__ cf, const float *__restrict__ rhs,
-                                                     float omega)
+                                                     const uint4 *__restrict__ cq, const float *__restrict__ cs,
+                                                     const float *__restrict__ rhs, float omega)
 {
     const float u0 = src[s];
-    const float *cv = cf + 8 * tile_coef_index(g, sp, tc);
-    const float4 c03 = ld_stream4(cv), c47 = ld_stream4(cv + 4);
-    const float a0 = c03.x, a1 = c03.y, a2 = c03.z, a3 = c03.w, a4 = c47.x, a5 = c47.y, a6 = c47.z, a7 = c47.w;
-    float S = a0 * ld_ro(oth + s - p + 1);
-    S = fmaf(a1, ld_ro(oth + s - p), S);
-    S = fmaf(a2, ld_ro(oth + s + Hy), S);
-    S = fmaf(a3, ld_ro(oth + s - Hy), S);
-    S = fmaf(a4, ld_ro(oth + s + Hz), S);
-    S = fmaf(a5, ld_ro(oth + s - Hz), S);
-    S = fmaf(a6, ld_ro(oth + s + Hw), S);
-    S = fmaf(a7, ld_ro(oth + s - Hw), S);
-    const float diag = 1.f + (((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7)));
-    const float r = fmaf(diag, u0, -(S + ld_stream(rhs + s)));
-    return Sweep32Out{r, fmaf(-omega / diag, r, u0)};
+    float w[8];
+    const float sc = load_coef16(cq, cs, tile_coef_index(g, sp, tc), w);
+    const float nb[8] = {ld_ro(oth + s - p + 1), ld_ro(oth + s - p), ld_ro(oth + s + Hy), ld_ro(oth + s - Hy),
+                         ld_ro(oth + s + Hz),    ld_ro(oth + s - Hz), ld_ro(oth + s + Hw), ld_ro(oth + s - Hw)};
+    float diag;
+    const float r = resid32(w, sc, nb, u0, ld_stream(rhs + s), diag);
+    // the relaxation weight omega / diag to a few ulp (diag in [1, 2^126))
+    return Sweep32Out{r, fmaf(-__fdividef(omega, diag), r, u0)};
 }
 
 // ---------------------------------------------------------------------------

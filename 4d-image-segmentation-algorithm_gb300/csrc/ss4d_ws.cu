@@ -111,7 +111,8 @@ __global__ void __launch_bounds__(256) k_ws_check(Geo g, Split sp, SweepCfg cfg,
         const int ds = st->dsrc;
         const float *own = COL == 0 ? pick(b.dR, ds) : b.dB;
         const float *__restrict__ oth = COL == 0 ? b.dB : pick(b.dR, ds);
-        const float *__restrict__ cf = b.coef32[COL];
+        const uint4 *__restrict__ cq = b.coefq[COL];
+        const float *__restrict__ cs = b.coefs[COL];
         const float *__restrict__ rhs = b.r32[COL];
         const long long Hy = sp.Hs, Hz = Hy * g.jM, Hw = Hz * g.kM;
         const int tx = threadIdx.x & (cfg.XT - 1), ty = threadIdx.x / cfg.XT;
@@ -124,18 +125,12 @@ __global__ void __launch_bounds__(256) k_ws_check(Geo g, Split sp, SweepCfg cfg,
             if (2 * tc.xi + 2 - p > g.nx)
                 continue;
             const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * Hy + tc.xi + sp.A;
-            const float *cv = cf + 8 * tile_coef_index(g, sp, tc);
-            const float4 c03 = ld_stream4(cv), c47 = ld_stream4(cv + 4);
-            float S = c03.x * oth[s - p + 1];
-            S = fmaf(c03.y, oth[s - p], S);
-            S = fmaf(c03.z, oth[s + Hy], S);
-            S = fmaf(c03.w, oth[s - Hy], S);
-            S = fmaf(c47.x, oth[s + Hz], S);
-            S = fmaf(c47.y, oth[s - Hz], S);
-            S = fmaf(c47.z, oth[s + Hw], S);
-            S = fmaf(c47.w, oth[s - Hw], S);
-            const float diag = 1.f + (((c03.x + c03.y) + (c03.z + c03.w)) + ((c47.x + c47.y) + (c47.z + c47.w)));
-            const float r = fmaf(diag, own[s], -(S + rhs[s]));
+            float w[8];
+            const float sc = load_coef16(cq, cs, tile_coef_index(g, sp, tc), w);
+            const float nb[8] = {oth[s - p + 1], oth[s - p], oth[s + Hy], oth[s - Hy],
+                                 oth[s + Hz],    oth[s - Hz], oth[s + Hw], oth[s - Hw]};
+            float diag;
+            const float r = resid32(w, sc, nb, own[s], rhs[s], diag);
             acc = fmaf(r, r, acc);
         }
         tot = acc;

@@ -39,14 +39,16 @@ WORKLOAD = ("segmentation time steps, 256x256x128x20 multi-object drifting scene
             "boundary erasure), K=1000, eps2=1e-3, tau=0.5, omega=1.8, gsTol=1e-6")
 # algorithmic bytes per interior voxel (each reference array touched once)
 BYTES_FP64_ITER = 88.0  # read u, prev, 8 coefficients; write u
-BYTES_FP32_ITER = 44.0  # the same arrays in FP32
+# FP32 correction sweep: the 20-byte record (8 16-bit fractions + FP32 scale),
+# right-hand side, correction read and written (44 B with 8 FP32 coefficients)
+BYTES_FP32_ITER = 32.0
 # DRAM bytes per target voxel of one half-sweep launch (dram__bytes_read.sum +
 # dram__bytes_write.sum from ncu), scaled by the targets of a launch at the
 # benchmarked size: k_sweep32 from two launches at 256x256x128x20
 # (83,886,080 targets; a one-pass capture), k_sweep64 from one launch at
 # 128x128x64x8 (4,194,304 targets)
 EXTRAP_ORDER = 3  # the extrap form's order (ss4d_solver_set_extrapolation)
-TRAFFIC_PER_TARGET = {"k_sweep32": 51.6, "k_sweep64": 118.6}
+TRAFFIC_PER_TARGET = {"k_sweep32": 39.8, "k_sweep64": 118.6}
 FP64_INSTR_PER_TARGET = 11.4  # k_sweep64, ncu at 128x128x64x8
 TRAFFIC_SOURCE = {"k_sweep32": "ncu capture of two launches at 256x256x128x20",
                   "k_sweep64": "ncu capture of one launch at 128x128x64x8"}

@@ -105,9 +105,12 @@ def test_seg_balls_rescale_path(ss4d, cuda, arith):
         for step in range(3):
             st = S.seg_time_step(p, u, prev, g, mmask=mm, balls=balls)
             if arith == "mixed":
-                # five iterations are the cap here: both stop at the cap
+                # five iterations are the cap here: both stop at the cap, before
+                # the tolerance, so the mixed iterate differs from the reference's
+                # by what five sweeps on its own inner operator make of it (its
+                # FP32 sweeps' coefficients are 16-bit fractions of the row sum)
                 assert st["iterations"] <= p.maxNoGSIteration
-                assert rel_err(host(u), d["u_steps"][step]) <= 1e-5
+                assert rel_err(host(u), d["u_steps"][step]) <= 1e-4
             else:
                 assert st["iterations"] == d["its"][step]
                 assert rel_err(host(u), d["u_steps"][step]) <= TOL[arith]

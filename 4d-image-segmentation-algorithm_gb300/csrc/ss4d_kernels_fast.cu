@@ -446,8 +446,14 @@ __global__ void k_zero_delta(Split sp, SplitBufs b, const LoopState *__restrict_
     }
 }
 
+// FP32 half-sweep of colour COL: each thread updates two adjacent targets of
+// a row (pc: pair_cfg), so the pair shares its index arithmetic and reads its
+// own values, right-hand sides and the y/z/w neighbours as 8-byte pairs; each
+// target's arithmetic is sweep32_target's (resid32 and the relaxed update).
+// The launch has the solver's persistent grid, whose every block writes its
+// partial residual sum.
 template <int COL>
-__global__ void __launch_bounds__(256) k_sweep32(Geo g, Split sp, SweepCfg cfg, SplitBufs b,
+__global__ void __launch_bounds__(256) k_sweep32(Geo g, Split sp, SweepCfg pc, SplitBufs b,
                                                  const DevParams *__restrict__ dp, const LoopState *__restrict__ st)
 {
     const int mode = st->mode;
@@ -470,21 +476,54 @@ __global__ void __launch_bounds__(256) k_sweep32(Geo g, Split sp, SweepCfg cfg, 
     const float *__restrict__ cs = b.coefs[COL];
     const float *__restrict__ rhs = b.r32[COL];
     const float omega = (float)dp->omega;
-    const long long Hy = sp.Hs, Hz = Hy * g.jM, Hw = Hz * g.kM;
-    const int tx = threadIdx.x & (cfg.XT - 1), ty = threadIdx.x / cfg.XT;
+    // 32-bit offsets: a colour array holds fewer than 2^31 elements
+    const unsigned Hy = (unsigned)sp.Hs, Hz = Hy * (unsigned)g.jM, Hw = Hz * (unsigned)g.kM;
+    const int tx = threadIdx.x & (pc.XT - 1), ty = threadIdx.x / pc.XT;
     float acc = 0.f;
-    for (long long t = blockIdx.x; t < cfg.ntiles; t += gridDim.x) {
-        const TileCoord tc = tile_coord(g, cfg, t, tx, ty);
+    for (long long t = blockIdx.x; t < pc.ntiles; t += gridDim.x) {
+        const TileCoord tc = tile_coord(g, pc, t, tx, ty);
         if (!tc.ok)
             continue;
         const int p = (COL + tc.j + tc.k + tc.l) & 1;
-        const int i = 2 * tc.xi + 2 - p;
+        const int xi = 2 * tc.xi; // the pair's first target; the second is xi + 1
+        const int i = 2 * xi + 2 - p;
         if (i > g.nx)
             continue;
-        const long long s = (((long long)tc.l * g.kM + tc.k) * g.jM + tc.j) * Hy + tc.xi + sp.A;
-        const Sweep32Out o = sweep32_target(g, sp, tc, p, s, Hy, Hz, Hw, src, oth, cq, cs, rhs, omega);
-        acc = fmaf(o.r, o.r, acc);
-        dst[s] = o.u;
+        const bool two = i + 2 <= g.nx;
+        // xi, Hs and A are even: every pair starts on an 8-byte boundary
+        const unsigned s = (((unsigned)tc.l * g.kM + tc.k) * g.jM + tc.j) * Hy + xi + sp.A;
+        const unsigned tq = ((((unsigned)tc.l - 1) * g.nz + (tc.k - 1)) * g.ny + (tc.j - 1)) * sp.nxh + xi;
+        const float2 u = *reinterpret_cast<const float2 *>(src + s);
+        const float2 rh = __ldcs(reinterpret_cast<const float2 *>(rhs + s));
+        float w0[8], w1[8];
+        const float sc0 = load_coef16(cq, cs, tq, w0);
+        float sc1 = 0.f;
+        if (two)
+            sc1 = load_coef16(cq, cs, tq + 1, w1);
+        // x neighbours of the pair: the other colour's columns s - p .. s - p + 2
+        const float2 vx = ld_ro(reinterpret_cast<const float2 *>(oth + s));
+        const float ex = ld_ro(oth + (p ? s - 1 : s + 2));
+        const float2 yp = ld_ro(reinterpret_cast<const float2 *>(oth + s + Hy));
+        const float2 ym = ld_ro(reinterpret_cast<const float2 *>(oth + s - Hy));
+        const float2 zp = ld_ro(reinterpret_cast<const float2 *>(oth + s + Hz));
+        const float2 zm = ld_ro(reinterpret_cast<const float2 *>(oth + s - Hz));
+        const float2 wp = ld_ro(reinterpret_cast<const float2 *>(oth + s + Hw));
+        const float2 wm = ld_ro(reinterpret_cast<const float2 *>(oth + s - Hw));
+        // record order: +x (column s_t - p + 1), -x (s_t - p), +y, -y, +z, -z, +w, -w
+        const float nb0[8] = {p ? vx.x : vx.y, p ? ex : vx.x, yp.x, ym.x, zp.x, zm.x, wp.x, wm.x};
+        float d0;
+        const float r0 = resid32(w0, sc0, nb0, u.x, rh.x, d0);
+        const float o0 = fmaf(-__fdividef(omega, d0), r0, u.x);
+        acc = fmaf(r0, r0, acc);
+        if (two) {
+            const float nb1[8] = {p ? vx.y : ex, p ? vx.x : vx.y, yp.y, ym.y, zp.y, zm.y, wp.y, wm.y};
+            float d1;
+            const float r1 = resid32(w1, sc1, nb1, u.y, rh.y, d1);
+            acc = fmaf(r1, r1, acc);
+            *reinterpret_cast<float2 *>(dst + s) = make_float2(o0, fmaf(-__fdividef(omega, d1), r1, u.y));
+        } else {
+            dst[s] = o0;
+        }
     }
     const double tot = block_sum((double)acc);
     if (threadIdx.x == 0)
@@ -693,14 +732,31 @@ void launch_zero_delta(const Split &s, SplitBufs b, LoopState *state, cudaStream
     k_zero_delta<<<1024, 256, 0, st>>>(s, b, state);
 }
 
+// Tiles of the paired FP32 sweep: the cfg.XT targets of a row chunk are
+// taken by cfg.XT / 2 threads with two adjacent targets each, so a tile has
+// twice the rows; the tile order and the grid stay the solver's.
+static SweepCfg pair_cfg(const Geo &g, const Split &s, const SweepCfg &cfg)
+{
+    SweepCfg c = cfg;
+    c.XT = cfg.XT >= 2 ? cfg.XT / 2 : 1;
+    c.TJ = c.threads / c.XT;
+    c.nXC = (s.nxh + 2 * c.XT - 1) / (2 * c.XT);
+    c.nJG = (g.ny + c.TJ - 1) / c.TJ;
+    c.ntiles = (long long)c.nXC * c.nJG * c.KB * g.nt * c.nKB;
+    c.dXC = make_fastdiv((unsigned)c.nXC);
+    c.dJG = make_fastdiv((unsigned)c.nJG);
+    return c;
+}
+
 void launch_sweep32(const Geo &g, const Split &s, const SweepCfg &cfg, int colour, SplitBufs b, const DevParams *dp,
                     LoopState *state, int start_mode, cudaStream_t st)
 {
     (void)start_mode;
+    const SweepCfg pc = pair_cfg(g, s, cfg);
     if (colour == 0)
-        k_sweep32<0><<<cfg.grid, cfg.threads, 0, st>>>(g, s, cfg, b, dp, state);
+        k_sweep32<0><<<cfg.grid, cfg.threads, 0, st>>>(g, s, pc, b, dp, state);
     else
-        k_sweep32<1><<<cfg.grid, cfg.threads, 0, st>>>(g, s, cfg, b, dp, state);
+        k_sweep32<1><<<cfg.grid, cfg.threads, 0, st>>>(g, s, pc, b, dp, state);
 }
 
 void launch_ctrl_mixed(SplitBufs b, int nparts, const DevParams *dp, LoopState *state, unsigned long long cond_handle,

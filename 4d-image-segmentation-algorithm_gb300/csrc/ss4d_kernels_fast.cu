@@ -447,7 +447,7 @@ __global__ void k_zero_delta(Split sp, SplitBufs b, const LoopState *__restrict_
 }
 
 // FP32 half-sweep of colour COL: each thread updates two adjacent targets of
-// a row (pc: pair_cfg), so the pair shares its index arithmetic and reads its
+// a row (pc: make_pair_cfg), so the pair shares its index arithmetic and reads its
 // own values, right-hand sides and the y/z/w neighbours as 8-byte pairs; each
 // target's arithmetic is sweep32_target's (resid32 and the relaxed update).
 // The launch has the solver's persistent grid, whose every block writes its
@@ -489,41 +489,9 @@ __global__ void __launch_bounds__(256) k_sweep32(Geo g, Split sp, SweepCfg pc, S
         const int i = 2 * xi + 2 - p;
         if (i > g.nx)
             continue;
-        const bool two = i + 2 <= g.nx;
-        // xi, Hs and A are even: every pair starts on an 8-byte boundary
         const unsigned s = (((unsigned)tc.l * g.kM + tc.k) * g.jM + tc.j) * Hy + xi + sp.A;
         const unsigned tq = ((((unsigned)tc.l - 1) * g.nz + (tc.k - 1)) * g.ny + (tc.j - 1)) * sp.nxh + xi;
-        const float2 u = *reinterpret_cast<const float2 *>(src + s);
-        const float2 rh = __ldcs(reinterpret_cast<const float2 *>(rhs + s));
-        float w0[8], w1[8];
-        const float sc0 = load_coef16(cq, cs, tq, w0);
-        float sc1 = 0.f;
-        if (two)
-            sc1 = load_coef16(cq, cs, tq + 1, w1);
-        // x neighbours of the pair: the other colour's columns s - p .. s - p + 2
-        const float2 vx = ld_ro(reinterpret_cast<const float2 *>(oth + s));
-        const float ex = ld_ro(oth + (p ? s - 1 : s + 2));
-        const float2 yp = ld_ro(reinterpret_cast<const float2 *>(oth + s + Hy));
-        const float2 ym = ld_ro(reinterpret_cast<const float2 *>(oth + s - Hy));
-        const float2 zp = ld_ro(reinterpret_cast<const float2 *>(oth + s + Hz));
-        const float2 zm = ld_ro(reinterpret_cast<const float2 *>(oth + s - Hz));
-        const float2 wp = ld_ro(reinterpret_cast<const float2 *>(oth + s + Hw));
-        const float2 wm = ld_ro(reinterpret_cast<const float2 *>(oth + s - Hw));
-        // record order: +x (column s_t - p + 1), -x (s_t - p), +y, -y, +z, -z, +w, -w
-        const float nb0[8] = {p ? vx.x : vx.y, p ? ex : vx.x, yp.x, ym.x, zp.x, zm.x, wp.x, wm.x};
-        float d0;
-        const float r0 = resid32(w0, sc0, nb0, u.x, rh.x, d0);
-        const float o0 = fmaf(-__fdividef(omega, d0), r0, u.x);
-        acc = fmaf(r0, r0, acc);
-        if (two) {
-            const float nb1[8] = {p ? vx.y : ex, p ? vx.x : vx.y, yp.y, ym.y, zp.y, zm.y, wp.y, wm.y};
-            float d1;
-            const float r1 = resid32(w1, sc1, nb1, u.y, rh.y, d1);
-            acc = fmaf(r1, r1, acc);
-            *reinterpret_cast<float2 *>(dst + s) = make_float2(o0, fmaf(-__fdividef(omega, d1), r1, u.y));
-        } else {
-            dst[s] = o0;
-        }
+        acc = sweep32_pair(p, s, tq, i + 2 <= g.nx, Hy, Hz, Hw, src, dst, oth, cq, cs, rhs, omega, acc);
     }
     const double tot = block_sum((double)acc);
     if (threadIdx.x == 0)
@@ -735,7 +703,7 @@ void launch_zero_delta(const Split &s, SplitBufs b, LoopState *state, cudaStream
 // Tiles of the paired FP32 sweep: the cfg.XT targets of a row chunk are
 // taken by cfg.XT / 2 threads with two adjacent targets each, so a tile has
 // twice the rows; the tile order and the grid stay the solver's.
-static SweepCfg pair_cfg(const Geo &g, const Split &s, const SweepCfg &cfg)
+static SweepCfg make_pair_cfg(const Geo &g, const Split &s, const SweepCfg &cfg)
 {
     SweepCfg c = cfg;
     c.XT = cfg.XT >= 2 ? cfg.XT / 2 : 1;
@@ -752,7 +720,7 @@ void launch_sweep32(const Geo &g, const Split &s, const SweepCfg &cfg, int colou
                     LoopState *state, int start_mode, cudaStream_t st)
 {
     (void)start_mode;
-    const SweepCfg pc = pair_cfg(g, s, cfg);
+    const SweepCfg pc = make_pair_cfg(g, s, cfg);
     if (colour == 0)
         k_sweep32<0><<<cfg.grid, cfg.threads, 0, st>>>(g, s, pc, b, dp, state);
     else

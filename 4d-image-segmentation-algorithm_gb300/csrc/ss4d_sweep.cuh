@@ -269,6 +269,52 @@ __device__ __forceinline__ Sweep32Out sweep32_target(const Geo &g, const Split &
     return Sweep32Out{r, fmaf(-__fdividef(omega, diag), r, u0)};
 }
 
+// Two adjacent targets xi, xi + 1 of one row of an FP32 half-sweep (the
+// second only when `two`), row phase p, split index s of the first (even:
+// xi, Hs and A are), compact record index tq of the first; 32-bit offsets
+// (a colour array holds fewer than 2^31 elements).  The pair reads its own
+// values, right-hand sides and y/z/w neighbours as 8-byte pairs and shares
+// its index arithmetic; each target's arithmetic is sweep32_target's.
+// Returns acc plus the squared pre-update residuals (first target first).
+__device__ __forceinline__ float sweep32_pair(int p, unsigned s, unsigned tq, bool two, unsigned Hy, unsigned Hz,
+                                              unsigned Hw, const float *src, float *dst, const float *__restrict__ oth,
+                                              const uint4 *__restrict__ cq, const float *__restrict__ cs,
+                                              const float *__restrict__ rhs, float omega, float acc)
+{
+    const float2 u = *reinterpret_cast<const float2 *>(src + s);
+    const float2 rh = __ldcs(reinterpret_cast<const float2 *>(rhs + s));
+    float w0[8], w1[8];
+    const float sc0 = load_coef16(cq, cs, tq, w0);
+    float sc1 = 0.f;
+    if (two)
+        sc1 = load_coef16(cq, cs, tq + 1, w1);
+    // x neighbours of the pair: the other colour's columns s - p .. s - p + 2
+    const float2 vx = ld_ro(reinterpret_cast<const float2 *>(oth + s));
+    const float ex = ld_ro(oth + (p ? s - 1 : s + 2));
+    const float2 yp = ld_ro(reinterpret_cast<const float2 *>(oth + s + Hy));
+    const float2 ym = ld_ro(reinterpret_cast<const float2 *>(oth + s - Hy));
+    const float2 zp = ld_ro(reinterpret_cast<const float2 *>(oth + s + Hz));
+    const float2 zm = ld_ro(reinterpret_cast<const float2 *>(oth + s - Hz));
+    const float2 wp = ld_ro(reinterpret_cast<const float2 *>(oth + s + Hw));
+    const float2 wm = ld_ro(reinterpret_cast<const float2 *>(oth + s - Hw));
+    // record order: +x (column s_t - p + 1), -x (s_t - p), +y, -y, +z, -z, +w, -w
+    const float nb0[8] = {p ? vx.x : vx.y, p ? ex : vx.x, yp.x, ym.x, zp.x, zm.x, wp.x, wm.x};
+    float d0;
+    const float r0 = resid32(w0, sc0, nb0, u.x, rh.x, d0);
+    const float o0 = fmaf(-__fdividef(omega, d0), r0, u.x);
+    acc = fmaf(r0, r0, acc);
+    if (two) {
+        const float nb1[8] = {p ? vx.y : ex, p ? vx.x : vx.y, yp.y, ym.y, zp.y, zm.y, wp.y, wm.y};
+        float d1;
+        const float r1 = resid32(w1, sc1, nb1, u.y, rh.y, d1);
+        acc = fmaf(r1, r1, acc);
+        *reinterpret_cast<float2 *>(dst + s) = make_float2(o0, fmaf(-__fdividef(omega, d1), r1, u.y));
+    } else {
+        dst[s] = o0;
+    }
+    return acc;
+}
+
 // ---------------------------------------------------------------------------
 // stopping tests, one volume: a and c are the summed red and black partials
 // of the body that just ran.  Both return true when the loop stops.

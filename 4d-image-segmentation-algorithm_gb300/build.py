@@ -39,6 +39,7 @@ CUDA_UNITS = {
     "ss4d_conv_tc.cu": [],
     "ss4d_assemble_ff.cu": [],
     "ss4d_front_ff.cu": [],
+    "ss4d_project.cu": [],
 }
 C_UNITS = {"ss4d_scene.c": ["-fopenmp"], "ss4d_vtk.c": [], "ss4d_slab.c": []}
 

@@ -138,6 +138,8 @@ struct ss4d_solver {
     int have_dprev;  // steps in a row whose change was kept: dR[0] / dB hold the next start correction
     int pre_next;    // the next mixed loop's first refinement pass was formed by the assembly
     float *hist[4];  // earlier steps' changes (split layout): h1 red, h1 black, h2 red, h2 black
+    int proj;        // start the first round from the projection onto the earlier changes (ss4d_project.cu)
+    double *d_proj;  // its per-block sums (18 * n_partial / 2 doubles) and coefficients (3 floats after them)
     double inner_omega; // mixed form: relaxation factor of the FP32 sweeps (0: omega_c)
     // per-kernel timing (ss4d_solver_set_timing)
     int timing;
@@ -319,7 +321,7 @@ extern "C" ss4d_status ss4d_solver_destroy(ss4d_solver *s)
     void *dev[] = {s->d_partial, s->d_scalar, s->d_state, s->d_params, s->d_scratch, s->d_coef_nat,
                    s->sb.R[0], s->sb.P[0], s->sb.coef[0], s->sb.coefq[0], s->sb.dR[0], s->sb.r32[0], s->sb.fn[0],
                    s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz, s->ws_x0, s->ws_y,
-                   s->hist[0], s->hist[1], s->hist[2], s->hist[3], s->sb.fd[0], s->d_ff};
+                   s->hist[0], s->hist[1], s->hist[2], s->hist[3], s->sb.fd[0], s->d_ff, s->d_proj};
     for (void *p : dev)
         if (p)
             cudaFree(p);
@@ -668,6 +670,7 @@ static ss4d_status finish_stats(ss4d_solver *s, ss4d_step_stats *stats, int mixe
         stats->status = L.status;
         stats->warm_started = L.warm;
         stats->near_tolerance = L.near;
+        stats->projected = mixed ? L.proj : 0;
     }
     if (L.status != SS4D_OK) {
         set_err("SOR residual became non-finite at iteration %d", L.z);
@@ -849,6 +852,37 @@ extern "C" ss4d_status ss4d_solver_set_extrapolation(ss4d_solver *s, int order)
     return SS4D_OK;
 }
 
+extern "C" ss4d_status ss4d_solver_set_projection(ss4d_solver *s, int enable)
+{
+    REQ(s, "solver is NULL");
+    s->proj = enable ? 1 : 0;
+    return SS4D_OK;
+}
+
+// the first round's start projected onto the earlier changes: with the
+// extrapolation of order 3 applied by the assembly (whose first refinement
+// pass's residual is then in rpre) and at least two earlier changes, when no
+// learned warm start supplies the start
+static ss4d_status project_start(ss4d_solver *s, int pre)
+{
+    if (!s->proj || !pre || s->extrap != 3 || !extrapolating(s) || s->have_dprev < 2 || ws_this_step(s, 1))
+        return SS4D_OK;
+    for (int q = 0; q < 4; ++q)
+        if (!s->hist[q])
+            return SS4D_OK;
+    if (!s->d_proj) {
+        const size_t nd = 9 * (size_t)s->n_partial; // 18 * grid with n_partial >= 2 * grid
+        CKS(dmalloc(s, (void **)&s->d_proj, sizeof(double) * nd + 4 * sizeof(float)));
+    }
+    float *c = reinterpret_cast<float *>(s->d_proj + 9 * (size_t)s->n_partial);
+    const int m = s->have_dprev >= 3 ? 3 : 2;
+    timed(s, SS4D_K_PROJECT, true, [&] {
+        launch_projection(s->geo, s->sp, s->cfg, s->sb, s->hist, m, s->d_proj, c, s->d_state, s->sm_count, s->stream);
+    });
+    s->launches += 4;
+    return SS4D_OK;
+}
+
 // the loop on the split buffers; u/prev already packed, coefficients assembled
 static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixed)
 {
@@ -872,6 +906,7 @@ static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixe
         s->launches += 1;
         if (ws_this_step(s, mixed))
             CKS(warm_start_prologue(s));
+        CKS(project_start(s, pre));
     }
     CKS(last_launch());
     bool graphed = false;
@@ -1310,9 +1345,13 @@ static ss4d_status unpack_plan(ss4d_solver *s, int mixed, UnpackPlan *u)
     u->terms = u->keep = 0;
     if (u->save) {
         u->keep = s->extrap - 1;
-        for (int q = 0; q < 2 * u->keep; ++q)
-            if (!s->hist[q])
+        for (int q = 0; q < 2 * u->keep; ++q) {
+            if (!s->hist[q]) {
                 CKS(dmalloc(s, (void **)&s->hist[q], sizeof(float) * s->sp.cs));
+                // ghost and padding cells stay zero (the projection reads them as neighbours)
+                CK(cudaMemsetAsync(s->hist[q], 0, sizeof(float) * s->sp.cs, s->stream));
+            }
+        }
         u->terms = s->have_dprev + 1 < s->extrap ? s->have_dprev + 1 : s->extrap;
     }
     return SS4D_OK;

@@ -171,6 +171,9 @@ bool _allocateMem_(void)
     const char *xv = getenv("SS4D_EXTRAPOLATE"); /* mixed form: extrapolation order 1..3 */
     if (xv && xv[0] >= '1' && xv[0] <= '3')
         ss4d_solver_set_extrapolation(g_solver, xv[0] - '0');
+    const char *pv = getenv("SS4D_PROJECT"); /* with order 3: projected start of the first round */
+    if (pv && pv[0] == '1')
+        ss4d_solver_set_projection(g_solver, 1);
     g_bytes = sizeof(double) * (size_t)iMax * jMax * kMax * lMax;
     for (int a = 0; a < A_COUNT; ++a) {
         void *hp = NULL, *dp = NULL;

@@ -82,6 +82,8 @@ struct LoopState {
     int near;        // 1 once a stop test saw |R - tol| <= near_band
     int pre;         // mixed form: the next refinement pass's residual is in rpre (formed by the
                      // assembly, which also applied the start correction); cleared by that pass
+    int proj;        // mixed form: the first round starts from the projection onto the previous
+                     // steps' changes (ss4d_project.cu)
     double R;        // last FP64 residual (sum r^2 h^4)
     double R_first;  // FP64 residual after iteration 1 (fast) / initial (mixed)
     double Rd;       // mixed form: last FP32 correction residual
@@ -249,7 +251,16 @@ struct SolverView {
     SweepCfg cfg;
     SplitBufs b;
 };
+// the first round's start from the previous steps' changes (ss4d_project.cu):
+// hist = the extrapolation history arrays (h1 red, h1 black, h2 red, h2 black),
+// m = 2 or 3 vectors, part = 18 * cfg.grid doubles, c = 3 floats
+void launch_projection(const Geo &g, const Split &sp, const SweepCfg &cfg, SplitBufs b, float *const *hist, int m,
+                       double *part, float *c, LoopState *st, int sm_count, cudaStream_t s);
 SweepCfg make_sweep_cfg_xt(const Geo &g, const Split &s, int sm_count, int kb, int xt);
+// tiles of the kernels that give each thread two adjacent targets of a row
+// (the FP32 sweep, the projection's products): cfg's row chunks of cfg.XT
+// targets taken by cfg.XT / 2 threads, twice the rows per tile
+SweepCfg make_pair_cfg(const Geo &g, const Split &s, const SweepCfg &cfg);
 ss4d_status solver_view(ss4d_solver *s, SolverView *out);      // allocates the FP64 split buffers
 ss4d_status solver_set_shape(ss4d_solver *s, int xt, int kb);  // tile width (threads along x) and k-block depth
 // assemble the coefficients of u and pack u (= prev) into the split buffers;

@@ -288,6 +288,7 @@ __global__ void k_loop_init(LoopState *st, int mode, int pre)
     st->keep = 0;
     st->warm = 0;
     st->near = 0;
+    st->proj = 0;
     st->R = 0.0;
     st->R_first = 0.0;
     st->Rd = 0.0;
@@ -703,7 +704,7 @@ void launch_zero_delta(const Split &s, SplitBufs b, LoopState *state, cudaStream
 // Tiles of the paired FP32 sweep: the cfg.XT targets of a row chunk are
 // taken by cfg.XT / 2 threads with two adjacent targets each, so a tile has
 // twice the rows; the tile order and the grid stay the solver's.
-static SweepCfg make_pair_cfg(const Geo &g, const Split &s, const SweepCfg &cfg)
+SweepCfg make_pair_cfg(const Geo &g, const Split &s, const SweepCfg &cfg)
 {
     SweepCfg c = cfg;
     c.XT = cfg.XT >= 2 ? cfg.XT / 2 : 1;

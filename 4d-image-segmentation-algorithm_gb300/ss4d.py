@@ -51,7 +51,7 @@ class Params(C.Structure):
 class StepStats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("status", C.c_int), ("residual", C.c_double),
                 ("first_residual", C.c_double), ("refinements", C.c_int), ("warm_started", C.c_int),
-                ("ms", C.c_float), ("near_tolerance", C.c_int)]
+                ("ms", C.c_float), ("near_tolerance", C.c_int), ("projected", C.c_int)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -89,7 +89,7 @@ def mcf_params(n: int, steps: int = 4, **over) -> Params:
 
 
 _lib = None
-ABI_VERSION = 2  # include/ss4d.h SS4D_ABI_VERSION: the structures above mirror it
+ABI_VERSION = 3  # include/ss4d.h SS4D_ABI_VERSION: the structures above mirror it
 
 
 # t-slab callbacks (include/ss4d.h: ss4d_slab_comm, ss4d_slab_ops)
@@ -262,6 +262,7 @@ def lib() -> C.CDLL:
         "ss4d_ws_features": ([vp, C.POINTER(Params), vp, P8, vp, vp, dp], st),
         "ss4d_solver_set_warm_start": ([vp, vp, vp], st),
         "ss4d_solver_set_extrapolation": ([vp, C.c_int], st),
+        "ss4d_solver_set_projection": ([vp, C.c_int], st),
         "ss4d_solver_set_inner_omega": ([vp, C.c_double], st),
         "ss4d_solver_set_warm_start_gate": ([vp, C.c_int], st),
         "ss4d_slab_partition": ([C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)], st),
@@ -443,6 +444,11 @@ class Solver:
         time of the earlier steps' changes (0 off, order 1, 2 or 3)"""
         _check(self.L.ss4d_solver_set_extrapolation(self.h, int(order)), "set_extrapolation")
 
+    def set_projection(self, enable: bool):
+        """mixed form with extrapolation of order 3: start each step's first
+        FP32 round from the least-residual combination of the earlier changes"""
+        _check(self.L.ss4d_solver_set_projection(self.h, 1 if enable else 0), "set_projection")
+
     def set_stream(self, stream: int | None):
         _check(self.L.ss4d_solver_set_stream(self.h, stream), "set_stream")
 
@@ -454,7 +460,7 @@ class Solver:
         in blocks of n k planes across the frames"""
         _check(self.L.ss4d_solver_set_assembly_order(self.h, planes), "set_assembly_order")
 
-    KERNELS = ("sweep64", "sweep32", "refine", "assemble", "pack", "warm")
+    KERNELS = ("sweep64", "sweep32", "refine", "assemble", "pack", "warm", "project")
 
     def set_timing(self, on: bool):
         _check(self.L.ss4d_solver_set_timing(self.h, 1 if on else 0), "set_timing")

@@ -57,6 +57,7 @@ TRAFFIC_SOURCE = {"k_sweep32": "ncu capture of two launches at 256x256x128x20",
 NAMED_FORMS = ("learned", "learned_x")
 FORM_LABEL = {"fp64": "plain FP64 sweeps", "mixed": "mixed (FP32 sweeps, FP64 residual/refinement)",
               "extrap": "mixed + cubic extrapolated start (no network)",
+              "proj": "mixed + cubic extrapolated start, first round projected onto the earlier changes (no network)",
               "learned": "mixed + learned warm start (the metric's named form)",
               "learned_x": "mixed + learned warm start at the extrapolated start (the metric's named form)",
               "extrap_w": "mixed + extrapolated start, FP32 sweeps relaxed by --inner-omega (reported only)"}
@@ -69,10 +70,11 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--size", type=int, nargs=4, default=[256, 256, 128, 20], metavar=("NX", "NY", "NZ", "NT"))
-    ap.add_argument("--forms", default="fp64,mixed,extrap,learned,learned_x,extrap_w",
+    ap.add_argument("--forms", default="fp64,mixed,extrap,proj,learned,learned_x,extrap_w",
                     help="fp64: plain FP64 sweeps; mixed: FP32 sweeps + FP64 refinement; extrap: mixed started "
                          "from the cubic extrapolation u^n + 3 d_(n-1) - 3 d_(n-2) + d_(n-3) of the earlier "
-                         "changes; learned: mixed started from the warm-start network (weights/wsnet_seg.npy); "
+                         "changes; proj: extrap whose first FP32 round starts from the least-residual combination "
+                         "of the last changes and the extrapolation; learned: mixed started from the warm-start network (weights/wsnet_seg.npy); "
                          "learned_x: the learned warm start at the extrapolated start (the network predicts the "
                          "correction the extrapolation leaves), run while it pays (--ws-gate); "
                          "extrap_w: extrap with --inner-omega")
@@ -256,10 +258,11 @@ def run_ours(args, rank, world, dist):
         net.set_params(np.load(os.path.join(PKG, "weights", "wsnet_seg.npy")))
 
     def use_form(form):
-        S.set_arith("mixed" if form in ("learned", "learned_x", "extrap", "extrap_w") else form)
+        S.set_arith("mixed" if form in ("learned", "learned_x", "extrap", "proj", "extrap_w") else form)
         S.set_warm_start(net if form in ("learned", "learned_x") else None, i0)
         S.set_warm_start_gate(args.ws_gate if form == "learned_x" else 0)
-        S.set_extrapolation(EXTRAP_ORDER if form in ("extrap", "extrap_w", "learned_x") else 0)
+        S.set_extrapolation(EXTRAP_ORDER if form in ("extrap", "proj", "extrap_w", "learned_x") else 0)
+        S.set_projection(form == "proj")
         S.set_inner_omega(args.inner_omega if form == "extrap_w" else 0.0)
         if args.assembly_order is not None:
             S.set_assembly_order(args.assembly_order)
@@ -321,6 +324,7 @@ def run_ours(args, rank, world, dist):
             "iterations": [s["iterations"] for s in steps],
             "refinements_per_step": statistics.mean(s["refinements"] for s in steps),
             "warm_started_steps": sum(s["warm_started"] for s in steps),
+            "projected_steps": sum(s["projected"] for s in steps),
             "max_residual": max(s["residual"] for s in steps),
             "converged": ok,
             "launches": launches,
@@ -344,7 +348,7 @@ def run_ours(args, rank, world, dist):
     for form in forms:
         use_form(form)
         u = finals[form].clone()
-        if form in ("extrap", "extrap_w", "learned_x"):  # untimed steps rebuild the history
+        if form in ("extrap", "proj", "extrap_w", "learned_x"):  # untimed steps rebuild the history
             for _ in range(EXTRAP_ORDER):
                 S.seg_time_step(p, u, None, g)
         S.set_timing(True)
@@ -361,7 +365,7 @@ def run_ours(args, rank, world, dist):
         if form == "mixed":
             ms, n = kt["sweep32"]
             per_unit = BYTES_FP32_ITER
-        elif form in ("learned", "learned_x", "extrap", "extrap_w"):
+        elif form in ("learned", "learned_x", "extrap", "proj", "extrap_w"):
             ms, n = kt["sweep32"]
             per_unit = BYTES_FP32_ITER
         else:
@@ -395,7 +399,7 @@ def run_ours(args, rank, world, dist):
 
     # error of the mixed forms against the plain FP64 form after the same steps
     err = {}
-    for form in ("mixed", "extrap", "extrap_w", "learned", "learned_x"):
+    for form in ("mixed", "extrap", "proj", "extrap_w", "learned", "learned_x"):
         if "fp64" not in finals or form not in finals:
             continue
         a = finals[form][1:-1, 1:-1, 1:-1, 1:-1]
@@ -557,8 +561,9 @@ def run_e2e(args, form, ctx):
     import ss4d
 
     shape, n_pad, n_int, p, i0h, u0h, _ = ctx
-    os.environ["SS4D_ARITH"] = "mixed" if form == "extrap" else form
-    os.environ["SS4D_EXTRAPOLATE"] = str(EXTRAP_ORDER) if form == "extrap" else "0"
+    os.environ["SS4D_ARITH"] = "mixed" if form in ("extrap", "proj") else form
+    os.environ["SS4D_EXTRAPOLATE"] = str(EXTRAP_ORDER) if form in ("extrap", "proj") else "0"
+    os.environ["SS4D_PROJECT"] = "1" if form == "proj" else "0"
     L = C.CDLL(ss4d.SEG_PATH, mode=os.RTLD_LOCAL)
     lM, kM, jM, iM = shape
     for nm, v in (("iMax", iM), ("jMax", jM), ("kMax", kM), ("lMax", lM), ("maxNoGSIteration", p.maxNoGSIteration),
@@ -961,7 +966,7 @@ def main():
     forms = list(results)
     # headline: the faster of the mixed forms (with and without the learned
     # warm start) among those that converged every step, else plain FP64
-    fast = [f for f in ("mixed", "extrap", "learned", "learned_x") if f in results and results[f]["converged"]]
+    fast = [f for f in ("mixed", "extrap", "proj", "learned", "learned_x") if f in results and results[f]["converged"]]
     head = max(fast, key=lambda f: results[f]["steps_per_s"]) if fast else forms[0]
     r = results[head]
     line = {"metric": METRIC, "value": r["steps_per_s"], "unit": "time-steps/s", "n_gpus": world,
@@ -969,6 +974,7 @@ def main():
             "scaling": "weak", "vs_baseline": None,
             "dtype": {"fp64": "f64", "mixed": "f32 sweeps + f64 residual/refinement",
                       "extrap": "f32 sweeps + f64 residual/refinement",
+                      "proj": "f32 sweeps + f64 residual/refinement",
                       "learned": "f32 sweeps + f64 residual/refinement, bf16 warm-start network",
                       "learned_x": "f32 sweeps + f64 residual/refinement, bf16 warm-start network"}[head],
             "data": "synthetic",
@@ -987,7 +993,7 @@ def main():
                                             if "fp64" in results else None),
                               "steps100_per_s": nf.get("steps100", {}).get("steps_per_s")}
     if "fp64" in results:
-        for f in ("mixed", "extrap", "extrap_w", "learned", "learned_x"):
+        for f in ("mixed", "extrap", "proj", "extrap_w", "learned", "learned_x"):
             if f in results:
                 line[f"{f}_over_fp64"] = results[f]["steps_per_s"] / results["fp64"]["steps_per_s"]
         if args.steps100 > 0:
@@ -995,7 +1001,7 @@ def main():
                                           results["fp64"]["steps100"]["steps_per_s"] for f in forms}
         line["roofline_fp64"] = roofline("fp64")
         line["error_vs_fp64"] = err
-    for f in ("mixed", "extrap", "learned", "learned_x"):
+    for f in ("mixed", "extrap", "proj", "learned", "learned_x"):
         if f in results and f != head:
             line[f"roofline_{f}"] = roofline(f)
     if rank == 0 and world == 1 and not args.no_e2e:

@@ -32,8 +32,8 @@
 extern "C" {
 #endif
 
-/* 2: ss4d_step_stats.near_tolerance */
-#define SS4D_ABI_VERSION 2
+/* 2: ss4d_step_stats.near_tolerance; 3: .projected, SS4D_K_PROJECT */
+#define SS4D_ABI_VERSION 3
 
 typedef enum ss4d_status {
     SS4D_OK = 0,
@@ -112,6 +112,9 @@ typedef struct ss4d_step_stats {
                                * gsTol: the reference's serial sum of the same terms
                                * could have decided that test the other way (one
                                * iteration more or fewer); reported, not corrected   */
+    int    projected;       /* mixed form: 1 when the first FP32 round started from the
+                               projection onto the previous steps' changes
+                               (ss4d_solver_set_projection)                          */
 } ss4d_step_stats;
 
 typedef struct ss4d_solver ss4d_solver;
@@ -151,6 +154,15 @@ ss4d_status ss4d_solver_set_assembly_order(ss4d_solver *s, int planes);
  * the handle.  No counterpart in the reference (each of its solves starts
  * from u^n). */
 ss4d_status ss4d_solver_set_extrapolation(ss4d_solver *s, int order);
+/* Mixed form with extrapolation of order 3: start each step's first FP32
+ * round not from zero but from the combination of the last changes d_{n-1},
+ * d_{n-2} and the extrapolation (d_{n-1}, d_{n-2} after two steps) whose
+ * residual in the correction equation is least in the 2-norm (a projection
+ * onto the previous solutions, Fischer 1998; enable 1, default 0).  The
+ * FP64 stop rule is unchanged, so only the iteration count depends on it;
+ * ss4d_step_stats.projected reports the steps that used it.  Not in the
+ * batched loop.  No counterpart in the reference. */
+ss4d_status ss4d_solver_set_projection(ss4d_solver *s, int enable);
 /* Mixed form: relaxation factor of the FP32 sweeps on the correction
  * equation (0, the default: the step's omega_c).  Only the iteration count
  * depends on it: the stop rule is the FP64 residual of u.  No counterpart in
@@ -168,7 +180,8 @@ typedef enum ss4d_kernel_kind {
     SS4D_K_ASSEMBLE = 3,  /* coefficient assembly                             */
     SS4D_K_PACK = 4,      /* natural <-> colour-split copies                  */
     SS4D_K_WARM = 5,      /* learned warm start: features, network, checks    */
-    SS4D_K_COUNT = 6
+    SS4D_K_PROJECT = 6,   /* start projected onto the previous steps' changes  */
+    SS4D_K_COUNT = 7
 } ss4d_kernel_kind;
 ss4d_status ss4d_solver_set_timing(ss4d_solver *s, int enable);
 ss4d_status ss4d_solver_kernel_time(const ss4d_solver *s, int kind, double *total_ms, long long *launches);

@@ -24,7 +24,9 @@
  * call when the environment variable SS4D_COMPAT_STRICT=1 is set.
  * SS4D_ARITH=reference|fp64|mixed selects the arithmetic form (default fp64);
  * with mixed, SS4D_EXTRAPOLATE=1, 2 or 3 starts each step from the extrapolation
- * of that order of the earlier steps (ss4d_solver_set_extrapolation).
+ * of that order of the earlier steps (ss4d_solver_set_extrapolation), and with
+ * order 3 SS4D_PROJECT=1 starts each step's first FP32 round from the
+ * projection onto the earlier changes (ss4d_solver_set_projection).
  *
  * Behaviour the reference leaves undefined is an error here instead:
  * a rescale ball whose box leaves the array makes _rescale4DdataToZeroOne_

@@ -29,7 +29,7 @@ def test_native_library_exports_header(ss4d):
     assert len(names) >= 30
     missing = [n for n in names if n not in syms]
     assert not missing, missing
-    assert ss4d.lib().ss4d_abi_version() == ss4d.ABI_VERSION == 2
+    assert ss4d.lib().ss4d_abi_version() == ss4d.ABI_VERSION == 3
 
 
 def test_reference_named_libraries_export_reference_interface(ss4d):

@@ -26,17 +26,21 @@ def test_mixed_forms_against_fp64(ss4d, cuda, kind, dims, steps):
     finals, its = {}, {}
     with ss4d.Solver(*shape[::-1], arith="fp64") as S:
         S.edge_detector(p, i0, None, g)
-        for form in ("fp64", "mixed", "extrap"):
+        for form in ("fp64", "mixed", "extrap", "proj"):
             S.set_arith("fp64" if form == "fp64" else "mixed")
-            S.set_extrapolation(3 if form == "extrap" else 0)
+            S.set_extrapolation(3 if form in ("extrap", "proj") else 0)
+            S.set_projection(form == "proj")
             u = torch.from_numpy(u0h).cuda()
             st = [S.seg_time_step(p, u, None, g) for _ in range(steps)]
             assert all(s["status"] == 0 and s["residual"] <= p.gsTol for s in st), form
             finals[form] = u[1:-1, 1:-1, 1:-1, 1:-1].cpu().numpy()
             its[form] = sum(s["iterations"] for s in st)
+            # the projected start from the third step on (two earlier changes)
+            assert [s["projected"] for s in st[:2]] == [0, 0]
+            assert all(s["projected"] == (form == "proj") for s in st[2:]), form
     ref = finals["fp64"]
     lev = 0.5 * (ref.min() + ref.max())
-    for form in ("mixed", "extrap"):
+    for form in ("mixed", "extrap", "proj"):
         d = finals[form] - ref
         max_rel = float(np.abs(d).max() / np.abs(ref).max())
         rel_l2 = float(np.linalg.norm(d) / np.linalg.norm(ref))
@@ -46,7 +50,7 @@ def test_mixed_forms_against_fp64(ss4d, cuda, kind, dims, steps):
         # both states meet the same residual tolerance every step; their
         # distance is that of two such iterates (no parity bar), the masks agree
         assert max_rel <= 2e-3 and dice >= 0.999
-    assert its["extrap"] < its["mixed"]
+    assert its["proj"] < its["extrap"] < its["mixed"]
 
 
 @pytest.mark.parametrize("arith", ["fp64", "mixed"])
@@ -147,3 +151,47 @@ def test_assembly_order_changes_no_bit(ss4d, cuda, host_arrays):
     for order, (u, its) in results.items():
         assert its == want_its, (order, its, want_its)
         assert np.array_equal(u, want_u), order
+
+
+def test_projected_start_same_on_host_arrays(ss4d, cuda):
+    """The projected start (the first FP32 round from the least-residual
+    combination of the earlier changes) through the host-array step equals the
+    device-array step bit for bit, steps and iteration counts alike; a solver
+    without extrapolation of order 3 ignores it."""
+    from test_gpu_parity import _pinned
+
+    torch = cuda
+    nx, ny, nz, nt = 33, 26, 17, 9
+    p = ss4d.scene_params()
+    i0h, u0h = ss4d.scene(3, nx, ny, nz, nt, seed=83)
+    shape = i0h.shape
+    i0 = torch.from_numpy(i0h).cuda()
+    g = [torch.zeros_like(i0) for _ in range(8)]
+    with ss4d.Solver(*shape[::-1], arith="fp64") as S:
+        S.edge_detector(p, i0, None, g)
+    with ss4d.Solver(*shape[::-1], arith="mixed") as S:
+        S.set_extrapolation(3)
+        S.set_projection(True)
+        u = torch.from_numpy(u0h).cuda()
+        dev = [S.seg_time_step(p, u, None, g) for _ in range(6)]
+        want = u.cpu().numpy()
+    hu, free_u = _pinned(ss4d, shape)
+    hp, free_p = _pinned(ss4d, shape)
+    try:
+        with ss4d.Solver(*shape[::-1], arith="mixed") as S:
+            S.set_extrapolation(3)
+            S.set_projection(True)
+            hu[...] = u0h
+            du = torch.zeros_like(i0)
+            host = [S.seg_time_step_host(p, hu, du, g, h_prev=hp) for _ in range(6)]
+            got = hu.copy()
+    finally:
+        free_u(), free_p()
+    assert [s["projected"] for s in dev] == [0, 0, 1, 1, 1, 1]
+    assert [(s["iterations"], s["projected"]) for s in host] == [(s["iterations"], s["projected"]) for s in dev]
+    assert np.array_equal(got, want)
+    with ss4d.Solver(*shape[::-1], arith="mixed") as S:
+        S.set_extrapolation(2)
+        S.set_projection(True)
+        u = torch.from_numpy(u0h).cuda()
+        assert not any(S.seg_time_step(p, u, None, g)["projected"] for _ in range(4))

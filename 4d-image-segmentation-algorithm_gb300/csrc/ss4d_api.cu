@@ -863,7 +863,7 @@ extern "C" ss4d_status ss4d_solver_set_projection(ss4d_solver *s, int enable)
 // extrapolation of order 3 applied by the assembly (whose first refinement
 // pass's residual is then in rpre) and at least two earlier changes, when no
 // learned warm start supplies the start
-static ss4d_status project_start(ss4d_solver *s, int pre)
+static ss4d_status project_start(ss4d_solver *s, int pre, LoopState *d_state)
 {
     if (!s->proj || !pre || s->extrap != 3 || !extrapolating(s) || s->have_dprev < 2 || ws_this_step(s, 1))
         return SS4D_OK;
@@ -877,7 +877,7 @@ static ss4d_status project_start(ss4d_solver *s, int pre)
     float *c = reinterpret_cast<float *>(s->d_proj + 9 * (size_t)s->n_partial);
     const int m = s->have_dprev >= 3 ? 3 : 2;
     timed(s, SS4D_K_PROJECT, true, [&] {
-        launch_projection(s->geo, s->sp, s->cfg, s->sb, s->hist, m, s->d_proj, c, s->d_state, s->sm_count, s->stream);
+        launch_projection(s->geo, s->sp, s->cfg, s->sb, s->hist, m, s->d_proj, c, d_state, s->sm_count, s->stream);
     });
     s->launches += 4;
     return SS4D_OK;
@@ -906,7 +906,7 @@ static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixe
         s->launches += 1;
         if (ws_this_step(s, mixed))
             CKS(warm_start_prologue(s));
-        CKS(project_start(s, pre));
+        CKS(project_start(s, pre, s->d_state));
     }
     CKS(last_launch());
     bool graphed = false;
@@ -1965,6 +1965,11 @@ ss4d_status ss4d::solver_prepare_step(ss4d_solver *s, const ss4d_params *p, doub
         CKS(clear_corrections(s));
     }
     return last_launch();
+}
+
+ss4d_status ss4d::solver_project_start(ss4d_solver *s, int pre, LoopState *d_state)
+{
+    return project_start(s, pre == 2, d_state);
 }
 
 ss4d_status ss4d::solver_finish_step(ss4d_solver *s, const LoopState *d_state, double *d_u)

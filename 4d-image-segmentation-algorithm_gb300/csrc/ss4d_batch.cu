@@ -758,6 +758,15 @@ extern "C" ss4d_status ss4d_batch_set_extrapolation(ss4d_batch *b, int order)
     return SS4D_OK;
 }
 
+extern "C" ss4d_status ss4d_batch_set_projection(ss4d_batch *b, int enable)
+{
+    if (!b)
+        return bfail(SS4D_ERR_INVALID, "invalid argument: batch is NULL");
+    for (int v = 0; v < b->n; ++v)
+        BCKS(ss4d_solver_set_projection(b->vol[v], enable));
+    return SS4D_OK;
+}
+
 extern "C" ss4d_status ss4d_batch_set_shape(ss4d_batch *b, int v, int xt, int k_block)
 {
     if (!b || v < 0 || v >= b->n)
@@ -917,6 +926,9 @@ extern "C" ss4d_status ss4d_batch_seg_time_step(ss4d_batch *b, const ss4d_params
     BCK(cudaMemcpyAsync(b->d_pre, b->h_pre, sizeof(int) * b->n, cudaMemcpyHostToDevice, b->stream));
     const int ib = (b->n + 63) / 64;
     k_binit<<<ib, 64, 0, b->stream>>>(b->d_st, b->n, 0, b->d_pre); // mixed: mode 0, refine first
+    if (b->mixed) // each volume's projected start (when enabled), on its own loop state
+        for (int v = 0; v < b->n; ++v)
+            BCKS(solver_project_start(b->vol[v], b->h_pre[v], b->d_st + v));
     if (!b->mixed) {
         launch_bsweep(b, 0, b->stream); // the first red half-sweep
         k_binit<<<ib, 64, 0, b->stream>>>(b->d_st, b->n, 1, nullptr);
@@ -1007,6 +1019,7 @@ extern "C" ss4d_status ss4d_batch_seg_time_step(ss4d_batch *b, const ss4d_params
             stats[v].refinements = b->mixed ? L.refinements : 0;
             stats[v].status = L.status;
             stats[v].near_tolerance = L.near;
+            stats[v].projected = b->mixed ? L.proj : 0;
             stats[v].ms = ms;
         }
         if (L.status != SS4D_OK)

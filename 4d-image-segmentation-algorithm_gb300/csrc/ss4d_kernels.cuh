@@ -271,6 +271,10 @@ ss4d_status solver_prepare_step(ss4d_solver *s, const ss4d_params *p, double *d_
                                 int *pre_out = nullptr);
 // unpack the red buffer state->final_red and black into the interior of u
 ss4d_status solver_finish_step(ss4d_solver *s, const LoopState *d_state, double *d_u);
+// the first round's projected start (ss4d_solver_set_projection) for a loop
+// whose state is *d_state, when the step's assembly applied the
+// extrapolation (pre == 2 from solver_prepare_step); nothing otherwise
+ss4d_status solver_project_start(ss4d_solver *s, int pre, LoopState *d_state);
 // device time of `iters` (black + red) FP64 sweep pairs with the current shape
 ss4d_status solver_time_sweeps(ss4d_solver *s, const ss4d_params *p, int iters, float *ms);
 int solver_sm_count(const ss4d_solver *s);

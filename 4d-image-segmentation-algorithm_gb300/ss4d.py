@@ -243,6 +243,7 @@ def lib() -> C.CDLL:
         "ss4d_batch_set_test_withhold_barrier": ([vp, C.c_int], st),
         "ss4d_batch_set_arith": ([vp, C.c_int], st),
         "ss4d_batch_set_extrapolation": ([vp, C.c_int], st),
+        "ss4d_batch_set_projection": ([vp, C.c_int], st),
         "ss4d_batch_set_shape": ([vp, C.c_int, C.c_int, C.c_int], st),
         "ss4d_batch_autotune": ([vp, C.POINTER(Params), C.POINTER(vp), C.POINTER(vp), C.POINTER(C.c_int),
                                  C.POINTER(C.c_int)], st),
@@ -710,6 +711,10 @@ class Batch:
 
     def set_extrapolation(self, order: int):
         _check(self.L.ss4d_batch_set_extrapolation(self.h, order), "batch_set_extrapolation")
+
+    def set_projection(self, enable: bool):
+        """every volume's first FP32 round from its projected start (with order 3)"""
+        _check(self.L.ss4d_batch_set_projection(self.h, 1 if enable else 0), "batch_set_projection")
 
     @staticmethod
     def _args(params, us, gs):

@@ -796,8 +796,9 @@ def batch_line(args, steps, warmup, forms_arg, config="16x_64-192", sequential=F
     U[48..96] x U[8..24] per axis by default), single-ellipsoid scenes with
     per-volume K in [500, 2000] and tau in [0.25, 1], stepped together (the
     SOR loop of all volumes in one persistent launch, per-volume convergence,
-    autotuned tile shapes), in the forms of --forms among fp64, mixed and
-    extrap (mixed with the cubic extrapolated start), each from the same
+    autotuned tile shapes), in the forms of --forms among fp64, mixed, extrap
+    (mixed with the cubic extrapolated start) and proj (extrap with the
+    projected start of each first round), each from the same
     start; `value` is the FP64 form's (or the first form's) aggregate
     voxel-updates/s, every form's numbers are in `forms`.  With sequential,
     each form is also timed with the same volumes solved one after another
@@ -826,7 +827,7 @@ def batch_line(args, steps, warmup, forms_arg, config="16x_64-192", sequential=F
         gs.append(g)
     dims = [(nx + 2, ny + 2, nz + 2, nt + 2) for nx, ny, nz, nt in sizes]
     vox = [nx * ny * nz * nt for nx, ny, nz, nt in sizes]
-    forms = [f for f in forms_arg.split(",") if f in ("fp64", "mixed", "extrap")] or ["fp64"]
+    forms = [f for f in forms_arg.split(",") if f in ("fp64", "mixed", "extrap", "proj")] or ["fp64"]
     stream = torch.cuda.current_stream(dev)
     shapes = None
     results = {}
@@ -837,8 +838,9 @@ def batch_line(args, steps, warmup, forms_arg, config="16x_64-192", sequential=F
         B.set_persistent(args.batch_loop == "persistent")
         if form != "fp64":
             B.set_arith("mixed")
-        if form == "extrap":
+        if form in ("extrap", "proj"):
             B.set_extrapolation(EXTRAP_ORDER)
+        B.set_projection(form == "proj")
         if shapes is None:
             shapes = B.autotune(params, us, gs)
         else:
@@ -868,7 +870,8 @@ def batch_line(args, steps, warmup, forms_arg, config="16x_64-192", sequential=F
             handles = [ss4d.Solver(*d, arith="fp64" if form == "fp64" else "mixed", stream=stream.cuda_stream)
                        for d in dims]
             for S in handles:
-                S.set_extrapolation(EXTRAP_ORDER if form == "extrap" else 0)
+                S.set_extrapolation(EXTRAP_ORDER if form in ("extrap", "proj") else 0)
+                S.set_projection(form == "proj")
             for _ in range(warmup):
                 for v, S in enumerate(handles):
                     S.seg_time_step(params[v], us[v], None, gs[v])
@@ -1018,8 +1021,8 @@ def main():
     if rank == 0 and world == 1 and not args.no_batch:
         # the batched workload, short: per-volume iteration counts of the last
         # step only (the full record is `--workload batch`)
-        b = batch_line(args, 10, 3, "fp64,extrap", sequential=True)
-        small = batch_line(args, 10, 3, "fp64,extrap", config="48x_24-48", sequential=True)
+        b = batch_line(args, 10, 3, "fp64,extrap,proj", sequential=True)
+        small = batch_line(args, 10, 3, "fp64,extrap,proj", config="48x_24-48", sequential=True)
         for bl in (b, small):
             for f in bl["forms"].values():
                 f["iterations_last_step"] = f.pop("iterations_per_volume")[-1]

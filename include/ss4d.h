@@ -160,8 +160,8 @@ ss4d_status ss4d_solver_set_extrapolation(ss4d_solver *s, int order);
  * residual in the correction equation is least in the 2-norm (a projection
  * onto the previous solutions, Fischer 1998; enable 1, default 0).  The
  * FP64 stop rule is unchanged, so only the iteration count depends on it;
- * ss4d_step_stats.projected reports the steps that used it.  Not in the
- * batched loop.  No counterpart in the reference. */
+ * ss4d_step_stats.projected reports the steps that used it (batched solves:
+ * ss4d_batch_set_projection).  No counterpart in the reference. */
 ss4d_status ss4d_solver_set_projection(ss4d_solver *s, int enable);
 /* Mixed form: relaxation factor of the FP32 sweeps on the correction
  * equation (0, the default: the step's omega_c).  Only the iteration count
@@ -423,6 +423,9 @@ ss4d_status ss4d_batch_set_arith(ss4d_batch *b, ss4d_arith arith);
 /* Mixed form: start every volume's step from the extrapolation of order
  * 0..3 of its earlier steps (ss4d_solver_set_extrapolation per volume). */
 ss4d_status ss4d_batch_set_extrapolation(ss4d_batch *b, int order);
+/* Mixed form with extrapolation of order 3: every volume's first FP32 round
+ * starts from its projected start (ss4d_solver_set_projection per volume). */
+ss4d_status ss4d_batch_set_projection(ss4d_batch *b, int enable);
 /* Tile shape of volume v: xt threads along x (power of two, 8..256; 0 =
  * automatic) and k-block depth k_block (>= 1).  Results do not depend on it. */
 ss4d_status ss4d_batch_set_shape(ss4d_batch *b, int v, int xt, int k_block);

@@ -75,15 +75,18 @@ def test_batch_autotuned_shapes_do_not_change_results(ss4d, oracle, cuda):
 
 
 @pytest.mark.parametrize("loop", ["persistent", "graph"])
-@pytest.mark.parametrize("extrap", [0, 3])
+@pytest.mark.parametrize("extrap", [0, 3, "proj"])
 def test_mixed_batch_matches_single_volume_mixed_solves(ss4d, oracle, cuda, extrap, loop):
     """The mixed form batched (refinement passes and FP32 sweeps of all volumes
     in one persistent launch, or as kernels of a graph's while loop, every
     volume in its own phase) gives each volume what its own mixed-form solver
-    gives it, step after step, with and without the extrapolated start: the
-    same counts, the same u, the FP64 tolerance met.  Both have the assembly
-    form each step's first refinement pass (start correction and FP64
-    residual)."""
+    gives it, step after step, with and without the extrapolated start, and
+    with the projected start ("proj": extrapolation of order 3 whose first
+    round starts from the projection onto the earlier changes): the same
+    counts, the same u, the FP64 tolerance met.  Both have the assembly form
+    each step's first refinement pass (start correction and FP64 residual)."""
+    proj = extrap == "proj"
+    extrap = 3 if proj else extrap
     torch = cuda
     sizes = [(20, 16, 12, 5), (33, 9, 14, 7), (12, 24, 10, 3)]
     vols = _volumes(ss4d, oracle, sizes, seed=11)
@@ -94,10 +97,11 @@ def test_mixed_batch_matches_single_volume_mixed_solves(ss4d, oracle, cuda, extr
         gd = [_dev(torch, a) for a in g]
         with ss4d.Solver.for_interior(*dims, arith="mixed") as S:
             S.set_extrapolation(extrap)
+            S.set_projection(proj)
             rec = []
             for _ in range(steps):
                 st = S.seg_time_step(p, u, None, gd)
-                rec.append((st["iterations"], st["refinements"], u.cpu().numpy()))
+                rec.append((st["iterations"], st["refinements"], st["projected"], u.cpu().numpy()))
         want.append(rec)
     us = [_dev(torch, u0) for _, u0, _ in vols]
     gs = [[_dev(torch, a) for a in g] for _, _, g in vols]
@@ -105,13 +109,15 @@ def test_mixed_batch_matches_single_volume_mixed_solves(ss4d, oracle, cuda, extr
     with ss4d.Batch([(d[0] + 2, d[1] + 2, d[2] + 2, d[3] + 2) for d in sizes]) as B:
         B.set_arith("mixed")
         B.set_extrapolation(extrap)
+        B.set_projection(proj)
         B.set_persistent(loop == "persistent")
         for step in range(steps):
             stats = B.seg_time_step(params, us, gs)
             for v, st in enumerate(stats):
-                its, refs, u_want = want[v][step]
+                its, refs, prj, u_want = want[v][step]
                 assert st["residual"] <= params[v].gsTol, (v, step)
-                assert (st["iterations"], st["refinements"]) == (its, refs), (v, step)
+                assert (st["iterations"], st["refinements"], st["projected"]) == (its, refs, prj), (v, step)
+                assert prj == (proj and step >= 2), (v, step)
                 assert np.array_equal(us[v].cpu().numpy(), u_want), (v, step)
 
 

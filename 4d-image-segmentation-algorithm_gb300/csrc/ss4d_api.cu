@@ -883,8 +883,12 @@ static ss4d_status project_start(ss4d_solver *s, int pre, LoopState *d_state)
     return SS4D_OK;
 }
 
-// the loop on the split buffers; u/prev already packed, coefficients assembled
-static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixed)
+static ss4d_status drive_loop(ss4d_solver *s, const ss4d_params *p, int mixed, int mode);
+
+// the loop on the split buffers; u/prev already packed, coefficients assembled.
+// spec (mixed form): the loop pauses when a round ends, before that round's
+// refinement pass (LoopState.paused), for the caller to run that pass itself
+static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixed, int spec = 0)
 {
     const int pre = mixed ? s->pre_next : 0; // consumed by this loop only
     s->pre_next = 0;
@@ -902,13 +906,24 @@ static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixe
         // the first refinement pass adds the correction in dR[0] / dB to u
         // (or the assembly did, and formed the pass's residual: pre_next)
         CKS(clear_corrections(s));
-        launch_loop_init(s->d_state, 0, s->stream, pre);
+        launch_loop_init(s->d_state, 0, s->stream, pre, spec);
         s->launches += 1;
         if (ws_this_step(s, mixed))
             CKS(warm_start_prologue(s));
         CKS(project_start(s, pre, s->d_state));
     }
     CKS(last_launch());
+    // the mode the controller left for the first body
+    return drive_loop(s, p, mixed, mixed && ws_this_step(s, mixed) ? 1 : 0);
+}
+
+// the loop from the state the controller left (mode: that state's mode),
+// as the graph's while loop or host-driven, until it stops or pauses
+static ss4d_status drive_loop(ss4d_solver *s, const ss4d_params *p, int mixed, int mode)
+{
+    const Geo &g = s->geo;
+    const Split &sp = s->sp;
+    const SweepCfg &cfg = s->cfg;
     bool graphed = false;
     if (s->use_graph && !s->graph_failed && !s->timing) {
         cudaGraphExec_t ex = mixed ? s->execmx : s->exec64;
@@ -924,7 +939,6 @@ static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixe
     }
     if (!graphed) {
         // host-driven form of the same loop: one small readback per iteration
-        int mode = ws_this_step(s, mixed) ? 1 : 0; // the mode the controller left for this body
         for (int guard = 0; guard < 4 * (p->maxNoGSIteration + 4) + 16; ++guard) {
             if (!mixed) {
                 timed(s, SS4D_K_SWEEP64, true,
@@ -951,13 +965,27 @@ static ss4d_status run_split_loop(ss4d_solver *s, const ss4d_params *p, int mixe
             CKS(last_launch());
             CK(cudaMemcpyAsync(s->h_state, s->d_state, sizeof(LoopState), cudaMemcpyDeviceToHost, s->stream));
             CK(cudaStreamSynchronize(s->stream));
-            if (s->h_state->stop)
+            if (s->h_state->stop || s->h_state->paused)
                 break;
             mode = s->h_state->mode;
         }
     }
     s->last_graphed = graphed ? 1 : 0;
     return SS4D_OK;
+}
+
+// the refinement pass a paused loop left for later (one host-driven body in
+// mode 0: only the refinement kernels and the controller do work)
+static ss4d_status refine_paused(ss4d_solver *s)
+{
+    const Geo &g = s->geo;
+    const Split &sp = s->sp;
+    const SweepCfg &cfg = s->cfg;
+    timed(s, SS4D_K_REFINE, true, [&] { launch_refine(g, sp, cfg, 0, s->sb, s->d_params, s->d_state, s->stream); });
+    timed(s, SS4D_K_REFINE, true, [&] { launch_refine(g, sp, cfg, 1, s->sb, s->d_params, s->d_state, s->stream); });
+    launch_ctrl_mixed(s->sb, cfg.grid, s->d_params, s->d_state, 0, 0, s->stream);
+    s->launches += 4;
+    return last_launch();
 }
 
 // count the kernels of a graphed loop after the fact: the controller counts
@@ -1595,7 +1623,9 @@ extern "C" ss4d_status ss4d_seg_time_step_host(ss4d_solver *s, const ss4d_params
     s->cur_g = gi;
     s->have_g = 1;
     s->pre_next = pre != 0;
-    CKS(run_split_loop(s, p, mixed));
+    // mixed form: the loop pauses when a round ends; u formed from that round
+    // goes down while its refinement pass decides (below)
+    CKS(run_split_loop(s, p, mixed, mixed));
     // the unpack and the rescale per chunk of interior frames, each chunk's
     // download on the side stream as soon as it is done
     UnpackPlan up;
@@ -1604,24 +1634,59 @@ extern "C" ss4d_status ss4d_seg_time_step_host(ss4d_solver *s, const ss4d_params
         CK(cudaStreamWaitEvent(s->stream, s->mask_ev, 0));
     hc.join(); // prev has its copy of u before any chunk of u comes down
     const int nt = g.lM - 2, Ci = nt < SS4D_HOST_CHUNKS ? nt : SS4D_HOST_CHUNKS;
-    for (int c = 0; c < Ci; ++c) {
-        const int a = 1 + (int)((long long)c * nt / Ci), e = 1 + (int)((long long)(c + 1) * nt / Ci);
-        launch_unpack_range(g, s->sp, s->sb, s->d_state, d_u, s->stream, up.terms, up.keep, s->hist, a, e);
-        s->launches += 1;
-        if (have_balls) {
-            launch_rescale_balls_range(g, d_u, s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz,
-                                       p->ballRadius, a, e, s->stream);
+    auto download = [&](int what) -> ss4d_status {
+        // the side stream's earlier downloads of d_u first (a retried round)
+        CK(cudaEventRecord(s->side_ev, s->side));
+        CK(cudaStreamWaitEvent(s->stream, s->side_ev, 0));
+        for (int c = 0; c < Ci; ++c) {
+            const int a = 1 + (int)((long long)c * nt / Ci), e = 1 + (int)((long long)(c + 1) * nt / Ci);
+            launch_unpack_range(g, s->sp, s->sb, s->d_state, d_u, s->stream, up.terms, up.keep, s->hist, a, e, what);
             s->launches += 1;
+            if (have_balls) {
+                launch_rescale_balls_range(g, d_u, s->d_frame_first, s->d_frame_count, s->d_bx, s->d_by, s->d_bz,
+                                           p->ballRadius, a, e, s->stream);
+                s->launches += 1;
+            }
+            if (h_Mmask) {
+                launch_mask_zero_range(g, d_u, d_Mmask, a, e, s->stream);
+                s->launches += 1;
+            }
+            CK(cudaEventRecord(s->chunk_ev[c], s->stream));
+            CK(cudaStreamWaitEvent(s->side, s->chunk_ev[c], 0));
+            CK(cudaMemcpyAsync(h_u + a * frame, d_u + a * frame, sizeof(double) * frame * (e - a),
+                               cudaMemcpyDeviceToHost, s->side));
         }
-        if (h_Mmask) {
-            launch_mask_zero_range(g, d_u, d_Mmask, a, e, s->stream);
-            s->launches += 1;
+        return last_launch();
+    };
+    // A paused loop's u (the split u plus the round's correction, added as
+    // its refinement pass adds it) goes down at once; the pass runs beside the
+    // download, and when it ends the step (as a round aimed below the
+    // tolerance almost always does) that u is the step's result: only the
+    // extrapolation history is left to write.  Otherwise the loop resumes and
+    // the result of a later round goes down.
+    bool done = false;
+    for (int guard = 0; mixed && guard < 4 * (p->maxNoGSIteration + 4) + 16; ++guard) {
+        CK(cudaMemcpyAsync(s->h_state, s->d_state, sizeof(LoopState), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        if (s->h_state->stop || !s->h_state->paused)
+            break; // stopped at the step's first refinement pass: as without pausing
+        CKS(download(UNPACK_PAUSED));
+        CKS(refine_paused(s));
+        CK(cudaMemcpyAsync(s->h_state, s->d_state, sizeof(LoopState), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        if (s->h_state->stop) {
+            if (up.terms > 0) {
+                launch_unpack_range(g, s->sp, s->sb, s->d_state, d_u, s->stream, up.terms, up.keep, s->hist, 1,
+                                    g.lM - 1, UNPACK_HISTORY);
+                s->launches += 1;
+            }
+            done = true;
+            break;
         }
-        CK(cudaEventRecord(s->chunk_ev[c], s->stream));
-        CK(cudaStreamWaitEvent(s->side, s->chunk_ev[c], 0));
-        CK(cudaMemcpyAsync(h_u + a * frame, d_u + a * frame, sizeof(double) * frame * (e - a), cudaMemcpyDeviceToHost,
-                           s->side));
+        CKS(drive_loop(s, p, mixed, s->h_state->mode));
     }
+    if (!done)
+        CKS(download(UNPACK_ALL));
     CKS(last_launch());
     unpack_done(s, up);
     s->have_g = 0;

@@ -84,6 +84,9 @@ struct LoopState {
                      // assembly, which also applied the start correction); cleared by that pass
     int proj;        // mixed form: the first round starts from the projection onto the previous
                      // steps' changes (ss4d_project.cu)
+    int spec;        // mixed form: pause the loop when a round ends, before its refinement pass
+                     // (the host-array step downloads the round's result meanwhile)
+    int paused;      // set by the controller when it paused the loop (spec); the refinement clears it
     double R;        // last FP64 residual (sum r^2 h^4)
     double R_first;  // FP64 residual after iteration 1 (fast) / initial (mixed)
     double Rd;       // mixed form: last FP32 correction residual
@@ -186,8 +189,12 @@ void launch_assemble_ff_faces_range(const Geo &g, const Split &s, CPtrs8 gin, in
 // [l0, l1) (1 <= l0 < l1 <= lMax-1) for the unpack and the rescale
 void launch_pack_range(const Geo &g, const Split &s, const double *u, const double *prev, SplitBufs b, int l0, int l1,
                        cudaStream_t st);
+// what k_unpack writes: u and the extrapolation history (UNPACK_ALL), only u
+// of a loop paused before its last refinement pass (UNPACK_PAUSED: the split u
+// plus the round's correction), only the history (UNPACK_HISTORY)
+enum { UNPACK_ALL = 0, UNPACK_PAUSED = 1, UNPACK_HISTORY = 2 };
 void launch_unpack_range(const Geo &g, const Split &s, SplitBufs b, const LoopState *state, double *u, cudaStream_t st,
-                         int terms, int keep, float *const *hist, int l0, int l1);
+                         int terms, int keep, float *const *hist, int l0, int l1, int what = UNPACK_ALL);
 void launch_mask_zero_range(const Geo &g, double *v, const double *Mmask, int l0, int l1, cudaStream_t st);
 void launch_rescale_balls_range(const Geo &g, double *v, const int *frame_first, const int *frame_count,
                                 const double *bx, const double *by, const double *bz, double R, int l0, int l1,
@@ -213,7 +220,7 @@ void launch_pack_coef(const Geo &g, const Split &s, CPtrs8 a, const ss4d_params 
 // terms/keep/hist: the mixed form's extrapolated start (k_unpack); hist = {h1 red, h1 black, h2 red, h2 black}
 void launch_unpack(const Geo &g, const Split &s, SplitBufs b, const LoopState *state, double *u, cudaStream_t st,
                    int terms = 0, int keep = 0, float *const *hist = nullptr);
-void launch_loop_init(LoopState *state, int mode, cudaStream_t st, int pre = 0);
+void launch_loop_init(LoopState *state, int mode, cudaStream_t st, int pre = 0, int spec = 0);
 void launch_sweep64(const Geo &g, const Split &s, const SweepCfg &cfg, int colour, SplitBufs b, const DevParams *dp,
                     LoopState *state, cudaStream_t st);
 void launch_advance(LoopState *state, cudaStream_t st);

@@ -230,8 +230,12 @@ struct History {
     float *h2[2];
 };
 
+// what: UNPACK_ALL (u and the history), UNPACK_PAUSED (only u, formed from a
+// loop paused before its last refinement pass: the split u plus the round's
+// correction, with that pass's own FP64 additions, so it equals what the pass
+// then writes), UNPACK_HISTORY (only the history and the next start)
 __global__ void k_unpack(Geo g, Split sp, SplitBufs b, const LoopState *__restrict__ st, double *u, int terms,
-                         int keep, History hs, int l_off)
+                         int keep, History hs, int l_off, int what)
 {
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
@@ -240,6 +244,15 @@ __global__ void k_unpack(Geo g, Split sp, SplitBufs b, const LoopState *__restri
         return;
     const int col = (i + j + k + l) & 1;
     const long long s = (((long long)l * g.kM + k) * g.jM + j) * sp.Hs + ((i + 1) >> 1) + sp.A - 1;
+    if (what == UNPACK_PAUSED) {
+        // the refinement's red update own + down (k_refine<0>) and black one
+        // Bk += dB (k_apply_black)
+        const double v = col == 0 ? b.R[0][s] + f2d_bits(pick(b.dR, st->dsrc)[s]) : b.Bk[s] + f2d_bits(b.dB[s]);
+        u[nat_index(g, i, j, k, l)] = v;
+        return;
+    }
+    if (what == UNPACK_HISTORY && terms <= 0)
+        return;
     // every load before the first store (which could alias them for the
     // compiler): one round trip to memory, not two
     float *h1 = pick(hs.h1, col), *h2 = pick(hs.h2, col);
@@ -254,7 +267,8 @@ __global__ void k_unpack(Geo g, Split sp, SplitBufs b, const LoopState *__restri
     }
     const int fr = st->final_red;
     const double v = col == 0 ? pick(b.R, fr)[s] : b.Bk[s];
-    u[nat_index(g, i, j, k, l)] = v;
+    if (what != UNPACK_HISTORY)
+        u[nat_index(g, i, j, k, l)] = v;
     if (terms > 0) {
         const float d = d2f_bits(v - pv);
         float guess = d;
@@ -273,9 +287,11 @@ __global__ void k_unpack(Geo g, Split sp, SplitBufs b, const LoopState *__restri
     }
 }
 
-__global__ void k_loop_init(LoopState *st, int mode, int pre)
+__global__ void k_loop_init(LoopState *st, int mode, int pre, int spec)
 {
     st->pre = pre;
+    st->spec = spec;
+    st->paused = 0;
     st->z = 0;
     st->stop = 0;
     st->status = 0;
@@ -521,8 +537,8 @@ __global__ void k_ctrl_mixed(SplitBufs b, int nparts, const DevParams *__restric
     if (threadIdx.x != 0)
         return;
     const bool stop = ctrl_mixed_update(st, a, c, dp);
-    if (use_cond)
-        cudaGraphSetConditional(h, stop ? 0u : 1u);
+    if (use_cond) // a paused loop leaves the graph too
+        cudaGraphSetConditional(h, stop || st->paused ? 0u : 1u);
 }
 
 // ---------------------------------------------------------------------------
@@ -647,7 +663,7 @@ void launch_unpack(const Geo &g, const Split &s, SplitBufs b, const LoopState *s
 }
 
 void launch_unpack_range(const Geo &g, const Split &s, SplitBufs b, const LoopState *state, double *u, cudaStream_t st,
-                         int terms, int keep, float *const *hist, int l0, int l1)
+                         int terms, int keep, float *const *hist, int l0, int l1, int what)
 {
     dim3 gr, bl;
     interior_grid(g, gr, bl);
@@ -657,12 +673,12 @@ void launch_unpack_range(const Geo &g, const Split &s, SplitBufs b, const LoopSt
         hs.h1[c] = hist ? hist[c] : nullptr;
         hs.h2[c] = hist ? hist[2 + c] : nullptr;
     }
-    k_unpack<<<gr, bl, 0, st>>>(g, s, b, state, u, terms, keep, hs, l0 - 1);
+    k_unpack<<<gr, bl, 0, st>>>(g, s, b, state, u, terms, keep, hs, l0 - 1, what);
 }
 
-void launch_loop_init(LoopState *state, int mode, cudaStream_t st, int pre)
+void launch_loop_init(LoopState *state, int mode, cudaStream_t st, int pre, int spec)
 {
-    k_loop_init<<<1, 1, 0, st>>>(state, mode, pre);
+    k_loop_init<<<1, 1, 0, st>>>(state, mode, pre, spec);
 }
 
 void launch_advance(LoopState *state, cudaStream_t st)

@@ -357,7 +357,8 @@ __device__ inline bool ctrl_mixed_update(LoopState *st, double a, double c, cons
     st->bodies += 1;
     bool stop = false;
     if (mode == 0) {
-        st->pre = 0; // later passes form their own residual
+        st->pre = 0;    // later passes form their own residual
+        st->paused = 0; // the pass a paused loop left for later has now run
         const double R = (a + c) * dp->h4;
         if (st->refinements == 0)
             st->R_first = R;
@@ -391,7 +392,8 @@ __device__ inline bool ctrl_mixed_update(LoopState *st, double a, double c, cons
         st->z += 1;
         st->round_z += 1;
         if (!isfinite(Rd) || !(Rd > st->target) || st->z >= dp->maxit) {
-            st->mode = 0; // refine with the red correction of this iteration
+            st->mode = 0;          // refine with the red correction of this iteration
+            st->paused = st->spec; // (and, with spec, leave that pass to the caller)
         } else {
             st->dsrc ^= 1;
         }

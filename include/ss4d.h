@@ -277,7 +277,11 @@ ss4d_status ss4d_seg_time_step(ss4d_solver *s, const ss4d_params *p, double *d_u
  * u goes up in SS4D_HOST_CHUNKS chunks of frames on the handle's side stream
  * while the step's first kernels (the pack; in the mixed form the whole
  * coefficient assembly) work on the frames that have arrived, and comes down
- * in chunks as the unpack and the rescale finish them; the results equal
+ * in chunks as the unpack and the rescale finish them.  In the mixed form
+ * the SOR loop pauses after each round of FP32 sweeps, and u formed from
+ * that round goes down while the refinement pass decides whether it meets
+ * gsTol; when it does, that download is the result, otherwise the loop goes
+ * on and u goes down again at its end.  The results equal
  * ss4d_seg_time_step's.  Returns when h_u holds the result. */
 #define SS4D_HOST_CHUNKS 16
 ss4d_status ss4d_seg_time_step_host(ss4d_solver *s, const ss4d_params *p, double *h_u, double *d_u,

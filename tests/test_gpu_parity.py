@@ -505,16 +505,20 @@ def _pinned(ss4d, shape):
     return a, (lambda: L.ss4d_host_free(ptr))
 
 
-@pytest.mark.parametrize("form", ["fp64", "mixed", "extrap"])
+@pytest.mark.parametrize("form", ["fp64", "mixed", "extrap", "tight"])
 @pytest.mark.parametrize("nt", [1, 3, 6])
 def test_host_array_step_equals_device_step(ss4d, oracle, cuda, form, nt):
     """ss4d_seg_time_step_host (u up and down in frame chunks overlapped with
     the step's first and last kernels, Mmask beside the solve, prev_u copied
-    on the host) gives, step after step, the u of ss4d_seg_time_step on device
-    arrays with the same Mmask and balls, and prev_u = the step's input."""
+    on the host; in the mixed form u formed from a round goes down while that
+    round's refinement pass decides) gives, step after step, the u of
+    ss4d_seg_time_step on device arrays with the same Mmask and balls, and
+    prev_u = the step's input.  "tight": the mixed form with extrapolation at
+    gsTol 1e-13, where rounds fall short of the tolerance and the loop goes
+    on after the download that a refinement pass rejected."""
     torch = cuda
     nx, ny, nz = 20, 18, 14
-    p = ss4d.scene_params(ballRadius=3.0)
+    p = ss4d.scene_params(ballRadius=3.0, gsTol=1e-13 if form == "tight" else 1e-6)
     i0h, u0h = ss4d.scene(1, nx, ny, nz, nt, seed=8)
     shape = i0h.shape
     g = [dev(torch, a) for a in oracle.gfaces(p, i0h, np.zeros_like(i0h))]
@@ -532,15 +536,20 @@ def test_host_array_step_equals_device_step(ss4d, oracle, cuda, form, nt):
         du, dm = torch.zeros_like(g[0]), torch.zeros_like(g[0])
         ref_u, ref_m = dev(torch, u0h), dev(torch, mask)
         with ss4d.Solver(*shape[::-1], arith=arith) as A, ss4d.Solver(*shape[::-1], arith=arith) as B:
-            A.set_extrapolation(3 if form == "extrap" else 0)
-            B.set_extrapolation(3 if form == "extrap" else 0)
+            A.set_extrapolation(3 if form in ("extrap", "tight") else 0)
+            B.set_extrapolation(3 if form in ("extrap", "tight") else 0)
+            rounds = []
             for _ in range(3):
                 before = hu.copy()
                 sa = A.seg_time_step_host(p, hu, du, g, h_prev=hp, h_mmask=hm, d_mmask=dm, balls=balls)
                 sb = B.seg_time_step(p, ref_u, None, g, ref_m, balls)
                 B.synchronize()
                 assert sa["iterations"] == sb["iterations"] and sa["status"] == 0
+                assert sa["refinements"] == sb["refinements"]
                 assert np.array_equal(hu, host(ref_u))
                 assert np.array_equal(hp, before)
+                rounds.append(sa["refinements"])
+            if form == "tight":  # some step needed more than one round
+                assert max(rounds) > 2, rounds
     finally:
         free_u(), free_p(), free_m()

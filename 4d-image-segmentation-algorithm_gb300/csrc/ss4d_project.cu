@@ -38,12 +38,29 @@ struct ProjVecs {
     const float *v[3][2];
 };
 
+// fraction f of a compressed record's packed fractions q, decoded where it
+// is used (three products share a record; the decoded values are not held)
+__device__ __forceinline__ float wq(const uint4 q, int f)
+{
+    const unsigned x = f < 2 ? q.x : f < 4 ? q.y : f < 6 ? q.z : q.w;
+    return (f & 1) ? q16_hi(x) : q16_lo(x);
+}
+
+// sum of the eight fractions: their 16-bit integers summed (at most 20
+// bits) and scaled, exactly the FP32 sum of the decoded fractions
+__device__ __forceinline__ float qsum(const uint4 q)
+{
+    const unsigned a = (q.x & 0xFFFFu) + (q.x >> 16) + (q.y & 0xFFFFu) + (q.y >> 16) + (q.z & 0xFFFFu) + (q.z >> 16) +
+                       (q.w & 0xFFFFu) + (q.w >> 16);
+    return (float)a * 0x1p-16f;
+}
+
 // A v at the pair of targets s, s + 1 (the second only when `two`; row
 // phase p) for one vector: its own values and its other-colour neighbours
 // read as 8-byte pairs, as the FP32 sweep reads them (sweep32_pair)
 __device__ __forceinline__ float2 av_pair(const float *__restrict__ own, const float *__restrict__ oth, unsigned s,
-                                          int p, bool two, unsigned Hy, unsigned Hz, unsigned Hw, const float w0[8],
-                                          const float w1[8], float sc0, float sc1, float dg0, float dg1)
+                                          int p, bool two, unsigned Hy, unsigned Hz, unsigned Hw, const uint4 q0,
+                                          const uint4 q1, float sc0, float sc1, float dg0, float dg1)
 {
     const float2 u = __ldg(reinterpret_cast<const float2 *>(own + s));
     const float2 vx = __ldg(reinterpret_cast<const float2 *>(oth + s));
@@ -56,19 +73,19 @@ __device__ __forceinline__ float2 av_pair(const float *__restrict__ own, const f
     const float2 wm = __ldg(reinterpret_cast<const float2 *>(oth + s - Hw));
     // record order: +x (column s_t - p + 1), -x (s_t - p), +y, -y, +z, -z, +w, -w
     const float n0[8] = {p ? vx.x : vx.y, p ? ex : vx.x, yp.x, ym.x, zp.x, zm.x, wp.x, wm.x};
-    float T = w0[0] * n0[0];
+    float T = wq(q0, 0) * n0[0];
 #pragma unroll
     for (int f = 1; f < 8; ++f)
-        T = fmaf(w0[f], n0[f], T);
+        T = fmaf(wq(q0, f), n0[f], T);
     float2 r;
     r.x = fmaf(dg0, u.x, -sc0 * T);
     r.y = 0.f;
     if (two) {
         const float n1[8] = {p ? vx.y : ex, p ? vx.x : vx.y, yp.y, ym.y, zp.y, zm.y, wp.y, wm.y};
-        T = w1[0] * n1[0];
+        T = wq(q1, 0) * n1[0];
 #pragma unroll
         for (int f = 1; f < 8; ++f)
-            T = fmaf(w1[f], n1[f], T);
+            T = fmaf(wq(q1, f), n1[f], T);
         r.y = fmaf(dg1, u.y, -sc1 * T);
     }
     return r;
@@ -101,21 +118,23 @@ __global__ void __launch_bounds__(256, 4) k_proj_dots(Geo g, Split sp, SweepCfg 
         const bool two = i + 2 <= g.nx;
         const unsigned s = (((unsigned)tc.l * g.kM + tc.k) * g.jM + tc.j) * Hy + xi + sp.A;
         const unsigned tq = ((((unsigned)tc.l - 1) * g.nz + (tc.k - 1)) * g.ny + (tc.j - 1)) * sp.nxh + xi;
-        float w0[8], w1[8];
-        const float sc0 = load_coef16(cq, cs, tq, w0);
+        const uint4 q0 = __ldcs(cq + tq);
+        const float sc0 = __ldcs(cs + tq);
+        uint4 q1 = make_uint4(0u, 0u, 0u, 0u);
         float sc1 = 0.f;
-        if (two)
-            sc1 = load_coef16(cq, cs, tq + 1, w1);
-        const float dg0 = fmaf(sc0, ((w0[0] + w0[1]) + (w0[2] + w0[3])) + ((w0[4] + w0[5]) + (w0[6] + w0[7])), 1.f);
-        const float dg1 =
-            two ? fmaf(sc1, ((w1[0] + w1[1]) + (w1[2] + w1[3])) + ((w1[4] + w1[5]) + (w1[6] + w1[7])), 1.f) : 0.f;
+        if (two) {
+            q1 = __ldcs(cq + tq + 1);
+            sc1 = __ldcs(cs + tq + 1);
+        }
+        const float dg0 = fmaf(sc0, qsum(q0), 1.f);
+        const float dg1 = two ? fmaf(sc1, qsum(q1), 1.f) : 0.f;
         // rpre holds A u0 - b: the correction equation's right-hand side is its negative
         const double2 r2 = __ldcs(reinterpret_cast<const double2 *>(rp + s));
         const float rh0 = -d2f_bits(r2.x), rh1 = two ? -d2f_bits(r2.y) : 0.f;
         float2 Av[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k)
-            Av[k] = k < m ? av_pair(V.v[k][COL], V.v[k][COL ^ 1], s, p, two, Hy, Hz, Hw, w0, w1, sc0, sc1, dg0, dg1)
+            Av[k] = k < m ? av_pair(V.v[k][COL], V.v[k][COL ^ 1], s, p, two, Hy, Hz, Hw, q0, q1, sc0, sc1, dg0, dg1)
                           : make_float2(0.f, 0.f);
         // the second target's terms are zero when it does not exist
         acc[0] = fmaf(Av[0].x, Av[0].x, fmaf(Av[0].y, Av[0].y, acc[0]));

@@ -195,3 +195,36 @@ def test_projected_start_same_on_host_arrays(ss4d, cuda):
         S.set_projection(True)
         u = torch.from_numpy(u0h).cuda()
         assert not any(S.seg_time_step(p, u, None, g)["projected"] for _ in range(4))
+
+
+@pytest.mark.parametrize("dims", [(1, 1, 1, 1), (2, 3, 2, 5), (9, 7, 5, 3), (33, 6, 4, 2), (17, 9, 5, 1)])
+def test_projected_start_on_ragged_and_minimal_sizes_matches_oracle(ss4d, oracle, cuda, dims):
+    """Six steps of the projected form (the projection from the third step on)
+    on odd, one-voxel and one-frame shapes, where the earlier changes can be
+    linearly dependent and the normal equations singular: every step meets the
+    FP64 tolerance and u stays within the mixed form's bar of the oracle's
+    FP64 steps, as the extrapolated form without the projection does."""
+    from conftest import rel_err
+
+    torch = cuda
+    nx, ny, nz, nt = dims
+    steps = 6
+    p = ss4d.scene_params(gsTol=1e-14)
+    i0h, u0h = ss4d.scene(1, nx, ny, nz, nt, seed=19)
+    g = oracle.gfaces(p, i0h, np.zeros_like(i0h))
+    want = u0h.copy()
+    oprev = np.zeros_like(want)
+    for _ in range(steps):
+        oracle.seg_time_step(p, want, oprev, g, mmask=np.ones_like(want))
+    gd = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in g]
+    for proj in (False, True):
+        u = torch.from_numpy(u0h.copy()).cuda()
+        with ss4d.Solver(*u0h.shape[::-1], arith="mixed") as S:
+            S.set_extrapolation(3)
+            S.set_projection(proj)
+            st = [S.seg_time_step(p, u, None, gd) for _ in range(steps)]
+        assert all(s["status"] == 0 and s["residual"] <= p.gsTol for s in st), (proj, st)
+        assert not any(s["projected"] for s in st[:2])
+        if not proj:
+            assert not any(s["projected"] for s in st)
+        assert rel_err(u.cpu().numpy(), want) <= 1e-6, proj

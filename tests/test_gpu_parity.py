@@ -505,7 +505,7 @@ def _pinned(ss4d, shape):
     return a, (lambda: L.ss4d_host_free(ptr))
 
 
-@pytest.mark.parametrize("form", ["fp64", "mixed", "extrap", "tight"])
+@pytest.mark.parametrize("form", ["fp64", "mixed", "extrap", "tight", "proj", "capped"])
 @pytest.mark.parametrize("nt", [1, 3, 6])
 def test_host_array_step_equals_device_step(ss4d, oracle, cuda, form, nt):
     """ss4d_seg_time_step_host (u up and down in frame chunks overlapped with
@@ -515,10 +515,14 @@ def test_host_array_step_equals_device_step(ss4d, oracle, cuda, form, nt):
     ss4d_seg_time_step on device arrays with the same Mmask and balls, and
     prev_u = the step's input.  "tight": the mixed form with extrapolation at
     gsTol 1e-13, where rounds fall short of the tolerance and the loop goes
-    on after the download that a refinement pass rejected."""
+    on after the download that a refinement pass rejected; "proj": with the
+    projected start (the third step); "capped": gsTol 1e-13 with at most 3
+    iterations, so every step ends at the cap inside a round."""
     torch = cuda
     nx, ny, nz = 20, 18, 14
-    p = ss4d.scene_params(ballRadius=3.0, gsTol=1e-13 if form == "tight" else 1e-6)
+    tight = form in ("tight", "capped")
+    p = ss4d.scene_params(ballRadius=3.0, gsTol=1e-13 if tight else 1e-6,
+                          **({"maxNoGSIteration": 3} if form == "capped" else {}))
     i0h, u0h = ss4d.scene(1, nx, ny, nz, nt, seed=8)
     shape = i0h.shape
     g = [dev(torch, a) for a in oracle.gfaces(p, i0h, np.zeros_like(i0h))]
@@ -536,8 +540,9 @@ def test_host_array_step_equals_device_step(ss4d, oracle, cuda, form, nt):
         du, dm = torch.zeros_like(g[0]), torch.zeros_like(g[0])
         ref_u, ref_m = dev(torch, u0h), dev(torch, mask)
         with ss4d.Solver(*shape[::-1], arith=arith) as A, ss4d.Solver(*shape[::-1], arith=arith) as B:
-            A.set_extrapolation(3 if form in ("extrap", "tight") else 0)
-            B.set_extrapolation(3 if form in ("extrap", "tight") else 0)
+            for S in (A, B):
+                S.set_extrapolation(3 if form in ("extrap", "tight", "proj", "capped") else 0)
+                S.set_projection(form == "proj")
             rounds = []
             for _ in range(3):
                 before = hu.copy()
@@ -548,6 +553,9 @@ def test_host_array_step_equals_device_step(ss4d, oracle, cuda, form, nt):
                 assert sa["refinements"] == sb["refinements"]
                 assert np.array_equal(hu, host(ref_u))
                 assert np.array_equal(hp, before)
+                assert sa["projected"] == sb["projected"]
+                if form == "capped":
+                    assert sa["iterations"] == p.maxNoGSIteration
                 rounds.append(sa["refinements"])
             if form == "tight":  # some step needed more than one round
                 assert max(rounds) > 2, rounds

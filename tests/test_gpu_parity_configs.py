@@ -15,7 +15,8 @@ reference's serial loop; a stop test inside that rounding band is reported
 by the GPU as near_tolerance, and only then may the counts differ (by one).
 
 At 128^3 x 16 the mixed forms (FP32 sweeps with FP64 refinement, with and
-without the extrapolated start, and with the learned warm start) are
+without the extrapolated start, with the projected start, and with the
+learned warm start) are
 compared with the oracle directly as well: every step meets the FP64
 tolerance and the final mask (level (min+max)/2 of the oracle's u) agrees
 with Dice >= 0.999.
@@ -113,15 +114,16 @@ def test_config2_fp64_matches_oracle(ss4d, cuda, config2):
                 break
 
 
-@pytest.mark.parametrize("form", ["mixed", "extrap", "learned"])
+@pytest.mark.parametrize("form", ["mixed", "extrap", "proj", "learned"])
 def test_config2_mixed_forms_against_oracle(ss4d, cuda, config2, form):
     torch = cuda
     p, i0h, u0h, oi0, g, steps = config2
     gd = [_dev(torch, a) for a in g]
     net = None
     with ss4d.Solver(*i0h.shape[::-1], arith="mixed") as S:
-        if form == "extrap":
+        if form in ("extrap", "proj"):
             S.set_extrapolation(3)
+            S.set_projection(form == "proj")
         if form == "learned":
             net = ss4d.Wsnet(seed=None)
             net.set_params(np.load(WEIGHTS))
@@ -133,6 +135,8 @@ def test_config2_mixed_forms_against_oracle(ss4d, cuda, config2, form):
     if net is not None:
         net.close()
     assert all(s["status"] == 0 and s["residual"] <= p.gsTol for s in stats)
+    # the projected start from the third step (two earlier changes)
+    assert [s["projected"] for s in stats] == [0, 0, 1 if form == "proj" else 0]
     want = steps[-1][2]
     inner = (slice(1, -1),) * 4
     a, b = got[inner], want[inner]

@@ -93,24 +93,49 @@ __global__ void __launch_bounds__(256) k_fdiff(Geo g, Split sp, const double *__
 // plane pk and frame fl (both from 0) of block z of a grid over P planes of
 // F frames: frame by frame (kb <= 0 or kb >= P), else in blocks of kb
 // planes, the planes of a block for each frame in turn (the last block
-// holds the remaining P mod kb planes)
-__device__ __forceinline__ void plane_frame(int z, int P, int F, int kb, int &pk, int &fl)
+// holds the remaining P mod kb planes).  The divisors are fixed per launch:
+// PlaneOrder carries them with their FastDiv multipliers (z < 2^31), since a
+// thread of these kernels handles one voxel and three integer divisions per
+// thread cost the issue-bound faces kernel a few per cent.
+struct PlaneOrder {
+    int blocked;              // 0: frame by frame
+    int P, kb, blk, full, rest; // blk = kb F, full = P / kb, rest = P - full kb
+    FastDiv fP, fkb, fblk, frest;
+};
+
+static PlaneOrder make_plane_order(int P, int F, int kb)
 {
-    if (kb <= 0 || kb >= P) {
-        pk = z % P;
-        fl = z / P;
+    PlaneOrder o;
+    o.blocked = !(kb <= 0 || kb >= P);
+    o.P = P;
+    o.kb = o.blocked ? kb : 1;
+    o.blk = o.kb * F;
+    o.full = P / o.kb;
+    o.rest = P - o.full * o.kb;
+    o.fP = make_fastdiv((unsigned)P);
+    o.fkb = make_fastdiv((unsigned)o.kb);
+    o.fblk = make_fastdiv((unsigned)(o.blk > 0 ? o.blk : 1));
+    o.frest = make_fastdiv((unsigned)(o.rest > 0 ? o.rest : 1));
+    return o;
+}
+
+__device__ __forceinline__ void plane_frame(unsigned z, const PlaneOrder &o, int &pk, int &fl)
+{
+    if (!o.blocked) {
+        const unsigned q = fdiv(z, o.fP);
+        pk = (int)(z - q * (unsigned)o.P);
+        fl = (int)q;
         return;
     }
-    const int full = P / kb, blk = kb * F;
-    const int b = z / blk;
-    if (b < full) {
-        const int r = z - b * blk;
-        fl = r / kb;
-        pk = b * kb + r % kb;
+    const unsigned b = fdiv(z, o.fblk);
+    if (b < (unsigned)o.full) {
+        const unsigned r = z - b * (unsigned)o.blk, q = fdiv(r, o.fkb);
+        fl = (int)q;
+        pk = (int)(b * (unsigned)o.kb + (r - q * (unsigned)o.kb));
     } else {
-        const int rest = P - full * kb, r = z - full * blk;
-        fl = r / rest;
-        pk = full * kb + r % rest;
+        const unsigned r = z - (unsigned)o.full * (unsigned)o.blk, q = fdiv(r, o.frest);
+        fl = (int)q;
+        pk = (int)((unsigned)o.full * (unsigned)o.kb + (r - q * (unsigned)o.rest));
     }
 }
 
@@ -142,14 +167,18 @@ __device__ __forceinline__ ff cdiff(const float2 *__restrict__ fa, unsigned x, u
 template <int D>
 __device__ __forceinline__ void face_val(const FFConst &K, const ff Dv[4], const ff Dn[4], ff cn, ff gv, ff &r, ff &q)
 {
-    ff tt = ff_make(0.f, 0.f); // sum of squares: positive terms, renormalised once
+    // sum of squares of the tangential central differences: positive terms,
+    // renormalised once; the first term starts the sum (adding it to zero
+    // would give the same pair)
+    ff tt;
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
         if (a == D)
             continue;
         const ff t = ff_add(Dn[a], Dv[a]); // may cancel: renormalised before squaring
         const float p = t.h * t.h;
-        tt = ff_add_nr(tt, ff_make(p, fmaf(2.f * t.h, t.l, fmaf(t.h, t.h, -p))));
+        const ff sq = ff_make(p, fmaf(2.f * t.h, t.l, fmaf(t.h, t.h, -p)));
+        tt = a == (D == 0 ? 1 : 0) ? sq : ff_add_nr(tt, sq);
     }
     tt = ff_norm(tt);
     const ff cn2 = ff_sqr(cn);
@@ -177,7 +206,7 @@ __device__ __forceinline__ void face_ff(const FFConst &K, const ff Dv[4], const 
 template <int D, int UPPER>
 __device__ __forceinline__ ff face_g(const CPtrs8 &gin, int has_g, unsigned x)
 {
-    return has_g ? ff_from_d(__ldg(gin.p[2 * D + UPPER] + x)) : ff_make(1.f, 0.f);
+    return has_g ? ff_from_pos_d(__ldg(gin.p[2 * D + UPPER] + x)) : ff_make(1.f, 0.f);
 }
 
 // the single face along D of a voxel v whose index along D is 0 (and >= 1
@@ -202,14 +231,14 @@ __device__ __forceinline__ void boundary_face(const FFConst &K, const CPtrs8 &gi
 // a few bytes of spill) ran 6.28 ms at 256^2 x 128 x 20 against 6.93 ms
 // at 5 blocks (48 registers) and 6.74 ms at 6.
 __global__ void __launch_bounds__(FTX *FTY, 8) k_faces_ff(Geo g, CPtrs8 gin, int has_g, FFConst K, SplitBufs b,
-                                                           int l_off, int kblock)
+                                                           int l_off, PlaneOrder po)
 {
     __shared__ float2 sD[4][FTY + 1][FTX + 1];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int i0 = 1 + blockIdx.x * FTX, j0 = 1 + blockIdx.y * FTY;
     const int i = i0 + tx, j = j0 + ty;
     int k, lf;
-    plane_frame(blockIdx.z, g.nz + 1, gridDim.z / (g.nz + 1), kblock, k, lf);
+    plane_frame(blockIdx.z, po, k, lf);
     const int l = l_off + lf;
     const unsigned st[4] = {1u, (unsigned)g.sy, (unsigned)g.sz, (unsigned)g.sw};
     const float2 *const F[4] = {reinterpret_cast<const float2 *>(b.fd[0]), reinterpret_cast<const float2 *>(b.fd[1]),
@@ -355,12 +384,12 @@ __device__ __forceinline__ void voxel_coef(const Geo &g, const Split &sp, const 
 
 template <int PRE>
 __global__ void __launch_bounds__(256, PRE ? 6 : 8) k_voxel_coef_ff(Geo g, Split sp, FFConst K, SplitBufs b, int l_off,
-                                                                    int kblock)
+                                                                    PlaneOrder po)
 {
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
     int kk, lf;
-    plane_frame(blockIdx.z, g.nz, gridDim.z / g.nz, kblock, kk, lf);
+    plane_frame(blockIdx.z, po, kk, lf);
     const int k = 1 + kk, l = 1 + l_off + lf;
     if (i > g.nx || j > g.ny)
         return;
@@ -441,17 +470,19 @@ void launch_assemble_ff_faces_range(const Geo &g, const Split &s, CPtrs8 gin, in
     const FFConst K = make_ffconst(p);
     if (f1 > f0) {
         dim3 gr((g.nx + FTX - 1) / FTX, (g.ny + FTY - 1) / FTY, (g.nz + 1) * (f1 - f0));
-        k_faces_ff<<<gr, dim3(FTX, FTY, 1), 0, st>>>(g, gin, has_g, K, b, f0, kblock);
+        k_faces_ff<<<gr, dim3(FTX, FTY, 1), 0, st>>>(g, gin, has_g, K, b, f0,
+                                                     make_plane_order(g.nz + 1, f1 - f0, kblock));
     }
     {
         const int bx = g.nx >= 128 ? 128 : (g.nx >= 64 ? 64 : 32);
         const int by = 256 / bx;
         dim3 bl(bx, by, 1);
         dim3 gr((g.nx + bx - 1) / bx, (g.ny + by - 1) / by, g.nz * (v1 - v0));
+        const PlaneOrder po = make_plane_order(g.nz, v1 - v0, kblock);
         if (v1 > v0 && pre)
-            k_voxel_coef_ff<1><<<gr, bl, 0, st>>>(g, s, K, b, v0 - 1, kblock);
+            k_voxel_coef_ff<1><<<gr, bl, 0, st>>>(g, s, K, b, v0 - 1, po);
         else if (v1 > v0)
-            k_voxel_coef_ff<0><<<gr, bl, 0, st>>>(g, s, K, b, v0 - 1, kblock);
+            k_voxel_coef_ff<0><<<gr, bl, 0, st>>>(g, s, K, b, v0 - 1, po);
     }
 }
 

@@ -99,6 +99,21 @@ __device__ __forceinline__ ff ff_from_d(double d)
     return ff_make(h, l);
 }
 
+// ff_from_d for a positive double in [2^-74, 2^127) (the range of the edge
+// detector's g = 1 / (1 + K x) in (0, 1]): the same pair by fewer integer
+// operations (the high part's bits in one funnel shift); any other value
+// takes ff_from_d
+__device__ __forceinline__ ff ff_from_pos_d(double d)
+{
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const unsigned e = hi >> 20; // biased exponent; the sign bit makes it >= 2048
+    if (e - 949u > 1150u - 949u)
+        return ff_from_d(d);
+    const float h = __uint_as_float(__funnelshift_l(lo, hi - (896u << 20), 3));
+    const float l = __uint2float_rz(lo & 0x1FFFFFFFu) * __uint_as_float((e - 948u) << 23);
+    return ff_make(h, l);
+}
+
 __device__ __forceinline__ double ff_to_d(ff a)
 {
     return f2d_bits(a.h) + f2d_bits(a.l);

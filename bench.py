@@ -48,6 +48,15 @@ BYTES_FP32_ITER = 32.0
 # (83,886,080 targets; a one-pass capture), k_sweep64 from one launch at
 # 128x128x64x8 (4,194,304 targets)
 EXTRAP_ORDER = 3  # the extrap form's order (ss4d_solver_set_extrapolation)
+# one step's coefficient assembly (_gs_coefficients_ with the prev_u copy):
+# read u and the 8 g faces, write the 8 coefficients, copy u to prev
+BYTES_ASSEMBLY = 152.0
+# DRAM bytes per interior voxel of the mixed form's three assembly kernels
+# (first differences with the pack, faces, coefficient records with the first
+# refinement pass's residual), one ncu capture at 128x128x64x8: 82.7 + 142.9
+# + 190.5 (the first-difference kernel's 62.2 B per padded voxel counted per
+# interior voxel)
+TRAFFIC_ASSEMBLY = 416.1
 TRAFFIC_PER_TARGET = {"k_sweep32": 39.8, "k_sweep64": 118.6}
 FP64_INSTR_PER_TARGET = 11.4  # k_sweep64, ncu at 128x128x64x8
 TRAFFIC_SOURCE = {"k_sweep32": "ncu capture of two launches at 256x256x128x20",
@@ -397,6 +406,25 @@ def run_ours(args, rank, world, dist):
                 "share_of_step_kernel_time": (ms / tot) if tot else None,
                 "kernel_ms": {k: v[0] for k, v in kt.items()}, "fp64_pipe": fp64}
 
+    def roofline_assembly(form):
+        """the mixed form's coefficient assembly of one step (three kernels,
+        timed together) against the copy bandwidth, with its algorithmic bytes"""
+        ms, n = roof[form]["assemble"]
+        if n == 0:
+            return None
+        avg = ms / n
+        ach = BYTES_ASSEMBLY * n_int / (avg / 1e3) / 1e9
+        return {"bound": "hbm", "kernels": "k_fdiff<2> + k_faces_ff + k_voxel_coef_ff<1>", "achieved": ach,
+                "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "peak_source": how,
+                "bytes_per_voxel": BYTES_ASSEMBLY, "traffic": TRAFFIC_ASSEMBLY * n_int,
+                "traffic_source": f"ncu capture of the three kernels at 128x128x64x8: {TRAFFIC_ASSEMBLY} DRAM "
+                                  f"B/voxel x voxels",
+                "avg_ms_per_step": avg,
+                "note": "float-float arithmetic on the FP32 pipe; beyond the algorithmic bytes the kernels move "
+                        "their intermediates (first differences, face quantities), the FP32 sweep records, the "
+                        "split copies of u and the first refinement pass's residual; the coefficient kernel is "
+                        "bound by the FP64 pipe (18 FP64 instructions per voxel), the faces kernel by issue"}
+
     # error of the mixed forms against the plain FP64 form after the same steps
     err = {}
     for form in ("mixed", "extrap", "proj", "extrap_w", "learned", "learned_x"):
@@ -415,7 +443,7 @@ def run_ours(args, rank, world, dist):
     S.close()
     if net is not None:
         net.close()
-    return results, roofline, err, (shape, n_pad, n_int, p, i0h, u0h, first_fp64)
+    return results, roofline, roofline_assembly, err, (shape, n_pad, n_int, p, i0h, u0h, first_fp64)
 
 
 def frontend_balls(nx, ny, nz, nt, seed, per_frame=5, radius=8.0):
@@ -965,7 +993,7 @@ def main():
         import torch.distributed as dist  # noqa: F811
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group("nccl")
-    results, roofline, err, ctx = run_ours(args, rank, world, dist)
+    results, roofline, roofline_assembly, err, ctx = run_ours(args, rank, world, dist)
     forms = list(results)
     # headline: the faster of the mixed forms (with and without the learned
     # warm start) among those that converged every step, else plain FP64
@@ -1007,6 +1035,8 @@ def main():
     for f in ("mixed", "extrap", "proj", "learned", "learned_x"):
         if f in results and f != head:
             line[f"roofline_{f}"] = roofline(f)
+    if head != "fp64":
+        line["roofline_assembly"] = roofline_assembly(head)
     if rank == 0 and world == 1 and not args.no_e2e:
         try:
             # the reference-named layer runs the mixed form without the network

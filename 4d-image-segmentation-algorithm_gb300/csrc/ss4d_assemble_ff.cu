@@ -90,55 +90,6 @@ __global__ void __launch_bounds__(256) k_fdiff(Geo g, Split sp, const double *__
     }
 }
 
-// plane pk and frame fl (both from 0) of block z of a grid over P planes of
-// F frames: frame by frame (kb <= 0 or kb >= P), else in blocks of kb
-// planes, the planes of a block for each frame in turn (the last block
-// holds the remaining P mod kb planes).  The divisors are fixed per launch:
-// PlaneOrder carries them with their FastDiv multipliers (z < 2^31), since a
-// thread of these kernels handles one voxel and three integer divisions per
-// thread cost the issue-bound faces kernel a few per cent.
-struct PlaneOrder {
-    int blocked;              // 0: frame by frame
-    int P, kb, blk, full, rest; // blk = kb F, full = P / kb, rest = P - full kb
-    FastDiv fP, fkb, fblk, frest;
-};
-
-static PlaneOrder make_plane_order(int P, int F, int kb)
-{
-    PlaneOrder o;
-    o.blocked = !(kb <= 0 || kb >= P);
-    o.P = P;
-    o.kb = o.blocked ? kb : 1;
-    o.blk = o.kb * F;
-    o.full = P / o.kb;
-    o.rest = P - o.full * o.kb;
-    o.fP = make_fastdiv((unsigned)P);
-    o.fkb = make_fastdiv((unsigned)o.kb);
-    o.fblk = make_fastdiv((unsigned)(o.blk > 0 ? o.blk : 1));
-    o.frest = make_fastdiv((unsigned)(o.rest > 0 ? o.rest : 1));
-    return o;
-}
-
-__device__ __forceinline__ void plane_frame(unsigned z, const PlaneOrder &o, int &pk, int &fl)
-{
-    if (!o.blocked) {
-        const unsigned q = fdiv(z, o.fP);
-        pk = (int)(z - q * (unsigned)o.P);
-        fl = (int)q;
-        return;
-    }
-    const unsigned b = fdiv(z, o.fblk);
-    if (b < (unsigned)o.full) {
-        const unsigned r = z - b * (unsigned)o.blk, q = fdiv(r, o.fkb);
-        fl = (int)q;
-        pk = (int)(b * (unsigned)o.kb + (r - q * (unsigned)o.kb));
-    } else {
-        const unsigned r = z - (unsigned)o.full * (unsigned)o.blk, q = fdiv(r, o.frest);
-        fl = (int)q;
-        pk = (int)((unsigned)o.full * (unsigned)o.kb + (r - q * (unsigned)o.rest));
-    }
-}
-
 // --- faces ------------------------------------------------------------------
 // A block takes a tile of FTX x FTY voxels (i, j) of one (k, l) plane.  The
 // central differences D_a of every voxel are formed once, by its own thread,
